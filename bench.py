@@ -1,0 +1,366 @@
+#!/usr/bin/env python3
+"""Benchmark of the dense-CRF mean-field hot path on GB300.
+
+Workload ("plain_vga"): DenseCRF2D 640x480, 21 labels, smooth-random-field
+unary, 40-cell Voronoi image, addPairwiseGaussian(sxy=3, compat=3) +
+addPairwiseBilateral(sxy=80, srgb=13, compat=10) with Potts compatibility,
+10 mean-field iterations, float32.  Seeded synthetic inputs
+(pydensecrf_gb300.synthetic.plain_vga); no dataset is involved.
+
+One STEP is one complete solve of that image: both lattice builds and
+normalisations plus the 10 iterations.  Metric: MPix*label*iter/s =
+W*H*M*T / step time (higher is better).
+
+* value -- inputs resident in HBM (unary and image on the device), the C ABI
+  with device pointers; CUDA events on the engine's stream around each step;
+  L2 flushed (a 512 MiB write) between timed steps, outside the events.
+* e2e   -- the public Python API (DenseCRF2D / setUnaryEnergy /
+  addPairwise* / inference) with the unary and image in pinned host memory:
+  every step copies them host->device and reads the marginals back.
+* cpu_baseline -- the CPU oracle (a C restatement of the reference's
+  algorithm, oracle/dcrf_oracle.c) on a bounded sample of the same workload,
+  one solve per host thread in parallel.
+* --impl reference -- the reference's CPU path for this workload on the host
+  cores (the oracle port: the reference itself is not built on this machine),
+  same metric and step definition.
+
+Under torchrun (--gpus N > 1) every rank solves its own image: replicas, no
+collective on the data path (scaling "weak"); value = all ranks' work / the
+slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W, H, M, T = 640, 480, 21, 10
+UNITS_PER_STEP = W * H * M * T / 1e6  # MPix*label*iter per solve
+METRIC = "MPix*label*iter/s, 640x480x21, 10 iterations (Gaussian+bilateral), full solve incl. lattice build"
+WORKLOAD = "DenseCRF2D 640x480 M=21 T=10, Gaussian(sxy=3,c=3)+bilateral(sxy=80,srgb=13,c=10) Potts"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx = float(p[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------
+def cpu_oracle_rate(cfg, threads: int, solves_per_thread: int = 1):
+    """Throughput of the CPU oracle on full solves of the workload, `threads` in parallel."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    U = np.ascontiguousarray(cfg["U"].T)
+    fg = O.features_gaussian_2d(W, H, 3.0, 3.0)
+    fb = O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13)
+
+    def solve():
+        c = O.OracleCRF(W * H, M)
+        c.set_unary(U)
+        c.add_pairwise(fg, 3.0)
+        c.add_pairwise(fb, 10.0)
+        c.inference(T)
+
+    def worker():
+        for _ in range(solves_per_thread):
+            solve()
+
+    t0 = time.perf_counter()
+    ths = [threading.Thread(target=worker) for _ in range(threads)]
+    for t in ths:
+        t.start()
+    for t in ths:
+        t.join()
+    dt = time.perf_counter() - t0
+    n = threads * solves_per_thread
+    return n * UNITS_PER_STEP / dt, dt, n
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from pydensecrf_gb300 import synthetic as S
+
+    cfg = S.plain_vga(0)
+    cores = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_oracle_rate(cfg, cores)
+    times = []
+    for _ in range(args.steps):
+        _, dt, n = cpu_oracle_rate(cfg, cores)
+        times.append(dt)
+    total = sum(times)
+    value = args.steps * cores * UNITS_PER_STEP / total
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "MPix*label*iter/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded plain_vga generator)", "impl": "reference",
+        "config": {"workload": WORKLOAD, "step": f"{cores} full solves in parallel (one per host thread)"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "MPix*label*iter/s", "cores": cores, "kind": "port",
+                         "sample": f"{cores} concurrent full solves per step, {args.steps} steps"},
+        "e2e": {"value": round(value, 3), "unit": "MPix*label*iter/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+# ----------------------------------------------------------------------------
+def run_gpu(args):
+    import torch
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist_mod
+
+        dist_mod.init_process_group("nccl")
+        dist = dist_mod
+    dev = torch.device("cuda", local)
+
+    from pydensecrf_gb300 import _lib, synthetic as S
+    from pydensecrf_gb300 import densecrf as dcrf
+
+    lib = _lib.load()
+    cfg = S.plain_vga(rank)
+    U_d = torch.from_numpy(cfg["U"]).to(dev)
+    img_d = torch.from_numpy(cfg["img"]).to(dev)
+    Q_d = torch.empty((M, W * H), dtype=torch.float32, device=dev)
+    h = ctypes.c_void_p()
+    _lib.check(lib.dcrf_create_2d(W, H, M, ctypes.byref(h)))
+    stream = torch.cuda.current_stream(dev)
+    _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    cg = np.array([3.0], np.float32)
+    cb = np.array([10.0], np.float32)
+
+    def step_device():
+        _lib.check(lib.dcrf_clear_pairwise(h))
+        _lib.check(lib.dcrf_set_unary(h, ctypes.c_void_p(U_d.data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE))
+        _lib.check(lib.dcrf_add_pairwise_gaussian(h, 3.0, 3.0, _lib.COMPAT_POTTS, cg.ctypes.data, 1, 3, None))
+        _lib.check(lib.dcrf_add_pairwise_bilateral(h, 80.0, 80.0, 13.0, 13.0, 13.0, ctypes.c_void_p(img_d.data_ptr()),
+                                                   _lib.DEVICE, _lib.COMPAT_POTTS, cb.ctypes.data, 1, 3, None))
+        _lib.check(lib.dcrf_inference(h, T, ctypes.c_void_p(Q_d.data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE))
+
+    flush = torch.empty(128 * 1024 * 1024, dtype=torch.float32, device=dev)  # 512 MiB > L2
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step_device()
+    cnt0 = ctypes.c_ulonglong()
+    cnt1 = ctypes.c_ulonglong()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    lib.dcrf_launch_count(ctypes.byref(cnt0))
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            step_device()
+            ev[k][1].record(stream)
+        barrier()
+    lib.dcrf_launch_count(ctypes.byref(cnt1))
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(sum(step_ms))
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world * args.steps * UNITS_PER_STEP / (total_ms / 1e3)
+    launches = int(cnt1.value - cnt0.value)
+
+    # ---- breakdown and roofline: a profiled pass (events around every launch)
+    _lib.check(lib.dcrf_set_profiling(h, 1))
+    nprof = 3
+    for _ in range(nprof):
+        flush.zero_()
+        step_device()
+    prof = {}
+    for cls, name in ((0, "point"), (1, "reduce"), (2, "blur"), (3, "lattice"), (4, "other")):
+        ms, n = ctypes.c_double(), ctypes.c_longlong()
+        _lib.check(lib.dcrf_profile(h, cls, ctypes.byref(ms), ctypes.byref(n)))
+        prof[name] = {"ms_per_step": ms.value / nprof, "launches_per_step": n.value // nprof,
+                      "avg_us": 1e3 * ms.value / max(1, n.value)}
+    _lib.check(lib.dcrf_set_profiling(h, 0))
+    Ls, Ps = [], []
+    for term in range(2):
+        L, P, nt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _lib.check(lib.dcrf_term_stats(h, term, ctypes.byref(L), ctypes.byref(P), ctypes.byref(nt)))
+        Ls.append(L.value)
+        Ps.append(P.value)
+    N = W * H
+    MP = 24
+    d_terms = (2, 5)
+    # algorithmic bytes of one mean-field point pass (slice + compatibility + softmax + tile splat):
+    # unary read, per term: corner offsets + slice weights, norm, every vertex row once, tile member
+    # lists (uint16 point + float weight), partial rows written; plus the slot map.
+    pp_bytes = N * M * 4 + N * 4 + sum(N * (d + 1) * 8 + N * 4 + L * MP * 4 + N * (d + 1) * 6 + P * MP * 4
+                                       for d, L, P in zip(d_terms, Ls, Ps))
+    peak, peak_kind = measured_peak()
+    avg_s = prof["point"]["avg_us"] / 1e6
+    achieved = pp_bytes / avg_s / 1e9
+    roofline = {"bound": "hbm", "kernel": "pointpass_kernel<24>", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3), "traffic": args.traffic,
+                "algorithmic_bytes_per_launch": int(pp_bytes), "avg_launch_us": round(prof["point"]["avg_us"], 2),
+                "peak_kind": peak_kind}
+
+    # ---- end to end through the public Python API, pinned host buffers
+    U_h = torch.from_numpy(cfg["U"]).pin_memory().numpy()
+    img_h = torch.from_numpy(cfg["img"]).pin_memory().numpy()
+
+    def step_e2e():
+        d = dcrf.DenseCRF2D(W, H, M)
+        d.setUnaryEnergy(U_h)
+        d.addPairwiseGaussian(sxy=3, compat=3)
+        d.addPairwiseBilateral(sxy=80, srgb=13, rgbim=img_h, compat=10)
+        Q = d.inference(T)
+        return Q
+
+    for _ in range(max(1, args.warmup)):
+        step_e2e()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        Q = step_e2e()
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = world * args.steps * UNITS_PER_STEP / e2e_s
+
+    # ---- CPU baseline (rank 0, single GPU runs only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, dt, n = cpu_oracle_rate(cfg, threads)
+        cpu = {"value": round(rate, 3), "unit": "MPix*label*iter/s", "cores": threads, "kind": "port",
+               "sample": f"{n} full solves of the same workload, one per thread, {dt:.1f} s"}
+
+    lib.dcrf_destroy(h)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "MPix*label*iter/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded plain_vga generator)",
+            "config": {"workload": WORKLOAD, "step": "one full solve: 2 lattice builds + norms + 10 iterations",
+                       "l2": "flushed between timed steps (512 MiB write)", "parallelism": f"replicas x{world}"},
+            "e2e": {"value": round(e2e_value, 3), "unit": "MPix*label*iter/s",
+                    "h2d_bytes_per_step": int(cfg["U"].nbytes + cfg["img"].nbytes),
+                    "d2h_bytes_per_step": int(N * M * 4), "ms_per_step": round(1e3 * e2e_s / args.steps, 3)},
+            "gpu_launches": launches,
+            "breakdown_ms_per_step": {k: round(v["ms_per_step"], 4) for k, v in prof.items()},
+            "iteration_ms": round((prof["point"]["ms_per_step"] + prof["reduce"]["ms_per_step"]
+                                   + prof["blur"]["ms_per_step"]) / T, 4),
+            "lattice": {"L": Ls, "partials": Ps},
+            "roofline": roofline,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--traffic", type=float, default=None,
+                    help="DRAM bytes per point-pass launch from an ncu capture (reported as roofline.traffic)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

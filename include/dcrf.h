@@ -1,0 +1,215 @@
+/*
+ * dcrf.h -- C ABI of the GB300 dense-CRF engine (libdcrf_gb300.so).
+ *
+ * Drop-in boundary for the mean-field path of pydensecrf: each entry point
+ * names the reference interface it replaces (paths inside the pydensecrf
+ * project).  The reference binds its C++ core through Cython
+ * (pydensecrf/densecrf.pxd:47-84); this library exposes the same operations as
+ * plain C with opaque handles, integer status codes and raw pointers.
+ *
+ * Conventions
+ *   - Every function returns DCRF_OK (0) or a negative DCRF_ERR_* code; the
+ *     message of the last failure on the calling thread is available from
+ *     dcrf_last_error().  (The reference raises C++ exceptions that Cython
+ *     maps to Python exceptions: densecrf.pxd:9-26.)
+ *   - `where` says whether a pointer is host (DCRF_HOST) or device
+ *     (DCRF_DEVICE) memory; host buffers are copied through the handle's
+ *     stream, device buffers are used in place.
+ *   - Label-major layout (DCRF_LAYOUT_LM): an M x N quantity is stored as M
+ *     rows of N floats -- the numpy (M, N) C-order array that
+ *     DenseCRF.setUnaryEnergy takes (densecrf.pyx:80-89).  Point-major
+ *     (DCRF_LAYOUT_PM): N rows of M floats -- the memory of the reference's
+ *     column-major Eigen MatrixXf that inference() returns (eigen.pyx:68-81).
+ *   - Features are (d, N) C-order (densecrf.pyx:71-75).
+ *   - A handle is used by one host thread at a time; all work of a handle is
+ *     ordered on its stream.  Calls return after the result is complete (the
+ *     host-visible outputs are written) unless stated otherwise.
+ *   - Lattice arithmetic: the reference compiles a different lattice build on
+ *     x86 (SSE) and on other hosts (scalar) (permutohedral.cpp:36-47,
+ *     140-474).  DCRF_VARIANT_SSE (the default) reproduces the x86 build,
+ *     DCRF_VARIANT_SCALAR the scalar build, table for table.
+ */
+#ifndef DCRF_GB300_H
+#define DCRF_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DCRF_ABI_VERSION 1
+
+/* status codes */
+#define DCRF_OK 0
+#define DCRF_ERR_INVALID_ARG -1  /* bad shape, null pointer, unsupported size */
+#define DCRF_ERR_CUDA -2         /* a CUDA runtime call failed */
+#define DCRF_ERR_OOM -3          /* device allocation failed */
+#define DCRF_ERR_HASH_FULL -4    /* lattice hash table overflowed (internal retry failed) */
+#define DCRF_ERR_KEY_OVERFLOW -5 /* a lattice coordinate left the int16 range of the reference's keys */
+#define DCRF_ERR_NO_DEVICE -6    /* no usable CUDA device */
+#define DCRF_ERR_STATE -7        /* call not valid in the handle's current state */
+#define DCRF_ERR_TIMEOUT -8      /* a bounded device-side wait gave up */
+
+#define DCRF_HOST 0
+#define DCRF_DEVICE 1
+
+#define DCRF_LAYOUT_LM 0 /* label-major: M rows of N */
+#define DCRF_LAYOUT_PM 1 /* point-major: N rows of M */
+
+#define DCRF_VARIANT_SSE 0
+#define DCRF_VARIANT_SCALAR 1
+
+/* enums of pydensecrf/densecrf/include/pairwise.h:32-42 (same values) */
+#define DCRF_NO_NORMALIZATION 0
+#define DCRF_NORMALIZE_BEFORE 1
+#define DCRF_NORMALIZE_AFTER 2
+#define DCRF_NORMALIZE_SYMMETRIC 3
+#define DCRF_CONST_KERNEL 0
+#define DCRF_DIAG_KERNEL 1
+#define DCRF_FULL_KERNEL 2
+
+/* label compatibility kinds (labelcompatibility.h:44-88) */
+#define DCRF_COMPAT_POTTS 0    /* compat = &w (1 float):     out = -w * Q          */
+#define DCRF_COMPAT_DIAGONAL 1 /* compat = v (M floats):      out = diag(v) Q       */
+#define DCRF_COMPAT_MATRIX 2   /* compat = m (M*M, row-major): out = 1/2(m+m^T) Q   */
+
+typedef struct dcrf_crf dcrf_crf;
+
+/* ABI version (DCRF_ABI_VERSION). No reference counterpart. */
+int dcrf_abi_version(void);
+
+/* Copies the last error message of the calling thread into buf (always
+ * NUL-terminated when len > 0); returns the last status code.  Replaces the
+ * exception text the Cython layer raises (densecrf.pyx:73,82,134,136). */
+int dcrf_last_error(char *buf, size_t len);
+
+/* DenseCRF(N, M): densecrf.pyx:51-63 -> densecrf.cpp:39-40.
+ * Binds the handle to the current CUDA device and creates its own stream. */
+int dcrf_create(int N, int M, dcrf_crf **out);
+
+/* DenseCRF2D(W, H, M): densecrf.pyx:107-118 -> densecrf.cpp:47-48. */
+int dcrf_create_2d(int W, int H, int M, dcrf_crf **out);
+
+/* Destructor: densecrf.pyx:65-69 -> densecrf.cpp:41-46. NULL is a no-op. */
+int dcrf_destroy(dcrf_crf *h);
+
+/* Orders the handle's work on a caller-provided cudaStream_t (NULL restores
+ * the handle's own stream).  No reference counterpart (the reference is
+ * synchronous CPU code). */
+int dcrf_set_stream(dcrf_crf *h, void *cuda_stream);
+
+/* Selects the lattice arithmetic (DCRF_VARIANT_*) for terms added after the
+ * call; see the file comment.  No reference counterpart (compile-time there). */
+int dcrf_set_variant(dcrf_crf *h, int variant);
+
+/* setUnaryEnergy(u): densecrf.pyx:80-89 -> densecrf.cpp:89-91
+ * (ConstUnaryEnergy, unary.cpp:42-46).  U is M x N in `layout`. */
+int dcrf_set_unary(dcrf_crf *h, const float *U, int layout, int where);
+
+/* addPairwiseEnergy(features, compat, kernel, normalization):
+ * densecrf.pyx:71-75 -> densecrf.cpp:54-57 -> pairwise.cpp:116-122,170-172.
+ * feat is (d, N) C-order.  Builds the lattice and the normalisation on the
+ * device.  The compat buffer is copied (the reference takes ownership of a heap
+ * object, densecrf.pyx:11-20).  *term_out (may be NULL) receives the term index. */
+int dcrf_add_pairwise(dcrf_crf *h, const float *feat, int d, int where, int compat_kind, const float *compat,
+                      int kernel_type, int normalization_type, int *term_out);
+
+/* DenseCRF2D.addPairwiseGaussian(sxy, compat, kernel, normalization):
+ * densecrf.pyx:120-124 -> densecrf.cpp:61-69; features (i/sx, j/sy) for pixel
+ * j*W+i are generated on the device. */
+int dcrf_add_pairwise_gaussian(dcrf_crf *h, float sx, float sy, int compat_kind, const float *compat,
+                               int kernel_type, int normalization_type, int *term_out);
+
+/* DenseCRF2D.addPairwiseBilateral(sxy, srgb, rgbim, compat, ...):
+ * densecrf.pyx:126-140 -> densecrf.cpp:70-81. rgb is H x W x 3 uint8, C-order. */
+int dcrf_add_pairwise_bilateral(dcrf_crf *h, float sx, float sy, float sr, float sg, float sb, const uint8_t *rgb,
+                                int where, int compat_kind, const float *compat, int kernel_type,
+                                int normalization_type, int *term_out);
+
+/* inference(n): densecrf.pyx:91-92 -> densecrf.cpp:115-131.  Writes the M x N
+ * marginals to Q in `layout`. */
+int dcrf_inference(dcrf_crf *h, int n_iterations, float *Q, int layout, int where);
+
+/* startInference(): densecrf.pyx:94-95 -> densecrf.cpp:178-186 (all zeros when
+ * no unary is set). */
+int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where);
+
+/* stepInference(Q, tmp1, tmp2): densecrf.pyx:97-98 -> densecrf.cpp:187-201.
+ * One mean-field update of Q, in place. */
+int dcrf_step_inference(dcrf_crf *h, float *Q, int layout, int where);
+
+/* klDivergence(Q): densecrf.pyx:100-101 -> densecrf.cpp:214-235.  Accumulated
+ * in double on the device (the reference sums the pairwise term in float). */
+int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, double *kl_out);
+
+/* map(n): densecrf.cpp:132-137 + currentMap 202-211 (declared but not wrapped
+ * by densecrf.pxd:61-62): argmax labels (first maximum) after n iterations. */
+int dcrf_map(dcrf_crf *h, int n_iterations, int16_t *labels, int where);
+
+/* Blocks until the handle's stream is idle. */
+int dcrf_synchronize(dcrf_crf *h);
+
+/* Removes every pairwise term (frees their lattices); the unary stays.  No
+ * reference counterpart (a reference user creates a new DenseCRF instead);
+ * lets one handle solve a sequence of images without reallocating. */
+int dcrf_clear_pairwise(dcrf_crf *h);
+
+/* ---- measurement -------------------------------------------------------- */
+
+/* Number of kernels this library has launched in the process so far. */
+int dcrf_launch_count(unsigned long long *count);
+
+/* Kernel classes timed by the profiling mode. */
+#define DCRF_KCLASS_POINT 0   /* slice + compatibility + softmax + tile splat */
+#define DCRF_KCLASS_REDUCE 1  /* per-vertex sum of the splat partials */
+#define DCRF_KCLASS_BLUR 2    /* one blur axis */
+#define DCRF_KCLASS_LATTICE 3 /* lattice build (all of its launches) */
+#define DCRF_KCLASS_OTHER 4   /* layout conversions, feature generation */
+#define DCRF_NUM_KCLASSES 5
+
+/* on = 1: bracket every kernel launch of the handle with CUDA events on its
+ * stream (adds a little overhead); 0: off.  Resets the accumulated profile. */
+int dcrf_set_profiling(dcrf_crf *h, int on);
+
+/* Accumulated device time (ms, from the events) and launch count of a kernel
+ * class since profiling was switched on.  Synchronises the handle's stream. */
+int dcrf_profile(dcrf_crf *h, int kernel_class, double *total_ms, long long *launches);
+
+/* Sizes of term `term`: lattice vertices L, splat partials P, tiles. */
+int dcrf_term_stats(dcrf_crf *h, int term, int *L, int *P, int *ntiles);
+
+/* ---- introspection (test and debugging aids) ---------------------------- */
+
+/* Number of points, labels and pairwise terms. */
+int dcrf_info(dcrf_crf *h, int *N, int *M, int *n_terms);
+
+/* Lattice dimension d and vertex count L of term `term`. */
+int dcrf_lattice_info(dcrf_crf *h, int term, int *d, int *L);
+
+/* Copies term `term`'s lattice tables to HOST buffers in the layout of the
+ * reference's Permutohedral members (permutohedral.h:49-53): offset, rank and
+ * bary as N x (d+1) (point-major), neighbors as (d+1) x L pairs (n1, n2) with
+ * -1 for a missing neighbour, keys as L x d int16.  Any pointer may be NULL. */
+int dcrf_lattice_dump(dcrf_crf *h, int term, int *offset, int *rank, float *bary, int *neighbors, int16_t *keys);
+
+/* The normalisation vector of term `term` (DenseKernel::norm_,
+ * pairwise.cpp:40-62) to a HOST buffer of N floats. */
+int dcrf_term_norm(dcrf_crf *h, int term, float *norm);
+
+/* Copies a working buffer of term `term` to a HOST buffer of `count` floats:
+ * which = 0 / 1: the two lattice-value buffers ((L+1) rows of the padded label
+ * count; row 0 is the zero sentinel); 2: the per-tile splat partials. */
+int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count);
+
+/* Lattice filter of term `term` alone (Permutohedral::compute,
+ * permutohedral.cpp:596-604): out = K in for value_size rows, both
+ * (value_size, N) label-major on the HOST; reverse = transposed (reverse-order
+ * blur).  value_size must equal 1 or the handle's M. */
+int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DCRF_GB300_H */

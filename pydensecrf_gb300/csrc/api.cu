@@ -1,0 +1,931 @@
+// api.cu -- the C ABI of include/dcrf.h: handles, device memory, and the
+// launch sequences of lattice build, normalisation and mean-field inference.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lattice.cuh"
+#include "meanfield.cuh"
+
+using namespace dcrf;
+
+namespace dcrf {
+static std::atomic<unsigned long long> g_launches{0};
+void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+}  // namespace dcrf
+
+namespace {
+
+thread_local std::string g_err;
+thread_local int g_code = DCRF_OK;
+
+int set_err(int code, const std::string &msg) {
+    g_err = msg;
+    g_code = code;
+    return code;
+}
+
+int ok() {
+    g_code = DCRF_OK;
+    return DCRF_OK;
+}
+
+#define CU(call)                                                                                  \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class T>
+int dev_alloc(T **p, size_t n) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n * sizeof(T), 16));
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(DCRF_ERR_OOM, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes failed");
+    }
+    *p = static_cast<T *>(q);
+    return DCRF_OK;
+}
+
+void dev_free(void *p) {
+    if (p) cudaFree(p);
+}
+
+// stream-ordered allocations of per-term buffers: rebuilding terms reuses the pool
+template <class T>
+int dev_alloc_async(T **p, size_t n, cudaStream_t s) {
+    void *q = nullptr;
+    cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(n * sizeof(T), 16), s);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return set_err(DCRF_ERR_OOM, "cudaMallocAsync of " + std::to_string(n * sizeof(T)) + " bytes failed");
+    }
+    *p = static_cast<T *>(q);
+    return DCRF_OK;
+}
+
+void dev_free_async(void *p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+}
+
+struct Term {
+    int d = 0, ktype = DCRF_DIAG_KERNEL, ntype = DCRF_NORMALIZE_SYMMETRIC, ckind = DCRF_COMPAT_POTTS;
+    int variant = DCRF_VARIANT_SSE;
+    float potts_w = 0.f;
+    LatticeDev lat;
+    float *feat = nullptr;  // [d][N] features as given (kernel parameters at identity)
+    float *norm = nullptr;  // [N]
+    float *V[2] = {nullptr, nullptr};
+    float *partial = nullptr;
+    float *compat = nullptr;  // device compat (Diagonal M / Matrix M*M symmetrised)
+    std::vector<float> compat_h;
+};
+
+}  // namespace
+
+struct dcrf_crf {
+    int N = 0, M = 0, MP = 0, W = 0, H = 0;
+    int variant = DCRF_VARIANT_SSE;
+    int device = 0;
+    cudaStream_t own = nullptr, stream = nullptr;
+    DevStatus *status = nullptr;
+    float *U = nullptr;
+    bool has_unary = false;
+    float *Q = nullptr;    // [M][N] device working marginals
+    float *tmp = nullptr;  // [N*M] layout conversions
+    int16_t *map = nullptr;
+    double *kl_part = nullptr;
+    int ntiles = 0;
+    int *slot_pt = nullptr;
+    int *tile_vbase = nullptr;
+    float hash_load = 2.0f;
+    std::vector<Term> terms;
+    // profiling: events bracketing launches, by kernel class
+    bool profiling = false;
+    struct Mark {
+        int cls;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks;
+    std::vector<cudaEvent_t> event_pool;
+};
+
+namespace {
+
+cudaEvent_t take_event(dcrf_crf *h) {
+    if (!h->event_pool.empty()) {
+        cudaEvent_t e = h->event_pool.back();
+        h->event_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Brackets one or more launches of class `cls` with events when profiling.
+struct ProfScope {
+    dcrf_crf *h;
+    int cls;
+    cudaEvent_t a = nullptr;
+    ProfScope(dcrf_crf *h_, int c) : h(h_), cls(c) {
+        if (h->profiling) {
+            a = take_event(h);
+            cudaEventRecord(a, h->stream);
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEvent_t b = take_event(h);
+            cudaEventRecord(b, h->stream);
+            h->marks.push_back({cls, a, b});
+        }
+    }
+};
+
+void release_marks(dcrf_crf *h) {
+    for (auto &m : h->marks) {
+        h->event_pool.push_back(m.a);
+        h->event_pool.push_back(m.b);
+    }
+    h->marks.clear();
+}
+
+int check_handle(dcrf_crf *h) {
+    if (!h) return set_err(DCRF_ERR_INVALID_ARG, "null handle");
+    cudaError_t e = cudaSetDevice(h->device);
+    if (e != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string("cudaSetDevice: ") + cudaGetErrorString(e));
+    return DCRF_OK;
+}
+
+// Tiles of the in-kernel splat.  A 2D grid uses 16x16 pixel blocks (the
+// corners of a block share far more lattice vertices than a raster strip of
+// the same size); a generic point set uses runs of 256 consecutive points.
+int build_tiles(dcrf_crf *h) {
+    std::vector<int> slot, vbase;
+    if (h->W > 0 && h->H > 0) {
+        int bx = (h->W + 15) / 16, by = (h->H + 15) / 16;
+        h->ntiles = bx * by;
+        slot.assign((size_t)h->ntiles * SPLAT_TILE, -1);
+        vbase.assign(h->ntiles + 1, 0);
+        for (int ty = 0; ty < by; ty++)
+            for (int tx = 0; tx < bx; tx++) {
+                int t = ty * bx + tx, cnt = 0;
+                for (int yy = 0; yy < 16; yy++)
+                    for (int xx = 0; xx < 16; xx++) {
+                        int y = ty * 16 + yy, x = tx * 16 + xx;
+                        if (y < h->H && x < h->W) {
+                            slot[(size_t)t * SPLAT_TILE + yy * 16 + xx] = y * h->W + x;
+                            cnt++;
+                        }
+                    }
+                vbase[t + 1] = vbase[t] + cnt;
+            }
+    } else {
+        h->ntiles = (h->N + SPLAT_TILE - 1) / SPLAT_TILE;
+        slot.assign((size_t)h->ntiles * SPLAT_TILE, -1);
+        vbase.assign(h->ntiles + 1, 0);
+        for (int s = 0; s < h->N; s++) slot[s] = s;
+        for (int t = 0; t < h->ntiles; t++) vbase[t + 1] = std::min(h->N, (t + 1) * SPLAT_TILE);
+    }
+    int rc;
+    if ((rc = dev_alloc(&h->slot_pt, slot.size() + 1))) return rc;
+    if ((rc = dev_alloc(&h->tile_vbase, vbase.size() + 1))) return rc;
+    if ((rc = dev_alloc(&h->kl_part, (size_t)h->ntiles + 1))) return rc;
+    CU(cudaMemcpy(h->slot_pt, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(h->tile_vbase, vbase.data(), vbase.size() * sizeof(int), cudaMemcpyHostToDevice));
+    return DCRF_OK;
+}
+
+int create(int N, int M, int W, int H, dcrf_crf **out) {
+    if (!out) return set_err(DCRF_ERR_INVALID_ARG, "null output pointer");
+    *out = nullptr;
+    if (N <= 0 || M <= 0) return set_err(DCRF_ERR_INVALID_ARG, "N and M must be positive");
+    if (M > DCRF_MAX_MP)
+        return set_err(DCRF_ERR_INVALID_ARG, "at most " + std::to_string(DCRF_MAX_MP) + " labels are supported, got " +
+                                                 std::to_string(M));
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return set_err(DCRF_ERR_NO_DEVICE, "no CUDA device available");
+    }
+    dcrf_crf *h = new dcrf_crf();
+    h->N = N;
+    h->M = M;
+    h->MP = pad_labels(M);
+    h->W = W;
+    h->H = H;
+    cudaGetDevice(&h->device);
+    int rc = DCRF_OK;
+    auto fail = [&](int code) {
+        dcrf_destroy(h);
+        return code;
+    };
+    if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess)
+        return fail(set_err(DCRF_ERR_CUDA, "cudaStreamCreate failed"));
+    h->stream = h->own;
+    if ((rc = dev_alloc(&h->status, 1))) return fail(rc);
+    if ((rc = dev_alloc(&h->U, (size_t)N * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->Q, (size_t)N * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->tmp, (size_t)N * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->map, (size_t)N))) return fail(rc);
+    if ((rc = build_tiles(h))) return fail(rc);
+    *out = h;
+    return ok();
+}
+
+// Copies an M x N quantity from the caller into the device's label-major dst.
+int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst) {
+    size_t bytes = sizeof(float) * (size_t)h->N * h->M;
+    cudaMemcpyKind kind = where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (layout == DCRF_LAYOUT_LM) {
+        CU(cudaMemcpyAsync(dst, src, bytes, kind, h->stream));
+    } else if (layout == DCRF_LAYOUT_PM) {
+        CU(cudaMemcpyAsync(h->tmp, src, bytes, kind, h->stream));
+        ProfScope ps(h, DCRF_KCLASS_OTHER);
+        CU(launch_transpose(h->tmp, dst, h->N, h->M, h->stream));
+    } else {
+        return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
+    }
+    return DCRF_OK;
+}
+
+int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where) {
+    size_t bytes = sizeof(float) * (size_t)h->N * h->M;
+    cudaMemcpyKind kind = where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (layout == DCRF_LAYOUT_LM) {
+        CU(cudaMemcpyAsync(dst, src, bytes, kind, h->stream));
+    } else if (layout == DCRF_LAYOUT_PM) {
+        ProfScope ps(h, DCRF_KCLASS_OTHER);
+        CU(launch_transpose(src, h->tmp, h->M, h->N, h->stream));
+        CU(cudaMemcpyAsync(dst, h->tmp, bytes, kind, h->stream));
+    } else {
+        return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
+    }
+    return DCRF_OK;
+}
+
+// Descriptor of term k for the forward filter (or its transpose).
+TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
+    TermDev t{};
+    t.d = T.d;
+    t.L = T.lat.L;
+    t.ckind = T.ckind;
+    bool sym = T.ntype == DCRF_NORMALIZE_SYMMETRIC;
+    bool before = T.ntype == DCRF_NORMALIZE_BEFORE, after = T.ntype == DCRF_NORMALIZE_AFTER;
+    t.pre_norm = sym || (before && !transpose) || (after && transpose);   // pairwise.cpp:65
+    t.post_norm = sym || (before && transpose) || (after && !transpose);  // pairwise.cpp:78
+    int vs = value1 ? 1 : h->M;
+    t.seq = (vs <= 2 || T.variant == DCRF_VARIANT_SCALAR) ? 1 : 0;  // permutohedral.cpp:600-603
+    t.potts_w = T.potts_w;
+    t.alpha = T.lat.alpha;
+    t.off = T.lat.off;
+    t.bary = T.lat.bary;
+    t.wslice = T.lat.wslice;
+    t.norm = T.norm;
+    t.compat = T.compat;
+    t.V = T.V[(T.d + 1) & 1];
+    t.partial = T.partial;
+    t.part_mbeg = T.lat.part_mbeg;
+    t.tile_pbeg = T.lat.tile_pbeg;
+    t.mem_pt = T.lat.mem_pt;
+    t.mem_w = T.lat.mem_w;
+    return t;
+}
+
+cudaError_t pp(dcrf_crf *h, const PPArgs &a, int MP) {
+    ProfScope ps(h, DCRF_KCLASS_POINT);
+    return launch_pointpass(a, MP, h->stream);
+}
+
+PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transpose, bool value1) {
+    PPArgs a{};
+    a.N = h->N;
+    a.M = value1 ? 1 : h->M;
+    a.mode = mode;
+    a.ntiles = h->ntiles;
+    a.slot_pt = h->slot_pt;
+    a.U = h->has_unary ? h->U : nullptr;
+    a.Qin = h->Q;
+    a.Qout = h->Q;
+    a.map_out = h->map;
+    a.kl_part = h->kl_part;
+    a.ts.n = (int)which.size();
+    for (size_t k = 0; k < which.size(); k++) {
+        a.ts.t[k] = term_dev(h, h->terms[which[k]], transpose, value1);
+        a.ntype[k] = h->terms[which[k]].ntype;
+        a.norm_out[k] = h->terms[which[k]].norm;
+    }
+    return a;
+}
+
+std::vector<int> all_terms(dcrf_crf *h) {
+    std::vector<int> w(h->terms.size());
+    for (size_t k = 0; k < w.size(); k++) w[k] = (int)k;
+    return w;
+}
+
+// reduce + d+1 blur passes for the listed terms (after a splat point pass)
+int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, bool value1) {
+    int MP = value1 ? 1 : h->MP;
+    bool seq = value1 || h->M <= 2;
+    ReduceArgs ra{};
+    ra.n = (int)which.size();
+    ra.begin[0] = 0;
+    int maxd = 0;
+    for (size_t k = 0; k < which.size(); k++) {
+        Term &T = h->terms[which[k]];
+        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.partial, T.V[0], T.lat.L};
+        ra.begin[k + 1] = ra.begin[k] + T.lat.L;
+        maxd = std::max(maxd, T.d);
+        if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
+    }
+    if (which.empty()) return DCRF_OK;
+    {
+        ProfScope ps(h, DCRF_KCLASS_REDUCE);
+        CU(launch_reduce(ra, MP, h->stream));
+    }
+    const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
+    for (int pass = 0; pass <= maxd; pass++) {
+        BlurArgs ba{};
+        ba.n = 0;
+        ba.begin[0] = 0;
+        for (size_t k = 0; k < which.size(); k++) {
+            Term &T = h->terms[which[k]];
+            if (pass > T.d) continue;
+            BlurArgs::T &bt = ba.t[ba.n];
+            bt.Vin = T.V[pass & 1];
+            bt.Vout = T.V[(pass + 1) & 1];
+            bt.nbr = T.lat.nbr;
+            bt.L = T.lat.L;
+            bt.axis = transpose ? T.d - pass : pass;  // reverse blur order for the transpose (permutohedral.cpp:556)
+            ba.begin[ba.n + 1] = ba.begin[ba.n] + (long long)T.lat.L * NV;
+            ba.n++;
+        }
+        // All listed terms share the arithmetic flavour: the scalar build and
+        // value size <= 2 use the double-precision blur.
+        ProfScope ps(h, DCRF_KCLASS_BLUR);
+        CU(launch_blur(ba, MP, seq, h->stream));
+    }
+    return DCRF_OK;
+}
+
+// The value-size-1 passes (normalisation, 1-row filters) use the lattice-value
+// buffers at stride 1, which overwrites entries that the stride-MP passes read
+// as the zero sentinel row (row 0).  Restore it afterwards.
+int zero_sentinels(dcrf_crf *h, Term &T) {
+    CU(cudaMemsetAsync(T.V[0], 0, sizeof(float) * h->MP, h->stream));
+    CU(cudaMemsetAsync(T.V[1], 0, sizeof(float) * h->MP, h->stream));
+    return DCRF_OK;
+}
+
+int sync_check(dcrf_crf *h) {
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(e));
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string("launch error: ") + cudaGetErrorString(e));
+    return DCRF_OK;
+}
+
+int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, const float *compat, int ktype,
+             int ntype, int *term_out) {
+    // feat_dev_owned: [d][N] device buffer, ownership passes to the term
+    Term T;
+    T.d = d;
+    T.ktype = ktype;
+    T.ntype = ntype;
+    T.ckind = compat_kind;
+    T.variant = h->variant;
+    T.feat = const_cast<float *>(feat_dev_owned);
+    int M = h->M, rc;
+    auto fail = [&](int code) {
+        dev_free_async(T.feat, h->stream);
+        dev_free_async(T.norm, h->stream);
+        dev_free_async(T.V[0], h->stream);
+        dev_free_async(T.V[1], h->stream);
+        dev_free_async(T.partial, h->stream);
+        dev_free_async(T.compat, h->stream);
+        lattice_free(&T.lat, h->stream);
+        return code;
+    };
+    if (compat_kind == DCRF_COMPAT_POTTS) {
+        T.potts_w = compat[0];
+    } else if (compat_kind == DCRF_COMPAT_DIAGONAL) {
+        T.compat_h.assign(compat, compat + M);
+    } else if (compat_kind == DCRF_COMPAT_MATRIX) {
+        T.compat_h.resize((size_t)M * M);
+        for (int a = 0; a < M; a++)  // MatrixCompatibility symmetrises: 0.5*(m + m^T) (labelcompatibility.cpp:79)
+            for (int b = 0; b < M; b++) {
+                float s = compat[a * M + b] + compat[b * M + a];
+                T.compat_h[(size_t)a * M + b] = 0.5f * s;
+            }
+    } else {
+        return fail(set_err(DCRF_ERR_INVALID_ARG, "unknown compatibility kind"));
+    }
+    if (!T.compat_h.empty()) {
+        if ((rc = dev_alloc_async(&T.compat, T.compat_h.size(), h->stream))) return fail(rc);
+        CU(cudaMemcpyAsync(T.compat, T.compat_h.data(), T.compat_h.size() * sizeof(float), cudaMemcpyHostToDevice,
+                           h->stream));
+    }
+    Segments seg;
+    seg.start = {0, h->N};
+    TileMapDev tm;
+    tm.ntiles = h->ntiles;
+    tm.slot_pt = h->slot_pt;
+    tm.tile_vbase = h->tile_vbase;
+    float load = h->hash_load;
+    for (int attempt = 0;; attempt++) {
+        ProfScope ps(h, DCRF_KCLASS_LATTICE);
+        rc = lattice_build(T.feat, d, h->N, seg, tm, h->variant, load, h->stream, h->status, &T.lat);
+        if (rc == DCRF_ERR_HASH_FULL && attempt < 3) {
+            load *= 4.f;
+            continue;
+        }
+        break;
+    }
+    if (rc) return fail(set_err(rc, lattice_last_message()));
+    size_t vrows = (size_t)T.lat.L + 1;
+    if ((rc = dev_alloc_async(&T.V[0], vrows * h->MP, h->stream))) return fail(rc);
+    if ((rc = dev_alloc_async(&T.V[1], vrows * h->MP, h->stream))) return fail(rc);
+    if ((rc = dev_alloc_async(&T.partial, (size_t)std::max(T.lat.P, 1) * h->MP, h->stream))) return fail(rc);
+    if ((rc = dev_alloc_async(&T.norm, (size_t)h->N, h->stream))) return fail(rc);
+    // the zero sentinel rows (row 0) are never written afterwards
+    CU(cudaMemsetAsync(T.V[0], 0, vrows * h->MP * sizeof(float), h->stream));
+    CU(cudaMemsetAsync(T.V[1], 0, vrows * h->MP * sizeof(float), h->stream));
+    h->terms.push_back(T);
+    int k = (int)h->terms.size() - 1;
+    // normalisation: K * 1 through the value-size-1 path (pairwise.cpp:44)
+    std::vector<int> one{k};
+    PPArgs a = pp_args(h, PP_ONES | PP_SPLAT, one, false, true);
+    a.ts.t[0].pre_norm = 0;
+    a.ts.t[0].post_norm = 0;
+    cudaError_t ce = pp(h, a, 1);
+    if (ce != cudaSuccess) {
+        h->terms.pop_back();
+        return fail(set_err(DCRF_ERR_CUDA, std::string("norm splat: ") + cudaGetErrorString(ce)));
+    }
+    if ((rc = filter_phase(h, one, false, true))) {
+        h->terms.pop_back();
+        return fail(rc);
+    }
+    a = pp_args(h, PP_NORM, one, false, true);
+    ce = pp(h, a, 1);
+    if (ce != cudaSuccess) {
+        h->terms.pop_back();
+        return fail(set_err(DCRF_ERR_CUDA, std::string("norm slice: ") + cudaGetErrorString(ce)));
+    }
+    if ((rc = zero_sentinels(h, h->terms.back()))) {
+        h->terms.pop_back();
+        return fail(rc);
+    }
+    if ((rc = sync_check(h))) {
+        h->terms.pop_back();
+        return fail(rc);
+    }
+    if (term_out) *term_out = k;
+    return ok();
+}
+
+int validate_compat(int kind, const float *compat) {
+    if (kind < DCRF_COMPAT_POTTS || kind > DCRF_COMPAT_MATRIX)
+        return set_err(DCRF_ERR_INVALID_ARG, "unknown compatibility kind");
+    if (!compat) return set_err(DCRF_ERR_INVALID_ARG, "null compatibility");
+    return DCRF_OK;
+}
+
+int validate_kn(int ktype, int ntype) {
+    if (ktype < DCRF_CONST_KERNEL || ktype > DCRF_FULL_KERNEL) return set_err(DCRF_ERR_INVALID_ARG, "unknown kernel type");
+    if (ntype < DCRF_NO_NORMALIZATION || ntype > DCRF_NORMALIZE_SYMMETRIC)
+        return set_err(DCRF_ERR_INVALID_ARG, "unknown normalization type");
+    return DCRF_OK;
+}
+
+// T mean-field iterations starting from softmax(-U); final Q in h->Q.
+int run_inference(dcrf_crf *h, int T, int final_mode) {
+    std::vector<int> w = all_terms(h);
+    int rc;
+    if (T <= 0 || w.empty()) {
+        CU(pp(h, pp_args(h, final_mode, w, false, false), h->MP));
+        return DCRF_OK;
+    }
+    CU(pp(h, pp_args(h, PP_SPLAT, w, false, false), h->MP));
+    for (int it = 1; it <= T; it++) {
+        if ((rc = filter_phase(h, w, false, false))) return rc;
+        int mode = PP_MSG | (it < T ? PP_SPLAT : final_mode);
+        CU(pp(h, pp_args(h, mode, w, false, false), h->MP));
+    }
+    return DCRF_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dcrf_abi_version(void) { return DCRF_ABI_VERSION; }
+
+int dcrf_last_error(char *buf, size_t len) {
+    if (buf && len) {
+        size_t n = std::min(len - 1, g_err.size());
+        std::memcpy(buf, g_err.data(), n);
+        buf[n] = 0;
+    }
+    return g_code;
+}
+
+int dcrf_create(int N, int M, dcrf_crf **out) { return create(N, M, 0, 0, out); }
+
+int dcrf_create_2d(int W, int H, int M, dcrf_crf **out) {
+    if (W <= 0 || H <= 0) return set_err(DCRF_ERR_INVALID_ARG, "W and H must be positive");
+    if ((long long)W * H > 0x7FFFFFFF) return set_err(DCRF_ERR_INVALID_ARG, "image too large");
+    return create(W * H, M, W, H, out);
+}
+
+int dcrf_destroy(dcrf_crf *h) {
+    if (!h) return ok();
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    release_marks(h);
+    for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
+    h->event_pool.clear();
+    for (Term &T : h->terms) {
+        dev_free_async(T.feat, h->stream);
+        dev_free_async(T.norm, h->stream);
+        dev_free_async(T.V[0], h->stream);
+        dev_free_async(T.V[1], h->stream);
+        dev_free_async(T.partial, h->stream);
+        dev_free_async(T.compat, h->stream);
+        lattice_free(&T.lat, h->stream ? h->stream : h->own);
+    }
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    dev_free(h->status);
+    dev_free(h->U);
+    dev_free(h->Q);
+    dev_free(h->tmp);
+    dev_free(h->map);
+    dev_free(h->kl_part);
+    dev_free(h->slot_pt);
+    dev_free(h->tile_vbase);
+    if (h->own) cudaStreamDestroy(h->own);
+    delete h;
+    return ok();
+}
+
+int dcrf_set_stream(dcrf_crf *h, void *s) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(h->stream));
+    h->stream = s ? (cudaStream_t)s : h->own;
+    return ok();
+}
+
+int dcrf_set_variant(dcrf_crf *h, int variant) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (variant != DCRF_VARIANT_SSE && variant != DCRF_VARIANT_SCALAR)
+        return set_err(DCRF_ERR_INVALID_ARG, "unknown variant");
+    for (const Term &T : h->terms)
+        if (T.variant != variant)
+            return set_err(DCRF_ERR_STATE, "the lattice variant must be chosen before adding pairwise terms");
+    h->variant = variant;
+    return ok();
+}
+
+int dcrf_set_unary(dcrf_crf *h, const float *U, int layout, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!U) return set_err(DCRF_ERR_INVALID_ARG, "null unary");
+    if ((rc = load_mn(h, U, layout, where, h->U))) return rc;
+    h->has_unary = true;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_add_pairwise(dcrf_crf *h, const float *feat, int d, int where, int compat_kind, const float *compat,
+                      int kernel_type, int normalization_type, int *term_out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!feat) return set_err(DCRF_ERR_INVALID_ARG, "null features");
+    if (d < 1 || d > DCRF_MAX_D) return set_err(DCRF_ERR_INVALID_ARG, "feature dimension must be in [1, 16]");
+    if ((rc = validate_compat(compat_kind, compat)) || (rc = validate_kn(kernel_type, normalization_type))) return rc;
+    if ((int)h->terms.size() >= DCRF_MAX_TERMS) return set_err(DCRF_ERR_INVALID_ARG, "too many pairwise terms");
+    float *f = nullptr;
+    if ((rc = dev_alloc_async(&f, (size_t)d * h->N, h->stream))) return rc;
+    cudaError_t e = cudaMemcpyAsync(f, feat, sizeof(float) * (size_t)d * h->N,
+                                    where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                    h->stream);
+    if (e != cudaSuccess) {
+        dev_free_async(f, h->stream);
+        return set_err(DCRF_ERR_CUDA, std::string("feature copy: ") + cudaGetErrorString(e));
+    }
+    return add_term(h, f, d, compat_kind, compat, kernel_type, normalization_type, term_out);
+}
+
+int dcrf_add_pairwise_gaussian(dcrf_crf *h, float sx, float sy, int compat_kind, const float *compat,
+                               int kernel_type, int normalization_type, int *term_out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (h->W <= 0) return set_err(DCRF_ERR_STATE, "addPairwiseGaussian needs a DenseCRF2D handle");
+    if ((rc = validate_compat(compat_kind, compat)) || (rc = validate_kn(kernel_type, normalization_type))) return rc;
+    if ((int)h->terms.size() >= DCRF_MAX_TERMS) return set_err(DCRF_ERR_INVALID_ARG, "too many pairwise terms");
+    float *f = nullptr;
+    if ((rc = dev_alloc_async(&f, (size_t)2 * h->N, h->stream))) return rc;
+    cudaError_t e = launch_features_2d(h->W, h->H, sx, sy, nullptr, 1.f, 1.f, 1.f, f, h->stream);
+    if (e != cudaSuccess) {
+        dev_free_async(f, h->stream);
+        return set_err(DCRF_ERR_CUDA, std::string("features: ") + cudaGetErrorString(e));
+    }
+    return add_term(h, f, 2, compat_kind, compat, kernel_type, normalization_type, term_out);
+}
+
+int dcrf_add_pairwise_bilateral(dcrf_crf *h, float sx, float sy, float sr, float sg, float sb, const uint8_t *rgb,
+                                int where, int compat_kind, const float *compat, int kernel_type,
+                                int normalization_type, int *term_out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (h->W <= 0) return set_err(DCRF_ERR_STATE, "addPairwiseBilateral needs a DenseCRF2D handle");
+    if (!rgb) return set_err(DCRF_ERR_INVALID_ARG, "null image");
+    if ((rc = validate_compat(compat_kind, compat)) || (rc = validate_kn(kernel_type, normalization_type))) return rc;
+    if ((int)h->terms.size() >= DCRF_MAX_TERMS) return set_err(DCRF_ERR_INVALID_ARG, "too many pairwise terms");
+    float *f = nullptr;
+    uint8_t *img = nullptr;
+    if ((rc = dev_alloc_async(&f, (size_t)5 * h->N, h->stream))) return rc;
+    const uint8_t *src = rgb;
+    if (where != DCRF_DEVICE) {
+        if ((rc = dev_alloc_async(&img, (size_t)3 * h->N, h->stream))) {
+            dev_free_async(f, h->stream);
+            return rc;
+        }
+        cudaError_t e = cudaMemcpyAsync(img, rgb, (size_t)3 * h->N, cudaMemcpyHostToDevice, h->stream);
+        if (e != cudaSuccess) {
+            dev_free_async(f, h->stream);
+            dev_free_async(img, h->stream);
+            return set_err(DCRF_ERR_CUDA, std::string("image copy: ") + cudaGetErrorString(e));
+        }
+        src = img;
+    }
+    cudaError_t e = launch_features_2d(h->W, h->H, sx, sy, src, sr, sg, sb, f, h->stream);
+    if (e != cudaSuccess) {
+        dev_free_async(f, h->stream);
+        dev_free_async(img, h->stream);
+        return set_err(DCRF_ERR_CUDA, std::string("features: ") + cudaGetErrorString(e));
+    }
+    rc = add_term(h, f, 5, compat_kind, compat, kernel_type, normalization_type, term_out);
+    dev_free_async(img, h->stream);
+    return rc;
+}
+
+int dcrf_inference(dcrf_crf *h, int n_iterations, float *Q, int layout, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
+    if ((rc = run_inference(h, n_iterations, PP_WRITE_Q))) return rc;
+    if ((rc = store_mn(h, h->Q, Q, layout, where))) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
+    if (!h->has_unary) {  // densecrf.cpp:179-184: zeros without a unary
+        CU(cudaMemsetAsync(h->Q, 0, sizeof(float) * (size_t)h->N * h->M, h->stream));
+    } else {
+        CU(pp(h, pp_args(h, PP_WRITE_Q, {}, false, false), h->MP));
+    }
+    if ((rc = store_mn(h, h->Q, Q, layout, where))) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_step_inference(dcrf_crf *h, float *Q, int layout, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null marginals");
+    if ((rc = load_mn(h, Q, layout, where, h->Q))) return rc;
+    std::vector<int> w = all_terms(h);
+    if (!w.empty()) {
+        CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
+        if ((rc = filter_phase(h, w, false, false))) return rc;
+    }
+    CU(pp(h, pp_args(h, PP_MSG | PP_WRITE_Q, w, false, false), h->MP));
+    if ((rc = store_mn(h, h->Q, Q, layout, where))) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, double *kl_out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!Q || !kl_out) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
+    if ((rc = load_mn(h, Q, layout, where, h->Q))) return rc;
+    std::vector<int> w = all_terms(h);
+    if (!w.empty()) {
+        CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
+        if ((rc = filter_phase(h, w, false, false))) return rc;
+    }
+    CU(pp(h, pp_args(h, PP_LOAD_Q | PP_MSG | PP_KL, w, false, false), h->MP));
+    std::vector<double> part(h->ntiles);
+    CU(cudaMemcpyAsync(part.data(), h->kl_part, sizeof(double) * h->ntiles, cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = sync_check(h))) return rc;
+    double s = 0.0;
+    for (double v : part) s += v;
+    *kl_out = s;
+    return ok();
+}
+
+int dcrf_map(dcrf_crf *h, int n_iterations, int16_t *labels, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!labels) return set_err(DCRF_ERR_INVALID_ARG, "null output");
+    if ((rc = run_inference(h, n_iterations, PP_MAP))) return rc;
+    CU(cudaMemcpyAsync(labels, h->map, sizeof(int16_t) * h->N,
+                       where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_synchronize(dcrf_crf *h) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_info(dcrf_crf *h, int *N, int *M, int *n_terms) {
+    if (!h) return set_err(DCRF_ERR_INVALID_ARG, "null handle");
+    if (N) *N = h->N;
+    if (M) *M = h->M;
+    if (n_terms) *n_terms = (int)h->terms.size();
+    return ok();
+}
+
+int dcrf_lattice_info(dcrf_crf *h, int term, int *d, int *L) {
+    if (!h) return set_err(DCRF_ERR_INVALID_ARG, "null handle");
+    if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    if (d) *d = h->terms[term].d;
+    if (L) *L = h->terms[term].lat.L;
+    return ok();
+}
+
+int dcrf_lattice_dump(dcrf_crf *h, int term, int *offset, int *rank, float *bary, int *neighbors, int16_t *keys) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    Term &T = h->terms[term];
+    const int N = h->N, d1 = T.d + 1, L = T.lat.L;
+    CU(cudaStreamSynchronize(h->stream));
+    if (offset) {
+        std::vector<int> o((size_t)d1 * N);
+        CU(cudaMemcpy(o.data(), T.lat.off, o.size() * sizeof(int), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < N; i++)
+            for (int r = 0; r < d1; r++) offset[(size_t)i * d1 + r] = o[(size_t)r * N + i];
+    }
+    if (rank) {
+        std::vector<uint8_t> o((size_t)d1 * N);
+        CU(cudaMemcpy(o.data(), T.lat.rank, o.size(), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < N; i++)
+            for (int r = 0; r < d1; r++) rank[(size_t)i * d1 + r] = o[(size_t)r * N + i];
+    }
+    if (bary) {
+        std::vector<float> o((size_t)d1 * N);
+        CU(cudaMemcpy(o.data(), T.lat.bary, o.size() * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < N; i++)
+            for (int r = 0; r < d1; r++) bary[(size_t)i * d1 + r] = o[(size_t)r * N + i];
+    }
+    if (neighbors) {
+        std::vector<int2> o((size_t)d1 * L);
+        CU(cudaMemcpy(o.data(), T.lat.nbr, o.size() * sizeof(int2), cudaMemcpyDeviceToHost));
+        for (size_t x = 0; x < o.size(); x++) {
+            neighbors[2 * x] = o[x].x - 1;
+            neighbors[2 * x + 1] = o[x].y - 1;
+        }
+    }
+    if (keys) {
+        std::vector<uint16_t> o((size_t)d1 * L);
+        CU(cudaMemcpy(o.data(), T.lat.vkeys, o.size() * sizeof(uint16_t), cudaMemcpyDeviceToHost));
+        for (int v = 0; v < L; v++)
+            for (int q = 0; q < T.d; q++) keys[(size_t)v * T.d + q] = (int16_t)o[(size_t)v * d1 + q + 1];
+    }
+    return ok();
+}
+
+int dcrf_term_norm(dcrf_crf *h, int term, float *norm) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size() || !norm) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
+    Term &T = h->terms[term];
+    CU(cudaStreamSynchronize(h->stream));
+    CU(cudaMemcpy(norm, T.norm, sizeof(float) * h->N, cudaMemcpyDeviceToHost));
+    if (T.ntype == DCRF_NO_NORMALIZATION) {  // pairwise.cpp:46-53: every entry = N / sum(K*1), float sum
+        float mean = 0.f;
+        for (int i = 0; i < h->N; i++) mean += norm[i];
+        mean = (float)h->N / mean;
+        for (int i = 0; i < h->N; i++) norm[i] = mean;
+    }
+    return ok();
+}
+
+int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
+    if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
+    bool v1 = value_size == 1;
+    int MP = v1 ? 1 : h->MP;
+    size_t bytes = sizeof(float) * (size_t)value_size * h->N;
+    CU(cudaMemcpyAsync(h->tmp, in, bytes, cudaMemcpyHostToDevice, h->stream));
+    std::vector<int> one{term};
+    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
+    a.ts.t[0].pre_norm = 0;
+    a.Qin = h->tmp;
+    CU(pp(h, a, MP));
+    if ((rc = filter_phase(h, one, reverse != 0, v1))) return rc;
+    a = pp_args(h, PP_FILTER, one, reverse != 0, v1);
+    a.Qout = h->tmp;
+    CU(pp(h, a, MP));
+    if (v1 && (rc = zero_sentinels(h, h->terms[term]))) return rc;
+    CU(cudaMemcpyAsync(out, h->tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_clear_pairwise(dcrf_crf *h) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    for (Term &T : h->terms) {
+        dev_free_async(T.feat, h->stream);
+        dev_free_async(T.norm, h->stream);
+        dev_free_async(T.V[0], h->stream);
+        dev_free_async(T.V[1], h->stream);
+        dev_free_async(T.partial, h->stream);
+        dev_free_async(T.compat, h->stream);
+        lattice_free(&T.lat, h->stream);
+    }
+    h->terms.clear();
+    return ok();
+}
+
+int dcrf_launch_count(unsigned long long *count) {
+    if (!count) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
+    *count = g_launches.load();
+    return ok();
+}
+
+int dcrf_set_profiling(dcrf_crf *h, int on) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(h->stream));
+    release_marks(h);
+    h->profiling = on != 0;
+    return ok();
+}
+
+int dcrf_profile(dcrf_crf *h, int kernel_class, double *total_ms, long long *launches) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (kernel_class < 0 || kernel_class >= DCRF_NUM_KCLASSES) return set_err(DCRF_ERR_INVALID_ARG, "bad class");
+    CU(cudaStreamSynchronize(h->stream));
+    double ms = 0.0;
+    long long n = 0;
+    for (auto &m : h->marks)
+        if (m.cls == kernel_class) {
+            float t = 0.f;
+            CU(cudaEventElapsedTime(&t, m.a, m.b));
+            ms += t;
+            n++;
+        }
+    if (total_ms) *total_ms = ms;
+    if (launches) *launches = n;
+    return ok();
+}
+
+int dcrf_term_stats(dcrf_crf *h, int term, int *L, int *P, int *ntiles) {
+    if (!h) return set_err(DCRF_ERR_INVALID_ARG, "null handle");
+    if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    if (L) *L = h->terms[term].lat.L;
+    if (P) *P = h->terms[term].lat.P;
+    if (ntiles) *ntiles = h->terms[term].lat.ntiles;
+    return ok();
+}
+
+int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size() || !out || which < 0 || which > 2)
+        return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
+    Term &T = h->terms[term];
+    size_t avail = which < 2 ? ((size_t)T.lat.L + 1) * h->MP : (size_t)std::max(T.lat.P, 1) * h->MP;
+    if (count > avail) return set_err(DCRF_ERR_INVALID_ARG, "count exceeds the buffer");
+    const float *src = which == 0 ? T.V[0] : which == 1 ? T.V[1] : T.partial;
+    CU(cudaStreamSynchronize(h->stream));
+    CU(cudaMemcpy(out, src, count * sizeof(float), cudaMemcpyDeviceToHost));
+    return ok();
+}
+
+}  // extern "C"

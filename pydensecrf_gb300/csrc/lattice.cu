@@ -1,0 +1,693 @@
+// lattice.cu -- GPU build of the permutohedral lattice (the device form of
+// Permutohedral::init, pydensecrf/densecrf/src/permutohedral.cpp:140-474).
+//
+// Pipeline (one launch each, all on the caller's stream):
+//   1. embed      thread per point: elevate, round to the 0-coloured simplex,
+//                 rank, wrap, barycentric weights and the d+1 corner keys
+//                 (P:191-275 on x86, P:359-435 scalar).  Keys are packed
+//                 16-bit fields (image id, d coordinates) in 64-bit words.
+//   2. insert     thread per corner: open-addressing hash on the packed key;
+//                 each slot keeps the SMALLEST corner index holding its key
+//                 (CAS then atomicMin), i.e. the key's first occurrence.
+//   3. compact    flag first occurrences, exclusive scan -> vertex id.  The
+//                 reference numbers vertices in hash-insertion order, which
+//                 is first-occurrence order, so the ids match the
+//                 reference's exactly -- no relabelling is needed.
+//   4. offsets    corner -> vertex id (offset_), vertex -> key.
+//   5. neighbours thread per (axis, vertex): look up key -1/+1 with +d/-d on
+//                 the axis.
+//   6. tiles      per tile of SPLAT_TILE consecutive points, the corners
+//                 grouped by vertex in point order (block bitonic sort): the
+//                 member lists of the in-kernel splat.
+//   7. reduce     stable radix sort of the tiles' partials by vertex: the
+//                 order in which a vertex's partial sums are added.
+// Bounded probing everywhere: a full table sets DCRF_ERR_HASH_FULL and the
+// host retries with a larger table; no kernel waits on another thread.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "lattice.cuh"
+#include "primitives.cuh"
+
+namespace dcrf {
+
+static thread_local std::string g_msg;
+const char *lattice_last_message() { return g_msg.c_str(); }
+
+constexpr uint32_t EMPTY = 0xFFFFFFFFu;
+
+template <int D>
+struct KeyW {
+    static constexpr int KW = (D + 4) / 4;  // ceil((D+1)/4) 64-bit words of 16-bit fields
+};
+
+__device__ __forceinline__ uint64_t mix64(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return x;
+}
+
+template <int KW>
+__device__ __forceinline__ uint32_t key_hash(const uint64_t *k) {
+    uint64_t h = 0x9E3779B97F4A7C15ULL;
+#pragma unroll
+    for (int w = 0; w < KW; w++) h = mix64(h ^ k[w]) + 0x632BE59BD9B4E019ULL * (w + 1);
+    return (uint32_t)(h ^ (h >> 32));
+}
+
+struct EmbedArgs {
+    const float *feat;  // [d][N]
+    int N;
+    int n_ph;
+    const int *ph_img;     // [n_ph] image of each padding point
+    const int *seg_start;  // [nseg+1]
+    int nseg;
+    float sf[DCRF_MAX_D];
+    float invdp1, dp1, alpha;
+    int variant;
+    float *bary;
+    float *wslice;
+    uint8_t *rank;
+    uint64_t *keys;  // [(N+n_ph)*(d+1)][KW]
+    DevStatus *st;
+};
+
+template <int D>
+__global__ void __launch_bounds__(128) embed_kernel(EmbedArgs a) {
+    constexpr int KW = KeyW<D>::KW;
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= a.N + a.n_ph) return;
+    int img;
+    float f[D];
+    if (p < a.N) {
+        int lo = 0, hi = a.nseg - 1;
+        while (lo < hi) {
+            int mid = (lo + hi + 1) >> 1;
+            if (a.seg_start[mid] <= p)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        img = lo;
+#pragma unroll
+        for (int j = 0; j < D; j++) f[j] = a.feat[(size_t)j * a.N + p];
+    } else {
+        img = a.ph_img[p - a.N];
+#pragma unroll
+        for (int j = 0; j < D; j++) f[j] = 0.f;
+    }
+    // Elevate (P:201-207 / P:364-370)
+    float el[D + 1], rem0[D + 1];
+    int rank[D + 1];
+    float sm = 0.f;
+#pragma unroll
+    for (int j = D; j > 0; j--) {
+        float cf = fmul(f[j - 1], a.sf[j - 1]);
+        el[j] = fsub(sm, fmul((float)j, cf));
+        sm = fadd(sm, cf);
+    }
+    el[0] = sm;
+#pragma unroll
+    for (int i = 0; i <= D; i++) rank[i] = 0;
+    if (a.variant == DCRF_VARIANT_SSE) {
+        // round-to-nearest-even of el/(d+1), float rank arithmetic
+        float sum = 0.f;
+#pragma unroll
+        for (int i = 0; i <= D; i++) {
+            float v = rintf(fmul(a.invdp1, el[i]));
+            rem0[i] = fmul(v, a.dp1);
+            sum = fadd(sum, v);
+        }
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            float di = fsub(el[i], rem0[i]);
+#pragma unroll
+            for (int j = i + 1; j <= D; j++) {
+                float dj = fsub(el[j], rem0[j]);
+                if (di < dj)
+                    rank[i]++;
+                else
+                    rank[j]++;
+            }
+        }
+        int isum = (int)sum;
+#pragma unroll
+        for (int i = 0; i <= D; i++) {
+            rank[i] += isum;
+            float add = rank[i] < 0 ? a.dp1 : 0.f;
+            float sub = rank[i] >= D + 1 ? a.dp1 : 0.f;
+            float adj = fsub(add, sub);
+            rank[i] += (int)adj;
+            rem0[i] = fadd(rem0[i], adj);
+        }
+    } else {
+        // distance-compared rounding (ties down), int sum that
+        // truncates on every add, short ranks
+        int sum = 0;
+#pragma unroll
+        for (int i = 0; i <= D; i++) {
+            float v = fmul(a.invdp1, el[i]);
+            float up = fmul(ceilf(v), a.dp1);
+            float down = fmul(floorf(v), a.dp1);
+            int rd2 = (fsub(up, el[i]) < fsub(el[i], down)) ? (int)(short)(int)up : (int)(short)(int)down;
+            rem0[i] = (float)rd2;
+            sum = __float2int_rz(fadd((float)sum, fmul((float)rd2, a.invdp1)));
+        }
+#pragma unroll
+        for (int i = 0; i < D; i++) {
+            float di = fsub(el[i], rem0[i]);
+#pragma unroll
+            for (int j = i + 1; j <= D; j++) {
+                if (di < fsub(el[j], rem0[j]))
+                    rank[i]++;
+                else
+                    rank[j]++;
+            }
+        }
+#pragma unroll
+        for (int i = 0; i <= D; i++) {
+            rank[i] = (short)(rank[i] + sum);
+            if (rank[i] < 0) {
+                rank[i] += D + 1;
+                rem0[i] = fadd(rem0[i], a.dp1);
+            } else if (rank[i] > D) {
+                rank[i] -= D + 1;
+                rem0[i] = fsub(rem0[i], a.dp1);
+            }
+        }
+    }
+    // Barycentric coordinates (P:244-263 / P:417-426), same operation order
+    float bary[D + 2];
+#pragma unroll
+    for (int q = 0; q < D + 2; q++) bary[q] = 0.f;
+#pragma unroll
+    for (int i = 0; i <= D; i++) {
+        float v = fmul(fsub(el[i], rem0[i]), a.invdp1);
+        int pidx = D - rank[i];
+#pragma unroll
+        for (int q = 0; q < D + 2; q++) {
+            if (q == pidx) bary[q] = fadd(bary[q], v);
+            if (q == pidx + 1) bary[q] = fsub(bary[q], v);
+        }
+    }
+    if (a.variant == DCRF_VARIANT_SSE)
+        bary[0] = fadd(bary[0], fadd(1.0f, bary[D + 1]));
+    else
+        bary[0] = __double2float_rn(__dadd_rn((double)bary[0], __dadd_rn(1.0, (double)bary[D + 1])));
+    if (p < a.N) {
+#pragma unroll
+        for (int r = 0; r <= D; r++) {
+            a.bary[(size_t)r * a.N + p] = bary[r];
+            a.wslice[(size_t)r * a.N + p] = fmul(bary[r], a.alpha);
+            a.rank[(size_t)r * a.N + p] = (uint8_t)rank[r];
+        }
+    }
+    // Corner keys (P:268-272 / P:429-432): rem0 + canonical simplex coordinate
+    bool overflow = false;
+#pragma unroll
+    for (int r = 0; r <= D; r++) {
+        uint64_t w[KW];
+#pragma unroll
+        for (int q = 0; q < KW; q++) w[q] = 0;
+        w[0] = (uint64_t)(uint16_t)img;
+#pragma unroll
+        for (int q = 0; q < D; q++) {
+            int canon = rank[q] <= D - r ? r : r - (D + 1);
+            int c = (int)fadd(rem0[q], (float)canon);
+            overflow |= (c < -32768 || c > 32767);
+            const int field = q + 1;
+            w[field >> 2] |= (uint64_t)(uint16_t)(short)c << (16 * (field & 3));
+        }
+        uint64_t *dst = a.keys + ((size_t)p * (D + 1) + r) * KW;
+#pragma unroll
+        for (int q = 0; q < KW; q++) dst[q] = w[q];
+    }
+    if (overflow) dcrf_set_error(a.st, DCRF_ERR_KEY_OVERFLOW, p);
+}
+
+template <int KW>
+__device__ __forceinline__ bool key_eq(const uint64_t *__restrict__ a, const uint64_t *b) {
+    bool eq = true;
+#pragma unroll
+    for (int w = 0; w < KW; w++) eq &= (a[w] == b[w]);
+    return eq;
+}
+
+template <int KW>
+__global__ void insert_kernel(const uint64_t *__restrict__ keys, size_t E, uint32_t *table, uint32_t mask,
+                              uint32_t *__restrict__ slot, DevStatus *st) {
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= E) return;
+    uint64_t key[KW];
+#pragma unroll
+    for (int w = 0; w < KW; w++) key[w] = keys[k * KW + w];
+    uint32_t h = key_hash<KW>(key) & mask;
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        uint32_t e = __ldcg(&table[h]);
+        if (e == EMPTY) {
+            e = atomicCAS(&table[h], EMPTY, (uint32_t)k);
+            if (e == EMPTY) {
+                slot[k] = h;
+                return;
+            }
+        }
+        if (key_eq<KW>(keys + (size_t)e * KW, key)) {
+            atomicMin(&table[h], (uint32_t)k);
+            slot[k] = h;
+            return;
+        }
+        h = (h + 1) & mask;
+    }
+    dcrf_set_error(st, DCRF_ERR_HASH_FULL, 0);
+}
+
+__global__ void first_flag_kernel(const uint32_t *__restrict__ table, const uint32_t *__restrict__ slot, size_t E,
+                                  uint32_t *__restrict__ flag) {
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= E) return;
+    flag[k] = table[slot[k]] == (uint32_t)k ? 1u : 0u;
+}
+
+template <int D>
+__global__ void offsets_kernel(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table,
+                               const uint32_t *__restrict__ slot, const uint32_t *__restrict__ vid, size_t E,
+                               int N, int *__restrict__ off, uint16_t *__restrict__ vkeys) {
+    constexpr int KW = KeyW<D>::KW;
+    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= E) return;
+    uint32_t rep = table[slot[k]];
+    uint32_t v = vid[rep];
+    if (k < (size_t)N * (D + 1)) {
+        size_t i = k / (D + 1);
+        int r = (int)(k - i * (D + 1));
+        off[(size_t)r * N + i] = (int)v;
+    }
+    if (rep == (uint32_t)k) {
+#pragma unroll
+        for (int q = 0; q <= D; q++) vkeys[(size_t)v * (D + 1) + q] = (uint16_t)(keys[k * KW + (q >> 2)] >> (16 * (q & 3)));
+    }
+}
+
+template <int D>
+__device__ __forceinline__ int lookup(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table,
+                                      uint32_t mask, const uint32_t *__restrict__ vid, const uint16_t *fields) {
+    constexpr int KW = KeyW<D>::KW;
+    uint64_t key[KW];
+#pragma unroll
+    for (int w = 0; w < KW; w++) key[w] = 0;
+#pragma unroll
+    for (int q = 0; q <= D; q++) key[q >> 2] |= (uint64_t)fields[q] << (16 * (q & 3));
+    uint32_t h = key_hash<KW>(key) & mask;
+    for (uint32_t probe = 0; probe <= mask; probe++) {
+        uint32_t e = table[h];
+        if (e == EMPTY) return -1;
+        if (key_eq<KW>(keys + (size_t)e * KW, key)) return (int)vid[e];
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+template <int D>
+__global__ void neighbors_kernel(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table, uint32_t mask,
+                                 const uint32_t *__restrict__ vid, const uint16_t *__restrict__ vkeys, int L,
+                                 int2 *__restrict__ nbr) {
+    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (size_t)L * (D + 1)) return;
+    int j = (int)(t / L);
+    int v = (int)(t - (size_t)j * L);
+    uint16_t kf[D + 1], n1[D + 1], n2[D + 1];
+#pragma unroll
+    for (int q = 0; q <= D; q++) kf[q] = vkeys[(size_t)v * (D + 1) + q];
+    n1[0] = n2[0] = kf[0];
+#pragma unroll
+    for (int q = 0; q < D; q++) {
+        short c = (short)kf[q + 1];
+        short a = (short)(c - 1), b = (short)(c + 1);
+        if (q == j) {
+            a = (short)(c + D);
+            b = (short)(c - D);
+        }
+        n1[q + 1] = (uint16_t)a;
+        n2[q + 1] = (uint16_t)b;
+    }
+    int i1 = lookup<D>(keys, table, mask, vid, n1);
+    int i2 = lookup<D>(keys, table, mask, vid, n2);
+    nbr[t] = make_int2(i1 + 1, i2 + 1);
+}
+
+// Block bitonic sort of one tile's corners by (vertex, corner) and count of
+// distinct vertices.  Corner idx = slot*(D+1) + r of the tile's slot.
+template <int D>
+__global__ void __launch_bounds__(256) tile_sort_kernel(const int *__restrict__ off, int N,
+                                                        const int *__restrict__ slot_pt,
+                                                        const int *__restrict__ tile_vbase, int n2max,
+                                                        unsigned long long *__restrict__ sorted,
+                                                        uint32_t *__restrict__ tile_nv) {
+    extern __shared__ unsigned long long s_keys[];
+    __shared__ uint32_t s_cnt;
+    const int t = blockIdx.x;
+    if (threadIdx.x == 0) s_cnt = 0;
+    for (int idx = threadIdx.x; idx < n2max; idx += blockDim.x) {
+        unsigned long long x = ~0ull;
+        if (idx < SPLAT_TILE * (D + 1)) {
+            int li = idx / (D + 1), r = idx - li * (D + 1);
+            int pt = slot_pt[(size_t)t * SPLAT_TILE + li];
+            if (pt >= 0) x = ((unsigned long long)(uint32_t)off[(size_t)r * N + pt] << 16) | (unsigned long long)idx;
+        }
+        s_keys[idx] = x;
+    }
+    __syncthreads();
+    for (int k = 2; k <= n2max; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n2max; i += blockDim.x) {
+                int ixj = i ^ j;
+                if (ixj > i) {
+                    unsigned long long a = s_keys[i], b = s_keys[ixj];
+                    bool asc = (i & k) == 0;
+                    if ((a > b) == asc) {
+                        s_keys[i] = b;
+                        s_keys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+    const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
+    const size_t base = (size_t)tile_vbase[t] * (D + 1);
+    uint32_t cnt = 0;
+    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
+        unsigned long long x = s_keys[idx];
+        sorted[base + idx] = x;
+        if (idx == 0 || (x >> 16) != (s_keys[idx - 1] >> 16)) cnt++;
+    }
+    atomicAdd(&s_cnt, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0) tile_nv[t] = s_cnt;
+}
+
+template <int D>
+__global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long *__restrict__ sorted,
+                                                        const float *__restrict__ bary, int N,
+                                                        const int *__restrict__ slot_pt,
+                                                        const int *__restrict__ tile_vbase,
+                                                        const uint32_t *__restrict__ tile_pbeg,
+                                                        int *__restrict__ part_v, int *__restrict__ part_mbeg,
+                                                        uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w) {
+    __shared__ uint32_t s_warp[8];
+    const int t = blockIdx.x;
+    const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
+    const size_t base = (size_t)tile_vbase[t] * (D + 1);
+    const int chunk = (n + blockDim.x - 1) / blockDim.x;
+    const int i0 = min(n, (int)threadIdx.x * chunk), i1 = min(n, i0 + chunk);
+    uint32_t cnt = 0;
+    for (int idx = i0; idx < i1; idx++)
+        if (idx == 0 || (sorted[base + idx] >> 16) != (sorted[base + idx - 1] >> 16)) cnt++;
+    // block exclusive scan of cnt
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int w = 0; w < warp; w++) before += s_warp[w];
+    uint32_t run = tile_pbeg[t] + before + x - cnt;
+    for (int idx = i0; idx < i1; idx++) {
+        unsigned long long s = sorted[base + idx];
+        int el = (int)(s & 0xFFFFull);
+        int li = el / (D + 1), r = el - li * (D + 1);
+        mem_pt[base + idx] = (uint16_t)li;
+        mem_w[base + idx] = bary[(size_t)r * N + slot_pt[(size_t)t * SPLAT_TILE + li]];
+        if (idx == 0 || (s >> 16) != (sorted[base + idx - 1] >> 16)) {
+            part_v[run] = (int)(s >> 16);
+            part_mbeg[run] = (int)(base + idx);
+            run++;
+        }
+    }
+}
+
+__global__ void count_kernel(const int *__restrict__ part_v, int P, uint32_t *__restrict__ cnt) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < P) atomicAdd(&cnt[part_v[p]], 1u);
+}
+
+__global__ void iota_kernel(uint32_t *__restrict__ a, int n) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p < n) a[p] = (uint32_t)p;
+}
+
+__global__ void set_int_kernel(int *p, int v) { *p = v; }
+
+// ---------------------------------------------------------------------------
+namespace {
+
+struct Pool {
+    cudaStream_t s;
+    std::vector<void *> ptrs;
+    bool failed = false;
+    template <class T>
+    T *get(size_t n) {
+        void *p = nullptr;
+        if (cudaMallocAsync(&p, std::max<size_t>(n * sizeof(T), 16), s) != cudaSuccess) {
+            failed = true;
+            return nullptr;
+        }
+        ptrs.push_back(p);
+        return static_cast<T *>(p);
+    }
+    void release() {
+        for (void *p : ptrs) cudaFreeAsync(p, s);
+        ptrs.clear();
+    }
+};
+
+int fail(int code, const std::string &m) {
+    g_msg = m;
+    return code;
+}
+
+template <class T>
+T *dalloc(size_t n, cudaStream_t s, size_t *acc) {
+    void *p = nullptr;
+    size_t b = std::max<size_t>(n * sizeof(T), 16);
+    if (cudaMallocAsync(&p, b, s) != cudaSuccess) return nullptr;
+    *acc += b;
+    return static_cast<T *>(p);
+}
+
+template <int D>
+int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
+            cudaStream_t s, DevStatus *status, LatticeDev *out) {
+    constexpr int KW = KeyW<D>::KW;
+    LatticeDev L{};
+    L.d = D;
+    L.N = N;
+    L.variant = variant;
+    const int nseg = (int)seg.start.size() - 1;
+    // padding points of the x86 build: each image's N_img rounded up to 4
+    std::vector<int> ph_img;
+    if (variant == DCRF_VARIANT_SSE)
+        for (int b = 0; b < nseg; b++) {
+            int nb = seg.start[b + 1] - seg.start[b];
+            for (int q = nb; q % 4 != 0; q++) ph_img.push_back(b);
+        }
+    const int n_ph = (int)ph_img.size();
+    const size_t E = (size_t)(N + n_ph) * (D + 1);
+    const size_t Ereal = (size_t)N * (D + 1);
+    if (E >= 0xFFFFFFF0ull) return fail(DCRF_ERR_INVALID_ARG, "lattice too large (more than 2^32 simplex corners)");
+
+    Pool tmp{s};
+    uint64_t *keys = tmp.get<uint64_t>(E * KW);
+    uint32_t *slot = tmp.get<uint32_t>(E);
+    uint32_t *vid = tmp.get<uint32_t>(E);
+    uint32_t *d_L = tmp.get<uint32_t>(4);
+    int *d_seg = tmp.get<int>(nseg + 1);
+    int *d_ph = tmp.get<int>(n_ph + 1);
+    size_t cap = 1024;
+    while ((double)cap < (double)load * (double)E && cap < (1ull << 31)) cap <<= 1;
+    uint32_t *table = tmp.get<uint32_t>(cap);
+    size_t scan_words = scan_temp_words(E);
+    uint32_t *stemp = tmp.get<uint32_t>(scan_words);
+    if (tmp.failed) {
+        tmp.release();
+        return fail(DCRF_ERR_OOM, "device allocation failed in lattice build");
+    }
+    auto bail = [&](int code, const std::string &m) {
+        tmp.release();
+        lattice_free(&L, s);
+        return fail(code, m);
+    };
+    cudaMemcpyAsync(d_seg, seg.start.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, s);
+    if (n_ph) cudaMemcpyAsync(d_ph, ph_img.data(), sizeof(int) * n_ph, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(table, 0xFF, cap * sizeof(uint32_t), s);
+
+    size_t acc = 0;
+    L.off = dalloc<int>(Ereal, s, &acc);
+    L.bary = dalloc<float>(Ereal, s, &acc);
+    L.wslice = dalloc<float>(Ereal, s, &acc);
+    L.rank = dalloc<uint8_t>(Ereal, s, &acc);
+    if (!L.off || !L.bary || !L.wslice || !L.rank) return bail(DCRF_ERR_OOM, "device allocation failed (lattice)");
+
+    EmbedArgs ea{};
+    ea.feat = feat;
+    ea.N = N;
+    ea.n_ph = n_ph;
+    ea.ph_img = d_ph;
+    ea.seg_start = d_seg;
+    ea.nseg = nseg;
+    {
+        // float(sqrt(2/3)*(d+1)), scale = float(1/sqrt((i+2)(i+1)) * inv_std_dev)
+        float inv_std_dev = (float)(std::sqrt(2.0 / 3.0) * (D + 1));
+        for (int i = 0; i < D; i++) ea.sf[i] = (float)(1.0 / std::sqrt((double)((i + 2) * (i + 1))) * (double)inv_std_dev);
+    }
+    ea.invdp1 = 1.0f / (float)(D + 1);
+    ea.dp1 = (float)(D + 1);
+    ea.alpha = 1.0f / (1.0f + std::pow(2.0f, (float)-D));
+    L.alpha = ea.alpha;
+    ea.variant = variant;
+    ea.bary = L.bary;
+    ea.wslice = L.wslice;
+    ea.rank = L.rank;
+    ea.keys = keys;
+    ea.st = status;
+    int npts = N + n_ph;
+    if (npts > 0) DCRF_LAUNCH(embed_kernel<D><<<ceil_div_u(npts, 128), 128, 0, s>>>(ea));
+    if (E > 0) DCRF_LAUNCH(insert_kernel<KW><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, E, table, (uint32_t)(cap - 1), slot, status));
+    if (E > 0) DCRF_LAUNCH(first_flag_kernel<<<ceil_div_u(E, 256), 256, 0, s>>>(table, slot, E, vid));
+    if (scan_exclusive_u32(vid, vid, E, d_L, stemp, s) != cudaSuccess) return bail(DCRF_ERR_CUDA, "scan failed");
+    uint32_t hL = 0;
+    DevStatus hst{};
+    cudaMemcpyAsync(&hL, d_L, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+    cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice build: ") + cudaGetErrorString(ce));
+    if (hst.code == DCRF_ERR_KEY_OVERFLOW)
+        return bail(DCRF_ERR_KEY_OVERFLOW,
+                    "a lattice coordinate of point " + std::to_string(hst.detail) +
+                        " leaves the int16 key range of the reference (features too large)");
+    if (hst.code == DCRF_ERR_HASH_FULL) return bail(DCRF_ERR_HASH_FULL, "lattice hash table full");
+    if (hst.code != 0) return bail(hst.code, "lattice build failed");
+    L.L = (int)hL;
+
+    L.nbr = dalloc<int2>((size_t)L.L * (D + 1), s, &acc);
+    L.vkeys = dalloc<uint16_t>((size_t)L.L * (D + 1), s, &acc);
+    if (!L.nbr || !L.vkeys) return bail(DCRF_ERR_OOM, "device allocation failed (neighbours)");
+    if (E > 0)
+        DCRF_LAUNCH(offsets_kernel<D><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, table, slot, vid, E, N, L.off, L.vkeys));
+    if (L.L > 0)
+        DCRF_LAUNCH(neighbors_kernel<D><<<ceil_div_u((size_t)L.L * (D + 1), 256), 256, 0, s>>>(keys, table, (uint32_t)(cap - 1),
+                                                                                  vid, L.vkeys, L.L, L.nbr));
+    // ---- splat tiles --------------------------------------------------------
+    L.ntiles = tm.ntiles;
+    L.tile_pbeg = dalloc<int>(L.ntiles + 1, s, &acc);
+    L.mem_pt = dalloc<uint16_t>(Ereal, s, &acc);
+    L.mem_w = dalloc<float>(Ereal, s, &acc);
+    unsigned long long *sorted = tmp.get<unsigned long long>(Ereal);
+    uint32_t *tile_nv = tmp.get<uint32_t>(L.ntiles + 1);
+    uint32_t *d_P = tmp.get<uint32_t>(4);
+    if (!L.tile_pbeg || !L.mem_pt || !L.mem_w || tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
+    int n2max = 1;
+    while (n2max < SPLAT_TILE * (D + 1)) n2max <<= 1;
+    size_t smem = (size_t)n2max * sizeof(unsigned long long);
+    if (smem > 48 * 1024) cudaFuncSetAttribute(tile_sort_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (L.ntiles > 0) {
+        DCRF_LAUNCH(tile_sort_kernel<D><<<L.ntiles, 256, smem, s>>>(L.off, N, tm.slot_pt, tm.tile_vbase, n2max, sorted, tile_nv));
+        if (scan_exclusive_u32(tile_nv, (uint32_t *)L.tile_pbeg, L.ntiles, d_P, stemp, s) != cudaSuccess)
+            return bail(DCRF_ERR_CUDA, "scan failed");
+    }
+    uint32_t hP = 0;
+    if (L.ntiles > 0) {
+        cudaMemcpyAsync(&hP, d_P, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        ce = cudaStreamSynchronize(s);
+        if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tiles: ") + cudaGetErrorString(ce));
+    }
+    L.P = (int)hP;
+    L.part_v = dalloc<int>((size_t)L.P + 1, s, &acc);
+    L.part_mbeg = dalloc<int>((size_t)L.P + 1, s, &acc);
+    L.red_beg = dalloc<int>((size_t)L.L + 1, s, &acc);
+    L.red_list = dalloc<int>((size_t)L.P + 1, s, &acc);
+    if (!L.part_v || !L.part_mbeg || !L.red_beg || !L.red_list) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
+    DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.tile_pbeg + L.ntiles, L.P));
+    if (L.ntiles > 0)
+        DCRF_LAUNCH(tile_fill_kernel<D><<<L.ntiles, 256, 0, s>>>(sorted, L.bary, N, tm.slot_pt, tm.tile_vbase,
+                                                     (const uint32_t *)L.tile_pbeg, L.part_v, L.part_mbeg, L.mem_pt,
+                                                     L.mem_w));
+    DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.part_mbeg + L.P, (int)Ereal));
+    // ---- reduce lists: partials grouped by vertex, in tile order ------------
+    {
+        uint32_t *cnt = tmp.get<uint32_t>((size_t)L.L + 1);
+        uint32_t *k0 = tmp.get<uint32_t>((size_t)L.P + 1), *v0 = tmp.get<uint32_t>((size_t)L.P + 1);
+        uint32_t *k1 = tmp.get<uint32_t>((size_t)L.P + 1), *v1 = tmp.get<uint32_t>((size_t)L.P + 1);
+        uint32_t *rtemp = tmp.get<uint32_t>(radix_temp_words((size_t)L.P) + scan_temp_words((size_t)L.L + 1));
+        if (tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (reduce lists)");
+        cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ((size_t)L.L + 1), s);
+        if (L.P > 0) DCRF_LAUNCH(count_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, cnt));
+        if (scan_exclusive_u32(cnt, (uint32_t *)L.red_beg, (size_t)L.L, (uint32_t *)(L.red_beg + L.L), rtemp, s) !=
+            cudaSuccess)
+            return bail(DCRF_ERR_CUDA, "scan failed");
+        if (L.L == 0) DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.red_beg, 0));
+        if (L.P > 0) {
+            cudaMemcpyAsync(k0, L.part_v, sizeof(uint32_t) * L.P, cudaMemcpyDeviceToDevice, s);
+            DCRF_LAUNCH(iota_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(v0, L.P));
+            int bits = 1;
+            while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)L.L) bits++;
+            int in_alt = 0;
+            if (radix_sort_pairs_u32(k0, v0, k1, v1, (size_t)L.P, bits, rtemp, s, &in_alt) != cudaSuccess)
+                return bail(DCRF_ERR_CUDA, "radix sort failed");
+            cudaMemcpyAsync(L.red_list, in_alt ? v1 : v0, sizeof(uint32_t) * L.P, cudaMemcpyDeviceToDevice, s);
+        }
+    }
+    ce = cudaStreamSynchronize(s);
+    tmp.release();
+    if (ce != cudaSuccess) {
+        lattice_free(&L, s);
+        return fail(DCRF_ERR_CUDA, std::string("lattice build: ") + cudaGetErrorString(ce));
+    }
+    ce = cudaGetLastError();
+    if (ce != cudaSuccess) {
+        lattice_free(&L, s);
+        return fail(DCRF_ERR_CUDA, std::string("lattice build launch: ") + cudaGetErrorString(ce));
+    }
+    L.bytes = acc;
+    *out = L;
+    return DCRF_OK;
+}
+
+}  // namespace
+
+void lattice_free(LatticeDev *L, cudaStream_t s) {
+    void *ps[] = {L->off, L->bary, L->wslice, L->rank, L->nbr, L->vkeys, L->part_v,
+                  L->part_mbeg, L->tile_pbeg, L->mem_pt, L->mem_w, L->red_beg, L->red_list};
+    for (void *p : ps)
+        if (p) cudaFreeAsync(p, s);
+    *L = LatticeDev{};
+}
+
+int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
+                  cudaStream_t s, DevStatus *status, LatticeDev *out) {
+    if (N < 0 || (seg.start.size() < 2)) return fail(DCRF_ERR_INVALID_ARG, "bad point segmentation");
+    if (cudaMemsetAsync(status, 0, sizeof(DevStatus), s) != cudaSuccess) return fail(DCRF_ERR_CUDA, "memset failed");
+    switch (d) {
+#define DCRF_CASE(D) \
+    case D:          \
+        return build_d<D>(feat, N, seg, tm, variant, load, s, status, out);
+        DCRF_CASE(1) DCRF_CASE(2) DCRF_CASE(3) DCRF_CASE(4) DCRF_CASE(5) DCRF_CASE(6) DCRF_CASE(7) DCRF_CASE(8)
+        DCRF_CASE(9) DCRF_CASE(10) DCRF_CASE(11) DCRF_CASE(12) DCRF_CASE(13) DCRF_CASE(14) DCRF_CASE(15)
+        DCRF_CASE(16)
+#undef DCRF_CASE
+        default:
+            return fail(DCRF_ERR_INVALID_ARG, "feature dimension must be in [1, 16], got " + std::to_string(d));
+    }
+}
+
+}  // namespace dcrf

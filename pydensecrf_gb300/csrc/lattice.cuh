@@ -1,0 +1,59 @@
+// lattice.cuh -- device permutohedral lattice of one pairwise term (or of one
+// term over a batch of images: every table below is then the concatenation of
+// the images' tables, and vertex ids are global).
+#pragma once
+#include <vector>
+
+#include "dcrf_common.cuh"
+
+namespace dcrf {
+
+constexpr int SPLAT_TILE = 256;  // points per tile of the in-kernel splat
+
+struct LatticeDev {
+    int d = 0, N = 0, L = 0, P = 0, ntiles = 0, variant = 0;
+    float alpha = 0.f;
+    int *off = nullptr;          // [d+1][N]
+    float *bary = nullptr;       // [d+1][N]
+    float *wslice = nullptr;     // [d+1][N]
+    uint8_t *rank = nullptr;     // [d+1][N]
+    int2 *nbr = nullptr;         // [d+1][L]
+    uint16_t *vkeys = nullptr;   // [L][d+1]: field 0 = image, 1..d = coordinates
+    int *part_v = nullptr;       // [P]
+    int *part_mbeg = nullptr;    // [P+1]
+    int *tile_pbeg = nullptr;    // [ntiles+1]
+    uint16_t *mem_pt = nullptr;  // [E]
+    float *mem_w = nullptr;      // [E]
+    int *red_beg = nullptr;      // [L+1]
+    int *red_list = nullptr;     // [P]
+    size_t bytes = 0;
+};
+
+// Image segmentation of the point set (a single image: nseg = 1).
+struct Segments {
+    std::vector<int> start;  // nseg+1 prefix offsets of the images' points
+};
+
+// Assignment of points to splat tiles: tile t owns slots [t*SPLAT_TILE,
+// (t+1)*SPLAT_TILE); slot_pt[slot] is a point index or -1.  tile_vbase[t] is
+// the number of valid slots in tiles before t (tile_vbase[ntiles] = N).
+struct TileMapDev {
+    int ntiles = 0;
+    const int *slot_pt = nullptr;     // device [ntiles*SPLAT_TILE]
+    const int *tile_vbase = nullptr;  // device [ntiles+1]
+};
+
+// Builds the lattice of `feat` ([d][N], device) on `s`.  `variant` selects the
+// x86 (SSE) or scalar arithmetic of the reference; SSE also inserts the
+// zero-feature padding points of each image (N_img % 4 != 0).  `load` is the
+// hash-table capacity factor (capacity = pow2 >= load * corners).  Returns a
+// DCRF status; on DCRF_ERR_HASH_FULL the caller may retry with a larger load.
+int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
+                  cudaStream_t s, DevStatus *status, LatticeDev *out);
+
+void lattice_free(LatticeDev *lat, cudaStream_t s);
+
+// Host-side error text of the last failing build.
+const char *lattice_last_message();
+
+}  // namespace dcrf

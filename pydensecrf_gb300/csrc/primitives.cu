@@ -1,0 +1,215 @@
+// primitives.cu -- device-wide exclusive scan and stable LSD radix sort.
+//
+// Used by the lattice build: compaction of first-occurrence corners into
+// vertex ids (the reference assigns ids in hash-insertion order,
+// permutohedral.cpp:105-111) and the grouping of per-tile splat partials by
+// vertex.  Both are deterministic: no float math, and the sort is stable.
+#include "dcrf_common.cuh"
+#include "primitives.cuh"
+
+namespace dcrf {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_ITEMS = 4;
+constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;
+
+// Block-wide exclusive scan of one value per thread; returns the block total.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp, uint32_t &total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < (SCAN_THREADS / 32) ? s_warp[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += y;
+        }
+        if (lane < (SCAN_THREADS / 32)) s_warp[lane] = w;
+    }
+    __syncthreads();
+    total = s_warp[SCAN_THREADS / 32 - 1];
+    uint32_t before = warp ? s_warp[warp - 1] : 0;
+    return before + x - v;
+}
+
+__global__ void scan_reduce_kernel(const uint32_t *__restrict__ in, size_t n, uint32_t *__restrict__ sums) {
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++)
+        if (base + k < n) s += in[base + k];
+    uint32_t total;
+    block_exclusive_scan(s, s_warp, total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of one tile plus the tile's offset; in-place safe.
+__global__ void scan_tile_kernel(const uint32_t *in, uint32_t *out, size_t n, const uint32_t *__restrict__ offsets,
+                                 uint32_t *__restrict__ d_total) {
+    __shared__ uint32_t s_warp[SCAN_THREADS / 32];
+    size_t base = (size_t)blockIdx.x * SCAN_TILE + (size_t)threadIdx.x * SCAN_ITEMS;
+    uint32_t v[SCAN_ITEMS];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        v[k] = base + k < n ? in[base + k] : 0;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t pre = block_exclusive_scan(s, s_warp, total);
+    uint32_t off = offsets ? offsets[blockIdx.x] : 0;
+    uint32_t run = off + pre;
+#pragma unroll
+    for (int k = 0; k < SCAN_ITEMS; k++) {
+        if (base + k < n) out[base + k] = run;
+        run += v[k];
+    }
+    if (d_total && threadIdx.x == 0) *d_total = off + total;
+}
+
+size_t scan_temp_words(size_t n) {
+    size_t w = 0;
+    while (n > (size_t)SCAN_TILE) {
+        n = (n + SCAN_TILE - 1) / SCAN_TILE;
+        w += (n + 63) / 64 * 64;
+    }
+    return w + 64;
+}
+
+static cudaError_t scan_rec(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_total, uint32_t *temp,
+                            cudaStream_t s) {
+    size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+    if (nb <= 1) {
+        DCRF_LAUNCH(scan_tile_kernel<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr, d_total));
+        return cudaGetLastError();
+    }
+    uint32_t *sums = temp;
+    temp += (nb + 63) / 64 * 64;
+    DCRF_LAUNCH(scan_reduce_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, n, sums));
+    cudaError_t e = scan_rec(sums, sums, nb, d_total, temp, s);
+    if (e != cudaSuccess) return e;
+    DCRF_LAUNCH(scan_tile_kernel<<<(unsigned)nb, SCAN_THREADS, 0, s>>>(in, out, n, sums, nullptr));
+    return cudaGetLastError();
+}
+
+cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_total, uint32_t *temp,
+                               cudaStream_t s) {
+    if (n == 0) {
+        if (d_total) return cudaMemsetAsync(d_total, 0, sizeof(uint32_t), s);
+        return cudaSuccess;
+    }
+    return scan_rec(in, out, n, d_total, temp, s);
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort of (key, value) uint32 pairs, 8-bit digits.
+// ---------------------------------------------------------------------------
+constexpr int RADIX_THREADS = 256;
+constexpr int RADIX_ROUNDS = 8;
+constexpr int RADIX_TILE = RADIX_THREADS * RADIX_ROUNDS;
+constexpr int RADIX_WARPS = RADIX_THREADS / 32;
+
+__global__ void radix_hist_kernel(const uint32_t *__restrict__ keys, size_t n, int shift, uint32_t *__restrict__ hist,
+                                  unsigned nblocks) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    size_t base = (size_t)blockIdx.x * RADIX_TILE;
+#pragma unroll
+    for (int r = 0; r < RADIX_ROUNDS; r++) {
+        size_t i = base + (size_t)r * RADIX_THREADS + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
+}
+
+__global__ void radix_scatter_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, size_t n,
+                                     int shift, const uint32_t *__restrict__ hist, unsigned nblocks,
+                                     uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out) {
+    __shared__ uint32_t s_wcnt[RADIX_WARPS][257];
+    __shared__ uint32_t s_run[256];
+    __shared__ uint32_t s_base[256];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    s_run[threadIdx.x] = 0;
+    s_base[threadIdx.x] = hist[(size_t)threadIdx.x * nblocks + blockIdx.x];
+    size_t base = (size_t)blockIdx.x * RADIX_TILE;
+    for (int r = 0; r < RADIX_ROUNDS; r++) {
+        for (int w = 0; w < RADIX_WARPS; w++) s_wcnt[w][threadIdx.x] = 0;
+        __syncthreads();
+        size_t i = base + (size_t)r * RADIX_THREADS + threadIdx.x;
+        bool valid = i < n;
+        uint32_t key = valid ? keys[i] : 0u;
+        uint32_t val = valid ? vals[i] : 0u;
+        uint32_t digit = valid ? ((key >> shift) & 255u) : 256u;
+        uint32_t peers = __match_any_sync(0xffffffffu, digit);
+        int leader = __ffs(peers) - 1;
+        uint32_t rank = __popc(peers & ((1u << lane) - 1u));
+        if (lane == leader && valid) s_wcnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = s_run[threadIdx.x];
+            for (int w = 0; w < RADIX_WARPS; w++) {
+                uint32_t c = s_wcnt[w][threadIdx.x];
+                s_wcnt[w][threadIdx.x] = run;
+                run += c;
+            }
+            s_run[threadIdx.x] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            // s_wcnt now holds, per (warp, digit), the count of earlier items of that digit
+            // in this tile (earlier rounds plus earlier warps of this round)
+            uint32_t pos = s_base[digit] + s_wcnt[warp][digit] + rank;
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+    }
+}
+
+size_t radix_temp_words(size_t n) {
+    size_t nb = (n + RADIX_TILE - 1) / RADIX_TILE;
+    size_t h = 256 * nb;
+    return (h + 63) / 64 * 64 + scan_temp_words(h);
+}
+
+cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
+                                 int bits, uint32_t *temp, cudaStream_t s, int *result_in_alt) {
+    *result_in_alt = 0;
+    if (n == 0) return cudaSuccess;
+    unsigned nb = (unsigned)((n + RADIX_TILE - 1) / RADIX_TILE);
+    size_t h = 256 * (size_t)nb;
+    uint32_t *hist = temp;
+    uint32_t *stemp = temp + (h + 63) / 64 * 64;
+    uint32_t *kin = keys, *vin = vals, *kout = keys_alt, *vout = vals_alt;
+    int passes = (bits + 7) / 8;
+    if (passes < 1) passes = 1;
+    for (int p = 0; p < passes; p++) {
+        int shift = 8 * p;
+        DCRF_LAUNCH(radix_hist_kernel<<<nb, RADIX_THREADS, 0, s>>>(kin, n, shift, hist, nb));
+        cudaError_t e = scan_exclusive_u32(hist, hist, h, nullptr, stemp, s);
+        if (e != cudaSuccess) return e;
+        DCRF_LAUNCH(radix_scatter_kernel<<<nb, RADIX_THREADS, 0, s>>>(kin, vin, n, shift, hist, nb, kout, vout));
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+        uint32_t *t = kin;
+        kin = kout;
+        kout = t;
+        t = vin;
+        vin = vout;
+        vout = t;
+        *result_in_alt ^= 1;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace dcrf

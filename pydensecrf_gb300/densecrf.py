@@ -1,0 +1,300 @@
+"""Drop-in for ``pydensecrf.densecrf`` backed by the GB300 engine.
+
+Same classes, methods, defaults, enums and argument checks as the reference's
+Cython module (pydensecrf/densecrf.pyx, pydensecrf/densecrf.pxd); every call
+goes through the C ABI of include/dcrf.h to hand-written sm_103a kernels.
+Marginals come back as :class:`pydensecrf_gb300.eigen.MatrixXf` with the
+reference's memory layout (column-major ``M x N``).
+"""
+from __future__ import annotations
+
+import ctypes
+from numbers import Number
+
+import numpy as np
+
+from . import _lib
+from .eigen import MatrixXf, as_float_buffer
+
+# enums of pydensecrf/densecrf/include/pairwise.h:32-42 (densecrf.pxd:43-44)
+NO_NORMALIZATION = 0
+NORMALIZE_BEFORE = 1
+NORMALIZE_AFTER = 2
+NORMALIZE_SYMMETRIC = 3
+CONST_KERNEL = 0
+DIAG_KERNEL = 1
+FULL_KERNEL = 2
+
+
+class NormalizationType(int):
+    NO_NORMALIZATION = NO_NORMALIZATION
+    NORMALIZE_BEFORE = NORMALIZE_BEFORE
+    NORMALIZE_AFTER = NORMALIZE_AFTER
+    NORMALIZE_SYMMETRIC = NORMALIZE_SYMMETRIC
+
+
+class KernelType(int):
+    CONST_KERNEL = CONST_KERNEL
+    DIAG_KERNEL = DIAG_KERNEL
+    FULL_KERNEL = FULL_KERNEL
+
+
+def _ptr(a: np.ndarray):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def _labelcomp(compat, M: int):
+    """Compatibility dispatch of densecrf.pyx:11-20 -> (kind, float32 buffer).
+
+    A Number gives Potts, a 1-D float32 buffer Diagonal, a 2-D float32 buffer
+    Matrix; other dtypes raise ValueError like the typed memoryviews do.
+    """
+    if isinstance(compat, Number):
+        return _lib.COMPAT_POTTS, np.array([float(compat)], dtype=np.float32)
+    ndim = memoryview(compat).ndim
+    if ndim == 1:
+        c = as_float_buffer(compat, 1, "compat")
+        if c.shape[0] != M:
+            raise ValueError(f"Diagonal compatibility needs {M} entries, got {c.shape[0]}")
+        return _lib.COMPAT_DIAGONAL, np.ascontiguousarray(c, np.float32)
+    if ndim == 2:
+        c = as_float_buffer(compat, 2, "compat")
+        if c.shape != (M, M):
+            raise ValueError(f"Matrix compatibility needs shape {(M, M)}, got {c.shape}")
+        return _lib.COMPAT_MATRIX, np.ascontiguousarray(c, np.float32)
+    raise ValueError("LabelCompatibility of dimension >2 not meaningful.")
+
+
+def _check_enum(v, lo, hi, what):
+    if not isinstance(v, (int, np.integer)) or not (lo <= int(v) <= hi):
+        raise TypeError(f"{what} must be one of the {what} constants")
+    return int(v)
+
+
+class Unary:
+    """Base of the unary holders (densecrf.pyx:23-36)."""
+
+    def _matrix(self, M: int, N: int) -> np.ndarray:
+        raise NotImplementedError
+
+
+class ConstUnary(Unary):
+    """Constant unary energy (densecrf.pyx:39-41, unary.cpp:42-46)."""
+
+    def __init__(self, u):
+        self.u = np.array(as_float_buffer(u, 2, "u"), dtype=np.float32, copy=True)
+
+    def _matrix(self, M, N):
+        return self.u
+
+
+class LogisticUnary(Unary):
+    """Logistic unary energy U = L f (densecrf.pyx:44-46, unary.cpp:48-52)."""
+
+    def __init__(self, L, f):
+        self.L = np.array(as_float_buffer(L, 2, "L"), dtype=np.float32, copy=True)
+        self.f = np.array(as_float_buffer(f, 2, "f"), dtype=np.float32, copy=True)
+
+    def _matrix(self, M, N):
+        return logistic_unary(self.L, self.f)
+
+
+def logistic_unary(L: np.ndarray, f: np.ndarray) -> np.ndarray:
+    """U = L @ f in float32, on the GPU (cuBLAS through torch, TF32 off)."""
+    import torch
+
+    if not torch.cuda.is_available():
+        raise RuntimeError("a CUDA device is required")
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        Ld = torch.from_numpy(np.ascontiguousarray(L)).cuda()
+        fd = torch.from_numpy(np.ascontiguousarray(f)).cuda()
+        return (Ld @ fd).cpu().numpy()
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+
+
+class DenseCRF:
+    """Fully connected CRF over ``nvar`` variables and ``nlabels`` labels
+    (densecrf.pyx:49-101 -> densecrf.cpp)."""
+
+    def __init__(self, nvar: int, nlabels: int, *_, **__):
+        self._nvar = int(nvar)
+        self._nlabel = int(nlabels)
+        self._h = ctypes.c_void_p()
+        if type(self) is DenseCRF:
+            lib = _lib.load()
+            _lib.check(lib.dcrf_create(self._nvar, self._nlabel, ctypes.byref(self._h)))
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and h.value:
+            try:
+                _lib.load().dcrf_destroy(h)
+            except Exception:
+                pass
+            h.value = None
+
+    # -- configuration ------------------------------------------------------
+    def set_variant(self, variant: int) -> None:
+        """Lattice arithmetic of the x86 (0, default) or scalar (1) reference build."""
+        _lib.check(_lib.load().dcrf_set_variant(self._h, int(variant)))
+
+    def addPairwiseEnergy(self, features, compat, kernel=DIAG_KERNEL, normalization=NORMALIZE_SYMMETRIC):
+        """densecrf.pyx:71-75."""
+        feat = as_float_buffer(features, 2, "features")
+        kernel = _check_enum(kernel, 0, 2, "KernelType")
+        normalization = _check_enum(normalization, 0, 3, "NormalizationType")
+        if feat.shape[1] != self._nvar:
+            raise ValueError("Bad shape for pairwise energy (Need (?, {}), got {})".format(
+                self._nvar, (feat.shape[0], feat.shape[1])))
+        kind, c = _labelcomp(compat, self._nlabel)
+        _lib.check(_lib.load().dcrf_add_pairwise(self._h, _ptr(feat), feat.shape[0], _lib.HOST, kind, _ptr(c),
+                                                 kernel, normalization, None))
+
+    def setUnary(self, u: Unary) -> None:
+        """densecrf.pyx:77-78."""
+        if not isinstance(u, Unary):
+            raise TypeError("Argument 'u' has incorrect type (expected Unary)")
+        self._set_unary_matrix(u._matrix(self._nlabel, self._nvar))
+
+    def setUnaryEnergy(self, u, f=None) -> None:
+        """densecrf.pyx:80-89; with ``f`` the unary is logistic, U = u f."""
+        u = as_float_buffer(u, 2, "u")
+        if u.shape[0] != self._nlabel or (f is None and u.shape[1] != self._nvar):
+            raise ValueError("Bad shape for unary energy (Need {}, got {})".format(
+                (self._nlabel, self._nvar), (u.shape[0], u.shape[1])))
+        if f is None:
+            self._set_unary_matrix(u)
+        else:
+            f = as_float_buffer(f, 2, "f")
+            self._set_unary_matrix(logistic_unary(u, f))
+
+    def _set_unary_matrix(self, U: np.ndarray) -> None:
+        U = np.ascontiguousarray(U, dtype=np.float32)
+        if U.shape != (self._nlabel, self._nvar):
+            raise ValueError("Bad shape for unary energy (Need {}, got {})".format(
+                (self._nlabel, self._nvar), U.shape))
+        _lib.check(_lib.load().dcrf_set_unary(self._h, _ptr(U), _lib.LAYOUT_LM, _lib.HOST))
+
+    # -- inference -------------------------------------------------------------
+    def _new_q(self) -> np.ndarray:
+        return np.empty((self._nvar, self._nlabel), np.float32)
+
+    def inference(self, niter: int) -> MatrixXf:
+        """densecrf.pyx:91-92."""
+        Q = self._new_q()
+        _lib.check(_lib.load().dcrf_inference(self._h, int(niter), _ptr(Q), _lib.LAYOUT_PM, _lib.HOST))
+        return MatrixXf().wrap_colmajor(Q)
+
+    def startInference(self):
+        """densecrf.pyx:94-95: (Q, tmp1, tmp2)."""
+        Q = self._new_q()
+        _lib.check(_lib.load().dcrf_start_inference(self._h, _ptr(Q), _lib.LAYOUT_PM, _lib.HOST))
+        return MatrixXf().wrap_colmajor(Q), MatrixXf(), MatrixXf()
+
+    def stepInference(self, Q: MatrixXf, tmp1: MatrixXf, tmp2: MatrixXf) -> None:
+        """densecrf.pyx:97-98: one mean-field update of Q, in place."""
+        if not isinstance(Q, MatrixXf):
+            raise TypeError("Argument 'Q' has incorrect type (expected MatrixXf)")
+        if Q.shape != (self._nlabel, self._nvar):
+            raise ValueError(f"Q must have shape {(self._nlabel, self._nvar)}, got {Q.shape}")
+        _lib.check(_lib.load().dcrf_step_inference(self._h, _ptr(Q.data), _lib.LAYOUT_PM, _lib.HOST))
+
+    def klDivergence(self, Q) -> float:
+        """densecrf.pyx:100-101."""
+        if isinstance(Q, MatrixXf):
+            data, layout = Q.data, _lib.LAYOUT_PM
+        else:
+            data, layout = np.ascontiguousarray(np.asarray(Q, np.float32)), _lib.LAYOUT_LM
+        if (data.size != self._nlabel * self._nvar):
+            raise ValueError("Q has the wrong size")
+        out = ctypes.c_double()
+        _lib.check(_lib.load().dcrf_kl_divergence(self._h, _ptr(data), layout, _lib.HOST, ctypes.byref(out)))
+        return out.value
+
+    def map(self, niter: int) -> np.ndarray:
+        """DenseCRF::map (densecrf.cpp:132-137): argmax labels after niter iterations."""
+        out = np.empty(self._nvar, np.int16)
+        _lib.check(_lib.load().dcrf_map(self._h, int(niter), _ptr(out), _lib.HOST))
+        return out
+
+    # -- introspection -----------------------------------------------------------
+    def lattice(self, term: int) -> dict:
+        """Lattice tables of pairwise term ``term`` in the reference's layout."""
+        lib = _lib.load()
+        d, L = ctypes.c_int(), ctypes.c_int()
+        _lib.check(lib.dcrf_lattice_info(self._h, term, ctypes.byref(d), ctypes.byref(L)))
+        d, L, N = d.value, L.value, self._nvar
+        out = dict(offset=np.empty((N, d + 1), np.int32), rank=np.empty((N, d + 1), np.int32),
+                   bary=np.empty((N, d + 1), np.float32), neighbors=np.empty((d + 1, L, 2), np.int32),
+                   keys=np.empty((L, d), np.int16), L=L, d=d)
+        _lib.check(lib.dcrf_lattice_dump(self._h, term, _ptr(out["offset"]), _ptr(out["rank"]), _ptr(out["bary"]),
+                                         _ptr(out["neighbors"]), _ptr(out["keys"])))
+        return out
+
+    def term_norm(self, term: int) -> np.ndarray:
+        out = np.empty(self._nvar, np.float32)
+        _lib.check(_lib.load().dcrf_term_norm(self._h, term, _ptr(out)))
+        return out
+
+    def lattice_filter(self, term: int, values: np.ndarray, reverse: bool = False) -> np.ndarray:
+        """Raw lattice filter K v of term ``term``; values is (value_size, N)."""
+        v = np.ascontiguousarray(values, np.float32)
+        out = np.empty_like(v)
+        _lib.check(_lib.load().dcrf_lattice_filter(self._h, term, _ptr(v), v.shape[0], int(bool(reverse)),
+                                                   _ptr(out)))
+        return out
+
+
+class DenseCRF2D(DenseCRF):
+    """CRF over a W x H pixel grid (densecrf.pyx:104-140)."""
+
+    def __init__(self, w: int, h: int, nlabels: int, *_, **__):
+        super().__init__(int(w) * int(h), nlabels)
+        self._w = int(w)
+        self._h2 = int(h)
+        if type(self) is DenseCRF2D:
+            lib = _lib.load()
+            _lib.check(lib.dcrf_create_2d(self._w, self._h2, self._nlabel, ctypes.byref(self._h)))
+
+    def addPairwiseGaussian(self, sxy, compat, kernel=DIAG_KERNEL, normalization=NORMALIZE_SYMMETRIC):
+        """densecrf.pyx:120-124."""
+        if isinstance(sxy, Number):
+            sxy = (sxy, sxy)
+        kernel = _check_enum(kernel, 0, 2, "KernelType")
+        normalization = _check_enum(normalization, 0, 3, "NormalizationType")
+        kind, c = _labelcomp(compat, self._nlabel)
+        _lib.check(_lib.load().dcrf_add_pairwise_gaussian(self._h, float(sxy[0]), float(sxy[1]), kind, _ptr(c),
+                                                          kernel, normalization, None))
+
+    def addPairwiseBilateral(self, sxy, srgb, rgbim, compat, kernel=DIAG_KERNEL, normalization=NORMALIZE_SYMMETRIC):
+        """densecrf.pyx:126-140."""
+        if isinstance(sxy, Number):
+            sxy = (sxy, sxy)
+        if isinstance(srgb, Number):
+            srgb = (srgb, srgb, srgb)
+        if rgbim is None:
+            raise TypeError("rgbim must not be None")
+        mv = memoryview(rgbim)
+        if mv.format not in ("B", "=B", "<B", "@B"):
+            raise ValueError(f"Buffer dtype mismatch, expected 'unsigned char' but got '{mv.format}'")
+        if mv.ndim != 3:
+            raise ValueError(f"Buffer has wrong number of dimensions (expected 3, got {mv.ndim})")
+        if not mv.c_contiguous:
+            raise ValueError("ndarray is not C-contiguous")
+        img = np.asarray(rgbim)
+        if img.shape[0] != self._h2 or img.shape[1] != self._w:
+            raise ValueError("Bad shape for pairwise bilateral (Need {}, got {})".format(
+                (self._h2, self._w, 3), img.shape))
+        if img.shape[2] != 3:
+            raise ValueError("addPairwiseBilateral only works for RGB images. For other types, use "
+                             "`utils.create_pairwise_bilateral` to construct your own pairwise energy and add it "
+                             "through `addPairwiseEnergy`.")
+        kernel = _check_enum(kernel, 0, 2, "KernelType")
+        normalization = _check_enum(normalization, 0, 3, "NormalizationType")
+        kind, c = _labelcomp(compat, self._nlabel)
+        _lib.check(_lib.load().dcrf_add_pairwise_bilateral(
+            self._h, float(sxy[0]), float(sxy[1]), float(srgb[0]), float(srgb[1]), float(srgb[2]), _ptr(img),
+            _lib.HOST, kind, _ptr(c), kernel, normalization, None))

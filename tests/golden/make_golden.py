@@ -1,0 +1,220 @@
+"""Generates the golden fixtures of tests/golden/ from the REFERENCE itself.
+
+Run in a container that holds the reference sources (it builds
+oracle/_ref/libdcrf_ref.so and libdcrf_ref_scalar.so from them via
+oracle/Makefile).  Outputs, all small:
+
+* lattice.npz   -- lattice tables (offset, rank, barycentric, neighbours) of
+                   seeded feature sets, from the reference's own
+                   Permutohedral::init, x86 (SSE) and scalar builds.
+* inference.npz -- marginals after T iterations, startInference, one
+                   stepInference and klDivergence of seeded small CRFs covering
+                   every compatibility and normalisation type, both builds.
+* examples.npz  -- the reference's example images and annotations
+                   (examples/im*.png, anno*.png) decoded, with the shipped
+                   outputs (out*.png) turned back into label maps, and the
+                   reference's MAP of the generic path of examples/inference.py.
+
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+"""
+from __future__ import annotations
+
+import os
+import struct
+import sys
+import zlib
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+
+REF_ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+
+
+# ---------------------------------------------------------------------------
+# minimal PNG decoder (8-bit RGB and 1/2/4/8-bit palette, non-interlaced)
+# ---------------------------------------------------------------------------
+def read_png(path: str) -> np.ndarray:
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n", path
+    pos, idat, plte = 8, b"", None
+    while pos < len(data):
+        n, typ = struct.unpack(">I4s", data[pos:pos + 8])
+        body = data[pos + 8:pos + 8 + n]
+        if typ == b"IHDR":
+            w, h, bd, ct, _, _, il = struct.unpack(">IIBBBBB", body)
+        elif typ == b"PLTE":
+            plte = np.frombuffer(body, np.uint8).reshape(-1, 3)
+        elif typ == b"IDAT":
+            idat += body
+        pos += 12 + n
+    assert il == 0, "interlaced PNG not supported"
+    raw = zlib.decompress(idat)
+    chans = {2: 3, 3: 1, 0: 1, 6: 4}[ct]
+    bpp = max(1, chans * bd // 8)
+    stride = (w * chans * bd + 7) // 8
+    out = np.zeros((h, stride), np.uint8)
+    prev = np.zeros(stride, np.int32)
+    p = 0
+    for y in range(h):
+        f = raw[p]
+        line = np.frombuffer(raw[p + 1:p + 1 + stride], np.uint8).astype(np.int32)
+        p += 1 + stride
+        cur = np.zeros(stride, np.int32)
+        for x in range(stride):
+            a = cur[x - bpp] if x >= bpp else 0
+            b = prev[x]
+            c = prev[x - bpp] if x >= bpp else 0
+            if f == 0:
+                v = line[x]
+            elif f == 1:
+                v = line[x] + a
+            elif f == 2:
+                v = line[x] + b
+            elif f == 3:
+                v = line[x] + ((a + b) >> 1)
+            else:
+                pa, pb, pc = abs(b - c), abs(a - c), abs(a + b - 2 * c)
+                pr = a if (pa <= pb and pa <= pc) else (b if pb <= pc else c)
+                v = line[x] + pr
+            cur[x] = v & 255
+        out[y] = cur
+        prev = cur
+    if ct == 3:
+        bits = np.unpackbits(out, axis=1)[:, :w * bd].reshape(h, w, bd)
+        idx = (bits * (1 << np.arange(bd - 1, -1, -1))).sum(-1)
+        return plte[idx]
+    return out[:, :w * chans].reshape(h, w, chans)
+
+
+def gen_lattice():
+    rng = np.random.default_rng(20240601)
+    cases = {}
+    specs = [(1, 7), (2, 1), (2, 9), (2, 300), (3, 257), (4, 300), (5, 13), (5, 400), (7, 200), (9, 100),
+             (12, 60), (16, 40)]
+    for ci, (d, N) in enumerate(specs):
+        f = rng.normal(0, 2.5, size=(N, d)).astype(np.float32)
+        cases[f"c{ci}"] = f
+    # integer-valued grid features (rounding ties) and image-like bilateral features
+    cases["grid"] = np.stack(np.meshgrid(np.arange(23, dtype=np.float32), np.arange(19, dtype=np.float32),
+                                         indexing="ij"), -1).reshape(-1, 2) / np.float32(1.0)
+    cases["grid3"] = np.stack(np.meshgrid(np.arange(9, dtype=np.float32), np.arange(7, dtype=np.float32),
+                                          np.arange(5, dtype=np.float32), indexing="ij"), -1).reshape(-1, 3)
+    img = rng.integers(0, 256, size=(17, 21, 3)).astype(np.uint8)
+    cases["bilat"] = O.features_bilateral_2d(img, 5.0, 5.0, 13.0, 13.0, 13.0)
+    out = {}
+    for name, f in cases.items():
+        out[f"{name}/feat"] = f
+        for vname, var in (("sse", O.VARIANT_SSE), ("scalar", O.VARIANT_SCALAR)):
+            lat = O.Lattice(f, "ref", var)
+            out[f"{name}/{vname}/offset"] = lat.offset
+            out[f"{name}/{vname}/rank"] = lat.rank
+            out[f"{name}/{vname}/bary"] = lat.bary
+            out[f"{name}/{vname}/neighbors"] = lat.neighbors
+    np.savez_compressed(os.path.join(HERE, "lattice.npz"), **out)
+    print("lattice.npz", len(cases), "feature sets")
+
+
+def gen_inference():
+    rng = np.random.default_rng(7)
+    out = {}
+    W, H, M = 20, 14, 5
+    N = W * H
+    img = rng.integers(0, 256, size=(H, W, 3)).astype(np.uint8)
+    img[4:11, 6:16] = [200, 40, 40]
+    logits = rng.normal(0, 2, size=(N, M)).astype(np.float32)
+    U = -np.log(np.exp(logits) / np.exp(logits).sum(1, keepdims=True)).astype(np.float32)  # (N, M)
+    fg = O.features_gaussian_2d(W, H, 3.0, 3.0)
+    fb = O.features_bilateral_2d(img, 8.0, 8.0, 13.0, 13.0, 13.0)
+    diag = rng.uniform(-3, 0, size=M).astype(np.float32)
+    mat = rng.uniform(0, 2, size=(M, M)).astype(np.float32)
+    cases = []
+    for ck, c in (("potts", 3.0), ("diag", diag), ("mat", mat)):
+        for nt in range(4):
+            cases.append((f"{ck}_n{nt}", [(fg, c, 1, nt), (fb, 5.0, 1, 3)], 1))
+    cases.append(("fullk", [(fg, 3.0, 2, 3), (fb, 10.0, 2, 3)], 2))
+    out["U"] = U
+    out["img"] = img
+    out["W"], out["H"], out["M"] = W, H, M
+    out["diag"], out["mat"] = diag, mat
+    T = 4
+    for name, terms, _ in cases:
+        for vname, var in (("sse", O.VARIANT_SSE), ("scalar", O.VARIANT_SCALAR)):
+            r = O.RefCRF(N, M, variant=var)
+            r.set_unary(U)
+            for f, c, kt, nt in terms:
+                r.add_pairwise(f, c, kt, nt)
+            Q = r.inference(T)
+            Q0 = r.start()
+            Q1 = Q0.copy()
+            r.step(Q1)
+            out[f"{name}/{vname}/Q"] = Q
+            out["Q0"] = Q0
+            out[f"{name}/{vname}/Q1"] = Q1
+            out[f"{name}/{vname}/kl"] = np.float64(r.kl(Q))
+    # two-label and M=2 path (seqCompute for the messages too)
+    U2 = U[:, :2].copy()
+    for vname, var in (("sse", O.VARIANT_SSE), ("scalar", O.VARIANT_SCALAR)):
+        r = O.RefCRF(N, 2, variant=var)
+        r.set_unary(U2)
+        r.add_pairwise(fb, 4.0, 1, 3)
+        out[f"m2/{vname}/Q"] = r.inference(5)
+    out["U2"] = U2
+    out["T"] = T
+    out["cases"] = np.array([c[0] for c in cases])
+    np.savez_compressed(os.path.join(HERE, "inference.npz"), **out)
+    print("inference.npz", len(cases), "cases")
+
+
+def gen_examples():
+    ex = os.path.join(REF_ROOT, "examples")
+    out = {}
+    for k in ("1", "2", "3"):
+        img = read_png(os.path.join(ex, f"im{k}.png"))[..., :3]
+        anno = read_png(os.path.join(ex, f"anno{k}.png")).astype(np.uint32)
+        outp = read_png(os.path.join(ex, f"out{k}.png")).astype(np.uint32)
+        lbl = anno[..., 0] + (anno[..., 1] << 8) + (anno[..., 2] << 16)
+        colors, labels = np.unique(lbl, return_inverse=True)
+        has_unk = 0 in colors
+        if has_unk:
+            colors = colors[1:]
+        n_labels = len(set(labels.flat)) - int(has_unk)
+        col_out = (outp[..., 0] + (outp[..., 1] << 8) + (outp[..., 2] << 16)).reshape(-1)
+        # shipped output as label indices (-1 where the colour is not a label colour)
+        lut = {int(c): i for i, c in enumerate(colors)}
+        shipped = np.array([lut.get(int(c), -1) for c in col_out], np.int16)
+        H, W = img.shape[:2]
+        # the reference's generic path (examples/inference.py:93-119)
+        from pydensecrf_gb300 import utils as U
+
+        Uu = U.unary_from_labels(labels, n_labels, gt_prob=0.7, zero_unsure=has_unk)
+        fg = U.create_pairwise_gaussian(sdims=(3, 3), shape=img.shape[:2])
+        fb = U.create_pairwise_bilateral(sdims=(80, 80), schan=(13, 13, 13), img=img, chdim=2)
+        r = O.RefCRF(W * H, n_labels)
+        r.set_unary(np.ascontiguousarray(Uu.T))
+        r.add_pairwise(np.ascontiguousarray(fg.T), 3.0, 1, 3)
+        r.add_pairwise(np.ascontiguousarray(fb.T), 10.0, 1, 3)
+        Q = r.inference(5)
+        ref_map = Q.argmax(1).astype(np.int16)
+        print(f"example {k}: reference MAP vs shipped out{k}.png agreement {(ref_map == shipped).mean():.4%}")
+        out[f"{k}/img"] = img.astype(np.uint8)
+        out[f"{k}/labels"] = labels.reshape(H, W).astype(np.int16)
+        out[f"{k}/has_unk"] = np.bool_(has_unk)
+        out[f"{k}/n_labels"] = np.int32(n_labels)
+        out[f"{k}/shipped_map"] = shipped
+        out[f"{k}/ref_map"] = ref_map
+    np.savez_compressed(os.path.join(HERE, "examples.npz"), **out)
+
+
+if __name__ == "__main__":
+    O.build()
+    if not (O.ref_available(O.VARIANT_SSE) and O.ref_available(O.VARIANT_SCALAR)):
+        sys.exit("the reference could not be built from " + REF_ROOT)
+    gen_lattice()
+    gen_inference()
+    gen_examples()

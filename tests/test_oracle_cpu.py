@@ -1,0 +1,123 @@
+"""CPU tests of the oracle: pinned against the reference's golden fixtures and,
+where the reference could be compiled here, against the reference itself."""
+import numpy as np
+import pytest
+
+
+def _bits(a):
+    return np.ascontiguousarray(a).view(np.int32)
+
+
+VARIANTS = (("sse", 0), ("scalar", 1))
+
+
+@pytest.mark.parametrize("vname,var", VARIANTS)
+def test_oracle_lattice_matches_golden(oracle_mod, golden, vname, var):
+    g = golden("lattice.npz")
+    names = sorted({k.split("/")[0] for k in g.files})
+    for name in names:
+        lat = oracle_mod.Lattice(g[f"{name}/feat"], "oracle", var)
+        assert np.array_equal(lat.offset, g[f"{name}/{vname}/offset"]), name
+        assert np.array_equal(lat.rank, g[f"{name}/{vname}/rank"]), name
+        assert np.array_equal(_bits(lat.bary), _bits(g[f"{name}/{vname}/bary"])), name
+        assert np.array_equal(lat.neighbors, g[f"{name}/{vname}/neighbors"]), name
+
+
+@pytest.mark.parametrize("vname,var", VARIANTS)
+def test_oracle_inference_matches_golden(oracle_mod, golden, vname, var):
+    g = golden("inference.npz")
+    O = oracle_mod
+    W, H, M, T = int(g["W"]), int(g["H"]), int(g["M"]), int(g["T"])
+    N = W * H
+    U, img = g["U"], g["img"]
+    fg = O.features_gaussian_2d(W, H, 3.0, 3.0)
+    fb = O.features_bilateral_2d(img, 8.0, 8.0, 13.0, 13.0, 13.0)
+    compat = {"potts": 3.0, "diag": g["diag"], "mat": g["mat"]}
+    for name in g["cases"]:
+        name = str(name)
+        c = O.OracleCRF(N, M, var)
+        c.set_unary(U)
+        if name == "fullk":
+            c.add_pairwise(fg, 3.0, 2, 3)
+            c.add_pairwise(fb, 10.0, 2, 3)
+        else:
+            ck, nt = name.split("_n")
+            c.add_pairwise(fg, compat[ck], 1, int(nt))
+            c.add_pairwise(fb, 5.0, 1, 3)
+        Q = c.inference(T)
+        # tolerance 1e-5: the only differences are libm expf vs Eigen's exp and sum order
+        assert np.abs(Q - g[f"{name}/{vname}/Q"]).max() < 1e-5, name
+        Q0 = c.start()
+        assert np.abs(Q0 - g["Q0"]).max() < 1e-6
+        c.step(Q0)
+        assert np.abs(Q0 - g[f"{name}/{vname}/Q1"]).max() < 1e-5, name
+        kl_ref = float(g[f"{name}/{vname}/kl"])
+        assert abs(c.kl(g[f"{name}/{vname}/Q"]) - kl_ref) <= 1e-5 * max(1.0, abs(kl_ref)), name
+
+
+def test_oracle_two_labels_golden(oracle_mod, golden):
+    g = golden("inference.npz")
+    O = oracle_mod
+    W, H = int(g["W"]), int(g["H"])
+    fb = O.features_bilateral_2d(g["img"], 8.0, 8.0, 13.0, 13.0, 13.0)
+    for vname, var in VARIANTS:
+        c = O.OracleCRF(W * H, 2, var)
+        c.set_unary(g["U2"])
+        c.add_pairwise(fb, 4.0, 1, 3)
+        assert np.abs(c.inference(5) - g[f"m2/{vname}/Q"]).max() < 1e-5
+
+
+def test_oracle_examples_golden(oracle_mod, golden):
+    """The reference's own example outputs (examples/out{1,2,3}.png) via the generic path."""
+    from pydensecrf_gb300 import utils as U
+    g = golden("examples.npz")
+    O = oracle_mod
+    for k in ("1", "2", "3"):
+        img, labels = g[f"{k}/img"], g[f"{k}/labels"]
+        n_labels, has_unk = int(g[f"{k}/n_labels"]), bool(g[f"{k}/has_unk"])
+        H, W = labels.shape
+        Uu = U.unary_from_labels(labels, n_labels, gt_prob=0.7, zero_unsure=has_unk)
+        fg = U.create_pairwise_gaussian(sdims=(3, 3), shape=(H, W))
+        fb = U.create_pairwise_bilateral(sdims=(80, 80), schan=(13, 13, 13), img=img, chdim=2)
+        c = O.OracleCRF(W * H, n_labels)
+        c.set_unary(np.ascontiguousarray(Uu.T))
+        c.add_pairwise(np.ascontiguousarray(fg.T), 3.0)
+        c.add_pairwise(np.ascontiguousarray(fb.T), 10.0)
+        m = c.inference(5).argmax(1)
+        assert (m == g[f"{k}/shipped_map"]).mean() == 1.0, k
+
+
+def test_oracle_fp64_close(oracle_mod):
+    """The float restatement stays within 1e-5 of the FP64 mean-field on a small case."""
+    O = oracle_mod
+    rng = np.random.default_rng(3)
+    N, M = 500, 4
+    f = rng.normal(0, 1.5, size=(N, 3)).astype(np.float32)
+    U = (rng.random((N, M)) * 3).astype(np.float32)
+    c = O.OracleCRF(N, M)
+    c.set_unary(U)
+    c.add_pairwise(f, 2.0)
+    assert np.abs(c.inference(5) - c.inference_f64(5)).max() < 1e-5
+
+
+requires_ref = pytest.mark.skipif("not __import__('oracle').ref_available()",
+                                  reason="the reference was not compiled on this machine")
+
+
+@requires_ref
+@pytest.mark.parametrize("vname,var", VARIANTS)
+def test_oracle_vs_reference_random(oracle_mod, vname, var):
+    O = oracle_mod
+    if not O.ref_available(var):
+        pytest.skip("variant not built")
+    rng = np.random.default_rng(11 + var)
+    for d in (1, 2, 3, 5, 6, 8):
+        for N in (1, 3, 4, 5, 77, 640):
+            f = rng.normal(0, 3, size=(N, d)).astype(np.float32)
+            a, b = O.Lattice(f, "oracle", var), O.Lattice(f, "ref", var)
+            assert a.L == b.L
+            assert np.array_equal(a.offset, b.offset) and np.array_equal(a.rank, b.rank)
+            assert np.array_equal(_bits(a.bary), _bits(b.bary)) and np.array_equal(a.neighbors, b.neighbors)
+            v = rng.random((N, 3)).astype(np.float32)
+            for rev in (False, True):
+                assert np.array_equal(_bits(a.compute(v, rev)), _bits(b.compute(v, rev)))
