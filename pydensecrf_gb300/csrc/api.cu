@@ -295,6 +295,9 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.tile_pbeg = T.lat.tile_pbeg;
     t.mem_pt = T.lat.mem_pt;
     t.mem_w = T.lat.mem_w;
+    t.part_v = T.lat.part_v;
+    t.tl_loc = T.lat.tl_loc;
+    t.tl_w = T.lat.tl_w;
     return t;
 }
 

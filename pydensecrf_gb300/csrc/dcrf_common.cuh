@@ -76,6 +76,9 @@ struct TermDev {
     const int *tile_pbeg;  // [ntiles+1] partial range of tile t
     const uint16_t *mem_pt;  // [E] tile-local point of member e
     const float *mem_w;      // [E] splat weight of member e
+    const int *part_v;       // [P] vertex of partial p
+    const uint16_t *tl_loc;  // [ntiles][d+1][SPLAT_TILE] corner -> index among the tile's partials
+    const float *tl_w;       // [ntiles][d+1][SPLAT_TILE] corner barycentric weight
 };
 
 struct TermSet {

@@ -16,9 +16,11 @@
 //   4. offsets    corner -> vertex id (offset_), vertex -> key.
 //   5. neighbours thread per (axis, vertex): look up key -1/+1 with +d/-d on
 //                 the axis.
-//   6. tiles      per tile of SPLAT_TILE consecutive points, the corners
-//                 grouped by vertex in point order (block bitonic sort): the
-//                 member lists of the in-kernel splat.
+//   6. tiles      per splat tile (a set of up to SPLAT_TILE points), the
+//                 corners grouped by vertex in point order (block bitonic
+//                 sort): the tile's distinct vertices ("partials"), the member
+//                 lists of the in-kernel splat, and per corner the index of its
+//                 vertex among the tile's partials (the tile-local slice table).
 //   7. reduce     stable radix sort of the tiles' partials by vertex: the
 //                 order in which a vertex's partial sums are added.
 // Bounded probing everywhere: a full table sets DCRF_ERR_HASH_FULL and the
@@ -399,7 +401,8 @@ __global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long
                                                         const int *__restrict__ tile_vbase,
                                                         const uint32_t *__restrict__ tile_pbeg,
                                                         int *__restrict__ part_v, int *__restrict__ part_mbeg,
-                                                        uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w) {
+                                                        uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
+                                                        uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w) {
     __shared__ uint32_t s_warp[8];
     const int t = blockIdx.x;
     const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
@@ -421,18 +424,23 @@ __global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long
     __syncthreads();
     uint32_t before = 0;
     for (int w = 0; w < warp; w++) before += s_warp[w];
-    uint32_t run = tile_pbeg[t] + before + x - cnt;
+    const uint32_t pbeg = tile_pbeg[t];
+    uint32_t run = pbeg + before + x - cnt;
     for (int idx = i0; idx < i1; idx++) {
         unsigned long long s = sorted[base + idx];
         int el = (int)(s & 0xFFFFull);
         int li = el / (D + 1), r = el - li * (D + 1);
+        const float w = bary[(size_t)r * N + slot_pt[(size_t)t * SPLAT_TILE + li]];
         mem_pt[base + idx] = (uint16_t)li;
-        mem_w[base + idx] = bary[(size_t)r * N + slot_pt[(size_t)t * SPLAT_TILE + li]];
+        mem_w[base + idx] = w;
         if (idx == 0 || (s >> 16) != (sorted[base + idx - 1] >> 16)) {
             part_v[run] = (int)(s >> 16);
             part_mbeg[run] = (int)(base + idx);
             run++;
         }
+        const size_t tl = ((size_t)t * (D + 1) + r) * SPLAT_TILE + li;
+        tl_loc[tl] = (uint16_t)(run - 1 - pbeg);
+        tl_w[tl] = w;
     }
 }
 
@@ -592,10 +600,17 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     L.tile_pbeg = dalloc<int>(L.ntiles + 1, s, &acc);
     L.mem_pt = dalloc<uint16_t>(Ereal, s, &acc);
     L.mem_w = dalloc<float>(Ereal, s, &acc);
+    const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
+    L.tl_loc = dalloc<uint16_t>(ntl, s, &acc);
+    L.tl_w = dalloc<float>(ntl, s, &acc);
     unsigned long long *sorted = tmp.get<unsigned long long>(Ereal);
     uint32_t *tile_nv = tmp.get<uint32_t>(L.ntiles + 1);
     uint32_t *d_P = tmp.get<uint32_t>(4);
-    if (!L.tile_pbeg || !L.mem_pt || !L.mem_w || tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
+    if (!L.tile_pbeg || !L.mem_pt || !L.mem_w || !L.tl_loc || !L.tl_w || tmp.failed)
+        return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
+    // empty slots: local index 0, weight 0
+    cudaMemsetAsync(L.tl_loc, 0, ntl * sizeof(uint16_t), s);
+    cudaMemsetAsync(L.tl_w, 0, ntl * sizeof(float), s);
     int n2max = 1;
     while (n2max < SPLAT_TILE * (D + 1)) n2max <<= 1;
     size_t smem = (size_t)n2max * sizeof(unsigned long long);
@@ -621,7 +636,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     if (L.ntiles > 0)
         DCRF_LAUNCH(tile_fill_kernel<D><<<L.ntiles, 256, 0, s>>>(sorted, L.bary, N, tm.slot_pt, tm.tile_vbase,
                                                      (const uint32_t *)L.tile_pbeg, L.part_v, L.part_mbeg, L.mem_pt,
-                                                     L.mem_w));
+                                                     L.mem_w, L.tl_loc, L.tl_w));
     DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.part_mbeg + L.P, (int)Ereal));
     // ---- reduce lists: partials grouped by vertex, in tile order ------------
     {
@@ -666,8 +681,8 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
 }  // namespace
 
 void lattice_free(LatticeDev *L, cudaStream_t s) {
-    void *ps[] = {L->off, L->bary, L->wslice, L->rank, L->nbr, L->vkeys, L->part_v,
-                  L->part_mbeg, L->tile_pbeg, L->mem_pt, L->mem_w, L->red_beg, L->red_list};
+    void *ps[] = {L->off,       L->bary,   L->wslice,  L->rank,    L->nbr,      L->vkeys,  L->part_v, L->part_mbeg,
+                  L->tile_pbeg, L->mem_pt, L->mem_w,   L->red_beg, L->red_list, L->tl_loc, L->tl_w};
     for (void *p : ps)
         if (p) cudaFreeAsync(p, s);
     *L = LatticeDev{};

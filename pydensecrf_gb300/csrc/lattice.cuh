@@ -26,6 +26,9 @@ struct LatticeDev {
     float *mem_w = nullptr;      // [E]
     int *red_beg = nullptr;      // [L+1]
     int *red_list = nullptr;     // [P]
+    // tile-ordered slice tables: corner r of slot li of tile t at (t*(d+1)+r)*SPLAT_TILE+li
+    uint16_t *tl_loc = nullptr;  // index of the corner's vertex among the tile's partials
+    float *tl_w = nullptr;       // the corner's barycentric weight
     size_t bytes = 0;
 };
 

@@ -61,176 +61,186 @@ __device__ __forceinline__ void load_row(const float *__restrict__ row, float (&
     }
 }
 
-// out = compatibility(acc) for the first M labels
+// x -= compatibility(acc) (mean-field update), or, with kl_mode, kl += sum q * compatibility(acc)
+// where x holds q.  Potts: -w acc; Diagonal: v * acc; Matrix: W acc (labelcompatibility.cpp:46-48,66-68,82-84).
 template <int MP>
-__device__ __forceinline__ void apply_compat(const TermDev &T, const float (&acc)[MP], float (&c)[MP], int M) {
+__device__ __forceinline__ void fold_compat(const TermDev &T, const float (&acc)[MP], float (&x)[MP], int M,
+                                            bool kl_mode, double &kl) {
     if (T.ckind == DCRF_COMPAT_POTTS) {
         const float nw = -T.potts_w;
 #pragma unroll
-        for (int m = 0; m < MP; m++) c[m] = fmul(nw, acc[m]);
+        for (int m = 0; m < MP; m++) {
+            const float c = fmul(nw, acc[m]);
+            if (kl_mode) {
+                if (m < M) kl += (double)fmul(x[m], c);
+            } else {
+                x[m] = fsub(x[m], c);
+            }
+        }
     } else if (T.ckind == DCRF_COMPAT_DIAGONAL) {
 #pragma unroll
-        for (int m = 0; m < MP; m++) c[m] = m < M ? fmul(__ldg(T.compat + m), acc[m]) : 0.f;
+        for (int m = 0; m < MP; m++)
+            if (m < M) {
+                const float c = fmul(__ldg(T.compat + m), acc[m]);
+                if (kl_mode)
+                    kl += (double)fmul(x[m], c);
+                else
+                    x[m] = fsub(x[m], c);
+            }
     } else {
 #pragma unroll
-        for (int m = 0; m < MP; m++) {
-            float s = 0.f;
+        for (int m = 0; m < MP; m++)
             if (m < M) {
                 const float *row = T.compat + (size_t)m * M;
+                float c = 0.f;
 #pragma unroll
                 for (int k = 0; k < MP; k++)
-                    if (k < M) s = fadd(s, fmul(__ldg(row + k), acc[k]));
+                    if (k < M) c = fadd(c, fmul(__ldg(row + k), acc[k]));
+                if (kl_mode)
+                    kl += (double)fmul(x[m], c);
+                else
+                    x[m] = fsub(x[m], c);
             }
-            c[m] = s;
+    }
+}
+
+// Shared-memory budget of the point pass: a union of the vertex-row stage
+// (slice phase) and the q rows + member lists (splat phase).
+template <int MP>
+struct PPSmem {
+    static constexpr int MCAP = SPLAT_TILE * 6;  // staged members (corners of d <= 5)
+    static constexpr int SPLAT_BYTES = SPLAT_TILE * MP * 4 + MCAP * 6 + (MCAP + 1) * 4;
+    static constexpr int SV_ROWS = (SPLAT_BYTES / (MP * 4)) < 128 ? 128 : (SPLAT_BYTES / (MP * 4));
+    static constexpr int BYTES = (SV_ROWS * MP * 4 > SPLAT_BYTES ? SV_ROWS * MP * 4 : SPLAT_BYTES);
+};
+
+// Slice of term T for the calling thread's point (tile-local tables), from the
+// staged rows when the tile's vertex rows fit in shared memory.
+template <int MP>
+__device__ __forceinline__ void slice_tiled(const TermDev &T, int t, int li, bool staged, int pb,
+                                            const float *__restrict__ sV, float (&acc)[MP]) {
+#pragma unroll
+    for (int m = 0; m < MP; m++) acc[m] = 0.f;
+    const size_t tbase = (size_t)t * (T.d + 1) * SPLAT_TILE + li;
+    for (int r = 0; r <= T.d; r++) {
+        const int loc = T.tl_loc[tbase + (size_t)r * SPLAT_TILE];
+        const float b = T.tl_w[tbase + (size_t)r * SPLAT_TILE];
+        float v[MP];
+        if (staged) {
+            if constexpr (MP % 4 == 0) {
+                const float4 *r4 = reinterpret_cast<const float4 *>(sV + loc * MP);
+#pragma unroll
+                for (int c = 0; c < MP / 4; c++) {
+                    float4 x = r4[c];
+                    v[4 * c] = x.x, v[4 * c + 1] = x.y, v[4 * c + 2] = x.z, v[4 * c + 3] = x.w;
+                }
+            } else {
+#pragma unroll
+                for (int m = 0; m < MP; m++) v[m] = sV[loc * MP + m];
+            }
+        } else {
+            load_row<MP>(T.V + (size_t)(T.part_v[pb + loc] + 1) * MP, v);
+        }
+        if (T.seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
+#pragma unroll
+            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(b, v[m]), T.alpha));
+        } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
+            const float w = fmul(b, T.alpha);
+#pragma unroll
+            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
         }
     }
 }
 
 template <int MP>
-__global__ void __launch_bounds__(SPLAT_TILE) pointpass_kernel(const __grid_constant__ PPArgs a) {
-    __shared__ __align__(16) float sQ[SPLAT_TILE * MP];
+__global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kernel(const __grid_constant__ PPArgs a) {
+    using SM = PPSmem<MP>;
+    __shared__ __align__(16) unsigned char smem[SM::BYTES];
     __shared__ double sKL[SPLAT_TILE / 32];
+    float *sV = reinterpret_cast<float *>(smem);
+    float *sQ = reinterpret_cast<float *>(smem);
+    float *sMw = reinterpret_cast<float *>(smem + SPLAT_TILE * MP * 4);
+    int *sPmb = reinterpret_cast<int *>(smem + SPLAT_TILE * MP * 4 + SM::MCAP * 4);
+    uint16_t *sMpt = reinterpret_cast<uint16_t *>(smem + SPLAT_TILE * MP * 4 + SM::MCAP * 4 + (SM::MCAP + 1) * 4);
+
     const int t = blockIdx.x;
     const int li = threadIdx.x;
     const int i = a.slot_pt[(size_t)t * SPLAT_TILE + li];
     const bool valid = i >= 0;
     const int N = a.N, M = a.M, mode = a.mode;
-    float q[MP];
+    // x: the logits of the update, or the given marginals (LOAD_Q / ONES); q after the softmax
+    float x[MP];
 #pragma unroll
-    for (int m = 0; m < MP; m++) q[m] = 0.f;
+    for (int m = 0; m < MP; m++) x[m] = 0.f;
     double kl = 0.0;
-    if (valid) {
-        if (mode & PP_NORM) {
-            // value size 1, seqCompute slice: out += (w * v) * alpha (permutohedral.cpp:513-521)
-            for (int k = 0; k < a.ts.n; k++) {
-                const TermDev &T = a.ts.t[k];
-                float n = 0.f;
-                for (int r = 0; r <= T.d; r++) {
-                    int o = T.off[(size_t)r * N + i] + 1;
-                    float w = T.bary[(size_t)r * N + i];
-                    n = fadd(n, fmul(fmul(w, __ldg(T.V + o)), T.alpha));
-                }
-                float out;
-                if (a.ntype[k] == DCRF_NORMALIZE_SYMMETRIC)  // pairwise.cpp:54-57
-                    out = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn((double)n, 1e-20))));
-                else if (a.ntype[k] == DCRF_NO_NORMALIZATION)
-                    out = n;  // raw K*1; the host derives the mean (pairwise.cpp:46-53)
-                else  // pairwise.cpp:58-61
-                    out = __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
-                a.norm_out[k][i] = out;
-            }
-        } else if (mode & PP_FILTER) {
-            const TermDev &T = a.ts.t[0];
-            float acc[MP];
-#pragma unroll
-            for (int m = 0; m < MP; m++) acc[m] = 0.f;
-            for (int r = 0; r <= T.d; r++) {
-                const int o = T.off[(size_t)r * N + i] + 1;
-                float v[MP];
-                load_row<MP>(T.V + (size_t)o * MP, v);
-                if (T.seq) {
-                    const float w = T.bary[(size_t)r * N + i];
-#pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(w, v[m]), T.alpha));
-                } else {
-                    const float w = T.wslice[(size_t)r * N + i];
-#pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
-                }
-            }
+    const bool given = (mode & (PP_LOAD_Q | PP_ONES)) != 0;
+    if (mode & PP_ONES) {
+        if (valid) x[0] = 1.f;
+    } else if (mode & PP_LOAD_Q) {
+        if (valid) {
 #pragma unroll
             for (int m = 0; m < MP; m++)
-                if (m < M) a.Qout[(size_t)m * N + i] = acc[m];
-        } else if (mode & PP_ONES) {
-            q[0] = 1.f;
-        } else if (mode & PP_LOAD_Q) {
-#pragma unroll
-            for (int m = 0; m < MP; m++)
-                if (m < M) q[m] = a.Qin[(size_t)m * N + i];
-        } else {
-            float lg[MP];
-#pragma unroll
-            for (int m = 0; m < MP; m++) lg[m] = (m < M && a.U) ? -a.U[(size_t)m * N + i] : 0.f;
-            if (mode & PP_MSG) {
-                for (int k = 0; k < a.ts.n; k++) {
-                    const TermDev &T = a.ts.t[k];
-                    float acc[MP];
-#pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = 0.f;
-                    for (int r = 0; r <= T.d; r++) {
-                        const int o = T.off[(size_t)r * N + i] + 1;
-                        float v[MP];
-                        load_row<MP>(T.V + (size_t)o * MP, v);
-                        if (T.seq) {
-                            const float w = T.bary[(size_t)r * N + i];
-#pragma unroll
-                            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(w, v[m]), T.alpha));
-                        } else {
-                            const float w = T.wslice[(size_t)r * N + i];
-#pragma unroll
-                            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
-                        }
-                    }
-                    if (T.post_norm) {
-                        const float nn = T.norm[i];
-#pragma unroll
-                        for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
-                    }
-                    float c[MP];
-                    apply_compat<MP>(T, acc, c, M);
-#pragma unroll
-                    for (int m = 0; m < MP; m++) lg[m] = fsub(lg[m], c[m]);
-                }
-            }
-            // softmax (densecrf.cpp:98-106)
-            float mx = lg[0];
-#pragma unroll
-            for (int m = 1; m < MP; m++)
-                if (m < M) mx = fmaxf(mx, lg[m]);
-            float s = 0.f;
-#pragma unroll
-            for (int m = 0; m < MP; m++)
-                if (m < M) {
-                    q[m] = expf(fsub(lg[m], mx));
-                    s = fadd(s, q[m]);
-                }
-#pragma unroll
-            for (int m = 0; m < MP; m++)
-                if (m < M) q[m] = __fdiv_rn(q[m], s);
+                if (m < M) x[m] = a.Qin[(size_t)m * N + i];
         }
-        if ((mode & PP_KL) && (mode & PP_MSG)) {
-            // pairwise part of klDivergence (densecrf.cpp:229-233): sum Q * compat(K Q)
-            for (int k = 0; k < a.ts.n; k++) {
-                const TermDev &T = a.ts.t[k];
-                float acc[MP];
+    } else {
 #pragma unroll
-                for (int m = 0; m < MP; m++) acc[m] = 0.f;
-                for (int r = 0; r <= T.d; r++) {
-                    const int o = T.off[(size_t)r * N + i] + 1;
-                    float v[MP];
-                    load_row<MP>(T.V + (size_t)o * MP, v);
-                    if (T.seq) {
-                        const float w = T.bary[(size_t)r * N + i];
-#pragma unroll
-                        for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(w, v[m]), T.alpha));
-                    } else {
-                        const float w = T.wslice[(size_t)r * N + i];
-#pragma unroll
-                        for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
+        for (int m = 0; m < MP; m++) x[m] = (valid && m < M && a.U) ? -a.U[(size_t)m * N + i] : 0.f;
+    }
+    if (mode & PP_MSG) {
+        for (int k = 0; k < a.ts.n; k++) {
+            const TermDev &T = a.ts.t[k];
+            const int pb = T.tile_pbeg[t], np = T.tile_pbeg[t + 1] - pb;
+            const bool staged = np <= SM::SV_ROWS;
+            if (staged) {
+                // stage the tile's vertex rows: row p = V[part_v[pb + p] + 1]
+                if constexpr (MP % 4 == 0) {
+                    constexpr int C4 = MP / 4;
+                    float4 *d4 = reinterpret_cast<float4 *>(sV);
+                    for (int x = li; x < np * C4; x += SPLAT_TILE) {
+                        const int p = x / C4, c = x - p * C4;
+                        d4[x] = __ldg(reinterpret_cast<const float4 *>(T.V + (size_t)(T.part_v[pb + p] + 1) * MP) + c);
+                    }
+                } else {
+                    for (int x = li; x < np * MP; x += SPLAT_TILE) {
+                        const int p = x / MP, c = x - p * MP;
+                        sV[x] = __ldg(T.V + (size_t)(T.part_v[pb + p] + 1) * MP + c);
                     }
                 }
+            }
+            __syncthreads();
+            if (valid) {
+                float acc[MP];
+                slice_tiled<MP>(T, t, li, staged, pb, sV, acc);
                 if (T.post_norm) {
                     const float nn = T.norm[i];
 #pragma unroll
                     for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
                 }
-                float c[MP];
-                apply_compat<MP>(T, acc, c, M);
-#pragma unroll
-                for (int m = 0; m < MP; m++)
-                    if (m < M) kl += (double)fmul(q[m], c[m]);
+                // with given marginals this is the pairwise part of klDivergence
+                // (densecrf.cpp:229-233): sum Q * compat(K Q)
+                fold_compat<MP>(T, acc, x, M, given, kl);
             }
+            __syncthreads();
         }
+    }
+    if (valid && !given) {
+        // softmax (densecrf.cpp:98-106)
+        float mx = x[0];
+#pragma unroll
+        for (int m = 1; m < MP; m++)
+            if (m < M) mx = fmaxf(mx, x[m]);
+        float s = 0.f;
+#pragma unroll
+        for (int m = 0; m < MP; m++)
+            if (m < M) {
+                x[m] = expf(fsub(x[m], mx));
+                s = fadd(s, x[m]);
+            }
+#pragma unroll
+        for (int m = 0; m < MP; m++) x[m] = m < M ? __fdiv_rn(x[m], s) : 0.f;
+    }
+    float (&q)[MP] = x;
+    if (valid) {
         if (mode & PP_KL) {
             // entropy and unary parts (densecrf.cpp:216-226); log() there is the double overload
 #pragma unroll
@@ -277,19 +287,37 @@ __global__ void __launch_bounds__(SPLAT_TILE) pointpass_kernel(const __grid_cons
             const float nn = (valid && T.pre_norm) ? T.norm[i] : 1.f;
 #pragma unroll
             for (int m = 0; m < MP; m++) sQ[li * MP + m] = T.pre_norm ? fmul(q[m], nn) : q[m];
-            __syncthreads();
             const int pb = T.tile_pbeg[t], pe = T.tile_pbeg[t + 1];
+            const int mbase = T.part_mbeg[pb], nmem = T.part_mbeg[pe] - mbase;
+            const bool staged = nmem <= SM::MCAP;
+            if (staged) {
+                for (int x = li; x < nmem; x += SPLAT_TILE) {
+                    sMpt[x] = T.mem_pt[mbase + x];
+                    sMw[x] = T.mem_w[mbase + x];
+                }
+                for (int x = li; x <= pe - pb; x += SPLAT_TILE) sPmb[x] = T.part_mbeg[pb + x] - mbase;
+            }
+            __syncthreads();
             for (int p = pb + gid; p < pe; p += NG) {
-                const int mb = T.part_mbeg[p], me = T.part_mbeg[p + 1];
                 float acc[CH];
 #pragma unroll
                 for (int c = 0; c < CH; c++) acc[c] = 0.f;
-                for (int e = mb; e < me; e++) {
-                    const int pt = T.mem_pt[e];
-                    const float w = T.mem_w[e];
-                    const float *row = sQ + pt * MP + lg_;
+                if (staged) {
+                    const int mb = sPmb[p - pb], me = sPmb[p - pb + 1];
+                    for (int e = mb; e < me; e++) {
+                        const float w = sMw[e];
+                        const float *row = sQ + sMpt[e] * MP + lg_;
 #pragma unroll
-                    for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], fmul(w, row[c * G]));
+                        for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], fmul(w, row[c * G]));
+                    }
+                } else {
+                    const int mb = T.part_mbeg[p], me = T.part_mbeg[p + 1];
+                    for (int e = mb; e < me; e++) {
+                        const float w = T.mem_w[e];
+                        const float *row = sQ + T.mem_pt[e] * MP + lg_;
+#pragma unroll
+                        for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], fmul(w, row[c * G]));
+                    }
                 }
                 float *dst = T.partial + (size_t)p * MP + lg_;
 #pragma unroll
@@ -298,6 +326,59 @@ __global__ void __launch_bounds__(SPLAT_TILE) pointpass_kernel(const __grid_cons
             __syncthreads();
         }
     }
+}
+
+// Value-size-1 normalisation slice and raw lattice filter (point-order gather;
+// used off the iteration loop).
+template <int MP>
+__global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPArgs a) {
+    const int t = blockIdx.x;
+    const int i = a.slot_pt[(size_t)t * SPLAT_TILE + threadIdx.x];
+    if (i < 0) return;
+    const int N = a.N, M = a.M;
+    if (a.mode & PP_NORM) {
+        // value size 1, seqCompute slice: out += (w * v) * alpha (permutohedral.cpp:513-521)
+        for (int k = 0; k < a.ts.n; k++) {
+            const TermDev &T = a.ts.t[k];
+            float n = 0.f;
+            for (int r = 0; r <= T.d; r++) {
+                int o = T.off[(size_t)r * N + i] + 1;
+                float w = T.bary[(size_t)r * N + i];
+                n = fadd(n, fmul(fmul(w, __ldg(T.V + o)), T.alpha));
+            }
+            float out;
+            if (a.ntype[k] == DCRF_NORMALIZE_SYMMETRIC)  // pairwise.cpp:54-57
+                out = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn((double)n, 1e-20))));
+            else if (a.ntype[k] == DCRF_NO_NORMALIZATION)
+                out = n;  // raw K*1; the host derives the mean (pairwise.cpp:46-53)
+            else  // pairwise.cpp:58-61
+                out = __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
+            a.norm_out[k][i] = out;
+        }
+        return;
+    }
+    // PP_FILTER: raw K v of term 0
+    const TermDev &T = a.ts.t[0];
+    float acc[MP];
+#pragma unroll
+    for (int m = 0; m < MP; m++) acc[m] = 0.f;
+    for (int r = 0; r <= T.d; r++) {
+        const int o = T.off[(size_t)r * N + i] + 1;
+        float v[MP];
+        load_row<MP>(T.V + (size_t)o * MP, v);
+        if (T.seq) {
+            const float w = T.bary[(size_t)r * N + i];
+#pragma unroll
+            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(w, v[m]), T.alpha));
+        } else {
+            const float w = T.wslice[(size_t)r * N + i];
+#pragma unroll
+            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < MP; m++)
+        if (m < M) a.Qout[(size_t)m * N + i] = acc[m];
 }
 
 template <int MP>
@@ -314,10 +395,25 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
     float acc[CH];
 #pragma unroll
     for (int c = 0; c < CH; c++) acc[c] = 0.f;
-    for (int s = s0; s < s1; s++) {
-        const float *row = T.partial + (size_t)T.red_list[s] * MP + lg_;
+    // the group's lanes fetch G partial indices at a time; the rows are then
+    // read back to back (independent loads), added in list order
+    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    for (int b = s0; b < s1; b += G) {
+        const int mine = (b + lg_ < s1) ? T.red_list[b + lg_] : 0;
+        const int cnt = min(G, s1 - b);
+        float rowv[G][CH];
 #pragma unroll
-        for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], row[c * G]);
+        for (int j = 0; j < G; j++) {
+            const int p = __shfl_sync(gmask, mine, j, G);
+#pragma unroll
+            for (int c = 0; c < CH; c++) rowv[j][c] = j < cnt ? T.partial[(size_t)p * MP + lg_ + c * G] : 0.f;
+        }
+#pragma unroll
+        for (int j = 0; j < G; j++)
+            if (j < cnt) {
+#pragma unroll
+                for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], rowv[j][c]);
+            }
     }
     float *dst = T.V + (size_t)(v + 1) * MP + lg_;
 #pragma unroll
@@ -435,7 +531,11 @@ __global__ void argmax_kernel(const float *__restrict__ Q, int M, int N, int16_t
 // ---------------------------------------------------------------------------
 template <int MP>
 static cudaError_t pp_launch(const PPArgs &a, cudaStream_t s) {
-    if (a.ntiles > 0) DCRF_LAUNCH(pointpass_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
+    if (a.ntiles <= 0) return cudaSuccess;
+    if (a.mode & (PP_NORM | PP_FILTER))
+        DCRF_LAUNCH(slice_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
+    else
+        DCRF_LAUNCH(pointpass_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
     return cudaGetLastError();
 }
 
