@@ -80,9 +80,10 @@ struct Term {
     LatticeDev lat;
     float *feat = nullptr;  // [d][N] features as given (kernel parameters at identity)
     float *norm = nullptr;  // [N]
-    float *V[2] = {nullptr, nullptr};
-    float *partial = nullptr;
+    float *V[2] = {nullptr, nullptr};  // [L+1][MP] blurred values, vertex order (ping-pong)
+    float *pv = nullptr;               // [P][MP] blurred values in partial order / splat partials
     float *compat = nullptr;  // device compat (Diagonal M / Matrix M*M symmetrised)
+    float *mem_wn = nullptr;  // splat member weights times the members' norm (forward pre-normalisation)
     std::vector<float> compat_h;
 };
 
@@ -94,10 +95,13 @@ struct dcrf_crf {
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
     DevStatus *status = nullptr;
-    float *U = nullptr;
+    float *U = nullptr;  // [M][nslots] unary, slot-major
     bool has_unary = false;
-    float *Q = nullptr;    // [M][N] device working marginals
-    float *tmp = nullptr;  // [N*M] layout conversions
+    float *Q = nullptr;      // [M][nslots] working marginals, slot-major
+    float *tmp = nullptr;    // [M][nslots] scratch of the raw-filter path
+    float *stage = nullptr;  // [N*M] user-layout staging of host copies
+    int nslots = 0;
+    int *pt_slot = nullptr;  // [N] slot of each point
     int16_t *map = nullptr;
     double *kl_part = nullptr;
     int ntiles = 0;
@@ -105,6 +109,11 @@ struct dcrf_crf {
     int *tile_vbase = nullptr;
     float hash_load = 2.0f;
     std::vector<Term> terms;
+    // CUDA graph of the last inference launch sequence (re-used through
+    // cudaGraphExecUpdate while its topology stays the same)
+    bool use_graphs = true;
+    cudaStream_t capture = nullptr;
+    cudaGraphExec_t gexec = nullptr;
     // profiling: events bracketing launches, by kernel class
     bool profiling = false;
     struct Mark {
@@ -156,6 +165,14 @@ void release_marks(dcrf_crf *h) {
     h->marks.clear();
 }
 
+// Sets kernel attributes (dynamic shared memory opt-in) outside any capture.
+void prepare_kernels() {
+    static bool done = false;
+    if (done) return;
+    prepare_pointpass_kernels();
+    done = true;
+}
+
 int check_handle(dcrf_crf *h) {
     if (!h) return set_err(DCRF_ERR_INVALID_ARG, "null handle");
     cudaError_t e = cudaSetDevice(h->device);
@@ -193,11 +210,17 @@ int build_tiles(dcrf_crf *h) {
         for (int s = 0; s < h->N; s++) slot[s] = s;
         for (int t = 0; t < h->ntiles; t++) vbase[t + 1] = std::min(h->N, (t + 1) * SPLAT_TILE);
     }
+    h->nslots = h->ntiles * SPLAT_TILE;
+    std::vector<int> inv(h->N, 0);
+    for (size_t sl = 0; sl < slot.size(); sl++)
+        if (slot[sl] >= 0) inv[slot[sl]] = (int)sl;
     int rc;
     if ((rc = dev_alloc(&h->slot_pt, slot.size() + 1))) return rc;
+    if ((rc = dev_alloc(&h->pt_slot, (size_t)h->N + 1))) return rc;
     if ((rc = dev_alloc(&h->tile_vbase, vbase.size() + 1))) return rc;
     if ((rc = dev_alloc(&h->kl_part, (size_t)h->ntiles + 1))) return rc;
     CU(cudaMemcpy(h->slot_pt, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(h->pt_slot, inv.data(), inv.size() * sizeof(int), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(h->tile_vbase, vbase.data(), vbase.size() * sizeof(int), cudaMemcpyHostToDevice));
     return DCRF_OK;
 }
@@ -226,51 +249,53 @@ int create(int N, int M, int W, int H, dcrf_crf **out) {
         dcrf_destroy(h);
         return code;
     };
-    if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess)
+    if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->capture, cudaStreamNonBlocking) != cudaSuccess)
         return fail(set_err(DCRF_ERR_CUDA, "cudaStreamCreate failed"));
+    prepare_kernels();
     h->stream = h->own;
     if ((rc = dev_alloc(&h->status, 1))) return fail(rc);
-    if ((rc = dev_alloc(&h->U, (size_t)N * M))) return fail(rc);
-    if ((rc = dev_alloc(&h->Q, (size_t)N * M))) return fail(rc);
-    if ((rc = dev_alloc(&h->tmp, (size_t)N * M))) return fail(rc);
-    if ((rc = dev_alloc(&h->map, (size_t)N))) return fail(rc);
     if ((rc = build_tiles(h))) return fail(rc);
+    if ((rc = dev_alloc(&h->U, (size_t)h->nslots * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->Q, (size_t)h->nslots * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->tmp, (size_t)h->nslots * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->stage, (size_t)N * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->map, (size_t)N))) return fail(rc);
+    CU(cudaMemset(h->status, 0, sizeof(DevStatus)));
     *out = h;
     return ok();
 }
 
-// Copies an M x N quantity from the caller into the device's label-major dst.
-int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst) {
-    size_t bytes = sizeof(float) * (size_t)h->N * h->M;
-    cudaMemcpyKind kind = where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    if (layout == DCRF_LAYOUT_LM) {
-        CU(cudaMemcpyAsync(dst, src, bytes, kind, h->stream));
-    } else if (layout == DCRF_LAYOUT_PM) {
-        CU(cudaMemcpyAsync(h->tmp, src, bytes, kind, h->stream));
-        ProfScope ps(h, DCRF_KCLASS_OTHER);
-        CU(launch_transpose(h->tmp, dst, h->N, h->M, h->stream));
-    } else {
-        return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
+// Copies an M x N quantity from the caller (label- or point-major, host or
+// device) into the slot-major device layout dst [M][nslots].
+int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst, int M = -1) {
+    if (M < 0) M = h->M;
+    if (layout != DCRF_LAYOUT_LM && layout != DCRF_LAYOUT_PM) return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
+    const float *dsrc = src;
+    if (where != DCRF_DEVICE) {
+        CU(cudaMemcpyAsync(h->stage, src, sizeof(float) * (size_t)h->N * M, cudaMemcpyHostToDevice, h->stream));
+        dsrc = h->stage;
     }
+    ProfScope ps(h, DCRF_KCLASS_OTHER);
+    CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, M, h->N, h->slot_pt, h->nslots, dst, h->stream));
     return DCRF_OK;
 }
 
-int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where) {
-    size_t bytes = sizeof(float) * (size_t)h->N * h->M;
-    cudaMemcpyKind kind = where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    if (layout == DCRF_LAYOUT_LM) {
-        CU(cudaMemcpyAsync(dst, src, bytes, kind, h->stream));
-    } else if (layout == DCRF_LAYOUT_PM) {
+// Copies the slot-major src [M][nslots] out to the caller's layout.
+int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where, int M = -1) {
+    if (M < 0) M = h->M;
+    if (layout != DCRF_LAYOUT_LM && layout != DCRF_LAYOUT_PM) return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
+    float *ddst = where == DCRF_DEVICE ? dst : h->stage;
+    {
         ProfScope ps(h, DCRF_KCLASS_OTHER);
-        CU(launch_transpose(src, h->tmp, h->M, h->N, h->stream));
-        CU(cudaMemcpyAsync(dst, h->tmp, bytes, kind, h->stream));
-    } else {
-        return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
+        CU(launch_from_slots(src, M, h->N, h->nslots, h->pt_slot, layout == DCRF_LAYOUT_PM, ddst, h->stream));
     }
+    if (where != DCRF_DEVICE)
+        CU(cudaMemcpyAsync(dst, h->stage, sizeof(float) * (size_t)h->N * M, cudaMemcpyDeviceToHost, h->stream));
     return DCRF_OK;
 }
 
-// Descriptor of term k for the forward filter (or its transpose).
+// Descriptor of a term for the forward filter (or its transpose).
 TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     TermDev t{};
     t.d = T.d;
@@ -287,18 +312,101 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.off = T.lat.off;
     t.bary = T.lat.bary;
     t.wslice = T.lat.wslice;
-    t.norm = T.norm;
-    t.compat = T.compat;
     t.V = T.V[(T.d + 1) & 1];
-    t.partial = T.partial;
-    t.part_mbeg = T.lat.part_mbeg;
     t.tile_pbeg = T.lat.tile_pbeg;
+    t.part_mend = T.lat.part_mend;
     t.mem_pt = T.lat.mem_pt;
-    t.mem_w = T.lat.mem_w;
-    t.part_v = T.lat.part_v;
+    // forward pre-normalisation is folded into the member weights; the
+    // transpose (and terms without one) use the plain weights
+    t.mem_w = (t.pre_norm && !transpose && !value1 && T.mem_wn) ? T.mem_wn : T.lat.mem_w;
     t.tl_loc = T.lat.tl_loc;
     t.tl_w = T.lat.tl_w;
+    t.task = T.lat.task;
+    t.tile_tbeg = T.lat.tile_tbeg;
+    t.pv = T.pv;
+    t.norm = T.norm;
+    t.compat = T.compat;
+    t.staged = 0;
+    t.vcap = 0;
     return t;
+}
+
+size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
+
+// Shared-memory plan of the point pass: per staged term its norm, member ends
+// and members (live to the end), and -- only with messages -- its corner
+// tables and blurred rows (dead once the slice is done; the splat's q rows
+// alias them).  Tiles with more partials than a term's vcap read their rows
+// from global memory; terms whose fixed blocks do not fit are not staged.
+void plan_smem(dcrf_crf *h, PPArgs &a, const std::vector<int> &which, bool msg, int MP) {
+    const int budget = pointpass_smem_budget(MP);
+    const int n = (int)which.size();
+    int max_nt = 0;
+    for (int k = 0; k < n; k++) max_nt = std::max(max_nt, h->terms[which[k]].lat.max_nt);
+    // splat phase: q rows + per-task results
+    const size_t sq = align128((size_t)SPLAT_TILE * MP * 4) + (size_t)max_nt * MP * 4;
+    a.sm_q = 0;
+    a.sm_res = (int)align128((size_t)SPLAT_TILE * MP * 4);
+    a.smem_bytes = (int)sq;
+    if (MP % 4 != 0 || sq > (size_t)budget) return;  // bulk copies need 16-byte rows
+    std::vector<int> staged(n, 1), vcap(n, 0);
+    for (int k = 0; k < n; k++) vcap[k] = msg ? h->terms[which[k]].lat.max_np : 0;
+    for (int attempt = 0; attempt < 64; attempt++) {
+        size_t off = 0;
+        for (int k = 0; k < n; k++) {
+            if (!staged[k]) continue;
+            const Term &T = h->terms[which[k]];
+            const size_t d1 = T.d + 1;
+            a.ts.t[k].sm_norm = (int)off;
+            off = align128(off + 1024);
+            a.ts.t[k].sm_task = (int)off;
+            off = align128(off + ((size_t)T.lat.max_nt + 8) * 4);
+            a.ts.t[k].sm_mpt = (int)off;
+            off = align128(off + d1 * SPLAT_TILE * 2);
+            a.ts.t[k].sm_mw = (int)off;
+            off = align128(off + d1 * SPLAT_TILE * 4);
+        }
+        const size_t persist = off;
+        for (int k = 0; k < n && msg; k++) {
+            if (!staged[k]) continue;
+            const Term &T = h->terms[which[k]];
+            const size_t d1 = T.d + 1;
+            a.ts.t[k].sm_loc = (int)off;
+            off = align128(off + d1 * SPLAT_TILE * 2);
+            a.ts.t[k].sm_w = (int)off;
+            off = align128(off + d1 * SPLAT_TILE * 4);
+            a.ts.t[k].sm_vp = (int)off;
+            off = align128(off + (size_t)vcap[k] * MP * 4);
+        }
+        const size_t total = std::max(off, persist + sq);
+        if (total <= (size_t)budget) {
+            for (int k = 0; k < n; k++) {
+                a.ts.t[k].staged = staged[k];
+                a.ts.t[k].vcap = staged[k] ? vcap[k] : 0;
+            }
+            a.sm_q = (int)persist;
+            a.sm_res = (int)(persist + align128((size_t)SPLAT_TILE * MP * 4));
+            a.smem_bytes = (int)total;
+            return;
+        }
+        // shrink: halve the largest row cache first, then drop the largest term
+        int big = -1;
+        for (int k = 0; k < n; k++)
+            if (staged[k] && vcap[k] > 0 && (big < 0 || vcap[k] > vcap[big])) big = k;
+        if (big >= 0) {
+            vcap[big] = vcap[big] > 16 ? vcap[big] / 2 : 0;
+            continue;
+        }
+        int drop = -1;
+        for (int k = 0; k < n; k++)
+            if (staged[k] && (drop < 0 || h->terms[which[k]].d > h->terms[which[drop]].d)) drop = k;
+        if (drop < 0) break;
+        staged[drop] = 0;
+    }
+    for (int k = 0; k < n; k++) a.ts.t[k].staged = 0;
+    a.sm_q = 0;
+    a.sm_res = (int)align128((size_t)SPLAT_TILE * MP * 4);
+    a.smem_bytes = (int)sq;
 }
 
 cudaError_t pp(dcrf_crf *h, const PPArgs &a, int MP) {
@@ -312,18 +420,21 @@ PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transp
     a.M = value1 ? 1 : h->M;
     a.mode = mode;
     a.ntiles = h->ntiles;
+    a.nslots = h->nslots;
     a.slot_pt = h->slot_pt;
     a.U = h->has_unary ? h->U : nullptr;
     a.Qin = h->Q;
     a.Qout = h->Q;
     a.map_out = h->map;
     a.kl_part = h->kl_part;
+    a.status = h->status;
     a.ts.n = (int)which.size();
     for (size_t k = 0; k < which.size(); k++) {
         a.ts.t[k] = term_dev(h, h->terms[which[k]], transpose, value1);
         a.ntype[k] = h->terms[which[k]].ntype;
         a.norm_out[k] = h->terms[which[k]].norm;
     }
+    plan_smem(h, a, which, (mode & PP_MSG) != 0, value1 ? 1 : h->MP);
     return a;
 }
 
@@ -333,8 +444,11 @@ std::vector<int> all_terms(dcrf_crf *h) {
     return w;
 }
 
-// reduce + d+1 blur passes for the listed terms (after a splat point pass)
-int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, bool value1) {
+// reduce + d+1 blur passes for the listed terms (after a splat point pass).
+// partial_order: the last pass writes the result in tile-partial order (pv,
+// input of the mean-field point pass) instead of vertex order (V, input of the
+// point-order slice).
+int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, bool value1, bool partial_order) {
     int MP = value1 ? 1 : h->MP;
     bool seq = value1 || h->M <= 2;
     ReduceArgs ra{};
@@ -343,7 +457,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
     int maxd = 0;
     for (size_t k = 0; k < which.size(); k++) {
         Term &T = h->terms[which[k]];
-        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.partial, T.V[0], T.lat.L};
+        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.pv, T.V[0], T.lat.L};
         ra.begin[k + 1] = ra.begin[k] + T.lat.L;
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
@@ -361,12 +475,16 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
         for (size_t k = 0; k < which.size(); k++) {
             Term &T = h->terms[which[k]];
             if (pass > T.d) continue;
+            const bool last = pass == T.d;
             BlurArgs::T &bt = ba.t[ba.n];
             bt.Vin = T.V[pass & 1];
-            bt.Vout = T.V[(pass + 1) & 1];
+            bt.Vout = (last && partial_order) ? nullptr : T.V[(pass + 1) & 1];
             bt.nbr = T.lat.nbr;
             bt.L = T.lat.L;
             bt.axis = transpose ? T.d - pass : pass;  // reverse blur order for the transpose (permutohedral.cpp:556)
+            bt.red_beg = T.lat.red_beg;
+            bt.red_list = T.lat.red_list;
+            bt.pv = (last && partial_order) ? T.pv : nullptr;
             ba.begin[ba.n + 1] = ba.begin[ba.n] + (long long)T.lat.L * NV;
             ba.n++;
         }
@@ -411,8 +529,9 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
         dev_free_async(T.norm, h->stream);
         dev_free_async(T.V[0], h->stream);
         dev_free_async(T.V[1], h->stream);
-        dev_free_async(T.partial, h->stream);
+        dev_free_async(T.pv, h->stream);
         dev_free_async(T.compat, h->stream);
+        dev_free_async(T.mem_wn, h->stream);
         lattice_free(&T.lat, h->stream);
         return code;
     };
@@ -455,8 +574,9 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
     size_t vrows = (size_t)T.lat.L + 1;
     if ((rc = dev_alloc_async(&T.V[0], vrows * h->MP, h->stream))) return fail(rc);
     if ((rc = dev_alloc_async(&T.V[1], vrows * h->MP, h->stream))) return fail(rc);
-    if ((rc = dev_alloc_async(&T.partial, (size_t)std::max(T.lat.P, 1) * h->MP, h->stream))) return fail(rc);
-    if ((rc = dev_alloc_async(&T.norm, (size_t)h->N, h->stream))) return fail(rc);
+    if ((rc = dev_alloc_async(&T.pv, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return fail(rc);
+    if ((rc = dev_alloc_async(&T.norm, (size_t)h->nslots, h->stream))) return fail(rc);
+    CU(cudaMemsetAsync(T.norm, 0, sizeof(float) * (size_t)h->nslots, h->stream));
     // the zero sentinel rows (row 0) are never written afterwards
     CU(cudaMemsetAsync(T.V[0], 0, vrows * h->MP * sizeof(float), h->stream));
     CU(cudaMemsetAsync(T.V[1], 0, vrows * h->MP * sizeof(float), h->stream));
@@ -472,7 +592,7 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
         h->terms.pop_back();
         return fail(set_err(DCRF_ERR_CUDA, std::string("norm splat: ") + cudaGetErrorString(ce)));
     }
-    if ((rc = filter_phase(h, one, false, true))) {
+    if ((rc = filter_phase(h, one, false, true, false))) {
         h->terms.pop_back();
         return fail(rc);
     }
@@ -485,6 +605,20 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
     if ((rc = zero_sentinels(h, h->terms.back()))) {
         h->terms.pop_back();
         return fail(rc);
+    }
+    {
+        Term &TT = h->terms.back();
+        const size_t nm = (size_t)h->ntiles * SPLAT_TILE * (TT.d + 1);
+        if ((rc = dev_alloc_async(&TT.mem_wn, nm, h->stream))) {
+            h->terms.pop_back();
+            return fail(rc);
+        }
+        T.mem_wn = TT.mem_wn;
+        ce = launch_scale_members(TT.lat.mem_pt, TT.lat.mem_w, TT.norm, h->ntiles, TT.d + 1, TT.mem_wn, h->stream);
+        if (ce != cudaSuccess) {
+            h->terms.pop_back();
+            return fail(set_err(DCRF_ERR_CUDA, std::string("member weights: ") + cudaGetErrorString(ce)));
+        }
     }
     if ((rc = sync_check(h))) {
         h->terms.pop_back();
@@ -508,8 +642,9 @@ int validate_kn(int ktype, int ntype) {
     return DCRF_OK;
 }
 
-// T mean-field iterations starting from softmax(-U); final Q in h->Q.
-int run_inference(dcrf_crf *h, int T, int final_mode) {
+// Launch sequence of T mean-field iterations starting from softmax(-U); the
+// final pass writes per final_mode (Q into h->Q, or the MAP labels).
+int issue_inference(dcrf_crf *h, int T, int final_mode) {
     std::vector<int> w = all_terms(h);
     int rc;
     if (T <= 0 || w.empty()) {
@@ -518,10 +653,52 @@ int run_inference(dcrf_crf *h, int T, int final_mode) {
     }
     CU(pp(h, pp_args(h, PP_SPLAT, w, false, false), h->MP));
     for (int it = 1; it <= T; it++) {
-        if ((rc = filter_phase(h, w, false, false))) return rc;
+        if ((rc = filter_phase(h, w, false, false, true))) return rc;
         int mode = PP_MSG | (it < T ? PP_SPLAT : final_mode);
         CU(pp(h, pp_args(h, mode, w, false, false), h->MP));
     }
+    return DCRF_OK;
+}
+
+// Runs issue_inference as one CUDA graph: captured on the handle's capture
+// stream, instantiated once and afterwards updated in place (same kernels,
+// new arguments), launched on the handle's stream.  Profiling launches the
+// kernels directly so that the per-launch events can be recorded.
+int run_inference(dcrf_crf *h, int T, int final_mode) {
+    if (h->profiling || !h->use_graphs) return issue_inference(h, T, final_mode);
+    cudaStream_t user = h->stream;
+    h->stream = h->capture;
+    CU(cudaStreamBeginCapture(h->capture, cudaStreamCaptureModeThreadLocal));
+    int rc = issue_inference(h, T, final_mode);
+    cudaGraph_t graph = nullptr;
+    cudaError_t ce = cudaStreamEndCapture(h->capture, &graph);
+    h->stream = user;
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (ce != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(ce));
+    bool updated = false;
+    if (h->gexec) {
+        cudaGraphExecUpdateResultInfo info;
+        if (cudaGraphExecUpdate(h->gexec, graph, &info) == cudaSuccess)
+            updated = true;
+        else {
+            cudaGetLastError();
+            cudaGraphExecDestroy(h->gexec);
+            h->gexec = nullptr;
+        }
+    }
+    if (!updated) {
+        ce = cudaGraphInstantiate(&h->gexec, graph, 0);
+        if (ce != cudaSuccess) {
+            cudaGraphDestroy(graph);
+            h->gexec = nullptr;
+            return set_err(DCRF_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce));
+        }
+    }
+    cudaGraphDestroy(graph);
+    CU(cudaGraphLaunch(h->gexec, h->stream));
     return DCRF_OK;
 }
 
@@ -560,8 +737,9 @@ int dcrf_destroy(dcrf_crf *h) {
         dev_free_async(T.norm, h->stream);
         dev_free_async(T.V[0], h->stream);
         dev_free_async(T.V[1], h->stream);
-        dev_free_async(T.partial, h->stream);
+        dev_free_async(T.pv, h->stream);
         dev_free_async(T.compat, h->stream);
+        dev_free_async(T.mem_wn, h->stream);
         lattice_free(&T.lat, h->stream ? h->stream : h->own);
     }
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -569,10 +747,14 @@ int dcrf_destroy(dcrf_crf *h) {
     dev_free(h->U);
     dev_free(h->Q);
     dev_free(h->tmp);
+    dev_free(h->stage);
+    dev_free(h->pt_slot);
     dev_free(h->map);
     dev_free(h->kl_part);
     dev_free(h->slot_pt);
     dev_free(h->tile_vbase);
+    if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->capture) cudaStreamDestroy(h->capture);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return ok();
@@ -714,7 +896,7 @@ int dcrf_step_inference(dcrf_crf *h, float *Q, int layout, int where) {
     std::vector<int> w = all_terms(h);
     if (!w.empty()) {
         CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
-        if ((rc = filter_phase(h, w, false, false))) return rc;
+        if ((rc = filter_phase(h, w, false, false, true))) return rc;
     }
     CU(pp(h, pp_args(h, PP_MSG | PP_WRITE_Q, w, false, false), h->MP));
     if ((rc = store_mn(h, h->Q, Q, layout, where))) return rc;
@@ -730,7 +912,7 @@ int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, doubl
     std::vector<int> w = all_terms(h);
     if (!w.empty()) {
         CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
-        if ((rc = filter_phase(h, w, false, false))) return rc;
+        if ((rc = filter_phase(h, w, false, false, true))) return rc;
     }
     CU(pp(h, pp_args(h, PP_LOAD_Q | PP_MSG | PP_KL, w, false, false), h->MP));
     std::vector<double> part(h->ntiles);
@@ -823,8 +1005,8 @@ int dcrf_term_norm(dcrf_crf *h, int term, float *norm) {
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size() || !norm) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     Term &T = h->terms[term];
-    CU(cudaStreamSynchronize(h->stream));
-    CU(cudaMemcpy(norm, T.norm, sizeof(float) * h->N, cudaMemcpyDeviceToHost));
+    if ((rc = store_mn(h, T.norm, norm, DCRF_LAYOUT_LM, DCRF_HOST, 1))) return rc;
+    if ((rc = sync_check(h))) return rc;
     if (T.ntype == DCRF_NO_NORMALIZATION) {  // pairwise.cpp:46-53: every entry = N / sum(K*1), float sum
         float mean = 0.f;
         for (int i = 0; i < h->N; i++) mean += norm[i];
@@ -841,19 +1023,19 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     bool v1 = value_size == 1;
     int MP = v1 ? 1 : h->MP;
-    size_t bytes = sizeof(float) * (size_t)value_size * h->N;
-    CU(cudaMemcpyAsync(h->tmp, in, bytes, cudaMemcpyHostToDevice, h->stream));
+    if ((rc = load_mn(h, in, DCRF_LAYOUT_LM, DCRF_HOST, h->tmp, value_size))) return rc;
     std::vector<int> one{term};
     PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
     a.ts.t[0].pre_norm = 0;
+    a.ts.t[0].mem_w = h->terms[term].lat.mem_w;  // raw filter: no normalisation folded in
     a.Qin = h->tmp;
     CU(pp(h, a, MP));
-    if ((rc = filter_phase(h, one, reverse != 0, v1))) return rc;
+    if ((rc = filter_phase(h, one, reverse != 0, v1, false))) return rc;
     a = pp_args(h, PP_FILTER, one, reverse != 0, v1);
     a.Qout = h->tmp;
     CU(pp(h, a, MP));
     if (v1 && (rc = zero_sentinels(h, h->terms[term]))) return rc;
-    CU(cudaMemcpyAsync(out, h->tmp, bytes, cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = store_mn(h, h->tmp, out, DCRF_LAYOUT_LM, DCRF_HOST, value_size))) return rc;
     if ((rc = sync_check(h))) return rc;
     return ok();
 }
@@ -866,8 +1048,9 @@ int dcrf_clear_pairwise(dcrf_crf *h) {
         dev_free_async(T.norm, h->stream);
         dev_free_async(T.V[0], h->stream);
         dev_free_async(T.V[1], h->stream);
-        dev_free_async(T.partial, h->stream);
+        dev_free_async(T.pv, h->stream);
         dev_free_async(T.compat, h->stream);
+        dev_free_async(T.mem_wn, h->stream);
         lattice_free(&T.lat, h->stream);
     }
     h->terms.clear();
@@ -925,7 +1108,7 @@ int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count)
     Term &T = h->terms[term];
     size_t avail = which < 2 ? ((size_t)T.lat.L + 1) * h->MP : (size_t)std::max(T.lat.P, 1) * h->MP;
     if (count > avail) return set_err(DCRF_ERR_INVALID_ARG, "count exceeds the buffer");
-    const float *src = which == 0 ? T.V[0] : which == 1 ? T.V[1] : T.partial;
+    const float *src = which == 0 ? T.V[0] : which == 1 ? T.V[1] : T.pv;
     CU(cudaStreamSynchronize(h->stream));
     CU(cudaMemcpy(out, src, count * sizeof(float), cudaMemcpyDeviceToHost));
     return ok();

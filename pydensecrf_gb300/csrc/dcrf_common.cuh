@@ -15,7 +15,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "../../include/dcrf.h"
+#include "dcrf.h"
 
 #define DCRF_MAX_TERMS 16
 #define DCRF_MAX_D 16
@@ -60,25 +60,31 @@ struct TermDev {
     int d;
     int L;
     int ckind;      // 0 Potts, 1 Diagonal, 2 Matrix
-    int pre_norm;   // multiply Q by norm before splatting (forward)
-    int post_norm;  // multiply the sliced value by norm (forward)
+    int pre_norm;   // multiply Q by norm before splatting
+    int post_norm;  // multiply the sliced value by norm
     int seq;        // seqCompute arithmetic (value size <= 2 or scalar build)
     float potts_w;
     float alpha;
-    const int *off;        // [d+1][N]
-    const float *bary;     // [d+1][N]
-    const float *wslice;   // [d+1][N]
-    const float *norm;     // [N]
-    const float *compat;   // Diagonal [M] / Matrix [M][M] (symmetrised)
-    const float *V;        // [L+1][MP] blurred values read by the slice
-    float *partial;        // [P][MP] written by the local splat
-    const int *part_mbeg;  // [P+1] member range of partial p
-    const int *tile_pbeg;  // [ntiles+1] partial range of tile t
-    const uint16_t *mem_pt;  // [E] tile-local point of member e
-    const float *mem_w;      // [E] splat weight of member e
-    const int *part_v;       // [P] vertex of partial p
+    // point-order tables (normalisation and raw-filter paths)
+    const int *off;       // [d+1][N]
+    const float *bary;    // [d+1][N]
+    const float *wslice;  // [d+1][N]
+    const float *V;       // [L+1][MP] blurred values in vertex order
+    // tile tables (mean-field point pass)
+    const int *tile_pbeg;    // [ntiles+1] partial range of each tile
+    const int *part_mend;    // [P+8] member end of each partial, tile-relative
+    const uint16_t *mem_pt;  // [ntiles][SPLAT_TILE*(d+1)] member -> tile slot
+    const float *mem_w;      // [ntiles][SPLAT_TILE*(d+1)] member weight
     const uint16_t *tl_loc;  // [ntiles][d+1][SPLAT_TILE] corner -> index among the tile's partials
     const float *tl_w;       // [ntiles][d+1][SPLAT_TILE] corner barycentric weight
+    const uint32_t *task;    // splat tasks (see LatticeDev::task)
+    const int *tile_tbeg;    // [ntiles+1] task range of each tile
+    float *pv;               // [P][MP] blurred values in partial order (read), splat partials (written)
+    const float *norm;       // [nslots]
+    const float *compat;     // Diagonal [M] / Matrix [M][M] (symmetrised)
+    // shared-memory plan of the point pass (byte offsets; staged = 0: global reads)
+    int staged, vcap;
+    int sm_loc, sm_w, sm_norm, sm_task, sm_mpt, sm_mw, sm_vp;
 };
 
 struct TermSet {

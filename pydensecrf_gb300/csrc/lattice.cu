@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(256) tile_sort_kernel(const int *__restrict__ 
         }
     }
     const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
-    const size_t base = (size_t)tile_vbase[t] * (D + 1);
+    const size_t base = (size_t)t * SPLAT_TILE * (D + 1);
     uint32_t cnt = 0;
     for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
         unsigned long long x = s_keys[idx];
@@ -400,13 +400,13 @@ __global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long
                                                         const int *__restrict__ slot_pt,
                                                         const int *__restrict__ tile_vbase,
                                                         const uint32_t *__restrict__ tile_pbeg,
-                                                        int *__restrict__ part_v, int *__restrict__ part_mbeg,
+                                                        int *__restrict__ part_v, int *__restrict__ part_mend,
                                                         uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
                                                         uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w) {
     __shared__ uint32_t s_warp[8];
     const int t = blockIdx.x;
     const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
-    const size_t base = (size_t)tile_vbase[t] * (D + 1);
+    const size_t base = (size_t)t * SPLAT_TILE * (D + 1);
     const int chunk = (n + blockDim.x - 1) / blockDim.x;
     const int i0 = min(n, (int)threadIdx.x * chunk), i1 = min(n, i0 + chunk);
     uint32_t cnt = 0;
@@ -435,12 +435,55 @@ __global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long
         mem_w[base + idx] = w;
         if (idx == 0 || (s >> 16) != (sorted[base + idx - 1] >> 16)) {
             part_v[run] = (int)(s >> 16);
-            part_mbeg[run] = (int)(base + idx);
             run++;
         }
+        if (idx == n - 1 || (s >> 16) != (sorted[base + idx + 1] >> 16)) part_mend[run - 1] = idx + 1;
         const size_t tl = ((size_t)t * (D + 1) + r) * SPLAT_TILE + li;
         tl_loc[tl] = (uint16_t)(run - 1 - pbeg);
         tl_w[tl] = w;
+    }
+}
+
+// Splat tasks of one tile: each partial's member run split into pieces of at
+// most SPLAT_TASK members.  Pass 0 counts, pass 1 writes.
+__global__ void __launch_bounds__(256) tile_tasks_kernel(const int *__restrict__ tile_pbeg,
+                                                         const int *__restrict__ part_mend, int pass,
+                                                         uint32_t *__restrict__ tile_nt, const uint32_t *tile_tbeg,
+                                                         uint32_t *__restrict__ task) {
+    __shared__ uint32_t s_warp[8];
+    const int t = blockIdx.x;
+    const int pb = tile_pbeg[t], np = tile_pbeg[t + 1] - pb;
+    const int chunk = (np + blockDim.x - 1) / blockDim.x;
+    const int j0 = min(np, (int)threadIdx.x * chunk), j1 = min(np, j0 + chunk);
+    uint32_t cnt = 0;
+    for (int j = j0; j < j1; j++) {
+        const int b = j == 0 ? 0 : part_mend[pb + j - 1], e = part_mend[pb + j];
+        cnt += (uint32_t)((e - b + SPLAT_TASK - 1) / SPLAT_TASK);
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (pass == 0) {
+        if (threadIdx.x == 0) {
+            uint32_t tot = 0;
+            for (int w = 0; w < 8; w++) tot += s_warp[w];
+            tile_nt[t] = tot;
+        }
+        return;
+    }
+    uint32_t before = 0;
+    for (int w = 0; w < warp; w++) before += s_warp[w];
+    uint32_t out = tile_tbeg[t] + before + x - cnt;
+    for (int j = j0; j < j1; j++) {
+        const int b = j == 0 ? 0 : part_mend[pb + j - 1], e = part_mend[pb + j];
+        for (int q = b; q < e; q += SPLAT_TASK)
+            task[out++] = ((uint32_t)j << 19) | ((uint32_t)q << 6) | (uint32_t)min(SPLAT_TASK, e - q);
     }
 }
 
@@ -598,19 +641,21 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     // ---- splat tiles --------------------------------------------------------
     L.ntiles = tm.ntiles;
     L.tile_pbeg = dalloc<int>(L.ntiles + 1, s, &acc);
-    L.mem_pt = dalloc<uint16_t>(Ereal, s, &acc);
-    L.mem_w = dalloc<float>(Ereal, s, &acc);
     const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
+    L.mem_pt = dalloc<uint16_t>(ntl, s, &acc);
+    L.mem_w = dalloc<float>(ntl, s, &acc);
     L.tl_loc = dalloc<uint16_t>(ntl, s, &acc);
     L.tl_w = dalloc<float>(ntl, s, &acc);
-    unsigned long long *sorted = tmp.get<unsigned long long>(Ereal);
+    unsigned long long *sorted = tmp.get<unsigned long long>(ntl);
     uint32_t *tile_nv = tmp.get<uint32_t>(L.ntiles + 1);
     uint32_t *d_P = tmp.get<uint32_t>(4);
     if (!L.tile_pbeg || !L.mem_pt || !L.mem_w || !L.tl_loc || !L.tl_w || tmp.failed)
         return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
-    // empty slots: local index 0, weight 0
+    // empty slots and padding: local index 0, weight 0
     cudaMemsetAsync(L.tl_loc, 0, ntl * sizeof(uint16_t), s);
     cudaMemsetAsync(L.tl_w, 0, ntl * sizeof(float), s);
+    cudaMemsetAsync(L.mem_pt, 0, ntl * sizeof(uint16_t), s);
+    cudaMemsetAsync(L.mem_w, 0, ntl * sizeof(float), s);
     int n2max = 1;
     while (n2max < SPLAT_TILE * (D + 1)) n2max <<= 1;
     size_t smem = (size_t)n2max * sizeof(unsigned long long);
@@ -621,23 +666,54 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
             return bail(DCRF_ERR_CUDA, "scan failed");
     }
     uint32_t hP = 0;
+    std::vector<uint32_t> hpbeg(L.ntiles + 1, 0);
     if (L.ntiles > 0) {
         cudaMemcpyAsync(&hP, d_P, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hpbeg.data(), L.tile_pbeg, sizeof(uint32_t) * L.ntiles, cudaMemcpyDeviceToHost, s);
         ce = cudaStreamSynchronize(s);
         if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tiles: ") + cudaGetErrorString(ce));
     }
     L.P = (int)hP;
+    hpbeg[L.ntiles] = hP;
+    for (int t = 0; t < L.ntiles; t++) L.max_np = std::max(L.max_np, (int)(hpbeg[t + 1] - hpbeg[t]));
     L.part_v = dalloc<int>((size_t)L.P + 1, s, &acc);
-    L.part_mbeg = dalloc<int>((size_t)L.P + 1, s, &acc);
+    L.part_mend = dalloc<int>((size_t)L.P + 8, s, &acc);
     L.red_beg = dalloc<int>((size_t)L.L + 1, s, &acc);
     L.red_list = dalloc<int>((size_t)L.P + 1, s, &acc);
-    if (!L.part_v || !L.part_mbeg || !L.red_beg || !L.red_list) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
+    if (!L.part_v || !L.part_mend || !L.red_beg || !L.red_list) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
+    cudaMemsetAsync(L.part_mend, 0, sizeof(int) * ((size_t)L.P + 8), s);
     DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.tile_pbeg + L.ntiles, L.P));
     if (L.ntiles > 0)
         DCRF_LAUNCH(tile_fill_kernel<D><<<L.ntiles, 256, 0, s>>>(sorted, L.bary, N, tm.slot_pt, tm.tile_vbase,
-                                                     (const uint32_t *)L.tile_pbeg, L.part_v, L.part_mbeg, L.mem_pt,
+                                                     (const uint32_t *)L.tile_pbeg, L.part_v, L.part_mend, L.mem_pt,
                                                      L.mem_w, L.tl_loc, L.tl_w));
-    DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.part_mbeg + L.P, (int)Ereal));
+    // ---- splat tasks -----------------------------------------------------------
+    {
+        uint32_t *tile_nt = tmp.get<uint32_t>(L.ntiles + 1);
+        uint32_t *d_T = tmp.get<uint32_t>(4);
+        L.tile_tbeg = dalloc<int>(L.ntiles + 1, s, &acc);
+        if (tmp.failed || !L.tile_tbeg) return bail(DCRF_ERR_OOM, "device allocation failed (tasks)");
+        uint32_t hT = 0;
+        std::vector<uint32_t> htb(L.ntiles + 1, 0);
+        if (L.ntiles > 0) {
+            DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 0, tile_nt, nullptr, nullptr));
+            if (scan_exclusive_u32(tile_nt, (uint32_t *)L.tile_tbeg, L.ntiles, d_T, stemp, s) != cudaSuccess)
+                return bail(DCRF_ERR_CUDA, "scan failed");
+            cudaMemcpyAsync(&hT, d_T, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+            cudaMemcpyAsync(htb.data(), L.tile_tbeg, sizeof(uint32_t) * L.ntiles, cudaMemcpyDeviceToHost, s);
+            ce = cudaStreamSynchronize(s);
+            if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tasks: ") + cudaGetErrorString(ce));
+        }
+        htb[L.ntiles] = hT;
+        for (int t = 0; t < L.ntiles; t++) L.max_nt = std::max(L.max_nt, (int)(htb[t + 1] - htb[t]));
+        L.task = dalloc<uint32_t>((size_t)hT + 8, s, &acc);
+        if (!L.task) return bail(DCRF_ERR_OOM, "device allocation failed (tasks)");
+        cudaMemsetAsync(L.task, 0, sizeof(uint32_t) * ((size_t)hT + 8), s);
+        DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.tile_tbeg + L.ntiles, (int)hT));
+        if (L.ntiles > 0)
+            DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 1, nullptr,
+                                                                   (const uint32_t *)L.tile_tbeg, L.task));
+    }
     // ---- reduce lists: partials grouped by vertex, in tile order ------------
     {
         uint32_t *cnt = tmp.get<uint32_t>((size_t)L.L + 1);
@@ -681,8 +757,9 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
 }  // namespace
 
 void lattice_free(LatticeDev *L, cudaStream_t s) {
-    void *ps[] = {L->off,       L->bary,   L->wslice,  L->rank,    L->nbr,      L->vkeys,  L->part_v, L->part_mbeg,
-                  L->tile_pbeg, L->mem_pt, L->mem_w,   L->red_beg, L->red_list, L->tl_loc, L->tl_w};
+    void *ps[] = {L->off,       L->bary,   L->wslice,  L->rank,    L->nbr,      L->vkeys,  L->part_v, L->part_mend,
+                  L->tile_pbeg, L->mem_pt, L->mem_w,   L->red_beg, L->red_list, L->tl_loc, L->tl_w,
+                  L->task,      L->tile_tbeg};
     for (void *p : ps)
         if (p) cudaFreeAsync(p, s);
     *L = LatticeDev{};

@@ -9,6 +9,7 @@
 namespace dcrf {
 
 constexpr int SPLAT_TILE = 256;  // points per tile of the in-kernel splat
+constexpr int SPLAT_TASK = 16;   // members per splat task (load balance of the in-kernel splat)
 
 struct LatticeDev {
     int d = 0, N = 0, L = 0, P = 0, ntiles = 0, variant = 0;
@@ -19,11 +20,17 @@ struct LatticeDev {
     uint8_t *rank = nullptr;     // [d+1][N]
     int2 *nbr = nullptr;         // [d+1][L]
     uint16_t *vkeys = nullptr;   // [L][d+1]: field 0 = image, 1..d = coordinates
-    int *part_v = nullptr;       // [P]
-    int *part_mbeg = nullptr;    // [P+1]
-    int *tile_pbeg = nullptr;    // [ntiles+1]
-    uint16_t *mem_pt = nullptr;  // [E]
-    float *mem_w = nullptr;      // [E]
+    int max_np = 0;              // largest number of partials of one tile
+    int *part_v = nullptr;       // [P] vertex of partial p
+    int *part_mend = nullptr;    // [P+8] end of partial p's members, relative to its tile's member block
+    int *tile_pbeg = nullptr;    // [ntiles+1] partial range of tile t
+    uint16_t *mem_pt = nullptr;  // [ntiles][SPLAT_TILE*(d+1)] tile-local point of each member
+    float *mem_w = nullptr;      // [ntiles][SPLAT_TILE*(d+1)] splat weight of each member
+    // splat tasks: runs of at most SPLAT_TASK members of one partial, in partial order;
+    // task = (local partial << 19) | (first member << 6) | length
+    int max_nt = 0;               // largest number of tasks of one tile
+    uint32_t *task = nullptr;     // [T+8]
+    int *tile_tbeg = nullptr;     // [ntiles+1] task range of tile t
     int *red_beg = nullptr;      // [L+1]
     int *red_list = nullptr;     // [P]
     // tile-ordered slice tables: corner r of slot li of tile t at (t*(d+1)+r)*SPLAT_TILE+li

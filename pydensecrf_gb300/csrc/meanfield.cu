@@ -8,27 +8,77 @@
 //           (permutohedral.cpp:545-553);
 //   blur    per axis j = 0..d (d..0 for the transpose): V' = V + 1/2 (V[n1] +
 //           V[n2]) with the zero sentinel row (permutohedral.cpp:556-569);
-//           terms of smaller d drop out of the later axis launches;
-//   point   thread per point (tile of 256 points per CTA): slice every term
-//           (permutohedral.cpp:574-584), apply the normalisation
-//           (pairwise.cpp:78-79) and the label compatibility
+//           terms of smaller d drop out of the later axis launches.  The last
+//           axis also scatters every vertex's value to the partials that
+//           reference it (tile-partial order), so each tile's inputs of the
+//           next phase are one contiguous block;
+//   point   one CTA per tile of 256 points (a 16x16 pixel block of a
+//           DenseCRF2D): an elected thread prefetches the tile's tables and
+//           blurred values with cp.async.bulk (TMA bulk copies) behind one
+//           mbarrier while every thread loads its unary; then per point:
+//           slice every term (permutohedral.cpp:574-584), normalise
+//           (pairwise.cpp:78-79), label compatibility
 //           (labelcompatibility.cpp:46-48,66-68,82-84), subtract from -U,
-//           softmax (densecrf.cpp:98-106) -- and then, still in the same CTA,
-//           splat the new Q of the tile into each term's per-(tile, vertex)
-//           partials from shared memory, so Q never makes a round trip
-//           through memory between iterations.
+//           softmax (densecrf.cpp:98-106); then, in the same CTA, splat the
+//           tile's new Q into each term's per-(tile, vertex) partials from
+//           shared memory.  Q never makes a round trip through memory between
+//           iterations.
 //
-// The splat is deterministic: a tile's corners are grouped by vertex at
-// lattice-build time (in point order), so every partial is a fixed-order sum,
-// and the reduce adds a vertex's partials in tile order.  There are no float
-// atomics anywhere.  Products and sums are rounded separately like the
-// reference's x86 build; the value-size <= 2 arithmetic of seqCompute (double
-// blur, (w*v)*alpha slice) is kept where the reference uses it.
+// Deterministic: a tile's corners are grouped by vertex at lattice-build time
+// (point order), every partial is a fixed-order sum, and the reduce adds a
+// vertex's partials in tile order; no float atomics.  Products and sums are
+// rounded separately like the reference's x86 build; the value-size <= 2
+// arithmetic of seqCompute (double blur, (w*v)*alpha slice) is kept where the
+// reference uses it.
 #include <math.h>
 
 #include "meanfield.cuh"
 
 namespace dcrf {
+
+// ---------------------------------------------------------------------------
+// TMA bulk copies and mbarriers (inline PTX)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// 1-D bulk copy global -> shared; 16-byte aligned addresses, size a multiple of 16.
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait on phase `parity`: returns false after ~2^22 polls (seconds).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 22); it++) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (it > 16) __nanosleep(128);
+    }
+    return false;
+}
 
 template <int MP>
 struct Grp {
@@ -58,6 +108,24 @@ __device__ __forceinline__ void load_row(const float *__restrict__ row, float (&
     } else {
 #pragma unroll
         for (int m = 0; m < MP; m++) v[m] = __ldg(row + m);
+    }
+}
+
+template <int MP>
+__device__ __forceinline__ void load_row_smem(const float *row, float (&v)[MP]) {
+    if constexpr (MP % 4 == 0) {
+        const float4 *r4 = reinterpret_cast<const float4 *>(row);
+#pragma unroll
+        for (int c = 0; c < MP / 4; c++) {
+            float4 x = r4[c];
+            v[4 * c + 0] = x.x;
+            v[4 * c + 1] = x.y;
+            v[4 * c + 2] = x.z;
+            v[4 * c + 3] = x.w;
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = row[m];
     }
 }
 
@@ -104,70 +172,84 @@ __device__ __forceinline__ void fold_compat(const TermDev &T, const float (&acc)
     }
 }
 
-// Shared-memory budget of the point pass: a union of the vertex-row stage
-// (slice phase) and the q rows + member lists (splat phase).
-template <int MP>
-struct PPSmem {
-    static constexpr int MCAP = SPLAT_TILE * 6;  // staged members (corners of d <= 5)
-    static constexpr int SPLAT_BYTES = SPLAT_TILE * MP * 4 + MCAP * 6 + (MCAP + 1) * 4;
-    static constexpr int SV_ROWS = (SPLAT_BYTES / (MP * 4)) < 128 ? 128 : (SPLAT_BYTES / (MP * 4));
-    static constexpr int BYTES = (SV_ROWS * MP * 4 > SPLAT_BYTES ? SV_ROWS * MP * 4 : SPLAT_BYTES);
+// Partial and task ranges of term T in tile t, and the 16-byte aligned window
+// of its tasks that the prefetch copies.
+struct TileBlocks {
+    int pb, np;       // partials [pb, pb+np)
+    int tb, nt;       // tasks [tb, tb+nt)
+    int a0, nwin;     // task window [a0, a0+nwin), a0 = tb rounded down to 4
+    int vp_staged;
 };
 
-// Slice of term T for the calling thread's point (tile-local tables), from the
-// staged rows when the tile's vertex rows fit in shared memory.
-template <int MP>
-__device__ __forceinline__ void slice_tiled(const TermDev &T, int t, int li, bool staged, int pb,
-                                            const float *__restrict__ sV, float (&acc)[MP]) {
-#pragma unroll
-    for (int m = 0; m < MP; m++) acc[m] = 0.f;
-    const size_t tbase = (size_t)t * (T.d + 1) * SPLAT_TILE + li;
-    for (int r = 0; r <= T.d; r++) {
-        const int loc = T.tl_loc[tbase + (size_t)r * SPLAT_TILE];
-        const float b = T.tl_w[tbase + (size_t)r * SPLAT_TILE];
-        float v[MP];
-        if (staged) {
-            if constexpr (MP % 4 == 0) {
-                const float4 *r4 = reinterpret_cast<const float4 *>(sV + loc * MP);
-#pragma unroll
-                for (int c = 0; c < MP / 4; c++) {
-                    float4 x = r4[c];
-                    v[4 * c] = x.x, v[4 * c + 1] = x.y, v[4 * c + 2] = x.z, v[4 * c + 3] = x.w;
-                }
-            } else {
-#pragma unroll
-                for (int m = 0; m < MP; m++) v[m] = sV[loc * MP + m];
-            }
-        } else {
-            load_row<MP>(T.V + (size_t)(T.part_v[pb + loc] + 1) * MP, v);
-        }
-        if (T.seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
-#pragma unroll
-            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(b, v[m]), T.alpha));
-        } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
-            const float w = fmul(b, T.alpha);
-#pragma unroll
-            for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
-        }
-    }
+__device__ __forceinline__ TileBlocks tile_blocks(const TermDev &T, int t) {
+    TileBlocks b;
+    b.pb = T.tile_pbeg[t];
+    b.np = T.tile_pbeg[t + 1] - b.pb;
+    b.tb = T.tile_tbeg[t];
+    b.nt = T.tile_tbeg[t + 1] - b.tb;
+    b.a0 = b.tb & ~3;
+    b.nwin = ((b.tb + b.nt + 3) & ~3) - b.a0;
+    b.vp_staged = b.np <= T.vcap;
+    return b;
 }
 
 template <int MP>
 __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kernel(const __grid_constant__ PPArgs a) {
-    using SM = PPSmem<MP>;
-    __shared__ __align__(16) unsigned char smem[SM::BYTES];
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ uint64_t mbar;
     __shared__ double sKL[SPLAT_TILE / 32];
-    float *sV = reinterpret_cast<float *>(smem);
-    float *sQ = reinterpret_cast<float *>(smem);
-    float *sMw = reinterpret_cast<float *>(smem + SPLAT_TILE * MP * 4);
-    int *sPmb = reinterpret_cast<int *>(smem + SPLAT_TILE * MP * 4 + SM::MCAP * 4);
-    uint16_t *sMpt = reinterpret_cast<uint16_t *>(smem + SPLAT_TILE * MP * 4 + SM::MCAP * 4 + (SM::MCAP + 1) * 4);
+    __shared__ TileBlocks sTB[DCRF_MAX_TERMS];
 
     const int t = blockIdx.x;
     const int li = threadIdx.x;
-    const int i = a.slot_pt[(size_t)t * SPLAT_TILE + li];
+    const size_t s = (size_t)t * SPLAT_TILE + li;
+    const int i = a.slot_pt[s];
     const bool valid = i >= 0;
-    const int N = a.N, M = a.M, mode = a.mode;
+    const int M = a.M, mode = a.mode, ns = a.nslots;
+
+    // ---- 1. prefetch the tile's tables (TMA bulk copies, one elected thread)
+    bool any_staged = false;
+    for (int k = 0; k < a.ts.n; k++) any_staged |= a.ts.t[k].staged != 0;
+    if (li < a.ts.n) sTB[li] = tile_blocks(a.ts.t[li], t);
+    if (any_staged && li == 0) {
+        mbar_init(&mbar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (any_staged && li == 0) {
+        uint32_t total = 0;
+        for (int k = 0; k < a.ts.n; k++) {
+            const TermDev &T = a.ts.t[k];
+            const TileBlocks b = sTB[k];
+            if (!T.staged) continue;
+            const uint32_t d1 = T.d + 1;
+            total += 1024u + (uint32_t)b.nwin * 4u + d1 * SPLAT_TILE * 6u;  // norm, tasks, members
+            if (mode & PP_MSG) {
+                total += d1 * SPLAT_TILE * 6u;                                // corner tables
+                if (b.vp_staged) total += (uint32_t)b.np * MP * 4u;           // blurred rows
+            }
+        }
+        mbar_arrive_expect_tx(&mbar, total);
+        for (int k = 0; k < a.ts.n; k++) {
+            const TermDev &T = a.ts.t[k];
+            if (!T.staged) continue;
+            const TileBlocks b = sTB[k];
+            const size_t d1 = T.d + 1;
+            const size_t tb = (size_t)t * SPLAT_TILE * d1;
+            bulk_g2s(smem + T.sm_norm, T.norm + (size_t)t * SPLAT_TILE, 1024u, &mbar);
+            bulk_g2s(smem + T.sm_task, T.task + b.a0, (uint32_t)b.nwin * 4u, &mbar);
+            bulk_g2s(smem + T.sm_mpt, T.mem_pt + tb, (uint32_t)(d1 * SPLAT_TILE * 2), &mbar);
+            bulk_g2s(smem + T.sm_mw, T.mem_w + tb, (uint32_t)(d1 * SPLAT_TILE * 4), &mbar);
+            if (mode & PP_MSG) {
+                bulk_g2s(smem + T.sm_loc, T.tl_loc + tb, (uint32_t)(d1 * SPLAT_TILE * 2), &mbar);
+                bulk_g2s(smem + T.sm_w, T.tl_w + tb, (uint32_t)(d1 * SPLAT_TILE * 4), &mbar);
+                if (b.vp_staged && b.np > 0)
+                    bulk_g2s(smem + T.sm_vp, T.pv + (size_t)b.pb * MP, (uint32_t)(b.np * MP * 4), &mbar);
+            }
+        }
+    }
+
+    // ---- 2. the point's own inputs, overlapping the copies
     // x: the logits of the update, or the given marginals (LOAD_Q / ONES); q after the softmax
     float x[MP];
 #pragma unroll
@@ -180,66 +262,85 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
         if (valid) {
 #pragma unroll
             for (int m = 0; m < MP; m++)
-                if (m < M) x[m] = a.Qin[(size_t)m * N + i];
+                if (m < M) x[m] = a.Qin[(size_t)m * ns + s];
         }
     } else {
 #pragma unroll
-        for (int m = 0; m < MP; m++) x[m] = (valid && m < M && a.U) ? -a.U[(size_t)m * N + i] : 0.f;
+        for (int m = 0; m < MP; m++) x[m] = (valid && m < M && a.U) ? -a.U[(size_t)m * ns + s] : 0.f;
     }
+
+    // ---- 3. wait for the copies (bounded; a timeout is reported, never a hang)
+    if (any_staged) {
+        const bool ok = mbar_wait_bounded(&mbar, 0);
+        if (__syncthreads_or(!ok)) {
+            if (li == 0) dcrf_set_error(a.status, DCRF_ERR_TIMEOUT, t);
+            mbar_wait_bounded(&mbar, 0);  // let this CTA's own copies land before it exits
+            return;
+        }
+    }
+
+    // ---- 4. messages of every term
     if (mode & PP_MSG) {
         for (int k = 0; k < a.ts.n; k++) {
             const TermDev &T = a.ts.t[k];
-            const int pb = T.tile_pbeg[t], np = T.tile_pbeg[t + 1] - pb;
-            const bool staged = np <= SM::SV_ROWS;
-            if (staged) {
-                // stage the tile's vertex rows: row p = V[part_v[pb + p] + 1]
-                if constexpr (MP % 4 == 0) {
-                    constexpr int C4 = MP / 4;
-                    float4 *d4 = reinterpret_cast<float4 *>(sV);
-                    for (int x = li; x < np * C4; x += SPLAT_TILE) {
-                        const int p = x / C4, c = x - p * C4;
-                        d4[x] = __ldg(reinterpret_cast<const float4 *>(T.V + (size_t)(T.part_v[pb + p] + 1) * MP) + c);
-                    }
-                } else {
-                    for (int x = li; x < np * MP; x += SPLAT_TILE) {
-                        const int p = x / MP, c = x - p * MP;
-                        sV[x] = __ldg(T.V + (size_t)(T.part_v[pb + p] + 1) * MP + c);
-                    }
-                }
-            }
-            __syncthreads();
-            if (valid) {
-                float acc[MP];
-                slice_tiled<MP>(T, t, li, staged, pb, sV, acc);
-                if (T.post_norm) {
-                    const float nn = T.norm[i];
+            const TileBlocks b = sTB[k];
+            if (!valid) continue;
+            float acc[MP];
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
+            for (int m = 0; m < MP; m++) acc[m] = 0.f;
+            const size_t tb = (size_t)t * SPLAT_TILE * (T.d + 1);
+            const uint16_t *locs = T.staged ? reinterpret_cast<const uint16_t *>(smem + T.sm_loc) : T.tl_loc + tb;
+            const float *ws = T.staged ? reinterpret_cast<const float *>(smem + T.sm_w) : T.tl_w + tb;
+            const float *vps = reinterpret_cast<const float *>(smem + T.sm_vp);
+            const bool rows_smem = T.staged && b.vp_staged;
+            const float alpha = T.alpha;
+            const bool seq = T.seq;
+            for (int r = 0; r <= T.d; r++) {
+                const int loc = locs[r * SPLAT_TILE + li];
+                const float bw = ws[r * SPLAT_TILE + li];
+                float v[MP];
+                if (rows_smem)
+                    load_row_smem<MP>(vps + loc * MP, v);
+                else
+                    load_row<MP>(T.pv + (size_t)(b.pb + loc) * MP, v);
+                if (seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
+#pragma unroll
+                    for (int m = 0; m < MP; m++) acc[m] = fmaf(fmul(bw, v[m]), alpha, acc[m]);
+                } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
+                    const float w = fmul(bw, alpha);
+#pragma unroll
+                    for (int m = 0; m < MP; m++) acc[m] = fmaf(w, v[m], acc[m]);
                 }
-                // with given marginals this is the pairwise part of klDivergence
-                // (densecrf.cpp:229-233): sum Q * compat(K Q)
-                fold_compat<MP>(T, acc, x, M, given, kl);
             }
-            __syncthreads();
+            if (T.post_norm) {
+                const float nn = T.staged ? reinterpret_cast<const float *>(smem + T.sm_norm)[li] : T.norm[s];
+#pragma unroll
+                for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
+            }
+            // with given marginals this is the pairwise part of klDivergence
+            // (densecrf.cpp:229-233): sum Q * compat(K Q)
+            fold_compat<MP>(T, acc, x, M, given, kl);
         }
     }
+
+    // ---- 5. softmax and outputs
     if (valid && !given) {
-        // softmax (densecrf.cpp:98-106)
         float mx = x[0];
 #pragma unroll
         for (int m = 1; m < MP; m++)
             if (m < M) mx = fmaxf(mx, x[m]);
-        float s = 0.f;
+        float sum = 0.f;
 #pragma unroll
         for (int m = 0; m < MP; m++)
             if (m < M) {
                 x[m] = expf(fsub(x[m], mx));
-                s = fadd(s, x[m]);
+                sum = fadd(sum, x[m]);
             }
+        const float rs = __frcp_rn(sum);
 #pragma unroll
-        for (int m = 0; m < MP; m++) x[m] = m < M ? __fdiv_rn(x[m], s) : 0.f;
+        for (int m = 0; m < MP; m++) x[m] = m < M ? fmul(x[m], rs) : 0.f;
     }
-    float (&q)[MP] = x;
+    float(&q)[MP] = x;
     if (valid) {
         if (mode & PP_KL) {
             // entropy and unary parts (densecrf.cpp:216-226); log() there is the double overload
@@ -247,13 +348,13 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
             for (int m = 0; m < MP; m++)
                 if (m < M) {
                     kl += (double)q[m] * log((double)fmaxf(q[m], 1e-20f));
-                    if (a.U) kl += (double)fmul(a.U[(size_t)m * N + i], q[m]);
+                    if (a.U) kl += (double)fmul(a.U[(size_t)m * ns + s], q[m]);
                 }
         }
         if (mode & PP_WRITE_Q) {
 #pragma unroll
             for (int m = 0; m < MP; m++)
-                if (m < M) a.Qout[(size_t)m * N + i] = q[m];
+                if (m < M) a.Qout[(size_t)m * ns + s] = q[m];
         }
         if (mode & PP_MAP) {
             int best = 0;
@@ -273,69 +374,89 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
         if ((li & 31) == 0) sKL[li >> 5] = kl;
         __syncthreads();
         if (li == 0) {
-            double s = 0.0;
-            for (int w = 0; w < SPLAT_TILE / 32; w++) s += sKL[w];
-            a.kl_part[t] = s;
+            double ssum = 0.0;
+            for (int w = 0; w < SPLAT_TILE / 32; w++) ssum += sKL[w];
+            a.kl_part[t] = ssum;
         }
     }
+
+    // ---- 6. splat the tile's q into each term's partials (every thread takes part)
+    // Each task sums at most SPLAT_TASK members of one partial (fixed order);
+    // a partial made of several tasks adds the task sums in task order.
     if (mode & PP_SPLAT) {
-        // splat the tile's q into each term's partials (every thread takes part)
-        constexpr int G = Grp<MP>::G, CH = Grp<MP>::CH, NG = SPLAT_TILE / G;
-        const int lg_ = li % G, gid = li / G;
-        for (int k = 0; k < a.ts.n; k++) {
-            const TermDev &T = a.ts.t[k];
-            const float nn = (valid && T.pre_norm) ? T.norm[i] : 1.f;
+        float *sQ = reinterpret_cast<float *>(smem + a.sm_q);
+        float *sRes = reinterpret_cast<float *>(smem + a.sm_res);
+        __syncthreads();  // the slice phase is done with the regions sQ aliases
 #pragma unroll
-            for (int m = 0; m < MP; m++) sQ[li * MP + m] = T.pre_norm ? fmul(q[m], nn) : q[m];
-            const int pb = T.tile_pbeg[t], pe = T.tile_pbeg[t + 1];
-            const int mbase = T.part_mbeg[pb], nmem = T.part_mbeg[pe] - mbase;
-            const bool staged = nmem <= SM::MCAP;
-            if (staged) {
-                for (int x = li; x < nmem; x += SPLAT_TILE) {
-                    sMpt[x] = T.mem_pt[mbase + x];
-                    sMw[x] = T.mem_w[mbase + x];
+        for (int m = 0; m < MP; m++) sQ[li * MP + m] = q[m];
+        __syncthreads();
+        for (int k = 0; k < a.ts.n; k++) {
+            // the normalisation before the filter (pairwise.cpp:65-66) is folded into
+            // the member weights of the term (w * norm of the member's point)
+            const TermDev &T = a.ts.t[k];
+            const TileBlocks b = sTB[k];
+            const size_t tbm = (size_t)t * SPLAT_TILE * (T.d + 1);
+            const uint32_t *tasks = T.staged ? reinterpret_cast<const uint32_t *>(smem + T.sm_task) + (b.tb - b.a0)
+                                             : T.task + b.tb;
+            const uint16_t *mpt = T.staged ? reinterpret_cast<const uint16_t *>(smem + T.sm_mpt) : T.mem_pt + tbm;
+            const float *mw = T.staged ? reinterpret_cast<const float *>(smem + T.sm_mw) : T.mem_w + tbm;
+            for (int j = li; j < b.nt; j += SPLAT_TILE) {
+                const uint32_t tk = tasks[j];
+                const int pl = (int)(tk >> 19), e0 = (int)((tk >> 6) & 0x1FFFu), len = (int)(tk & 63u);
+                float acc[MP];
+#pragma unroll
+                for (int m = 0; m < MP; m++) acc[m] = 0.f;
+                for (int e = e0; e < e0 + len; e++) {
+                    const float w = mw[e];
+                    float v[MP];
+                    load_row_smem<MP>(sQ + mpt[e] * MP, v);
+#pragma unroll
+                    for (int m = 0; m < MP; m++) acc[m] = fmaf(w, v[m], acc[m]);
                 }
-                for (int x = li; x <= pe - pb; x += SPLAT_TILE) sPmb[x] = T.part_mbeg[pb + x] - mbase;
+                const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
+                const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
+                float *dst = (first && last) ? T.pv + (size_t)(b.pb + pl) * MP : sRes + (size_t)j * MP;
+                if constexpr (MP % 4 == 0) {
+#pragma unroll
+                    for (int c = 0; c < MP / 4; c++)
+                        reinterpret_cast<float4 *>(dst)[c] =
+                            make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2], acc[4 * c + 3]);
+                } else {
+#pragma unroll
+                    for (int m = 0; m < MP; m++) dst[m] = acc[m];
+                }
             }
             __syncthreads();
-            for (int p = pb + gid; p < pe; p += NG) {
-                float acc[CH];
+            for (int j = li; j < b.nt; j += SPLAT_TILE) {
+                const int pl = (int)(tasks[j] >> 19);
+                const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
+                const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
+                if (!first || last) continue;
+                float acc[MP];
+                load_row_smem<MP>(sRes + (size_t)j * MP, acc);
+                for (int jj = j + 1; jj < b.nt && (int)(tasks[jj] >> 19) == pl; jj++) {
+                    float v[MP];
+                    load_row_smem<MP>(sRes + (size_t)jj * MP, v);
 #pragma unroll
-                for (int c = 0; c < CH; c++) acc[c] = 0.f;
-                if (staged) {
-                    const int mb = sPmb[p - pb], me = sPmb[p - pb + 1];
-                    for (int e = mb; e < me; e++) {
-                        const float w = sMw[e];
-                        const float *row = sQ + sMpt[e] * MP + lg_;
-#pragma unroll
-                        for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], fmul(w, row[c * G]));
-                    }
-                } else {
-                    const int mb = T.part_mbeg[p], me = T.part_mbeg[p + 1];
-                    for (int e = mb; e < me; e++) {
-                        const float w = T.mem_w[e];
-                        const float *row = sQ + T.mem_pt[e] * MP + lg_;
-#pragma unroll
-                        for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], fmul(w, row[c * G]));
-                    }
+                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], v[m]);
                 }
-                float *dst = T.partial + (size_t)p * MP + lg_;
+                float *dst = T.pv + (size_t)(b.pb + pl) * MP;
 #pragma unroll
-                for (int c = 0; c < CH; c++) dst[c * G] = acc[c];
+                for (int m = 0; m < MP; m++) dst[m] = acc[m];
             }
             __syncthreads();
         }
     }
 }
 
-// Value-size-1 normalisation slice and raw lattice filter (point-order gather;
-// used off the iteration loop).
+// Value-size-1 normalisation slice and raw lattice filter (point-order gather
+// from the vertex-order blurred values; used off the iteration loop).
 template <int MP>
 __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPArgs a) {
-    const int t = blockIdx.x;
-    const int i = a.slot_pt[(size_t)t * SPLAT_TILE + threadIdx.x];
+    const size_t s = (size_t)blockIdx.x * SPLAT_TILE + threadIdx.x;
+    const int i = a.slot_pt[s];
     if (i < 0) return;
-    const int N = a.N, M = a.M;
+    const int N = a.N, M = a.M, ns = a.nslots;
     if (a.mode & PP_NORM) {
         // value size 1, seqCompute slice: out += (w * v) * alpha (permutohedral.cpp:513-521)
         for (int k = 0; k < a.ts.n; k++) {
@@ -353,7 +474,7 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
                 out = n;  // raw K*1; the host derives the mean (pairwise.cpp:46-53)
             else  // pairwise.cpp:58-61
                 out = __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
-            a.norm_out[k][i] = out;
+            a.norm_out[k][s] = out;
         }
         return;
     }
@@ -378,14 +499,14 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
     }
 #pragma unroll
     for (int m = 0; m < MP; m++)
-        if (m < M) a.Qout[(size_t)m * N + i] = acc[m];
+        if (m < M) a.Qout[(size_t)m * ns + s] = acc[m];
 }
 
 template <int MP>
 __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ ReduceArgs a) {
     constexpr int G = Grp<MP>::G, CH = Grp<MP>::CH;
     const long long gidx = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
-    const int lg_ = threadIdx.x % G;
+    const int lgi = threadIdx.x % G;
     if (gidx >= a.begin[a.n]) return;
     int k = 0;
     while (gidx >= a.begin[k + 1]) k++;
@@ -399,14 +520,14 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
     // read back to back (independent loads), added in list order
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     for (int b = s0; b < s1; b += G) {
-        const int mine = (b + lg_ < s1) ? T.red_list[b + lg_] : 0;
+        const int mine = (b + lgi < s1) ? T.red_list[b + lgi] : 0;
         const int cnt = min(G, s1 - b);
         float rowv[G][CH];
 #pragma unroll
         for (int j = 0; j < G; j++) {
             const int p = __shfl_sync(gmask, mine, j, G);
 #pragma unroll
-            for (int c = 0; c < CH; c++) rowv[j][c] = j < cnt ? T.partial[(size_t)p * MP + lg_ + c * G] : 0.f;
+            for (int c = 0; c < CH; c++) rowv[j][c] = j < cnt ? T.partial[(size_t)p * MP + lgi + c * G] : 0.f;
         }
 #pragma unroll
         for (int j = 0; j < G; j++)
@@ -415,7 +536,7 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
                 for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], rowv[j][c]);
             }
     }
-    float *dst = T.V + (size_t)(v + 1) * MP + lg_;
+    float *dst = T.V + (size_t)(v + 1) * MP + lgi;
 #pragma unroll
     for (int c = 0; c < CH; c++) dst[c * G] = acc[c];
 }
@@ -451,33 +572,59 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
     }
 #pragma unroll
     for (int e = 0; e < VEC; e++) {
-        const float s = fadd(x1[e], x2[e]);
+        const float sm = fadd(x1[e], x2[e]);
         if (SEQ)  // seqCompute: old + 0.5*(n1+n2) evaluated in double (permutohedral.cpp:505)
-            y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)s));
+            y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)sm));
         else  // sseCompute: float (permutohedral.cpp:566)
-            y[e] = fadd(x0[e], fmul(0.5f, s));
+            y[e] = fadd(x0[e], fmul(0.5f, sm));
     }
-    if constexpr (VEC == 4) {
-        *reinterpret_cast<float4 *>(T.Vout + o0) = make_float4(y[0], y[1], y[2], y[3]);
-    } else {
+    if (T.Vout) {
+        if constexpr (VEC == 4) {
+            *reinterpret_cast<float4 *>(T.Vout + o0) = make_float4(y[0], y[1], y[2], y[3]);
+        } else {
 #pragma unroll
-        for (int e = 0; e < VEC; e++) T.Vout[o0 + e] = y[e];
+            for (int e = 0; e < VEC; e++) T.Vout[o0 + e] = y[e];
+        }
+    }
+    if (T.pv) {
+        const int s0 = T.red_beg[v], s1 = T.red_beg[v + 1];
+        for (int q = s0; q < s1; q++) {
+            float *dst = T.pv + (size_t)T.red_list[q] * MP + c * VEC;
+            if constexpr (VEC == 4) {
+                *reinterpret_cast<float4 *>(dst) = make_float4(y[0], y[1], y[2], y[3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < VEC; e++) dst[e] = y[e];
+            }
+        }
     }
 }
 
-__global__ void transpose_kernel(const float *__restrict__ in, float *__restrict__ out, int rows, int cols) {
-    __shared__ float tile[32][33];
-    int c = blockIdx.x * 32 + threadIdx.x;
-    int r0 = blockIdx.y * 32;
-    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-        int r = r0 + y;
-        if (r < rows && c < cols) tile[y][threadIdx.x] = in[(size_t)r * cols + c];
+// out[m][slot] = in(m, slot_pt[slot]) or 0
+__global__ void to_slots_kernel(const float *__restrict__ in, int point_major, int M, int N,
+                                const int *__restrict__ slot_pt, int nslots, float *__restrict__ out) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)nslots) return;
+    const int pt = slot_pt[s];
+    for (int m = 0; m < M; m++) {
+        float v = 0.f;
+        if (pt >= 0) v = point_major ? in[(size_t)pt * M + m] : in[(size_t)m * N + pt];
+        out[(size_t)m * nslots + s] = v;
     }
-    __syncthreads();
-    int oc = r0 + threadIdx.x;  // output column = input row
-    for (int y = threadIdx.y; y < 32; y += blockDim.y) {
-        int orow = blockIdx.x * 32 + y;  // output row = input column
-        if (orow < cols && oc < rows) out[(size_t)orow * rows + oc] = tile[threadIdx.x][y];
+}
+
+// out(m, pt) = in[m][pt_slot[pt]]
+__global__ void from_slots_kernel(const float *__restrict__ in, int M, int N, int nslots,
+                                  const int *__restrict__ pt_slot, int point_major, float *__restrict__ out) {
+    const size_t pt = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= (size_t)N) return;
+    const size_t s = (size_t)pt_slot[pt];
+    for (int m = 0; m < M; m++) {
+        const float v = in[(size_t)m * nslots + s];
+        if (point_major)
+            out[pt * M + m] = v;
+        else
+            out[(size_t)m * N + pt] = v;
     }
 }
 
@@ -513,30 +660,44 @@ __global__ void scale_features_kernel(const float *__restrict__ in, float *__res
     }
 }
 
-__global__ void argmax_kernel(const float *__restrict__ Q, int M, int N, int16_t *__restrict__ out) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= N) return;
-    int best = 0;
-    float bv = Q[p];
-    for (int m = 1; m < M; m++) {
-        float v = Q[(size_t)m * N + p];
-        if (v > bv) {
-            bv = v;
-            best = m;
-        }
-    }
-    out[p] = (int16_t)best;
+__global__ void scale_members_kernel(const uint16_t *__restrict__ mem_pt, const float *__restrict__ mem_w,
+                                     const float *__restrict__ norm, int d1, float *__restrict__ wn) {
+    const int t = blockIdx.x;
+    const size_t base = (size_t)t * SPLAT_TILE * d1;
+    for (int e = threadIdx.x; e < SPLAT_TILE * d1; e += blockDim.x)
+        wn[base + e] = fmul(mem_w[base + e], norm[(size_t)t * SPLAT_TILE + mem_pt[base + e]]);
 }
 
 // ---------------------------------------------------------------------------
+int pointpass_smem_budget(int MP) { return MP <= 20 ? 72 * 1024 : 108 * 1024; }
+
 template <int MP>
 static cudaError_t pp_launch(const PPArgs &a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
-    if (a.mode & (PP_NORM | PP_FILTER))
+    if (a.mode & (PP_NORM | PP_FILTER)) {
         DCRF_LAUNCH(slice_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
-    else
-        DCRF_LAUNCH(pointpass_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
+    } else {
+        DCRF_LAUNCH(pointpass_kernel<MP><<<a.ntiles, SPLAT_TILE, a.smem_bytes, s>>>(a));
+    }
     return cudaGetLastError();
+}
+
+template <int MP>
+static void pp_prepare() {
+    cudaFuncSetAttribute(pointpass_kernel<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, pointpass_smem_budget(MP));
+}
+
+void prepare_pointpass_kernels() {
+    pp_prepare<1>();
+    pp_prepare<2>();
+    pp_prepare<4>();
+    pp_prepare<8>();
+    pp_prepare<12>();
+    pp_prepare<16>();
+    pp_prepare<20>();
+    pp_prepare<24>();
+    pp_prepare<28>();
+    pp_prepare<32>();
 }
 
 cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s) {
@@ -586,8 +747,8 @@ static cudaError_t blur_launch(const BlurArgs &a, cudaStream_t s) {
 }
 
 cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s) {
-#define DCRF_BL(X)                                                    \
-    case X:                                                           \
+#define DCRF_BL(X) \
+    case X:        \
         return seq ? blur_launch<X, true>(a, s) : blur_launch<X, false>(a, s);
     switch (MP) {
         DCRF_BL(1) DCRF_BL(2) DCRF_BL(4) DCRF_BL(8) DCRF_BL(12) DCRF_BL(16) DCRF_BL(20) DCRF_BL(24) DCRF_BL(28)
@@ -597,10 +758,23 @@ cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s) {
 #undef DCRF_BL
 }
 
-cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t s) {
-    if (rows <= 0 || cols <= 0) return cudaSuccess;
-    dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
-    DCRF_LAUNCH(transpose_kernel<<<grid, block, 0, s>>>(in, out, rows, cols));
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *slot_pt, int nslots,
+                            float *out, cudaStream_t s) {
+    if (nslots > 0)
+        DCRF_LAUNCH(to_slots_kernel<<<(nslots + 255) / 256, 256, 0, s>>>(in, point_major, M, N, slot_pt, nslots, out));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_from_slots(const float *in, int M, int N, int nslots, const int *pt_slot, int point_major,
+                              float *out, cudaStream_t s) {
+    if (N > 0)
+        DCRF_LAUNCH(from_slots_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, N, nslots, pt_slot, point_major, out));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_scale_members(const uint16_t *mem_pt, const float *mem_w, const float *norm, int ntiles, int d1,
+                                 float *wn, cudaStream_t s) {
+    if (ntiles > 0) DCRF_LAUNCH(scale_members_kernel<<<ntiles, 256, 0, s>>>(mem_pt, mem_w, norm, d1, wn));
     return cudaGetLastError();
 }
 
@@ -614,11 +788,6 @@ cudaError_t launch_features_2d(int W, int H, float sx, float sy, const uint8_t *
 cudaError_t launch_scale_features(const float *in, float *out, const float *P, int d, int N, int full,
                                   cudaStream_t s) {
     if (N > 0) DCRF_LAUNCH(scale_features_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, out, P, d, N, full));
-    return cudaGetLastError();
-}
-
-cudaError_t launch_argmax(const float *Q, int M, int N, int16_t *out, cudaStream_t s) {
-    if (N > 0) DCRF_LAUNCH(argmax_kernel<<<(N + 255) / 256, 256, 0, s>>>(Q, M, N, out));
     return cudaGetLastError();
 }
 

@@ -20,14 +20,18 @@ enum : int {
 
 struct PPArgs {
     int N, M, mode;
-    int ntiles;
-    const int *slot_pt;  // [ntiles*SPLAT_TILE]
-    const float *U;      // [M][N] or nullptr (no unary: zero)
-    const float *Qin;    // [M][N]
-    float *Qout;         // [M][N]
-    int16_t *map_out;    // [N]
+    int ntiles, nslots;
+    const int *slot_pt;  // [nslots] point of each tile slot, -1 = empty
+    const float *U;      // [M][nslots] or nullptr (no unary: zero)
+    const float *Qin;    // [M][nslots]
+    float *Qout;         // [M][nslots]
+    int16_t *map_out;    // [N] (point order)
     double *kl_part;     // [ntiles]
-    // PP_NORM outputs, per term
+    DevStatus *status;
+    int smem_bytes;      // dynamic shared memory of the point pass
+    int sm_q;            // offset of the splat's q rows (aliases the slice-phase regions)
+    int sm_res;          // offset of the splat's per-task results (after the q rows)
+    // PP_NORM outputs, per term ([nslots] each)
     float *norm_out[DCRF_MAX_TERMS];
     int ntype[DCRF_MAX_TERMS];
     TermSet ts;
@@ -49,10 +53,13 @@ struct BlurArgs {
     int n;
     struct T {
         const float *Vin;
-        float *Vout;
-        const int2 *nbr;  // [d+1][L]
+        float *Vout;          // vertex order output (may be null when only scattering)
+        const int2 *nbr;      // [d+1][L]
         int L;
         int axis;
+        const int *red_beg;   // scatter of the result into partial order (last pass of the
+        const int *red_list;  // mean-field filter): pv[red_list[s]] = out[v], s in red_beg[v..v+1)
+        float *pv;            // null: no scatter
     } t[DCRF_MAX_TERMS];
     long long begin[DCRF_MAX_TERMS + 1];  // prefix of (vertex, vector) work over terms
 };
@@ -62,14 +69,23 @@ cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s);
 
-// Layout conversions between the device's label-major [M][N] and a padded or
-// point-major view.
-cudaError_t launch_transpose(const float *in, float *out, int rows, int cols, cudaStream_t s);  // out[c][r] = in[r][c]
+// Layout conversions between user layouts (label-major [M][N] or point-major
+// [N][M]) and the slot-major [M][nslots] device layout.
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *slot_pt, int nslots,
+                            float *out, cudaStream_t s);
+cudaError_t launch_from_slots(const float *in, int M, int N, int nslots, const int *pt_slot, int point_major,
+                              float *out, cudaStream_t s);
 // 2D features of DenseCRF2D (densecrf.cpp:61-81) into [d][N]
 cudaError_t launch_features_2d(int W, int H, float sx, float sy, const uint8_t *rgb, float sr, float sg, float sb,
                                float *feat, cudaStream_t s);
 cudaError_t launch_scale_features(const float *in, float *out, const float *scale_or_matrix, int d, int N, int full,
                                   cudaStream_t s);
-cudaError_t launch_argmax(const float *Q, int M, int N, int16_t *out, cudaStream_t s);
+// wn[e] = w[e] * norm[slot of member e] over the padded per-tile member lists
+cudaError_t launch_scale_members(const uint16_t *mem_pt, const float *mem_w, const float *norm, int ntiles, int d1,
+                                 float *wn, cudaStream_t s);
+// Opts every point-pass instantiation in to its dynamic shared-memory budget.
+void prepare_pointpass_kernels();
+// Largest dynamic shared memory the point pass may use per CTA.
+int pointpass_smem_budget(int MP);
 
 }  // namespace dcrf
