@@ -209,6 +209,34 @@ int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count)
  * blur).  value_size must equal 1 or the handle's M. */
 int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out);
 
+/* ---- allocation-free variant ---------------------------------------------- */
+
+/* Maximum scratch of dcrf_lattice_filter_noalloc, in floats (32 MiB), held in a
+ * static device array by every GPU that loads the library, until exit. */
+#define DCRF_NOALLOC_MAX_FLOATS (8u * 1024u * 1024u)
+
+/* The raw lattice filter of dcrf_lattice_filter, for callers that must not
+ * allocate device memory while they run: code working inside a fixed memory
+ * budget owned by another allocator (a framework's caching allocator, a
+ * serving runtime), or a pipeline that forbids cudaMalloc/cudaFree after
+ * start-up because they synchronise the device and take unbounded time.  It
+ * calls no cudaMalloc, cudaFree or allocating library routine: its scratch is
+ * one static device array of DCRF_NOALLOC_MAX_FLOATS floats.  Term `term` must
+ * already be built (dcrf_add_pairwise*).
+ *   in, out: DEVICE pointers, (value_size, N) label-major; value_size is 1 or M.
+ *   stream:  cudaStream_t the work is ordered on (NULL: the legacy default
+ *            stream); the call returns once the work is enqueued.
+ * The first call on a device resolves the array's address on that device
+ * (cudaGetSymbolAddress) and should come before any stream capture.  All calls
+ * share the one array and it keeps the last call's contents: calls that may
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  A problem whose scratch exceeds the maximum
+ * (value_size*slots + (partials+1)*P + 2*(vertices+1)*P floats, P the padded
+ * value size) is rejected with DCRF_ERR_INVALID_ARG.
+ * No counterpart in the reference (added for allocation-free callers). */
+int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out,
+                                void *stream);
+
 #ifdef __cplusplus
 }
 #endif

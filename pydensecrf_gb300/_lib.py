@@ -62,6 +62,7 @@ _SIGS = {
     "dcrf_profile": ([_vp, _i, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong)], _i),
     "dcrf_term_stats": ([_vp, _i, _pi, _pi, _pi], _i),
     "dcrf_term_buffer": ([_vp, _i, _i, _vp, ctypes.c_size_t], _i),
+    "dcrf_lattice_filter_noalloc": ([_vp, _i, _vp, _i, _i, _vp, _vp], _i),
 }
 
 _LIB = None

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -1115,3 +1116,99 @@ int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count)
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free raw filter: scratch in one static device array per GPU.
+// ---------------------------------------------------------------------------
+namespace {
+
+// Scratch of dcrf_lattice_filter_noalloc.  Every GPU that loads the library
+// holds these DCRF_NOALLOC_MAX_FLOATS floats until the process exits.
+static __device__ __align__(256) float g_noalloc_scratch[DCRF_NOALLOC_MAX_FLOATS];
+
+std::mutex g_noalloc_mu;
+float *g_noalloc_ptr[256] = {};
+
+// Device address of the scratch array on `device`, resolved once with that
+// device current.  (In host code the array's name is only a host-side stand-in,
+// never a device address.)
+int noalloc_scratch(int device, float **out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (device < 0 || device >= 256) return set_err(DCRF_ERR_INVALID_ARG, "device ordinal out of range");
+    if (!g_noalloc_ptr[device]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return set_err(DCRF_ERR_CUDA, std::string("cudaGetSymbolAddress of the scratch array: ") +
+                                              cudaGetErrorString(e));
+        g_noalloc_ptr[device] = static_cast<float *>(p);
+    }
+    *out = g_noalloc_ptr[device];
+    return DCRF_OK;
+}
+
+size_t pad64(size_t n) { return (n + 63) & ~(size_t)63; }
+
+}  // namespace
+
+extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *in, int value_size, int reverse,
+                                           float *out, void *stream) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
+    if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
+    const bool v1 = value_size == 1;
+    const int MPv = v1 ? 1 : h->MP;
+    Term &T = h->terms[term];
+    const size_t n_in = pad64((size_t)value_size * h->nslots);
+    const size_t n_pv = pad64(((size_t)T.lat.P + 1) * MPv);
+    const size_t n_v = pad64(((size_t)T.lat.L + 1) * MPv);
+    const size_t need = n_in + n_pv + 2 * n_v;
+    if (need > (size_t)DCRF_NOALLOC_MAX_FLOATS)
+        return set_err(DCRF_ERR_INVALID_ARG, "this filter needs " + std::to_string(need) +
+                                                 " floats of scratch; the allocation-free entry point has " +
+                                                 std::to_string((size_t)DCRF_NOALLOC_MAX_FLOATS));
+    float *scr = nullptr;
+    if ((rc = noalloc_scratch(h->device, &scr))) return rc;
+    float *in_s = scr, *pv = in_s + n_in, *V0 = pv + n_pv, *V1 = V0 + n_v;
+    float *Vb[2] = {V0, V1};
+    cudaStream_t s = (cudaStream_t)stream;
+    // the array keeps the previous call's contents: the zero sentinel rows are restored
+    CU(cudaMemsetAsync(V0, 0, sizeof(float) * MPv, s));
+    CU(cudaMemsetAsync(V1, 0, sizeof(float) * MPv, s));
+    CU(launch_to_slots(in, 0, value_size, h->N, h->slot_pt, h->nslots, in_s, s));
+    std::vector<int> one{term};
+    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
+    a.ts.t[0].pre_norm = 0;
+    a.ts.t[0].mem_w = T.lat.mem_w;
+    a.ts.t[0].pv = pv;
+    a.Qin = in_s;
+    CU(launch_pointpass(a, MPv, s));
+    ReduceArgs ra{};
+    ra.n = 1;
+    ra.begin[0] = 0;
+    ra.begin[1] = T.lat.L;
+    ra.t[0] = {T.lat.red_beg, T.lat.red_list, pv, V0, T.lat.L};
+    CU(launch_reduce(ra, MPv, s));
+    const int NV = MPv % 4 == 0 ? MPv / 4 : MPv % 2 == 0 ? MPv / 2 : MPv;
+    const bool seq = v1 || h->M <= 2 || T.variant == DCRF_VARIANT_SCALAR;
+    for (int pass = 0; pass <= T.d; pass++) {
+        BlurArgs ba{};
+        ba.n = 1;
+        ba.begin[0] = 0;
+        ba.begin[1] = (long long)T.lat.L * NV;
+        ba.t[0].Vin = Vb[pass & 1];
+        ba.t[0].Vout = Vb[(pass + 1) & 1];
+        ba.t[0].nbr = T.lat.nbr;
+        ba.t[0].L = T.lat.L;
+        ba.t[0].axis = reverse ? T.d - pass : pass;
+        ba.t[0].pv = nullptr;
+        CU(launch_blur(ba, MPv, seq, s));
+    }
+    PPArgs f = pp_args(h, PP_FILTER, one, reverse != 0, v1);
+    f.ts.t[0].V = Vb[(T.d + 1) & 1];
+    f.Qout = in_s;
+    CU(launch_pointpass(f, MPv, s));
+    CU(launch_from_slots(in_s, value_size, h->N, h->nslots, h->pt_slot, 0, out, s));
+    return ok();
+}
