@@ -156,6 +156,42 @@ int dcrf_synchronize(dcrf_crf *h);
  * lets one handle solve a sequence of images without reallocating. */
 int dcrf_clear_pairwise(dcrf_crf *h);
 
+/* ---- learning: parameters and the adjoint --------------------------------- */
+
+/* Replaces term `term`'s label compatibility (kind and values as in
+ * dcrf_add_pairwise).  Counterpart of LabelCompatibility::setParameters /
+ * DenseCRF::setLabelCompatibilityParameters (labelcompatibility.cpp:54-56,
+ * 73-75,95-100; densecrf.cpp:321-333), with full values instead of the
+ * reference's packed vector. */
+int dcrf_set_compat(dcrf_crf *h, int term, int compat_kind, const float *compat);
+
+/* Kernel parameters of term `term` (DenseKernel::setParameters,
+ * pairwise.cpp:140-151): DIAG_KERNEL d scales p (features become p_j * f_j),
+ * FULL_KERNEL a d x d matrix P, row-major (features become P f).  Rebuilds the
+ * lattice and the normalisation.  CONST_KERNEL has no parameters. */
+int dcrf_set_kernel_params(dcrf_crf *h, int term, const float *params);
+
+/* Number of compatibility and kernel parameters of term `term` in the layout
+ * of dcrf_backward: compatibility Potts 1, Diagonal M, Matrix M*M; kernel
+ * CONST 0, DIAG d, FULL d*d. */
+int dcrf_param_counts(dcrf_crf *h, int term, int *n_compat, int *n_kernel);
+
+/* inference(n) that also keeps every iterate Q_0..Q_T on the device, for
+ * dcrf_backward (the per-iteration storage of DenseCRF::gradient,
+ * densecrf.cpp:240-253). */
+int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int layout, int where);
+
+/* Adjoint of the last dcrf_inference_checkpointed (DenseCRF::gradient,
+ * densecrf.cpp:255-296, for any loss): given dQ = dL/dQ_T (M x N in `layout`,
+ * `where`), writes dU = dL/dU (same layout and place; NULL to skip), and, on the
+ * HOST, dcompat = dL/d(compatibility values) and dkernel = dL/d(kernel
+ * parameters), each the concatenation over terms in dcrf_param_counts order
+ * (NULL to skip; kernel gradients cost extra lattice passes).  For a Matrix
+ * compatibility the M*M values are dL/dW for the symmetrised W actually used.
+ * The lattice filter's transpose is the reverse-order blur
+ * (permutohedral.cpp:556). */
+int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU, double *dcompat, double *dkernel);
+
 /* ---- measurement -------------------------------------------------------- */
 
 /* Number of kernels this library has launched in the process so far. */

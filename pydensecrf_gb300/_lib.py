@@ -63,6 +63,11 @@ _SIGS = {
     "dcrf_term_stats": ([_vp, _i, _pi, _pi, _pi], _i),
     "dcrf_term_buffer": ([_vp, _i, _i, _vp, ctypes.c_size_t], _i),
     "dcrf_lattice_filter_noalloc": ([_vp, _i, _vp, _i, _i, _vp, _vp], _i),
+    "dcrf_set_compat": ([_vp, _i, _i, _vp], _i),
+    "dcrf_set_kernel_params": ([_vp, _i, _vp], _i),
+    "dcrf_param_counts": ([_vp, _i, _pi, _pi], _i),
+    "dcrf_inference_checkpointed": ([_vp, _i, _vp, _i, _i], _i),
+    "dcrf_backward": ([_vp, _vp, _i, _i, _vp, _vp, _vp], _i),
 }
 
 _LIB = None

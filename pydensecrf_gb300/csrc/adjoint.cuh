@@ -1,0 +1,37 @@
+// adjoint.cuh -- device kernels of the mean-field adjoint (see adjoint.cu).
+#pragma once
+#include "dcrf_common.cuh"
+
+namespace dcrf {
+
+struct SliceGradArgs {
+    int N, M, d, nslots;
+    const int *slot_pt;   // [nslots]
+    const int *off;       // [d+1][N]
+    const uint8_t *rank;  // [d+1][N]
+    const float *V;       // [L+1][MP] blurred values, vertex order
+    const float *z;       // [M][nslots] contraction values
+    float sf[DCRF_MAX_D];
+    float alpha;          // 1/(1+2^-d) / (d+1)
+    float *df;            // [N][d] accumulated feature gradient
+};
+
+cudaError_t launch_softmax_adjoint(const float *Q, const float *x, float *b, int M, int ns, const int *slot_pt,
+                                   cudaStream_t s);
+cudaError_t launch_compat(const float *x, float *y, int M, int ns, int kind, float potts_w, const float *C,
+                          int transpose, int accumulate, cudaStream_t s);
+cudaError_t launch_scale_norm(const float *x, float *y, const float *norm, int M, int ns, int pw, cudaStream_t s);
+cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const float *x4, float scale,
+                        const float *norm, int pw, float *y, int M, int ns, cudaStream_t s);
+cudaError_t launch_add(const float *x, float *y, size_t n, cudaStream_t s);
+cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cudaStream_t s);
+int label_products_blocks(int ns);
+// mode 0: out[m] (+)= sum a[m].*b[m]; mode 1: out[m*M+k] (+)= sum a[m].*b[k]; part: [blocks][K] doubles
+cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
+                                  double *part, double *out, int accumulate, cudaStream_t s);
+cudaError_t launch_slice_grad(const SliceGradArgs &a, int MP, cudaStream_t s);
+int kernel_param_blocks(int N);
+cudaError_t launch_kernel_param_grad(const float *f, const float *fg, int d, int N, int full, double *part,
+                                     double *out, int accumulate, cudaStream_t s);
+
+}  // namespace dcrf

@@ -9,6 +9,7 @@
 #include <string>
 #include <vector>
 
+#include "adjoint.cuh"
 #include "lattice.cuh"
 #include "meanfield.cuh"
 
@@ -85,7 +86,10 @@ struct Term {
     float *pv = nullptr;               // [P][MP] blurred values in partial order / splat partials
     float *compat = nullptr;  // device compat (Diagonal M / Matrix M*M symmetrised)
     float *mem_wn = nullptr;  // splat member weights times the members' norm (forward pre-normalisation)
+    float *df = nullptr;      // [N][d] accumulated feature gradient (adjoint)
     std::vector<float> compat_h;
+    std::vector<float> params;  // kernel parameters (DIAG d, FULL d*d row-major)
+    bool params_set = false;    // the lattice uses params (else the features as given)
 };
 
 }  // namespace
@@ -110,6 +114,15 @@ struct dcrf_crf {
     int *tile_vbase = nullptr;
     float hash_load = 2.0f;
     std::vector<Term> terms;
+    // model version (bumped by every change of unary, terms or parameters) and
+    // the per-iteration checkpoints of the last dcrf_inference_checkpointed
+    unsigned long long version = 0, ckpt_version = ~0ull;
+    int ckpt_T = -1;
+    float *ckpt = nullptr;  // [(T+1)][M][nslots]
+    size_t ckpt_cap = 0;
+    float *bw[14] = {};     // adjoint work buffers, [M][nslots] each
+    double *dpart = nullptr, *dacc = nullptr;
+    size_t dpart_cap = 0, dacc_cap = 0;
     // CUDA graph of the last inference launch sequence (re-used through
     // cudaGraphExecUpdate while its topology stays the same)
     bool use_graphs = true;
@@ -514,33 +527,34 @@ int sync_check(dcrf_crf *h) {
     return DCRF_OK;
 }
 
-int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, const float *compat, int ktype,
-             int ntype, int *term_out) {
-    // feat_dev_owned: [d][N] device buffer, ownership passes to the term
-    Term T;
-    T.d = d;
-    T.ktype = ktype;
-    T.ntype = ntype;
-    T.ckind = compat_kind;
-    T.variant = h->variant;
-    T.feat = const_cast<float *>(feat_dev_owned);
-    int M = h->M, rc;
-    auto fail = [&](int code) {
-        dev_free_async(T.feat, h->stream);
-        dev_free_async(T.norm, h->stream);
-        dev_free_async(T.V[0], h->stream);
-        dev_free_async(T.V[1], h->stream);
-        dev_free_async(T.pv, h->stream);
-        dev_free_async(T.compat, h->stream);
-        dev_free_async(T.mem_wn, h->stream);
-        lattice_free(&T.lat, h->stream);
-        return code;
-    };
-    if (compat_kind == DCRF_COMPAT_POTTS) {
+void free_term_lattice(dcrf_crf *h, Term &T) {
+    dev_free_async(T.norm, h->stream);
+    dev_free_async(T.V[0], h->stream);
+    dev_free_async(T.V[1], h->stream);
+    dev_free_async(T.pv, h->stream);
+    dev_free_async(T.mem_wn, h->stream);
+    dev_free_async(T.df, h->stream);
+    T.norm = T.V[0] = T.V[1] = T.pv = T.mem_wn = T.df = nullptr;
+    lattice_free(&T.lat, h->stream);
+}
+
+void free_term(dcrf_crf *h, Term &T) {
+    free_term_lattice(h, T);
+    dev_free_async(T.feat, h->stream);
+    dev_free_async(T.compat, h->stream);
+    T.feat = T.compat = nullptr;
+}
+
+// Label compatibility of a term (host values and device copy).
+int set_term_compat(dcrf_crf *h, Term &T, int kind, const float *compat) {
+    const int M = h->M;
+    T.ckind = kind;
+    T.compat_h.clear();
+    if (kind == DCRF_COMPAT_POTTS) {
         T.potts_w = compat[0];
-    } else if (compat_kind == DCRF_COMPAT_DIAGONAL) {
+    } else if (kind == DCRF_COMPAT_DIAGONAL) {
         T.compat_h.assign(compat, compat + M);
-    } else if (compat_kind == DCRF_COMPAT_MATRIX) {
+    } else if (kind == DCRF_COMPAT_MATRIX) {
         T.compat_h.resize((size_t)M * M);
         for (int a = 0; a < M; a++)  // MatrixCompatibility symmetrises: 0.5*(m + m^T) (labelcompatibility.cpp:79)
             for (int b = 0; b < M; b++) {
@@ -548,12 +562,38 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
                 T.compat_h[(size_t)a * M + b] = 0.5f * s;
             }
     } else {
-        return fail(set_err(DCRF_ERR_INVALID_ARG, "unknown compatibility kind"));
+        return set_err(DCRF_ERR_INVALID_ARG, "unknown compatibility kind");
     }
     if (!T.compat_h.empty()) {
-        if ((rc = dev_alloc_async(&T.compat, T.compat_h.size(), h->stream))) return fail(rc);
+        int rc;
+        if (!T.compat) {
+            if ((rc = dev_alloc_async(&T.compat, (size_t)M * M, h->stream))) return rc;
+        }
         CU(cudaMemcpyAsync(T.compat, T.compat_h.data(), T.compat_h.size() * sizeof(float), cudaMemcpyHostToDevice,
                            h->stream));
+    }
+    return DCRF_OK;
+}
+
+// (Re)builds term k's lattice from its features and kernel parameters, then
+// its normalisation (DenseKernel::initLattice, pairwise.cpp:40-62) and the
+// member weights with the normalisation folded in.
+int build_term(dcrf_crf *h, int k) {
+    Term &T = h->terms[k];
+    int rc;
+    free_term_lattice(h, T);
+    // features the lattice is built on: p_j f_j (DIAG) or P f (FULL) once parameters were set
+    const float *feat = T.feat;
+    float *scaled = nullptr;
+    if (T.params_set && T.ktype != DCRF_CONST_KERNEL) {
+        const size_t np = T.ktype == DCRF_FULL_KERNEL ? (size_t)T.d * T.d : (size_t)T.d;
+        float *dp = nullptr;
+        if ((rc = dev_alloc_async(&scaled, (size_t)T.d * h->N, h->stream))) return rc;
+        if ((rc = dev_alloc_async(&dp, np, h->stream))) return rc;
+        CU(cudaMemcpyAsync(dp, T.params.data(), np * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+        CU(launch_scale_features(T.feat, scaled, dp, T.d, h->N, T.ktype == DCRF_FULL_KERNEL, h->stream));
+        dev_free_async(dp, h->stream);
+        feat = scaled;
     }
     Segments seg;
     seg.start = {0, h->N};
@@ -564,66 +604,68 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
     float load = h->hash_load;
     for (int attempt = 0;; attempt++) {
         ProfScope ps(h, DCRF_KCLASS_LATTICE);
-        rc = lattice_build(T.feat, d, h->N, seg, tm, h->variant, load, h->stream, h->status, &T.lat);
+        rc = lattice_build(feat, T.d, h->N, seg, tm, T.variant, load, h->stream, h->status, &T.lat);
         if (rc == DCRF_ERR_HASH_FULL && attempt < 3) {
             load *= 4.f;
             continue;
         }
         break;
     }
-    if (rc) return fail(set_err(rc, lattice_last_message()));
+    dev_free_async(scaled, h->stream);
+    if (rc) return set_err(rc, lattice_last_message());
     size_t vrows = (size_t)T.lat.L + 1;
-    if ((rc = dev_alloc_async(&T.V[0], vrows * h->MP, h->stream))) return fail(rc);
-    if ((rc = dev_alloc_async(&T.V[1], vrows * h->MP, h->stream))) return fail(rc);
-    if ((rc = dev_alloc_async(&T.pv, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return fail(rc);
-    if ((rc = dev_alloc_async(&T.norm, (size_t)h->nslots, h->stream))) return fail(rc);
+    if ((rc = dev_alloc_async(&T.V[0], vrows * h->MP, h->stream))) return rc;
+    if ((rc = dev_alloc_async(&T.V[1], vrows * h->MP, h->stream))) return rc;
+    if ((rc = dev_alloc_async(&T.pv, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return rc;
+    if ((rc = dev_alloc_async(&T.norm, (size_t)h->nslots, h->stream))) return rc;
     CU(cudaMemsetAsync(T.norm, 0, sizeof(float) * (size_t)h->nslots, h->stream));
     // the zero sentinel rows (row 0) are never written afterwards
     CU(cudaMemsetAsync(T.V[0], 0, vrows * h->MP * sizeof(float), h->stream));
     CU(cudaMemsetAsync(T.V[1], 0, vrows * h->MP * sizeof(float), h->stream));
-    h->terms.push_back(T);
-    int k = (int)h->terms.size() - 1;
     // normalisation: K * 1 through the value-size-1 path (pairwise.cpp:44)
     std::vector<int> one{k};
     PPArgs a = pp_args(h, PP_ONES | PP_SPLAT, one, false, true);
     a.ts.t[0].pre_norm = 0;
     a.ts.t[0].post_norm = 0;
-    cudaError_t ce = pp(h, a, 1);
-    if (ce != cudaSuccess) {
-        h->terms.pop_back();
-        return fail(set_err(DCRF_ERR_CUDA, std::string("norm splat: ") + cudaGetErrorString(ce)));
-    }
-    if ((rc = filter_phase(h, one, false, true, false))) {
-        h->terms.pop_back();
-        return fail(rc);
-    }
+    CU(pp(h, a, 1));
+    if ((rc = filter_phase(h, one, false, true, false))) return rc;
     a = pp_args(h, PP_NORM, one, false, true);
-    ce = pp(h, a, 1);
-    if (ce != cudaSuccess) {
-        h->terms.pop_back();
-        return fail(set_err(DCRF_ERR_CUDA, std::string("norm slice: ") + cudaGetErrorString(ce)));
+    CU(pp(h, a, 1));
+    if ((rc = zero_sentinels(h, T))) return rc;
+    const size_t nm = (size_t)h->ntiles * SPLAT_TILE * (T.d + 1);
+    if ((rc = dev_alloc_async(&T.mem_wn, nm, h->stream))) return rc;
+    CU(launch_scale_members(T.lat.mem_pt, T.lat.mem_w, T.norm, h->ntiles, T.d + 1, T.mem_wn, h->stream));
+    if ((rc = sync_check(h))) return rc;
+    h->version++;
+    return DCRF_OK;
+}
+
+int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, const float *compat, int ktype,
+             int ntype, int *term_out) {
+    // feat_dev_owned: [d][N] device buffer, ownership passes to the term
+    Term T;
+    T.d = d;
+    T.ktype = ktype;
+    T.ntype = ntype;
+    T.variant = h->variant;
+    T.feat = const_cast<float *>(feat_dev_owned);
+    // kernel parameters start at the identity (pairwise.cpp:117-121)
+    if (ktype == DCRF_DIAG_KERNEL) T.params.assign(d, 1.f);
+    if (ktype == DCRF_FULL_KERNEL) {
+        T.params.assign((size_t)d * d, 0.f);
+        for (int j = 0; j < d; j++) T.params[(size_t)j * d + j] = 1.f;
     }
-    if ((rc = zero_sentinels(h, h->terms.back()))) {
-        h->terms.pop_back();
-        return fail(rc);
+    int rc = set_term_compat(h, T, compat_kind, compat);
+    if (rc) {
+        free_term(h, T);
+        return rc;
     }
-    {
-        Term &TT = h->terms.back();
-        const size_t nm = (size_t)h->ntiles * SPLAT_TILE * (TT.d + 1);
-        if ((rc = dev_alloc_async(&TT.mem_wn, nm, h->stream))) {
-            h->terms.pop_back();
-            return fail(rc);
-        }
-        T.mem_wn = TT.mem_wn;
-        ce = launch_scale_members(TT.lat.mem_pt, TT.lat.mem_w, TT.norm, h->ntiles, TT.d + 1, TT.mem_wn, h->stream);
-        if (ce != cudaSuccess) {
-            h->terms.pop_back();
-            return fail(set_err(DCRF_ERR_CUDA, std::string("member weights: ") + cudaGetErrorString(ce)));
-        }
-    }
-    if ((rc = sync_check(h))) {
+    h->terms.push_back(T);
+    const int k = (int)h->terms.size() - 1;
+    if ((rc = build_term(h, k))) {
+        free_term(h, h->terms[k]);
         h->terms.pop_back();
-        return fail(rc);
+        return rc;
     }
     if (term_out) *term_out = k;
     return ok();
@@ -645,18 +687,30 @@ int validate_kn(int ktype, int ntype) {
 
 // Launch sequence of T mean-field iterations starting from softmax(-U); the
 // final pass writes per final_mode (Q into h->Q, or the MAP labels).
-int issue_inference(dcrf_crf *h, int T, int final_mode) {
+int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
     std::vector<int> w = all_terms(h);
+    const size_t qsz = (size_t)h->M * h->nslots;
     int rc;
     if (T <= 0 || w.empty()) {
-        CU(pp(h, pp_args(h, final_mode, w, false, false), h->MP));
+        PPArgs a = pp_args(h, final_mode | (ckpt ? PP_WRITE_Q : 0), w, false, false);
+        if (ckpt) a.Qout = ckpt;
+        CU(pp(h, a, h->MP));
+        if (ckpt)  // every iterate equals Q_0 without pairwise terms
+            for (int it = 1; it <= T; it++)
+                CU(cudaMemcpyAsync(ckpt + it * qsz, ckpt, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
         return DCRF_OK;
     }
-    CU(pp(h, pp_args(h, PP_SPLAT, w, false, false), h->MP));
+    {
+        PPArgs a = pp_args(h, PP_SPLAT | (ckpt ? PP_WRITE_Q : 0), w, false, false);
+        if (ckpt) a.Qout = ckpt;
+        CU(pp(h, a, h->MP));
+    }
     for (int it = 1; it <= T; it++) {
         if ((rc = filter_phase(h, w, false, false, true))) return rc;
-        int mode = PP_MSG | (it < T ? PP_SPLAT : final_mode);
-        CU(pp(h, pp_args(h, mode, w, false, false), h->MP));
+        int mode = PP_MSG | (it < T ? PP_SPLAT : final_mode) | (ckpt ? PP_WRITE_Q : 0);
+        PPArgs a = pp_args(h, mode, w, false, false);
+        if (ckpt) a.Qout = ckpt + it * qsz;
+        CU(pp(h, a, h->MP));
     }
     return DCRF_OK;
 }
@@ -665,12 +719,12 @@ int issue_inference(dcrf_crf *h, int T, int final_mode) {
 // stream, instantiated once and afterwards updated in place (same kernels,
 // new arguments), launched on the handle's stream.  Profiling launches the
 // kernels directly so that the per-launch events can be recorded.
-int run_inference(dcrf_crf *h, int T, int final_mode) {
-    if (h->profiling || !h->use_graphs) return issue_inference(h, T, final_mode);
+int run_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
+    if (h->profiling || !h->use_graphs) return issue_inference(h, T, final_mode, ckpt);
     cudaStream_t user = h->stream;
     h->stream = h->capture;
     CU(cudaStreamBeginCapture(h->capture, cudaStreamCaptureModeThreadLocal));
-    int rc = issue_inference(h, T, final_mode);
+    int rc = issue_inference(h, T, final_mode, ckpt);
     cudaGraph_t graph = nullptr;
     cudaError_t ce = cudaStreamEndCapture(h->capture, &graph);
     h->stream = user;
@@ -703,6 +757,113 @@ int run_inference(dcrf_crf *h, int T, int final_mode) {
     return DCRF_OK;
 }
 
+// ---- adjoint helpers --------------------------------------------------------
+
+bool fwd_pre(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_BEFORE; }
+bool fwd_post(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_AFTER; }
+bool tr_pre(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_AFTER; }
+bool tr_post(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_BEFORE; }
+
+// Splat of in_s (plain or norm-folded member weights) and the d+1 blur passes
+// (reverse order for the transpose); the result is the term's vertex-order V.
+int splat_blur(dcrf_crf *h, int k, const float *in_s, bool transpose, bool fold_norm) {
+    Term &T = h->terms[k];
+    std::vector<int> one{k};
+    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, transpose, false);
+    a.ts.t[0].mem_w = fold_norm ? T.mem_wn : T.lat.mem_w;
+    a.Qin = in_s;
+    CU(pp(h, a, h->MP));
+    return filter_phase(h, one, transpose, false, false);
+}
+
+// out_s = K in_s (raw lattice filter; the transpose uses the reverse blur),
+// optionally with the term's normalisation on either side.
+int filter_into(dcrf_crf *h, int k, const float *in_s, float *out_s, bool transpose, bool pre, bool post) {
+    Term &T = h->terms[k];
+    int rc = splat_blur(h, k, in_s, transpose, pre);
+    if (rc) return rc;
+    std::vector<int> one{k};
+    PPArgs f = pp_args(h, PP_FILTER, one, transpose, false);
+    f.Qout = out_s;
+    CU(pp(h, f, h->MP));
+    if (post) CU(launch_scale_norm(out_s, out_s, T.norm, h->M, h->nslots, 1, h->stream));
+    return DCRF_OK;
+}
+
+// T.df += sign * d/dfeatures (x^T K y) (Permutohedral::gradient, permutohedral.cpp:612-695):
+// direction 0 slices the forward-blurred splat of x against y, direction 1 the
+// reverse-blurred splat of y against x.
+int lattice_grad(dcrf_crf *h, int k, const float *x, const float *y, float sign) {
+    Term &T = h->terms[k];
+    SliceGradArgs g{};
+    g.N = h->N;
+    g.M = h->M;
+    g.d = T.d;
+    g.nslots = h->nslots;
+    g.slot_pt = h->slot_pt;
+    g.off = T.lat.off;
+    g.rank = T.lat.rank;
+    g.V = T.V[(T.d + 1) & 1];
+    {
+        float inv_std_dev = (float)(std::sqrt(2.0 / 3.0) * (T.d + 1));
+        for (int i = 0; i < T.d; i++)
+            g.sf[i] = (float)(1.0 / std::sqrt((double)((i + 2) * (i + 1))) * (double)inv_std_dev);
+        g.alpha = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1);
+    }
+    g.df = T.df;
+    for (int dir = 0; dir < 2; dir++) {
+        int rc = splat_blur(h, k, dir ? y : x, dir == 1, false);
+        if (rc) return rc;
+        g.z = dir ? x : y;
+        // sign folded into the contraction values would need a copy; scale the
+        // alpha instead (the gradient is linear in the sliced values)
+        g.alpha = (1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1)) * sign;
+        CU(launch_slice_grad(g, h->MP, h->stream));
+    }
+    return DCRF_OK;
+}
+
+// Feature gradient of a^T C K(Q) with the normalisation's own dependence on
+// the features (DenseKernel::featureGradient, pairwise.cpp:87-114), added to T.df.
+int feature_grad(dcrf_crf *h, int k, const float *a, const float *bb) {
+    Term &T = h->terms[k];
+    const int M = h->M, ns = h->nslots;
+    float *an = h->bw[7], *bn = h->bw[8], *fa = h->bw[9], *fb = h->bw[10], *c1 = h->bw[11], *ones = h->bw[12];
+    int rc;
+    switch (T.ntype) {
+        case DCRF_NORMALIZE_SYMMETRIC:
+            CU(launch_scale_norm(a, an, T.norm, M, ns, 1, h->stream));
+            CU(launch_scale_norm(bb, bn, T.norm, M, ns, 1, h->stream));
+            if ((rc = filter_into(h, k, an, fa, true, false, false))) return rc;
+            if ((rc = filter_into(h, k, bn, fb, false, false, false))) return rc;
+            CU(launch_prod(a, fb, fa, bb, 0.5f, T.norm, 3, c1, M, ns, h->stream));
+            if ((rc = lattice_grad(h, k, c1, ones, -1.f))) return rc;
+            return lattice_grad(h, k, an, bn, 1.f);
+        case DCRF_NORMALIZE_AFTER:
+            if ((rc = filter_into(h, k, bb, fb, false, false, false))) return rc;
+            CU(launch_prod(a, fb, nullptr, nullptr, 1.f, T.norm, 2, c1, M, ns, h->stream));
+            if ((rc = lattice_grad(h, k, c1, ones, -1.f))) return rc;
+            CU(launch_scale_norm(a, an, T.norm, M, ns, 1, h->stream));
+            return lattice_grad(h, k, an, bb, 1.f);
+        case DCRF_NORMALIZE_BEFORE:
+            if ((rc = filter_into(h, k, a, fa, true, false, false))) return rc;
+            CU(launch_prod(fa, bb, nullptr, nullptr, 1.f, T.norm, 2, c1, M, ns, h->stream));
+            if ((rc = lattice_grad(h, k, c1, ones, -1.f))) return rc;
+            CU(launch_scale_norm(bb, bn, T.norm, M, ns, 1, h->stream));
+            return lattice_grad(h, k, a, bn, 1.f);
+        default:
+            return lattice_grad(h, k, a, bb, 1.f);
+    }
+}
+
+int compat_count(const dcrf_crf *h, const Term &T) {
+    return T.ckind == DCRF_COMPAT_POTTS ? 1 : T.ckind == DCRF_COMPAT_DIAGONAL ? h->M : h->M * h->M;
+}
+
+int kernel_count(const Term &T) {
+    return T.ktype == DCRF_FULL_KERNEL ? T.d * T.d : T.ktype == DCRF_DIAG_KERNEL ? T.d : 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -733,16 +894,11 @@ int dcrf_destroy(dcrf_crf *h) {
     release_marks(h);
     for (cudaEvent_t e : h->event_pool) cudaEventDestroy(e);
     h->event_pool.clear();
-    for (Term &T : h->terms) {
-        dev_free_async(T.feat, h->stream);
-        dev_free_async(T.norm, h->stream);
-        dev_free_async(T.V[0], h->stream);
-        dev_free_async(T.V[1], h->stream);
-        dev_free_async(T.pv, h->stream);
-        dev_free_async(T.compat, h->stream);
-        dev_free_async(T.mem_wn, h->stream);
-        lattice_free(&T.lat, h->stream ? h->stream : h->own);
-    }
+    for (Term &T : h->terms) free_term(h, T);
+    dev_free_async(h->ckpt, h->stream);
+    for (float *&b : h->bw) dev_free_async(b, h->stream);
+    dev_free_async(h->dpart, h->stream);
+    dev_free_async(h->dacc, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
     dev_free(h->status);
     dev_free(h->U);
@@ -787,6 +943,7 @@ int dcrf_set_unary(dcrf_crf *h, const float *U, int layout, int where) {
     if (!U) return set_err(DCRF_ERR_INVALID_ARG, "null unary");
     if ((rc = load_mn(h, U, layout, where, h->U))) return rc;
     h->has_unary = true;
+    h->version++;
     if ((rc = sync_check(h))) return rc;
     return ok();
 }
@@ -880,7 +1037,7 @@ int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where) {
     if (rc) return rc;
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
     if (!h->has_unary) {  // densecrf.cpp:179-184: zeros without a unary
-        CU(cudaMemsetAsync(h->Q, 0, sizeof(float) * (size_t)h->N * h->M, h->stream));
+        CU(cudaMemsetAsync(h->Q, 0, sizeof(float) * (size_t)h->nslots * h->M, h->stream));
     } else {
         CU(pp(h, pp_args(h, PP_WRITE_Q, {}, false, false), h->MP));
     }
@@ -1044,17 +1201,9 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
 int dcrf_clear_pairwise(dcrf_crf *h) {
     int rc = check_handle(h);
     if (rc) return rc;
-    for (Term &T : h->terms) {
-        dev_free_async(T.feat, h->stream);
-        dev_free_async(T.norm, h->stream);
-        dev_free_async(T.V[0], h->stream);
-        dev_free_async(T.V[1], h->stream);
-        dev_free_async(T.pv, h->stream);
-        dev_free_async(T.compat, h->stream);
-        dev_free_async(T.mem_wn, h->stream);
-        lattice_free(&T.lat, h->stream);
-    }
+    for (Term &T : h->terms) free_term(h, T);
     h->terms.clear();
+    h->version++;
     return ok();
 }
 
@@ -1112,6 +1261,165 @@ int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count)
     const float *src = which == 0 ? T.V[0] : which == 1 ? T.V[1] : T.pv;
     CU(cudaStreamSynchronize(h->stream));
     CU(cudaMemcpy(out, src, count * sizeof(float), cudaMemcpyDeviceToHost));
+    return ok();
+}
+
+int dcrf_set_compat(dcrf_crf *h, int term, int compat_kind, const float *compat) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    if ((rc = validate_compat(compat_kind, compat))) return rc;
+    if ((rc = set_term_compat(h, h->terms[term], compat_kind, compat))) return rc;
+    h->version++;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_set_kernel_params(dcrf_crf *h, int term, const float *params) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (term < 0 || term >= (int)h->terms.size() || !params) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
+    Term &T = h->terms[term];
+    if (T.ktype == DCRF_CONST_KERNEL) return ok();  // no parameters (pairwise.cpp:140-151)
+    T.params.assign(params, params + kernel_count(T));
+    T.params_set = true;
+    if ((rc = build_term(h, term))) return rc;
+    return ok();
+}
+
+int dcrf_param_counts(dcrf_crf *h, int term, int *n_compat, int *n_kernel) {
+    if (!h) return set_err(DCRF_ERR_INVALID_ARG, "null handle");
+    if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    if (n_compat) *n_compat = compat_count(h, h->terms[term]);
+    if (n_kernel) *n_kernel = kernel_count(h->terms[term]);
+    return ok();
+}
+
+int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int layout, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!Q || n_iterations < 0) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
+    const size_t qsz = (size_t)h->M * h->nslots, need = qsz * ((size_t)n_iterations + 1);
+    if (need > h->ckpt_cap) {
+        dev_free_async(h->ckpt, h->stream);
+        h->ckpt = nullptr;
+        h->ckpt_cap = 0;
+        if ((rc = dev_alloc_async(&h->ckpt, need, h->stream))) return rc;
+        h->ckpt_cap = need;
+    }
+    if ((rc = run_inference(h, n_iterations, 0, h->ckpt))) return rc;
+    if ((rc = store_mn(h, h->ckpt + (size_t)n_iterations * qsz, Q, layout, where))) return rc;
+    if ((rc = sync_check(h))) return rc;
+    h->ckpt_T = n_iterations;
+    h->ckpt_version = h->version;
+    return ok();
+}
+
+int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU, double *dcompat, double *dkernel) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!dQ) return set_err(DCRF_ERR_INVALID_ARG, "null gradient");
+    if (h->ckpt_T < 0 || h->ckpt_version != h->version)
+        return set_err(DCRF_ERR_STATE, "dcrf_backward needs a dcrf_inference_checkpointed of the current model");
+    const int M = h->M, ns = h->nslots, T = h->ckpt_T, nt = (int)h->terms.size();
+    const size_t qsz = (size_t)M * ns;
+    const bool want_compat = dcompat != nullptr, want_kernel = dkernel != nullptr;
+    for (float *&b : h->bw)
+        if (!b && (rc = dev_alloc_async(&b, qsz, h->stream))) return rc;
+    // reduction space: per term compat (M or M*M) and kernel (d*d) accumulators
+    std::vector<size_t> coff(nt), koff(nt);
+    size_t nacc = 0;
+    int maxd = 1;
+    for (int k = 0; k < nt; k++) {
+        const Term &Tk = h->terms[k];
+        coff[k] = nacc;
+        nacc += Tk.ckind == DCRF_COMPAT_MATRIX ? (size_t)M * M : (size_t)M;
+        koff[k] = nacc;
+        nacc += (size_t)Tk.d * Tk.d;
+        maxd = std::max(maxd, Tk.d);
+    }
+    const size_t npart = std::max((size_t)label_products_blocks(ns) * M * M,
+                                  (size_t)kernel_param_blocks(h->N) * maxd * maxd);
+    if (npart > h->dpart_cap) {
+        dev_free_async(h->dpart, h->stream);
+        h->dpart = nullptr;
+        if ((rc = dev_alloc_async(&h->dpart, npart, h->stream))) return rc;
+        h->dpart_cap = npart;
+    }
+    if (nacc + 1 > h->dacc_cap) {
+        dev_free_async(h->dacc, h->stream);
+        h->dacc = nullptr;
+        if ((rc = dev_alloc_async(&h->dacc, nacc + 1, h->stream))) return rc;
+        h->dacc_cap = nacc + 1;
+    }
+    CU(cudaMemsetAsync(h->dacc, 0, sizeof(double) * (nacc + 1), h->stream));
+    if (want_kernel)
+        for (Term &Tk : h->terms)
+            if (Tk.ktype != DCRF_CONST_KERNEL) {
+                if (!Tk.df && (rc = dev_alloc_async(&Tk.df, (size_t)h->N * Tk.d, h->stream))) return rc;
+                CU(cudaMemsetAsync(Tk.df, 0, sizeof(float) * (size_t)h->N * Tk.d, h->stream));
+            }
+    float *b = h->bw[0], *g = h->bw[1], *du = h->bw[2], *kq = h->bw[3], *a = h->bw[4], *xt = h->bw[5],
+          *bb = h->bw[6];
+    CU(launch_fill(h->bw[12], 1.f, M, ns, h->slot_pt, h->stream));
+    // seed: b = -dL/dA_{T-1} from dL/dQ_T (densecrf.cpp:256-258)
+    if ((rc = load_mn(h, dQ, layout, where, g))) return rc;
+    CU(launch_softmax_adjoint(h->ckpt + (size_t)T * qsz, g, b, M, ns, h->slot_pt, h->stream));
+    CU(cudaMemcpyAsync(du, b, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    for (int it = T - 1; it >= 0; it--) {
+        const float *Qt = h->ckpt + (size_t)it * qsz;
+        CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
+        for (int k = 0; k < nt; k++) {
+            Term &Tk = h->terms[k];
+            if (want_compat) {  // PairwisePotential::gradient, pairwise.cpp:190-195
+                if ((rc = filter_into(h, k, Qt, kq, false, fwd_pre(Tk), fwd_post(Tk)))) return rc;
+                CU(launch_label_products(b, kq, M, ns, h->slot_pt, Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0, h->dpart,
+                                         h->dacc + coff[k], 1, h->stream));
+            }
+            if (want_kernel && Tk.ktype != DCRF_CONST_KERNEL) {  // pairwise.cpp:202-207
+                CU(launch_compat(Qt, bb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                if ((rc = feature_grad(h, k, b, bb))) return rc;
+            }
+            // g += K^T C^T b (applyTranspose, pairwise.cpp:179-183)
+            CU(launch_compat(b, a, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 1, 0, h->stream));
+            if ((rc = filter_into(h, k, a, xt, true, tr_pre(Tk), tr_post(Tk)))) return rc;
+            CU(launch_add(xt, g, qsz, h->stream));
+        }
+        // b = -dL/dA_{it-1} (densecrf.cpp:290)
+        CU(launch_softmax_adjoint(Qt, g, b, M, ns, h->slot_pt, h->stream));
+        CU(launch_add(b, du, qsz, h->stream));
+    }
+    if (dU && (rc = store_mn(h, du, dU, layout, where))) return rc;
+    if (want_kernel)
+        for (int k = 0; k < nt; k++) {
+            Term &Tk = h->terms[k];
+            if (Tk.ktype == DCRF_CONST_KERNEL) continue;
+            CU(launch_kernel_param_grad(Tk.feat, Tk.df, Tk.d, h->N, Tk.ktype == DCRF_FULL_KERNEL, h->dpart,
+                                        h->dacc + koff[k], 0, h->stream));
+        }
+    std::vector<double> acc(nacc + 1);
+    CU(cudaMemcpyAsync(acc.data(), h->dacc, sizeof(double) * (nacc + 1), cudaMemcpyDeviceToHost, h->stream));
+    if ((rc = sync_check(h))) return rc;
+    size_t oc = 0, ok_ = 0;
+    for (int k = 0; k < nt; k++) {
+        const Term &Tk = h->terms[k];
+        if (dcompat) {
+            if (Tk.ckind == DCRF_COMPAT_POTTS) {  // m = -w KQ: dL/dw = -sum b.*KQ (labelcompatibility.cpp:57-61)
+                double sacc = 0.0;
+                for (int m = 0; m < M; m++) sacc += acc[coff[k] + m];
+                dcompat[oc] = -sacc;
+            } else {
+                const int n = compat_count(h, Tk);
+                for (int x = 0; x < n; x++) dcompat[oc + x] = acc[coff[k] + x];
+            }
+        }
+        oc += compat_count(h, Tk);
+        if (dkernel) {
+            const int n = kernel_count(Tk);
+            for (int x = 0; x < n; x++) dkernel[ok_ + x] = acc[koff[k] + x];
+        }
+        ok_ += kernel_count(Tk);
+    }
     return ok();
 }
 

@@ -220,6 +220,58 @@ class DenseCRF:
         _lib.check(_lib.load().dcrf_map(self._h, int(niter), _ptr(out), _lib.HOST))
         return out
 
+    # -- learning (the parameter API and adjoint of densecrf.cpp:238-360) -------
+    def setCompatibility(self, term: int, compat) -> None:
+        """Replace term ``term``'s label compatibility (Potts number, Diagonal
+        vector or Matrix), like LabelCompatibility::setParameters."""
+        kind, c = _labelcomp(compat, self._nlabel)
+        _lib.check(_lib.load().dcrf_set_compat(self._h, int(term), kind, _ptr(c)))
+
+    def setKernelParameters(self, term: int, params) -> None:
+        """Kernel parameters of term ``term`` (DenseKernel::setParameters):
+        DIAG d feature scales, FULL a d x d matrix (row-major).  Rebuilds the
+        lattice."""
+        p = np.ascontiguousarray(np.asarray(params, np.float32).reshape(-1))
+        _lib.check(_lib.load().dcrf_set_kernel_params(self._h, int(term), _ptr(p)))
+
+    def paramCounts(self, term: int):
+        """(number of compatibility values, number of kernel parameters) of a term."""
+        nc, nk = ctypes.c_int(), ctypes.c_int()
+        _lib.check(_lib.load().dcrf_param_counts(self._h, int(term), ctypes.byref(nc), ctypes.byref(nk)))
+        return nc.value, nk.value
+
+    def nTerms(self) -> int:
+        n = ctypes.c_int()
+        _lib.check(_lib.load().dcrf_info(self._h, None, None, ctypes.byref(n)))
+        return n.value
+
+    def inferenceCheckpointed(self, niter: int) -> np.ndarray:
+        """inference(niter) keeping every iterate on the device for backward();
+        returns Q as an (M, N) array."""
+        Q = np.empty((self._nlabel, self._nvar), np.float32)
+        _lib.check(_lib.load().dcrf_inference_checkpointed(self._h, int(niter), _ptr(Q), _lib.LAYOUT_LM,
+                                                           _lib.HOST))
+        return Q
+
+    def backward(self, dQ, want_compat: bool = True, want_kernel: bool = False):
+        """Adjoint of the last inferenceCheckpointed: given dL/dQ (M, N), returns
+        (dL/dU (M, N), [per-term dL/dcompat], [per-term dL/dkernel params])."""
+        dQ = np.ascontiguousarray(dQ, np.float32)
+        dU = np.empty_like(dQ)
+        counts = [self.paramCounts(k) for k in range(self.nTerms())]
+        dc = np.zeros(max(1, sum(c for c, _ in counts)), np.float64) if want_compat else None
+        dk = np.zeros(max(1, sum(k for _, k in counts)), np.float64) if want_kernel else None
+        _lib.check(_lib.load().dcrf_backward(self._h, _ptr(dQ), _lib.LAYOUT_LM, _lib.HOST, _ptr(dU),
+                                             _ptr(dc) if dc is not None else None,
+                                             _ptr(dk) if dk is not None else None))
+        cs, ks, oc, ok = [], [], 0, 0
+        for c, k in counts:
+            cs.append(dc[oc:oc + c].copy() if dc is not None else None)
+            ks.append(dk[ok:ok + k].copy() if dk is not None else None)
+            oc += c
+            ok += k
+        return dU, cs, ks
+
     # -- introspection -----------------------------------------------------------
     def lattice(self, term: int) -> dict:
         """Lattice tables of pairwise term ``term`` in the reference's layout."""

@@ -10,6 +10,11 @@ oracle/Makefile).  Outputs, all small:
 * inference.npz -- marginals after T iterations, startInference, one
                    stepInference and klDivergence of seeded small CRFs covering
                    every compatibility and normalisation type, both builds.
+* gradient.npz  -- the reference's own DenseCRF::gradient (log-likelihood of
+                   a label map) of seeded small CRFs: objective, dL/dU (through
+                   a logistic unary L*I), compatibility and kernel-parameter
+                   gradients, for every normalisation, compatibility and kernel
+                   type.
 * examples.npz  -- the reference's example images and annotations
                    (examples/im*.png, anno*.png) decoded, with the shipped
                    outputs (out*.png) turned back into label maps, and the
@@ -171,6 +176,45 @@ def gen_inference():
     print("inference.npz", len(cases), "cases")
 
 
+def gen_gradient():
+    rng = np.random.default_rng(99)
+    out = {}
+    W, H, M, T = 12, 10, 3, 3
+    N = W * H
+    img = rng.integers(0, 256, size=(H, W, 3)).astype(np.uint8)
+    img[3:8, 2:9] = [30, 200, 90]
+    logits = rng.normal(0, 1.5, size=(N, M)).astype(np.float32)
+    U = -np.log(np.exp(logits) / np.exp(logits).sum(1, keepdims=True)).astype(np.float32)  # (N, M)
+    gt = rng.integers(0, M, size=N).astype(np.int16)
+    fg = O.features_gaussian_2d(W, H, 2.0, 2.0)
+    fb = O.features_bilateral_2d(img, 5.0, 5.0, 40.0, 40.0, 40.0)
+    diag = rng.uniform(-2, -0.5, size=M).astype(np.float32)
+    mat = rng.uniform(-1, 1, size=(M, M)).astype(np.float32)
+    cases = []
+    for ck, c in (("potts", 2.0), ("diag", diag), ("mat", mat)):
+        for nt in range(4):
+            for kt in (1, 2):
+                cases.append((f"{ck}_n{nt}_k{kt}", c, nt, kt))
+    eye = np.eye(N, dtype=np.float32)
+    for name, c, nt, kt in cases:
+        r = O.RefCRF(N, M)
+        lib = r._lib
+        Lm = np.ascontiguousarray(U.T)  # L = U^T as M x N (column-major = point-major U), f = I
+        lib.ref_crf_set_unary_logistic(r._h, O._p(np.ascontiguousarray(U), O._f32p), O._p(eye, O._f32p), M, N, N)
+        r.add_pairwise(fg, c, kt, nt)
+        r.add_pairwise(fb, 3.0, kt, 3)
+        val, ug, cg, kg = r.gradient(T, gt, want_unary=True, want_compat=True, want_kernel=True)
+        out[f"{name}/obj"] = np.float64(val)
+        out[f"{name}/dU"] = ug.reshape(N, M)
+        out[f"{name}/dcompat"] = cg
+        out[f"{name}/dkernel"] = kg
+        out[f"{name}/Q"] = r.inference(T)
+    out.update(U=U, img=img, gt=gt, W=W, H=H, M=M, T=T, diag=diag, mat=mat,
+               cases=np.array([c[0] for c in cases]))
+    np.savez_compressed(os.path.join(HERE, "gradient.npz"), **out)
+    print("gradient.npz", len(cases), "cases")
+
+
 def gen_examples():
     ex = os.path.join(REF_ROOT, "examples")
     out = {}
@@ -217,4 +261,5 @@ if __name__ == "__main__":
         sys.exit("the reference could not be built from " + REF_ROOT)
     gen_lattice()
     gen_inference()
+    gen_gradient()
     gen_examples()
