@@ -184,6 +184,174 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------
+def learning_step_times(lib, _lib, dev, stream, reps: int = 2):
+    """Forward and forward+backward of the differentiable mean-field on the
+    training workload (512x512, 21 labels, 5 iterations, Gaussian Potts with
+    a CONST kernel + bilateral with a 21x21 Matrix compatibility and DIAG
+    kernel; loss =
+    cross-entropy against a 30-region label map), per image over 8 images.
+
+    forward  = both lattice builds + 5 checkpointed iterations;
+    backward = the adjoint: dL/dU, dL/d(compatibility) and dL/d(bilateral
+               kernel parameters).  CUDA events on the engine's stream."""
+    import torch
+
+    from pydensecrf_gb300 import synthetic as S
+
+    cfg = S.train_512(0)
+    Wt, Ht, Mt, Tt = cfg["W"], cfg["H"], cfg["M"], cfg["T"]
+    Nt = Wt * Ht
+    Us = [torch.from_numpy(u).to(dev) for u in cfg["U"]]
+    imgs = [torch.from_numpy(im).to(dev) for im in cfg["img"]]
+    gts = [torch.from_numpy(g).to(dev) for g in cfg["gt"]]
+    cg = np.array([3.0], np.float32)
+    cm = np.ascontiguousarray(cfg["compat"], np.float32)
+    Q = torch.empty((Mt, Nt), dtype=torch.float32, device=dev)
+    dU = torch.empty_like(Q)
+    h = ctypes.c_void_p()
+    _lib.check(lib.dcrf_create_2d(Wt, Ht, Mt, ctypes.byref(h)))
+    _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    cols = torch.arange(Nt, device=dev)
+    grads = {}
+
+    def grad_buffers():
+        # sized from the terms' parameter counts (Gaussian: Potts 1; bilateral: 21x21 + DIAG 5)
+        if not grads:
+            nc = nk = 0
+            for term in range(2):
+                c, k = ctypes.c_int(), ctypes.c_int()
+                _lib.check(lib.dcrf_param_counts(h, term, ctypes.byref(c), ctypes.byref(k)))
+                nc += c.value
+                nk += k.value
+            grads["c"] = np.zeros(max(1, nc), np.float64)
+            grads["k"] = np.zeros(max(1, nk), np.float64)
+        return grads["c"], grads["k"]
+
+    def fwd(i):
+        _lib.check(lib.dcrf_clear_pairwise(h))
+        _lib.check(lib.dcrf_set_unary(h, ctypes.c_void_p(Us[i].data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE))
+        # CONST kernel: the Gaussian bandwidth is not learned here
+        _lib.check(lib.dcrf_add_pairwise_gaussian(h, 3.0, 3.0, _lib.COMPAT_POTTS, cg.ctypes.data, 0, 3, None))
+        _lib.check(lib.dcrf_add_pairwise_bilateral(h, 80.0, 80.0, 13.0, 13.0, 13.0, ctypes.c_void_p(imgs[i].data_ptr()),
+                                                   _lib.DEVICE, _lib.COMPAT_MATRIX, cm.ctypes.data, 1, 3, None))
+        _lib.check(lib.dcrf_inference_checkpointed(h, Tt, ctypes.c_void_p(Q.data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE))
+
+    def bwd(i):
+        with torch.cuda.stream(stream):
+            dQ = torch.zeros_like(Q)
+            dQ[gts[i], cols] = -1.0 / (Nt * Q[gts[i], cols].clamp_min(1e-20))
+        dcomp, dkern = grad_buffers()
+        _lib.check(lib.dcrf_backward(h, ctypes.c_void_p(dQ.data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE,
+                                     ctypes.c_void_p(dU.data_ptr()), dcomp.ctypes.data, dkern.ctypes.data))
+
+    fwd(0)
+    bwd(0)
+    torch.cuda.synchronize()
+    f_ms, b_ms = [], []
+    for _ in range(reps):
+        for i in range(len(Us)):
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            e0.record(stream)
+            fwd(i)
+            e1.record(stream)
+            bwd(i)
+            e2.record(stream)
+            torch.cuda.synchronize()
+            f_ms.append(e0.elapsed_time(e1))
+            b_ms.append(e1.elapsed_time(e2))
+    lib.dcrf_destroy(h)
+    f, b = float(np.median(f_ms)), float(np.median(b_ms))
+    return {"workload": "512x512 M=21 T=5, Gaussian Potts + bilateral Matrix(21x21) DIAG, CE loss, 8 images",
+            "fwd_ms_per_img": round(f, 3), "bwd_ms_per_img": round(b, 3),
+            "fwd_plus_bwd_over_fwd": round((f + b) / f, 3),
+            "grads": "dU, dcompat (Potts + 21x21), dkernel (bilateral 5 scales)"}
+
+
+def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
+    """The batched form against a per-image loop on 64 uneven images
+    (W, H ~ U[256, 1024], M=21, T=10, Gaussian sxy=3 + bilateral sxy=80
+    srgb=13, both with one random symmetric 21x21 Matrix compatibility,
+    entries U(0, 2), zero diagonal).  Inputs resident in HBM; per image the
+    loop uses its own pre-created handle (lattice builds and inference in the
+    timed region, handle creation outside), the batch one handle for all.
+    Both solve the full problem: lattice builds, normalisations, 10 iterations."""
+    import torch
+
+    from pydensecrf_gb300 import synthetic as S
+
+    cfg = S.batch_uneven(0, B=n_images)
+    Mb, Tb = cfg["M"], cfg["T"]
+    sizes = cfg["sizes"]
+    Ns = [w * h for w, h in sizes]
+    Ntot = sum(Ns)
+    cm = np.ascontiguousarray(cfg["compat"], np.float32)
+    U_all = torch.from_numpy(np.concatenate([u.reshape(-1) for u in cfg["U"]])).to(dev)
+    img_all = torch.from_numpy(np.concatenate([im.reshape(-1) for im in cfg["img"]])).to(dev)
+    Q_all = torch.empty(Mb * Ntot, dtype=torch.float32, device=dev)
+    offs = np.concatenate([[0], np.cumsum(Ns)])
+
+    def ptr(t, off=0):
+        return ctypes.c_void_p(int(t.data_ptr() + int(off) * t.element_size()))
+
+    def solve(h, u, img, q):
+        _lib.check(lib.dcrf_clear_pairwise(h))
+        _lib.check(lib.dcrf_set_unary(h, u, _lib.LAYOUT_LM, _lib.DEVICE))
+        _lib.check(lib.dcrf_add_pairwise_gaussian(h, 3.0, 3.0, _lib.COMPAT_MATRIX, cm.ctypes.data, 1, 3, None))
+        _lib.check(lib.dcrf_add_pairwise_bilateral(h, 80.0, 80.0, 13.0, 13.0, 13.0, img, _lib.DEVICE,
+                                                   _lib.COMPAT_MATRIX, cm.ctypes.data, 1, 3, None))
+        _lib.check(lib.dcrf_inference(h, Tb, q, _lib.LAYOUT_LM, _lib.DEVICE))
+
+    Wa = np.ascontiguousarray([w for w, _ in sizes], np.int32)
+    Ha = np.ascontiguousarray([h for _, h in sizes], np.int32)
+    hb = ctypes.c_void_p()
+    _lib.check(lib.dcrf_create_batch_2d(len(sizes), Wa.ctypes.data, Ha.ctypes.data, Mb, ctypes.byref(hb)))
+    _lib.check(lib.dcrf_set_stream(hb, ctypes.c_void_p(stream.cuda_stream)))
+
+    def timed(fn):
+        fn()
+        torch.cuda.synchronize()
+        ms = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+            ms.append(a.elapsed_time(b))
+        return float(np.median(ms))
+
+    c0, c1 = ctypes.c_ulonglong(), ctypes.c_ulonglong()
+    lib.dcrf_launch_count(ctypes.byref(c0))
+    batch_ms = timed(lambda: solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all)))
+    lib.dcrf_launch_count(ctypes.byref(c1))
+    batch_launches = (c1.value - c0.value) // (reps + 1)
+    Qb = Q_all.clone()
+    lib.dcrf_destroy(hb)
+
+    hs = []
+    for w, h_ in sizes:
+        h = ctypes.c_void_p()
+        _lib.check(lib.dcrf_create_2d(w, h_, Mb, ctypes.byref(h)))
+        _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+        hs.append(h)
+
+    def loop():
+        for i, h in enumerate(hs):
+            solve(h, ptr(U_all, Mb * offs[i]), ptr(img_all, 3 * offs[i]), ptr(Q_all, Mb * offs[i]))
+
+    loop_ms = timed(loop)
+    for h in hs:
+        lib.dcrf_destroy(h)
+    same = bool(torch.equal(Qb, Q_all))
+    units = Ntot * Mb * Tb / 1e6
+    return {"workload": f"{len(sizes)} images W,H~U[256,1024] (sum {Ntot} px) M=21 T=10, Gaussian+bilateral, "
+                        "21x21 Matrix compat", "batched_ms": round(batch_ms, 3), "loop_ms": round(loop_ms, 3),
+            "speedup": round(loop_ms / batch_ms, 3),
+            "batched_value": round(units / (batch_ms / 1e3), 1), "loop_value": round(units / (loop_ms / 1e3), 1),
+            "unit": "MPix*label*iter/s", "batched_launches": int(batch_launches),
+            "batched_equals_loop": same}
+
+
 def run_gpu(args):
     import torch
 
@@ -321,6 +489,8 @@ def run_gpu(args):
                "sample": f"{n} full solves of the same workload, one per thread, {dt:.1f} s"}
 
     lib.dcrf_destroy(h)
+    learning = learning_step_times(lib, _lib, dev, stream) if (rank == 0 and not args.no_learning) else None
+    batched = batched_vs_loop(lib, _lib, dev, stream) if (rank == 0 and not args.no_batch) else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "MPix*label*iter/s", "n_gpus": world,
@@ -339,6 +509,8 @@ def run_gpu(args):
             "lattice": {"L": Ls, "partials": Ps},
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "learning": learning,
+            "batched": batched,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
@@ -354,6 +526,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
+    ap.add_argument("--no-learning", action="store_true", help="skip the forward+backward timing")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-loop timing")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per point-pass launch from an ncu capture (reported as roofline.traffic)")
     args = ap.parse_args()

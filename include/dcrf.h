@@ -92,6 +92,24 @@ int dcrf_create(int N, int M, dcrf_crf **out);
 /* DenseCRF2D(W, H, M): densecrf.pyx:107-118 -> densecrf.cpp:47-48. */
 int dcrf_create_2d(int W, int H, int M, dcrf_crf **out);
 
+/* Batches (no reference counterpart: the reference solves one DenseCRF per
+ * object).  One handle holds n_images independent problems with the same M
+ * and the same pairwise terms: N[b] points each (dcrf_create_batch, features
+ * given by dcrf_add_pairwise) or W[b] x H[b] pixels each
+ * (dcrf_create_batch_2d, dcrf_add_pairwise_gaussian/_bilateral with the
+ * images' RGB bytes one after another).  Points are numbered image after
+ * image.  Every image gets its own lattice (the image index is part of the
+ * lattice key), so results per image are those of a separate handle; all
+ * images run in the same launches.  Label-major buffers hold image b's
+ * M x N[b] block after those of images < b; point-major buffers are
+ * [sum N][M].  dcrf_kl_divergence sums over the images; compatibility and
+ * kernel gradients of dcrf_backward are summed over the images (shared
+ * parameters). */
+int dcrf_create_batch(int n_images, const int *N, int M, dcrf_crf **out);
+int dcrf_create_batch_2d(int n_images, const int *W, const int *H, int M, dcrf_crf **out);
+/* Number of images and their point offsets (n_images + 1 ints; either may be NULL). */
+int dcrf_batch_info(dcrf_crf *h, int *n_images, int *point_start);
+
 /* Destructor: densecrf.pyx:65-69 -> densecrf.cpp:41-46. NULL is a no-op. */
 int dcrf_destroy(dcrf_crf *h);
 

@@ -38,6 +38,9 @@ _SIGS = {
     "dcrf_last_error": ([ctypes.c_char_p, ctypes.c_size_t], _i),
     "dcrf_create": ([_i, _i, ctypes.POINTER(_vp)], _i),
     "dcrf_create_2d": ([_i, _i, _i, ctypes.POINTER(_vp)], _i),
+    "dcrf_create_batch": ([_i, _vp, _i, ctypes.POINTER(_vp)], _i),
+    "dcrf_create_batch_2d": ([_i, _vp, _vp, _i, ctypes.POINTER(_vp)], _i),
+    "dcrf_batch_info": ([_vp, _vp, _vp], _i),
     "dcrf_destroy": ([_vp], _i),
     "dcrf_set_stream": ([_vp, _vp], _i),
     "dcrf_set_variant": ([_vp, _i], _i),

@@ -96,6 +96,12 @@ struct Term {
 
 struct dcrf_crf {
     int N = 0, M = 0, MP = 0, W = 0, H = 0;
+    // the images of the handle: point ranges seg[b]..seg[b+1] (one image for
+    // DenseCRF/DenseCRF2D, several for a batch); grid2d with each image's W x H
+    bool grid2d = false;
+    std::vector<int> seg, imgW, imgH;
+    int *d_seg = nullptr;   // [nimg+1] device copy of seg
+    int *d_imgW = nullptr;  // [nimg] device copy of imgW (grid2d)
     int variant = DCRF_VARIANT_SSE;
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
@@ -194,36 +200,44 @@ int check_handle(dcrf_crf *h) {
     return DCRF_OK;
 }
 
-// Tiles of the in-kernel splat.  A 2D grid uses 16x16 pixel blocks (the
-// corners of a block share far more lattice vertices than a raster strip of
-// the same size); a generic point set uses runs of 256 consecutive points.
+// Tiles of the in-kernel splat, image by image (no tile holds points of two
+// images).  A 2D image uses 16x16 pixel blocks (the corners of a block share
+// far more lattice vertices than a raster strip of the same size); a generic
+// point set uses runs of 256 consecutive points.
 int build_tiles(dcrf_crf *h) {
-    std::vector<int> slot, vbase;
-    if (h->W > 0 && h->H > 0) {
-        int bx = (h->W + 15) / 16, by = (h->H + 15) / 16;
-        h->ntiles = bx * by;
-        slot.assign((size_t)h->ntiles * SPLAT_TILE, -1);
-        vbase.assign(h->ntiles + 1, 0);
-        for (int ty = 0; ty < by; ty++)
-            for (int tx = 0; tx < bx; tx++) {
-                int t = ty * bx + tx, cnt = 0;
-                for (int yy = 0; yy < 16; yy++)
-                    for (int xx = 0; xx < 16; xx++) {
-                        int y = ty * 16 + yy, x = tx * 16 + xx;
-                        if (y < h->H && x < h->W) {
-                            slot[(size_t)t * SPLAT_TILE + yy * 16 + xx] = y * h->W + x;
-                            cnt++;
+    std::vector<int> slot, vbase{0};
+    const int nimg = (int)h->seg.size() - 1;
+    for (int b = 0; b < nimg; b++) {
+        const int base = h->seg[b], nb = h->seg[b + 1] - h->seg[b];
+        if (h->grid2d) {
+            const int Wb = h->imgW[b], Hb = h->imgH[b];
+            const int bx = (Wb + 15) / 16, by = (Hb + 15) / 16;
+            for (int ty = 0; ty < by; ty++)
+                for (int tx = 0; tx < bx; tx++) {
+                    const size_t t0 = slot.size();
+                    slot.resize(t0 + SPLAT_TILE, -1);
+                    int cnt = 0;
+                    for (int yy = 0; yy < 16; yy++)
+                        for (int xx = 0; xx < 16; xx++) {
+                            const int y = ty * 16 + yy, x = tx * 16 + xx;
+                            if (y < Hb && x < Wb) {
+                                slot[t0 + yy * 16 + xx] = base + y * Wb + x;
+                                cnt++;
+                            }
                         }
-                    }
-                vbase[t + 1] = vbase[t] + cnt;
+                    vbase.push_back(vbase.back() + cnt);
+                }
+        } else {
+            for (int t0 = 0; t0 < nb; t0 += SPLAT_TILE) {
+                const size_t o = slot.size();
+                slot.resize(o + SPLAT_TILE, -1);
+                const int cnt = std::min(SPLAT_TILE, nb - t0);
+                for (int q = 0; q < cnt; q++) slot[o + q] = base + t0 + q;
+                vbase.push_back(vbase.back() + cnt);
             }
-    } else {
-        h->ntiles = (h->N + SPLAT_TILE - 1) / SPLAT_TILE;
-        slot.assign((size_t)h->ntiles * SPLAT_TILE, -1);
-        vbase.assign(h->ntiles + 1, 0);
-        for (int s = 0; s < h->N; s++) slot[s] = s;
-        for (int t = 0; t < h->ntiles; t++) vbase[t + 1] = std::min(h->N, (t + 1) * SPLAT_TILE);
+        }
     }
+    h->ntiles = (int)vbase.size() - 1;
     h->nslots = h->ntiles * SPLAT_TILE;
     std::vector<int> inv(h->N, 0);
     for (size_t sl = 0; sl < slot.size(); sl++)
@@ -233,16 +247,32 @@ int build_tiles(dcrf_crf *h) {
     if ((rc = dev_alloc(&h->pt_slot, (size_t)h->N + 1))) return rc;
     if ((rc = dev_alloc(&h->tile_vbase, vbase.size() + 1))) return rc;
     if ((rc = dev_alloc(&h->kl_part, (size_t)h->ntiles + 1))) return rc;
+    if ((rc = dev_alloc(&h->d_seg, h->seg.size()))) return rc;
+    if ((rc = dev_alloc(&h->d_imgW, h->seg.size()))) return rc;
     CU(cudaMemcpy(h->slot_pt, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(h->pt_slot, inv.data(), inv.size() * sizeof(int), cudaMemcpyHostToDevice));
     CU(cudaMemcpy(h->tile_vbase, vbase.data(), vbase.size() * sizeof(int), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(h->d_seg, h->seg.data(), h->seg.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if (h->grid2d) CU(cudaMemcpy(h->d_imgW, h->imgW.data(), h->imgW.size() * sizeof(int), cudaMemcpyHostToDevice));
     return DCRF_OK;
 }
 
-int create(int N, int M, int W, int H, dcrf_crf **out) {
+// A handle over one or more images: Ns[b] points each, and for a 2D handle
+// Ws[b] x Hs[b] pixels (Ns[b] = Ws[b] * Hs[b]).  Points of image b are
+// numbered after those of images 0..b-1.
+int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const std::vector<int> &Hs,
+           dcrf_crf **out) {
     if (!out) return set_err(DCRF_ERR_INVALID_ARG, "null output pointer");
     *out = nullptr;
-    if (N <= 0 || M <= 0) return set_err(DCRF_ERR_INVALID_ARG, "N and M must be positive");
+    if (Ns.empty()) return set_err(DCRF_ERR_INVALID_ARG, "no images");
+    long long total = 0;
+    for (int n : Ns) {
+        if (n <= 0) return set_err(DCRF_ERR_INVALID_ARG, "N and M must be positive");
+        total += n;
+    }
+    if (total > 0x7FFFFFF0LL) return set_err(DCRF_ERR_INVALID_ARG, "too many points (more than 2^31)");
+    const int N = (int)total;
+    if (M <= 0) return set_err(DCRF_ERR_INVALID_ARG, "N and M must be positive");
     if (M > DCRF_MAX_MP)
         return set_err(DCRF_ERR_INVALID_ARG, "at most " + std::to_string(DCRF_MAX_MP) + " labels are supported, got " +
                                                  std::to_string(M));
@@ -255,8 +285,13 @@ int create(int N, int M, int W, int H, dcrf_crf **out) {
     h->N = N;
     h->M = M;
     h->MP = pad_labels(M);
-    h->W = W;
-    h->H = H;
+    h->grid2d = !Ws.empty();
+    h->W = Ns.size() == 1 && h->grid2d ? Ws[0] : 0;
+    h->H = Ns.size() == 1 && h->grid2d ? Hs[0] : 0;
+    h->imgW = Ws;
+    h->imgH = Hs;
+    h->seg.assign(1, 0);
+    for (int n : Ns) h->seg.push_back(h->seg.back() + n);
     cudaGetDevice(&h->device);
     int rc = DCRF_OK;
     auto fail = [&](int code) {
@@ -291,7 +326,8 @@ int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst, in
         dsrc = h->stage;
     }
     ProfScope ps(h, DCRF_KCLASS_OTHER);
-    CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, M, h->N, h->slot_pt, h->nslots, dst, h->stream));
+    CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, M, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt,
+                       h->nslots, dst, h->stream));
     return DCRF_OK;
 }
 
@@ -302,7 +338,8 @@ int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where, i
     float *ddst = where == DCRF_DEVICE ? dst : h->stage;
     {
         ProfScope ps(h, DCRF_KCLASS_OTHER);
-        CU(launch_from_slots(src, M, h->N, h->nslots, h->pt_slot, layout == DCRF_LAYOUT_PM, ddst, h->stream));
+        CU(launch_from_slots(src, M, h->N, h->d_seg, (int)h->seg.size() - 1, h->nslots, h->pt_slot,
+                             layout == DCRF_LAYOUT_PM, ddst, h->stream));
     }
     if (where != DCRF_DEVICE)
         CU(cudaMemcpyAsync(dst, h->stage, sizeof(float) * (size_t)h->N * M, cudaMemcpyDeviceToHost, h->stream));
@@ -596,7 +633,7 @@ int build_term(dcrf_crf *h, int k) {
         feat = scaled;
     }
     Segments seg;
-    seg.start = {0, h->N};
+    seg.start = h->seg;
     TileMapDev tm;
     tm.ntiles = h->ntiles;
     tm.slot_pt = h->slot_pt;
@@ -879,12 +916,36 @@ int dcrf_last_error(char *buf, size_t len) {
     return g_code;
 }
 
-int dcrf_create(int N, int M, dcrf_crf **out) { return create(N, M, 0, 0, out); }
+int dcrf_create(int N, int M, dcrf_crf **out) { return create(M, {N}, {}, {}, out); }
 
 int dcrf_create_2d(int W, int H, int M, dcrf_crf **out) {
     if (W <= 0 || H <= 0) return set_err(DCRF_ERR_INVALID_ARG, "W and H must be positive");
     if ((long long)W * H > 0x7FFFFFFF) return set_err(DCRF_ERR_INVALID_ARG, "image too large");
-    return create(W * H, M, W, H, out);
+    return create(M, {W * H}, {W}, {H}, out);
+}
+
+int dcrf_create_batch(int n_images, const int *N, int M, dcrf_crf **out) {
+    if (n_images <= 0 || !N) return set_err(DCRF_ERR_INVALID_ARG, "a batch needs at least one image");
+    return create(M, std::vector<int>(N, N + n_images), {}, {}, out);
+}
+
+int dcrf_create_batch_2d(int n_images, const int *W, const int *H, int M, dcrf_crf **out) {
+    if (n_images <= 0 || !W || !H) return set_err(DCRF_ERR_INVALID_ARG, "a batch needs at least one image");
+    std::vector<int> Ns(n_images), Ws(W, W + n_images), Hs(H, H + n_images);
+    for (int b = 0; b < n_images; b++) {
+        if (W[b] <= 0 || H[b] <= 0) return set_err(DCRF_ERR_INVALID_ARG, "W and H must be positive");
+        if ((long long)W[b] * H[b] > 0x7FFFFFFF) return set_err(DCRF_ERR_INVALID_ARG, "image too large");
+        Ns[b] = W[b] * H[b];
+    }
+    return create(M, Ns, Ws, Hs, out);
+}
+
+int dcrf_batch_info(dcrf_crf *h, int *n_images, int *point_start) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n_images) *n_images = (int)h->seg.size() - 1;
+    if (point_start) std::memcpy(point_start, h->seg.data(), h->seg.size() * sizeof(int));
+    return ok();
 }
 
 int dcrf_destroy(dcrf_crf *h) {
@@ -910,6 +971,8 @@ int dcrf_destroy(dcrf_crf *h) {
     dev_free(h->kl_part);
     dev_free(h->slot_pt);
     dev_free(h->tile_vbase);
+    dev_free(h->d_seg);
+    dev_free(h->d_imgW);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->capture) cudaStreamDestroy(h->capture);
     if (h->own) cudaStreamDestroy(h->own);
@@ -972,12 +1035,13 @@ int dcrf_add_pairwise_gaussian(dcrf_crf *h, float sx, float sy, int compat_kind,
                                int kernel_type, int normalization_type, int *term_out) {
     int rc = check_handle(h);
     if (rc) return rc;
-    if (h->W <= 0) return set_err(DCRF_ERR_STATE, "addPairwiseGaussian needs a DenseCRF2D handle");
+    if (!h->grid2d) return set_err(DCRF_ERR_STATE, "addPairwiseGaussian needs a DenseCRF2D handle");
     if ((rc = validate_compat(compat_kind, compat)) || (rc = validate_kn(kernel_type, normalization_type))) return rc;
     if ((int)h->terms.size() >= DCRF_MAX_TERMS) return set_err(DCRF_ERR_INVALID_ARG, "too many pairwise terms");
     float *f = nullptr;
     if ((rc = dev_alloc_async(&f, (size_t)2 * h->N, h->stream))) return rc;
-    cudaError_t e = launch_features_2d(h->W, h->H, sx, sy, nullptr, 1.f, 1.f, 1.f, f, h->stream);
+    cudaError_t e = launch_features_2d(h->N, h->d_seg, h->d_imgW, (int)h->seg.size() - 1, sx, sy, nullptr, 1.f, 1.f, 1.f, f,
+                                       h->stream);
     if (e != cudaSuccess) {
         dev_free_async(f, h->stream);
         return set_err(DCRF_ERR_CUDA, std::string("features: ") + cudaGetErrorString(e));
@@ -990,7 +1054,7 @@ int dcrf_add_pairwise_bilateral(dcrf_crf *h, float sx, float sy, float sr, float
                                 int normalization_type, int *term_out) {
     int rc = check_handle(h);
     if (rc) return rc;
-    if (h->W <= 0) return set_err(DCRF_ERR_STATE, "addPairwiseBilateral needs a DenseCRF2D handle");
+    if (!h->grid2d) return set_err(DCRF_ERR_STATE, "addPairwiseBilateral needs a DenseCRF2D handle");
     if (!rgb) return set_err(DCRF_ERR_INVALID_ARG, "null image");
     if ((rc = validate_compat(compat_kind, compat)) || (rc = validate_kn(kernel_type, normalization_type))) return rc;
     if ((int)h->terms.size() >= DCRF_MAX_TERMS) return set_err(DCRF_ERR_INVALID_ARG, "too many pairwise terms");
@@ -1011,7 +1075,8 @@ int dcrf_add_pairwise_bilateral(dcrf_crf *h, float sx, float sy, float sr, float
         }
         src = img;
     }
-    cudaError_t e = launch_features_2d(h->W, h->H, sx, sy, src, sr, sg, sb, f, h->stream);
+    cudaError_t e = launch_features_2d(h->N, h->d_seg, h->d_imgW, (int)h->seg.size() - 1, sx, sy, src, sr, sg, sb, f,
+                                       h->stream);
     if (e != cudaSuccess) {
         dev_free_async(f, h->stream);
         dev_free_async(img, h->stream);
@@ -1484,7 +1549,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     // the array keeps the previous call's contents: the zero sentinel rows are restored
     CU(cudaMemsetAsync(V0, 0, sizeof(float) * MPv, s));
     CU(cudaMemsetAsync(V1, 0, sizeof(float) * MPv, s));
-    CU(launch_to_slots(in, 0, value_size, h->N, h->slot_pt, h->nslots, in_s, s));
+    CU(launch_to_slots(in, 0, value_size, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, in_s, s));
     std::vector<int> one{term};
     PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
     a.ts.t[0].pre_norm = 0;
@@ -1517,6 +1582,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     f.ts.t[0].V = Vb[(T.d + 1) & 1];
     f.Qout = in_s;
     CU(launch_pointpass(f, MPv, s));
-    CU(launch_from_slots(in_s, value_size, h->N, h->nslots, h->pt_slot, 0, out, s));
+    CU(launch_from_slots(in_s, value_size, h->N, h->d_seg, (int)h->seg.size() - 1, h->nslots, h->pt_slot, 0, out,
+                         s));
     return ok();
 }

@@ -545,6 +545,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     L.N = N;
     L.variant = variant;
     const int nseg = (int)seg.start.size() - 1;
+    if (nseg > 65536) return fail(DCRF_ERR_INVALID_ARG, "at most 65536 images per lattice (16-bit image field)");
     // padding points of the x86 build: each image's N_img rounded up to 4
     std::vector<int> ph_img;
     if (variant == DCRF_VARIANT_SSE)

@@ -600,40 +600,69 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
     }
 }
 
+// Image of point p: the b with seg[b] <= p < seg[b+1].
+__device__ __forceinline__ int image_of(const int *__restrict__ seg, int nseg, int p) {
+    int lo = 0, hi = nseg - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(seg + mid) <= p)
+            lo = mid;
+        else
+            hi = mid - 1;
+    }
+    return lo;
+}
+
+// Offset of (label m, point p) in a caller's buffer: point-major [N][M], or
+// label-major per image (image b's M x N_b block after those of images < b;
+// with one image simply [M][N]).
+__device__ __forceinline__ size_t user_offset(int point_major, int M, int N, const int *__restrict__ seg, int nseg,
+                                              int p, int m) {
+    if (point_major) return (size_t)p * M + m;
+    if (nseg == 1) return (size_t)m * N + p;
+    const int b = image_of(seg, nseg, p);
+    const int s0 = __ldg(seg + b), nb = __ldg(seg + b + 1) - s0;
+    return (size_t)s0 * M + (size_t)m * nb + (p - s0);
+}
+
 // out[m][slot] = in(m, slot_pt[slot]) or 0
 __global__ void to_slots_kernel(const float *__restrict__ in, int point_major, int M, int N,
-                                const int *__restrict__ slot_pt, int nslots, float *__restrict__ out) {
+                                const int *__restrict__ seg, int nseg, const int *__restrict__ slot_pt, int nslots,
+                                float *__restrict__ out) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)nslots) return;
     const int pt = slot_pt[s];
-    for (int m = 0; m < M; m++) {
-        float v = 0.f;
-        if (pt >= 0) v = point_major ? in[(size_t)pt * M + m] : in[(size_t)m * N + pt];
-        out[(size_t)m * nslots + s] = v;
+    size_t o0 = 0, step = 0;
+    if (pt >= 0) {
+        o0 = user_offset(point_major, M, N, seg, nseg, pt, 0);
+        step = M > 1 ? user_offset(point_major, M, N, seg, nseg, pt, 1) - o0 : 0;
     }
+    for (int m = 0; m < M; m++) out[(size_t)m * nslots + s] = pt >= 0 ? in[o0 + m * step] : 0.f;
 }
 
 // out(m, pt) = in[m][pt_slot[pt]]
-__global__ void from_slots_kernel(const float *__restrict__ in, int M, int N, int nslots,
-                                  const int *__restrict__ pt_slot, int point_major, float *__restrict__ out) {
-    const size_t pt = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (pt >= (size_t)N) return;
+__global__ void from_slots_kernel(const float *__restrict__ in, int M, int N, const int *__restrict__ seg, int nseg,
+                                  int nslots, const int *__restrict__ pt_slot, int point_major,
+                                  float *__restrict__ out) {
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= N) return;
     const size_t s = (size_t)pt_slot[pt];
-    for (int m = 0; m < M; m++) {
-        const float v = in[(size_t)m * nslots + s];
-        if (point_major)
-            out[pt * M + m] = v;
-        else
-            out[(size_t)m * N + pt] = v;
-    }
+    const size_t o0 = user_offset(point_major, M, N, seg, nseg, pt, 0);
+    const size_t step = M > 1 ? user_offset(point_major, M, N, seg, nseg, pt, 1) - o0 : 0;
+    for (int m = 0; m < M; m++) out[o0 + m * step] = in[(size_t)m * nslots + s];
 }
 
-__global__ void features_2d_kernel(int W, int H, float sx, float sy, const uint8_t *__restrict__ rgb, float sr,
-                                   float sg, float sb, float *__restrict__ feat) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    int N = W * H;
+// DenseCRF2D features (densecrf.cpp:61-81) of every image of the handle:
+// (x/sx, y/sy[, r/sr, g/sg, b/sb]) with (x, y) the pixel within its own image;
+// rgb holds the images' H x W x 3 bytes one after another.
+__global__ void features_2d_kernel(int N, const int *__restrict__ seg, const int *__restrict__ imgW, int nseg,
+                                   float sx, float sy, const uint8_t *__restrict__ rgb, float sr, float sg, float sb,
+                                   float *__restrict__ feat) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= N) return;
-    int j = p / W, i = p - j * W;
+    const int b = image_of(seg, nseg, p);
+    const int q = p - __ldg(seg + b), Wb = __ldg(imgW + b);
+    const int j = q / Wb, i = q - j * Wb;
     feat[p] = __fdiv_rn((float)i, sx);
     feat[(size_t)N + p] = __fdiv_rn((float)j, sy);
     if (rgb) {
@@ -758,17 +787,19 @@ cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s) {
 #undef DCRF_BL
 }
 
-cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *slot_pt, int nslots,
-                            float *out, cudaStream_t s) {
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *seg, int nseg,
+                            const int *slot_pt, int nslots, float *out, cudaStream_t s) {
     if (nslots > 0)
-        DCRF_LAUNCH(to_slots_kernel<<<(nslots + 255) / 256, 256, 0, s>>>(in, point_major, M, N, slot_pt, nslots, out));
+        DCRF_LAUNCH(to_slots_kernel<<<(nslots + 255) / 256, 256, 0, s>>>(in, point_major, M, N, seg, nseg, slot_pt,
+                                                                         nslots, out));
     return cudaGetLastError();
 }
 
-cudaError_t launch_from_slots(const float *in, int M, int N, int nslots, const int *pt_slot, int point_major,
-                              float *out, cudaStream_t s) {
+cudaError_t launch_from_slots(const float *in, int M, int N, const int *seg, int nseg, int nslots,
+                              const int *pt_slot, int point_major, float *out, cudaStream_t s) {
     if (N > 0)
-        DCRF_LAUNCH(from_slots_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, N, nslots, pt_slot, point_major, out));
+        DCRF_LAUNCH(from_slots_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, N, seg, nseg, nslots, pt_slot,
+                                                                      point_major, out));
     return cudaGetLastError();
 }
 
@@ -778,10 +809,11 @@ cudaError_t launch_scale_members(const uint16_t *mem_pt, const float *mem_w, con
     return cudaGetLastError();
 }
 
-cudaError_t launch_features_2d(int W, int H, float sx, float sy, const uint8_t *rgb, float sr, float sg, float sb,
-                               float *feat, cudaStream_t s) {
-    int N = W * H;
-    if (N > 0) DCRF_LAUNCH(features_2d_kernel<<<(N + 255) / 256, 256, 0, s>>>(W, H, sx, sy, rgb, sr, sg, sb, feat));
+cudaError_t launch_features_2d(int N, const int *seg, const int *imgW, int nseg, float sx, float sy,
+                               const uint8_t *rgb, float sr, float sg, float sb, float *feat, cudaStream_t s) {
+    if (N > 0)
+        DCRF_LAUNCH(features_2d_kernel<<<(N + 255) / 256, 256, 0, s>>>(N, seg, imgW, nseg, sx, sy, rgb, sr, sg, sb,
+                                                                       feat));
     return cudaGetLastError();
 }
 

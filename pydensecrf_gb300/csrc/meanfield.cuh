@@ -69,15 +69,17 @@ cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s);
 
-// Layout conversions between user layouts (label-major [M][N] or point-major
-// [N][M]) and the slot-major [M][nslots] device layout.
-cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *slot_pt, int nslots,
-                            float *out, cudaStream_t s);
-cudaError_t launch_from_slots(const float *in, int M, int N, int nslots, const int *pt_slot, int point_major,
-                              float *out, cudaStream_t s);
-// 2D features of DenseCRF2D (densecrf.cpp:61-81) into [d][N]
-cudaError_t launch_features_2d(int W, int H, float sx, float sy, const uint8_t *rgb, float sr, float sg, float sb,
-                               float *feat, cudaStream_t s);
+// Layout conversions between user layouts (point-major [N][M], or label-major:
+// per image an M x N_b block, images one after another -- [M][N] for one image)
+// and the slot-major [M][nslots] device layout.  seg[0..nseg] are the images'
+// point offsets on the device.
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *seg, int nseg,
+                            const int *slot_pt, int nslots, float *out, cudaStream_t s);
+cudaError_t launch_from_slots(const float *in, int M, int N, const int *seg, int nseg, int nslots,
+                              const int *pt_slot, int point_major, float *out, cudaStream_t s);
+// 2D features of DenseCRF2D (densecrf.cpp:61-81) of every image into [d][N]
+cudaError_t launch_features_2d(int N, const int *seg, const int *imgW, int nseg, float sx, float sy,
+                               const uint8_t *rgb, float sr, float sg, float sb, float *feat, cudaStream_t s);
 cudaError_t launch_scale_features(const float *in, float *out, const float *scale_or_matrix, int d, int N, int full,
                                   cudaStream_t s);
 // wn[e] = w[e] * norm[slot of member e] over the padded per-tile member lists
