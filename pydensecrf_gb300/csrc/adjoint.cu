@@ -9,60 +9,65 @@
 
 namespace dcrf {
 
+// All label-valued buffers here are slot rows [ns][ld] (ld = padded label
+// count); labels m >= M and empty slots are written as 0.
+
 // b = Q * sum(x .* Q) - x .* Q  per point: the softmax adjoint with the
 // reference's sign (sumAndNormalize, densecrf.cpp:107-114, applied to x .* Q).
 __global__ void softmax_adjoint_kernel(const float *__restrict__ Q, const float *__restrict__ x, float *__restrict__ b,
-                                       int M, int ns, const int *__restrict__ slot_pt) {
+                                       int M, int ld, int ns, const int *__restrict__ slot_pt) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
+    const float *q = Q + s * ld, *xx = x + s * ld;
+    float *o = b + s * ld;
     if (slot_pt[s] < 0) {
-        for (int m = 0; m < M; m++) b[(size_t)m * ns + s] = 0.f;
+        for (int m = 0; m < ld; m++) o[m] = 0.f;
         return;
     }
     float dot = 0.f;
-    for (int m = 0; m < M; m++) dot = fmaf(x[(size_t)m * ns + s], Q[(size_t)m * ns + s], dot);
-    for (int m = 0; m < M; m++) {
-        const float q = Q[(size_t)m * ns + s];
-        b[(size_t)m * ns + s] = fmaf(q, dot, -x[(size_t)m * ns + s] * q);
-    }
+    for (int m = 0; m < M; m++) dot = fmaf(xx[m], q[m], dot);
+    for (int m = 0; m < ld; m++) o[m] = m < M ? fmaf(q[m], dot, -xx[m] * q[m]) : 0.f;
 }
 
 // y (+)= C x, or C^T x, per point (labelcompatibility.cpp:46-48,66-68,82-87)
-__global__ void compat_kernel(const float *__restrict__ x, float *__restrict__ y, int M, int ns, int kind,
+__global__ void compat_kernel(const float *__restrict__ x, float *__restrict__ y, int M, int ld, int ns, int kind,
                               float potts_w, const float *__restrict__ C, int transpose, int accumulate) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
-    for (int m = 0; m < M; m++) {
-        float v;
-        if (kind == DCRF_COMPAT_POTTS) {
-            v = -potts_w * x[(size_t)m * ns + s];
-        } else if (kind == DCRF_COMPAT_DIAGONAL) {
-            v = C[m] * x[(size_t)m * ns + s];
-        } else {
-            v = 0.f;
-            for (int k = 0; k < M; k++) v = fmaf(transpose ? C[k * M + m] : C[m * M + k], x[(size_t)k * ns + s], v);
+    const float *xx = x + s * ld;
+    float *yy = y + s * ld;
+    for (int m = 0; m < ld; m++) {
+        float v = 0.f;
+        if (m < M) {
+            if (kind == DCRF_COMPAT_POTTS) {
+                v = -potts_w * xx[m];
+            } else if (kind == DCRF_COMPAT_DIAGONAL) {
+                v = C[m] * xx[m];
+            } else {
+                for (int k = 0; k < M; k++) v = fmaf(transpose ? C[k * M + m] : C[m * M + k], xx[k], v);
+            }
         }
         if (accumulate)
-            y[(size_t)m * ns + s] += v;
+            yy[m] += v;
         else
-            y[(size_t)m * ns + s] = v;
+            yy[m] = v;
     }
 }
 
 // y = x .* norm^pw per point (pw in 1..3)
 __global__ void scale_norm_kernel(const float *__restrict__ x, float *__restrict__ y, const float *__restrict__ norm,
-                                  int M, int ns, int pw) {
+                                  int ld, int ns, int pw) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
     const float n = norm[s];
     const float f = pw == 1 ? n : pw == 2 ? n * n : n * n * n;
-    for (int m = 0; m < M; m++) y[(size_t)m * ns + s] = x[(size_t)m * ns + s] * f;
+    for (int m = 0; m < ld; m++) y[s * ld + m] = x[s * ld + m] * f;
 }
 
 // y = scale * (x1 .* x2 + x3 .* x4) .* norm^pw per point (x3/x4 may be null; norm null: pw ignored)
 __global__ void prod_kernel(const float *__restrict__ x1, const float *__restrict__ x2, const float *__restrict__ x3,
                             const float *__restrict__ x4, float scale, const float *__restrict__ norm, int pw,
-                            float *__restrict__ y, int M, int ns) {
+                            float *__restrict__ y, int ld, int ns) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
     float f = scale;
@@ -70,8 +75,8 @@ __global__ void prod_kernel(const float *__restrict__ x1, const float *__restric
         const float n = norm[s];
         f *= pw == 1 ? n : pw == 2 ? n * n : n * n * n;
     }
-    for (int m = 0; m < M; m++) {
-        const size_t o = (size_t)m * ns + s;
+    for (int m = 0; m < ld; m++) {
+        const size_t o = s * ld + m;
         float v = x1[o] * x2[o];
         if (x3) v = fmaf(x3[o], x4[o], v);
         y[o] = v * f;
@@ -83,11 +88,11 @@ __global__ void add_kernel(const float *__restrict__ x, float *__restrict__ y, s
     if (i < n) y[i] += x[i];
 }
 
-__global__ void fill_kernel(float *__restrict__ y, float v, int M, int ns, const int *__restrict__ slot_pt) {
+__global__ void fill_kernel(float *__restrict__ y, float v, int M, int ld, int ns, const int *__restrict__ slot_pt) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
     const float val = slot_pt[s] >= 0 ? v : 0.f;
-    for (int m = 0; m < M; m++) y[(size_t)m * ns + s] = val;
+    for (int m = 0; m < ld; m++) y[s * ld + m] = m < M ? val : 0.f;
 }
 
 // Per-block partial sums of the label products over the occupied slots:
@@ -95,8 +100,8 @@ __global__ void fill_kernel(float *__restrict__ y, float v, int M, int ns, const
 //  mode 1 (outer):      part[blk][m*M+k]  = sum_s a[m][s] * b[k][s]
 // Padding slots (slot_pt < 0) hold no point and are left out whatever they contain.
 __global__ void __launch_bounds__(256) label_products_kernel(const float *__restrict__ a, const float *__restrict__ b,
-                                                             int M, int ns, const int *__restrict__ slot_pt, int mode,
-                                                             double *__restrict__ part) {
+                                                             int M, int ld, int ns, const int *__restrict__ slot_pt,
+                                                             int mode, double *__restrict__ part) {
     extern __shared__ double sred[];  // [8 warps][K]
     const int K = mode == 0 ? M : M * M;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -104,7 +109,7 @@ __global__ void __launch_bounds__(256) label_products_kernel(const float *__rest
     const bool ok = s < (size_t)ns && slot_pt[s] >= 0;
     for (int kk = 0; kk < K; kk++) {
         const int m = mode == 0 ? kk : kk / M, k = mode == 0 ? kk : kk % M;
-        double v = ok ? (double)a[(size_t)m * ns + s] * (double)b[(size_t)k * ns + s] : 0.0;
+        double v = ok ? (double)a[s * ld + m] * (double)b[s * ld + k] : 0.0;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
         if (lane == 0) sred[warp * K + kk] = v;
@@ -141,7 +146,7 @@ __global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
     const int d = a.d, N = a.N, M = a.M;
     float z[MP];
 #pragma unroll
-    for (int m = 0; m < MP; m++) z[m] = m < M ? a.z[(size_t)m * a.nslots + s] : 0.f;
+    for (int m = 0; m < MP; m++) z[m] = m < M ? a.z[s * MP + m] : 0.f;
     float sm[MP];
 #pragma unroll
     for (int m = 0; m < MP; m++) sm[m] = 0.f;
@@ -190,24 +195,25 @@ static unsigned blocks(size_t n) { return (unsigned)((n + 255) / 256); }
 
 cudaError_t launch_softmax_adjoint(const float *Q, const float *x, float *b, int M, int ns, const int *slot_pt,
                                    cudaStream_t s) {
-    DCRF_LAUNCH(softmax_adjoint_kernel<<<blocks(ns), 256, 0, s>>>(Q, x, b, M, ns, slot_pt));
+    DCRF_LAUNCH(softmax_adjoint_kernel<<<blocks(ns), 256, 0, s>>>(Q, x, b, M, pad_labels(M), ns, slot_pt));
     return cudaGetLastError();
 }
 
 cudaError_t launch_compat(const float *x, float *y, int M, int ns, int kind, float potts_w, const float *C,
                           int transpose, int accumulate, cudaStream_t s) {
-    DCRF_LAUNCH(compat_kernel<<<blocks(ns), 256, 0, s>>>(x, y, M, ns, kind, potts_w, C, transpose, accumulate));
+    DCRF_LAUNCH(compat_kernel<<<blocks(ns), 256, 0, s>>>(x, y, M, pad_labels(M), ns, kind, potts_w, C, transpose,
+                                                         accumulate));
     return cudaGetLastError();
 }
 
 cudaError_t launch_scale_norm(const float *x, float *y, const float *norm, int M, int ns, int pw, cudaStream_t s) {
-    DCRF_LAUNCH(scale_norm_kernel<<<blocks(ns), 256, 0, s>>>(x, y, norm, M, ns, pw));
+    DCRF_LAUNCH(scale_norm_kernel<<<blocks(ns), 256, 0, s>>>(x, y, norm, pad_labels(M), ns, pw));
     return cudaGetLastError();
 }
 
 cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const float *x4, float scale,
                         const float *norm, int pw, float *y, int M, int ns, cudaStream_t s) {
-    DCRF_LAUNCH(prod_kernel<<<blocks(ns), 256, 0, s>>>(x1, x2, x3, x4, scale, norm, pw, y, M, ns));
+    DCRF_LAUNCH(prod_kernel<<<blocks(ns), 256, 0, s>>>(x1, x2, x3, x4, scale, norm, pw, y, pad_labels(M), ns));
     return cudaGetLastError();
 }
 
@@ -217,7 +223,7 @@ cudaError_t launch_add(const float *x, float *y, size_t n, cudaStream_t s) {
 }
 
 cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cudaStream_t s) {
-    DCRF_LAUNCH(fill_kernel<<<blocks(ns), 256, 0, s>>>(y, v, M, ns, slot_pt));
+    DCRF_LAUNCH(fill_kernel<<<blocks(ns), 256, 0, s>>>(y, v, M, pad_labels(M), ns, slot_pt));
     return cudaGetLastError();
 }
 
@@ -233,7 +239,7 @@ cudaError_t launch_label_products(const float *a, const float *b, int M, int ns,
                                              (int)smem);
         if (e != cudaSuccess) return e;
     }
-    DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, ns, slot_pt, mode, part));
+    DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, pad_labels(M), ns, slot_pt, mode, part));
     DCRF_LAUNCH(sum_parts_kernel<<<blocks(K), 256, 0, s>>>(part, (int)nb, K, out, accumulate));
     return cudaGetLastError();
 }

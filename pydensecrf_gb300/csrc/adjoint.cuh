@@ -2,6 +2,8 @@
 #pragma once
 #include "dcrf_common.cuh"
 
+// Label-valued buffers are slot rows [ns][pad_labels(M)].
+
 namespace dcrf {
 
 struct SliceGradArgs {
@@ -10,7 +12,7 @@ struct SliceGradArgs {
     const int *off;       // [d+1][N]
     const uint8_t *rank;  // [d+1][N]
     const float *V;       // [L+1][MP] blurred values, vertex order
-    const float *z;       // [M][nslots] contraction values
+    const float *z;       // [nslots][MP] contraction values (slot rows)
     float sf[DCRF_MAX_D];
     float alpha;          // 1/(1+2^-d) / (d+1)
     float *df;            // [N][d] accumulated feature gradient

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <mutex>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -18,6 +19,38 @@ using namespace dcrf;
 namespace dcrf {
 static std::atomic<unsigned long long> g_launches{0};
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t s) {
+    static std::mutex mu;
+    static cudaMemPool_t pools[256] = {};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!pools[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            e = cudaMemPoolCreate(&pools[dev], &props);
+            if (e != cudaSuccess) return e;
+            uint64_t keep = ~0ull;
+            cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        pool = pools[dev];
+    }
+    return cudaMallocFromPoolAsync(p, bytes, pool, s);
+}
+
+bool pdl_enabled() {
+    static const bool on = [] {
+        const char *e = std::getenv("DCRF_PDL");
+        return !(e && e[0] == '0');
+    }();
+    return on;
+}
 }  // namespace dcrf
 
 namespace {
@@ -62,10 +95,10 @@ void dev_free(void *p) {
 template <class T>
 int dev_alloc_async(T **p, size_t n, cudaStream_t s) {
     void *q = nullptr;
-    cudaError_t e = cudaMallocAsync(&q, std::max<size_t>(n * sizeof(T), 16), s);
+    cudaError_t e = pool_malloc_async(&q, std::max<size_t>(n * sizeof(T), 16), s);
     if (e != cudaSuccess) {
         cudaGetLastError();
-        return set_err(DCRF_ERR_OOM, "cudaMallocAsync of " + std::to_string(n * sizeof(T)) + " bytes failed");
+        return set_err(DCRF_ERR_OOM, "stream-ordered allocation of " + std::to_string(n * sizeof(T)) + " bytes failed");
     }
     *p = static_cast<T *>(q);
     return DCRF_OK;
@@ -305,9 +338,9 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
     h->stream = h->own;
     if ((rc = dev_alloc(&h->status, 1))) return fail(rc);
     if ((rc = build_tiles(h))) return fail(rc);
-    if ((rc = dev_alloc(&h->U, (size_t)h->nslots * M))) return fail(rc);
-    if ((rc = dev_alloc(&h->Q, (size_t)h->nslots * M))) return fail(rc);
-    if ((rc = dev_alloc(&h->tmp, (size_t)h->nslots * M))) return fail(rc);
+    if ((rc = dev_alloc(&h->U, (size_t)h->nslots * h->MP))) return fail(rc);
+    if ((rc = dev_alloc(&h->Q, (size_t)h->nslots * h->MP))) return fail(rc);
+    if ((rc = dev_alloc(&h->tmp, (size_t)h->nslots * h->MP))) return fail(rc);
     if ((rc = dev_alloc(&h->stage, (size_t)N * M))) return fail(rc);
     if ((rc = dev_alloc(&h->map, (size_t)N))) return fail(rc);
     CU(cudaMemset(h->status, 0, sizeof(DevStatus)));
@@ -316,9 +349,10 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
 }
 
 // Copies an M x N quantity from the caller (label- or point-major, host or
-// device) into the slot-major device layout dst [M][nslots].
+// device) into device slot rows dst [nslots][ld] (ld = MP, or 1 for M = 1).
 int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst, int M = -1) {
     if (M < 0) M = h->M;
+    const int ld = M == h->M ? h->MP : M;
     if (layout != DCRF_LAYOUT_LM && layout != DCRF_LAYOUT_PM) return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
     const float *dsrc = src;
     if (where != DCRF_DEVICE) {
@@ -326,19 +360,20 @@ int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst, in
         dsrc = h->stage;
     }
     ProfScope ps(h, DCRF_KCLASS_OTHER);
-    CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, M, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt,
+    CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, M, ld, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt,
                        h->nslots, dst, h->stream));
     return DCRF_OK;
 }
 
-// Copies the slot-major src [M][nslots] out to the caller's layout.
+// Copies the slot rows src [nslots][ld] out to the caller's layout.
 int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where, int M = -1) {
     if (M < 0) M = h->M;
+    const int ld = M == h->M ? h->MP : M;
     if (layout != DCRF_LAYOUT_LM && layout != DCRF_LAYOUT_PM) return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
     float *ddst = where == DCRF_DEVICE ? dst : h->stage;
     {
         ProfScope ps(h, DCRF_KCLASS_OTHER);
-        CU(launch_from_slots(src, M, h->N, h->d_seg, (int)h->seg.size() - 1, h->nslots, h->pt_slot,
+        CU(launch_from_slots(src, M, ld, h->N, h->d_seg, (int)h->seg.size() - 1, h->pt_slot,
                              layout == DCRF_LAYOUT_PM, ddst, h->stream));
     }
     if (where != DCRF_DEVICE)
@@ -379,6 +414,7 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.compat = T.compat;
     t.staged = 0;
     t.vcap = 0;
+    t.sm_cmp = -1;
     return t;
 }
 
@@ -399,11 +435,24 @@ void plan_smem(dcrf_crf *h, PPArgs &a, const std::vector<int> &which, bool msg, 
     a.sm_q = 0;
     a.sm_res = (int)align128((size_t)SPLAT_TILE * MP * 4);
     a.smem_bytes = (int)sq;
-    if (MP % 4 != 0 || sq > (size_t)budget) return;  // bulk copies need 16-byte rows
+    if (MP % 4 != 0) return;  // bulk copies need 16-byte rows
+    // Matrix compatibilities of the message pass, [k][MP] each (first, never aliased)
+    size_t cmp_end = 0;
+    for (int k = 0; k < n && msg; k++)
+        if (h->terms[which[k]].ckind == DCRF_COMPAT_MATRIX) cmp_end = align128(cmp_end + (size_t)MP * MP * 4);
+    if (cmp_end + sq > (size_t)budget) return;
+    for (int k = 0, o = 0; k < n && msg; k++)
+        if (h->terms[which[k]].ckind == DCRF_COMPAT_MATRIX) {
+            a.ts.t[k].sm_cmp = o;
+            o += (int)align128((size_t)MP * MP * 4);
+        }
+    a.sm_q = (int)cmp_end;
+    a.sm_res = (int)(cmp_end + align128((size_t)SPLAT_TILE * MP * 4));
+    a.smem_bytes = (int)(cmp_end + sq);
     std::vector<int> staged(n, 1), vcap(n, 0);
     for (int k = 0; k < n; k++) vcap[k] = msg ? h->terms[which[k]].lat.max_np : 0;
     for (int attempt = 0; attempt < 64; attempt++) {
-        size_t off = 0;
+        size_t off = cmp_end;
         for (int k = 0; k < n; k++) {
             if (!staged[k]) continue;
             const Term &T = h->terms[which[k]];
@@ -455,9 +504,9 @@ void plan_smem(dcrf_crf *h, PPArgs &a, const std::vector<int> &which, bool msg, 
         staged[drop] = 0;
     }
     for (int k = 0; k < n; k++) a.ts.t[k].staged = 0;
-    a.sm_q = 0;
-    a.sm_res = (int)align128((size_t)SPLAT_TILE * MP * 4);
-    a.smem_bytes = (int)sq;
+    a.sm_q = (int)cmp_end;
+    a.sm_res = (int)(cmp_end + align128((size_t)SPLAT_TILE * MP * 4));
+    a.smem_bytes = (int)(cmp_end + sq);
 }
 
 cudaError_t pp(dcrf_crf *h, const PPArgs &a, int MP) {
@@ -726,7 +775,7 @@ int validate_kn(int ktype, int ntype) {
 // final pass writes per final_mode (Q into h->Q, or the MAP labels).
 int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
     std::vector<int> w = all_terms(h);
-    const size_t qsz = (size_t)h->M * h->nslots;
+    const size_t qsz = (size_t)h->MP * h->nslots;
     int rc;
     if (T <= 0 || w.empty()) {
         PPArgs a = pp_args(h, final_mode | (ckpt ? PP_WRITE_Q : 0), w, false, false);
@@ -1102,7 +1151,7 @@ int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where) {
     if (rc) return rc;
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
     if (!h->has_unary) {  // densecrf.cpp:179-184: zeros without a unary
-        CU(cudaMemsetAsync(h->Q, 0, sizeof(float) * (size_t)h->nslots * h->M, h->stream));
+        CU(cudaMemsetAsync(h->Q, 0, sizeof(float) * (size_t)h->nslots * h->MP, h->stream));
     } else {
         CU(pp(h, pp_args(h, PP_WRITE_Q, {}, false, false), h->MP));
     }
@@ -1364,7 +1413,7 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
     int rc = check_handle(h);
     if (rc) return rc;
     if (!Q || n_iterations < 0) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
-    const size_t qsz = (size_t)h->M * h->nslots, need = qsz * ((size_t)n_iterations + 1);
+    const size_t qsz = (size_t)h->MP * h->nslots, need = qsz * ((size_t)n_iterations + 1);
     if (need > h->ckpt_cap) {
         dev_free_async(h->ckpt, h->stream);
         h->ckpt = nullptr;
@@ -1387,7 +1436,7 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
     if (h->ckpt_T < 0 || h->ckpt_version != h->version)
         return set_err(DCRF_ERR_STATE, "dcrf_backward needs a dcrf_inference_checkpointed of the current model");
     const int M = h->M, ns = h->nslots, T = h->ckpt_T, nt = (int)h->terms.size();
-    const size_t qsz = (size_t)M * ns;
+    const size_t qsz = (size_t)h->MP * ns;
     const bool want_compat = dcompat != nullptr, want_kernel = dkernel != nullptr;
     for (float *&b : h->bw)
         if (!b && (rc = dev_alloc_async(&b, qsz, h->stream))) return rc;
@@ -1533,7 +1582,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     const bool v1 = value_size == 1;
     const int MPv = v1 ? 1 : h->MP;
     Term &T = h->terms[term];
-    const size_t n_in = pad64((size_t)value_size * h->nslots);
+    const size_t n_in = pad64((size_t)MPv * h->nslots);
     const size_t n_pv = pad64(((size_t)T.lat.P + 1) * MPv);
     const size_t n_v = pad64(((size_t)T.lat.L + 1) * MPv);
     const size_t need = n_in + n_pv + 2 * n_v;
@@ -1549,7 +1598,8 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     // the array keeps the previous call's contents: the zero sentinel rows are restored
     CU(cudaMemsetAsync(V0, 0, sizeof(float) * MPv, s));
     CU(cudaMemsetAsync(V1, 0, sizeof(float) * MPv, s));
-    CU(launch_to_slots(in, 0, value_size, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, in_s, s));
+    CU(launch_to_slots(in, 0, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, in_s,
+                       s));
     std::vector<int> one{term};
     PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
     a.ts.t[0].pre_norm = 0;
@@ -1582,7 +1632,6 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     f.ts.t[0].V = Vb[(T.d + 1) & 1];
     f.Qout = in_s;
     CU(launch_pointpass(f, MPv, s));
-    CU(launch_from_slots(in_s, value_size, h->N, h->d_seg, (int)h->seg.size() - 1, h->nslots, h->pt_slot, 0, out,
-                         s));
+    CU(launch_from_slots(in_s, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->pt_slot, 0, out, s));
     return ok();
 }

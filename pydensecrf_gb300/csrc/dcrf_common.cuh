@@ -2,7 +2,8 @@
 //
 // Data layout in device memory (N points, M labels, MP = padded label count,
 // d feature dims, L lattice vertices of one term, E = N*(d+1) simplex corners):
-//   U, Q          float [M][N]        label-major (the numpy (M, N) layout)
+//   U, Q          float [nslots][MP]  slot rows: point slot_pt[s] of tile s/256,
+//                                     labels m < M (padding labels and empty slots 0)
 //   feat          float [d][N]        feature-major (the numpy (d, N) layout)
 //   off           int   [d+1][N]      vertex id of corner r of point i
 //   bary          float [d+1][N]      barycentric weight of that corner
@@ -30,6 +31,44 @@ void note_launch();
         dcrf::note_launch();  \
         __VA_ARGS__;          \
     } while (0)
+
+namespace dcrf {
+// Programmatic dependent launch.  The mean-field kernels (point pass, reduce,
+// blur) are launched so that the next one may start while its predecessor on
+// the stream drains: each calls pdl_trigger() on entry and pdl_wait() before
+// its first access to memory that a kernel of the launch sequence reads or
+// writes; only tables fixed since the lattice build (and the unary) are read
+// before the wait.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// Whether launches use the programmatic-serialization attribute (default on;
+// DCRF_PDL=0 in the environment turns it off).
+bool pdl_enabled();
+
+// Stream-ordered allocation from the library's memory pool of the current
+// device.  The pool keeps freed blocks (release threshold: unlimited), so the
+// per-term buffers of a rebuilt lattice come back without new mappings; the
+// default pool would return them to the driver at every synchronisation.
+cudaError_t pool_malloc_async(void **p, size_t bytes, cudaStream_t s);
+
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                       Args &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = pdl_enabled() ? 1 : 0;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    note_launch();
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+}
+}  // namespace dcrf
 
 // Device status block: slot 0 = first error code (0 = fine), slot 1 = detail.
 struct DevStatus {
@@ -85,6 +124,7 @@ struct TermDev {
     // shared-memory plan of the point pass (byte offsets; staged = 0: global reads)
     int staged, vcap;
     int sm_loc, sm_w, sm_norm, sm_task, sm_mpt, sm_mw, sm_vp;
+    int sm_cmp;  // Matrix compatibility staged as [k][MP] (transposed, zero padded); -1: global reads
 };
 
 struct TermSet {

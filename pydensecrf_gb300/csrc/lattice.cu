@@ -509,7 +509,7 @@ struct Pool {
     template <class T>
     T *get(size_t n) {
         void *p = nullptr;
-        if (cudaMallocAsync(&p, std::max<size_t>(n * sizeof(T), 16), s) != cudaSuccess) {
+        if (pool_malloc_async(&p, std::max<size_t>(n * sizeof(T), 16), s) != cudaSuccess) {
             failed = true;
             return nullptr;
         }
@@ -531,7 +531,7 @@ template <class T>
 T *dalloc(size_t n, cudaStream_t s, size_t *acc) {
     void *p = nullptr;
     size_t b = std::max<size_t>(n * sizeof(T), 16);
-    if (cudaMallocAsync(&p, b, s) != cudaSuccess) return nullptr;
+    if (pool_malloc_async(&p, b, s) != cudaSuccess) return nullptr;
     *acc += b;
     return static_cast<T *>(p);
 }

@@ -112,16 +112,12 @@ __device__ __forceinline__ void load_row(const float *__restrict__ row, float (&
 }
 
 template <int MP>
-__device__ __forceinline__ void load_row_smem(const float *row, float (&v)[MP]) {
+__device__ __forceinline__ void load_row_s(const float *row, float (&v)[MP]) {
     if constexpr (MP % 4 == 0) {
-        const float4 *r4 = reinterpret_cast<const float4 *>(row);
 #pragma unroll
         for (int c = 0; c < MP / 4; c++) {
-            float4 x = r4[c];
-            v[4 * c + 0] = x.x;
-            v[4 * c + 1] = x.y;
-            v[4 * c + 2] = x.z;
-            v[4 * c + 3] = x.w;
+            const float4 x = reinterpret_cast<const float4 *>(row)[c];
+            v[4 * c + 0] = x.x, v[4 * c + 1] = x.y, v[4 * c + 2] = x.z, v[4 * c + 3] = x.w;
         }
     } else {
 #pragma unroll
@@ -129,46 +125,114 @@ __device__ __forceinline__ void load_row_smem(const float *row, float (&v)[MP]) 
     }
 }
 
-// x -= compatibility(acc) (mean-field update), or, with kl_mode, kl += sum q * compatibility(acc)
-// where x holds q.  Potts: -w acc; Diagonal: v * acc; Matrix: W acc (labelcompatibility.cpp:46-48,66-68,82-84).
 template <int MP>
-__device__ __forceinline__ void fold_compat(const TermDev &T, const float (&acc)[MP], float (&x)[MP], int M,
-                                            bool kl_mode, double &kl) {
+__device__ __forceinline__ void store_row(float *row, const float (&v)[MP]) {
+    if constexpr (MP % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < MP / 4; c++)
+            reinterpret_cast<float4 *>(row)[c] = make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+    } else {
+#pragma unroll
+        for (int m = 0; m < MP; m++) row[m] = v[m];
+    }
+}
+
+// Point groups of the point pass: a point's MP labels are spread over G lanes
+// of VW consecutive labels each (one float4 for MP >= 4), so every row access
+// of a point -- unary, marginals, blurred vertex rows, splat rows -- is one
+// contiguous, conflict-free vector access of the group.
+template <int MP>
+struct PG {
+    static constexpr int VW = MP >= 4 ? 4 : MP;             // labels per lane
+    static constexpr int G = MP / VW;                       // lanes per point
+    static constexpr int GPW = 32 / G;                      // groups per warp
+    static constexpr int NG = (SPLAT_TILE / 32) * GPW;      // groups per CTA
+    static constexpr int PPG = (SPLAT_TILE + NG - 1) / NG;  // points per group
+};
+
+template <int VW>
+__device__ __forceinline__ void vload(const float *p, float (&v)[VW]) {
+    if constexpr (VW == 4) {
+        const float4 x = *reinterpret_cast<const float4 *>(p);
+        v[0] = x.x, v[1] = x.y, v[2] = x.z, v[3] = x.w;
+    } else if constexpr (VW == 2) {
+        const float2 x = *reinterpret_cast<const float2 *>(p);
+        v[0] = x.x, v[1] = x.y;
+    } else {
+        v[0] = *p;
+    }
+}
+
+template <int VW>
+__device__ __forceinline__ void vload_g(const float *__restrict__ p, float (&v)[VW]) {
+    if constexpr (VW == 4) {
+        const float4 x = __ldg(reinterpret_cast<const float4 *>(p));
+        v[0] = x.x, v[1] = x.y, v[2] = x.z, v[3] = x.w;
+    } else if constexpr (VW == 2) {
+        const float2 x = __ldg(reinterpret_cast<const float2 *>(p));
+        v[0] = x.x, v[1] = x.y;
+    } else {
+        v[0] = __ldg(p);
+    }
+}
+
+template <int VW>
+__device__ __forceinline__ void vstore(float *p, const float (&v)[VW]) {
+    if constexpr (VW == 4) {
+        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    } else if constexpr (VW == 2) {
+        *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
+    } else {
+        *p = v[0];
+    }
+}
+
+// x -= compatibility(acc) (mean-field update), or, with kl_mode, kl += sum q *
+// compatibility(acc) where x holds q.  Potts: -w acc; Diagonal: v * acc;
+// Matrix: W acc with the sum over k in label order (labelcompatibility.cpp:
+// 46-48,66-68,82-84); the Matrix comes from shared memory transposed to
+// [k][MP] (sCT, broadcast row reads) or, without it, from global memory.
+template <int MP>
+__device__ __forceinline__ void fold_compat(const TermDev &T, const float *sCT, const float (&acc)[MP], float (&x)[MP],
+                                            int M, bool kl_mode, double &kl) {
+    float c[MP];
     if (T.ckind == DCRF_COMPAT_POTTS) {
         const float nw = -T.potts_w;
 #pragma unroll
-        for (int m = 0; m < MP; m++) {
-            const float c = fmul(nw, acc[m]);
-            if (kl_mode) {
-                if (m < M) kl += (double)fmul(x[m], c);
-            } else {
-                x[m] = fsub(x[m], c);
-            }
-        }
+        for (int m = 0; m < MP; m++) c[m] = fmul(nw, acc[m]);
     } else if (T.ckind == DCRF_COMPAT_DIAGONAL) {
 #pragma unroll
-        for (int m = 0; m < MP; m++)
-            if (m < M) {
-                const float c = fmul(__ldg(T.compat + m), acc[m]);
-                if (kl_mode)
-                    kl += (double)fmul(x[m], c);
-                else
-                    x[m] = fsub(x[m], c);
-            }
+        for (int m = 0; m < MP; m++) c[m] = m < M ? fmul(__ldg(T.compat + m), acc[m]) : 0.f;
     } else {
 #pragma unroll
-        for (int m = 0; m < MP; m++)
-            if (m < M) {
-                const float *row = T.compat + (size_t)m * M;
-                float c = 0.f;
+        for (int m = 0; m < MP; m++) c[m] = 0.f;
+        if (sCT && MP % 4 == 0) {
 #pragma unroll
-                for (int k = 0; k < MP; k++)
-                    if (k < M) c = fadd(c, fmul(__ldg(row + k), acc[k]));
-                if (kl_mode)
-                    kl += (double)fmul(x[m], c);
-                else
-                    x[m] = fsub(x[m], c);
-            }
+            for (int k = 0; k < MP; k++)
+                if (k < M) {
+                    float w[MP];
+                    load_row_s<MP>(sCT + k * MP, w);
+#pragma unroll
+                    for (int m = 0; m < MP; m++) c[m] = fadd(c[m], fmul(w[m], acc[k]));
+                }
+        } else {
+#pragma unroll
+            for (int m = 0; m < MP; m++)
+                if (m < M) {
+                    const float *row = T.compat + (size_t)m * M;
+#pragma unroll
+                    for (int k = 0; k < MP; k++)
+                        if (k < M) c[m] = fadd(c[m], fmul(__ldg(row + k), acc[k]));
+                }
+        }
+    }
+#pragma unroll
+    for (int m = 0; m < MP; m++) {
+        if (m >= M) continue;
+        if (kl_mode)
+            kl += (double)fmul(x[m], c[m]);
+        else
+            x[m] = fsub(x[m], c[m]);
     }
 }
 
@@ -193,8 +257,12 @@ __device__ __forceinline__ TileBlocks tile_blocks(const TermDev &T, int t) {
     return b;
 }
 
+// One CTA per tile of SPLAT_TILE points; marginals and unaries are slot rows
+// of MP floats ([nslots][MP]).
 template <int MP>
-__global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kernel(const __grid_constant__ PPArgs a) {
+__global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_constant__ PPArgs a) {
+    using P = PG<MP>;
+    constexpr int VW = P::VW, G = P::G, GPW = P::GPW, NG = P::NG;
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t mbar;
     __shared__ double sKL[SPLAT_TILE / 32];
@@ -202,12 +270,19 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
 
     const int t = blockIdx.x;
     const int li = threadIdx.x;
-    const size_t s = (size_t)t * SPLAT_TILE + li;
-    const int i = a.slot_pt[s];
-    const bool valid = i >= 0;
-    const int M = a.M, mode = a.mode, ns = a.nslots;
+    const int lane = li & 31, warp = li >> 5;
+    const int g = lane / G;                  // group within the warp
+    const bool gactive = g < GPW;            // lanes past the last full group idle
+    const int gc = gactive ? g : GPW - 1;
+    const int c = lane - gc * G;             // lane within the group
+    const int gbase = gc * G;                // first lane of the group
+    const int gid = warp * GPW + gc;         // group within the CTA
+    const int m0 = c * VW;                   // first label of the lane
+    const int M = a.M, mode = a.mode;
+    pdl_trigger();
 
-    // ---- 1. prefetch the tile's tables (TMA bulk copies, one elected thread)
+    // ---- 1. prefetch the tile's tables (TMA bulk copies, one elected thread):
+    // the lattice tables first, the blurred rows once the previous kernel is done
     bool any_staged = false;
     for (int k = 0; k < a.ts.n; k++) any_staged |= a.ts.t[k].staged != 0;
     if (li < a.ts.n) sTB[li] = tile_blocks(a.ts.t[li], t);
@@ -243,33 +318,52 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
             if (mode & PP_MSG) {
                 bulk_g2s(smem + T.sm_loc, T.tl_loc + tb, (uint32_t)(d1 * SPLAT_TILE * 2), &mbar);
                 bulk_g2s(smem + T.sm_w, T.tl_w + tb, (uint32_t)(d1 * SPLAT_TILE * 4), &mbar);
-                if (b.vp_staged && b.np > 0)
-                    bulk_g2s(smem + T.sm_vp, T.pv + (size_t)b.pb * MP, (uint32_t)(b.np * MP * 4), &mbar);
+            }
+        }
+        pdl_wait();
+        for (int k = 0; k < a.ts.n && (mode & PP_MSG); k++) {
+            const TermDev &T = a.ts.t[k];
+            const TileBlocks b = sTB[k];
+            if (T.staged && b.vp_staged && b.np > 0)
+                bulk_g2s(smem + T.sm_vp, T.pv + (size_t)b.pb * MP, (uint32_t)(b.np * MP * 4), &mbar);
+        }
+    }
+    // Matrix compatibilities, transposed into [k][MP] (zero padded), by every thread
+    if (mode & PP_MSG) {
+        for (int k = 0; k < a.ts.n; k++) {
+            const TermDev &T = a.ts.t[k];
+            if (T.ckind != DCRF_COMPAT_MATRIX || T.sm_cmp < 0) continue;
+            float *sCT = reinterpret_cast<float *>(smem + T.sm_cmp);
+            for (int e = li; e < MP * MP; e += SPLAT_TILE) {
+                const int kk = e / MP, m = e - kk * MP;
+                sCT[e] = (kk < M && m < M) ? T.compat[(size_t)m * M + kk] : 0.f;
             }
         }
     }
 
-    // ---- 2. the point's own inputs, overlapping the copies
+    // the point's own inputs, overlapping the copies (one thread per point)
+    const size_t s = (size_t)t * SPLAT_TILE + li;
+    const int i = a.slot_pt[s];
+    const bool valid = i >= 0;
+    const bool given = (mode & (PP_LOAD_Q | PP_ONES)) != 0;
+    double kl = 0.0;
     // x: the logits of the update, or the given marginals (LOAD_Q / ONES); q after the softmax
     float x[MP];
 #pragma unroll
     for (int m = 0; m < MP; m++) x[m] = 0.f;
-    double kl = 0.0;
-    const bool given = (mode & (PP_LOAD_Q | PP_ONES)) != 0;
-    if (mode & PP_ONES) {
-        if (valid) x[0] = 1.f;
-    } else if (mode & PP_LOAD_Q) {
-        if (valid) {
+    if (valid && !(mode & (PP_ONES | PP_LOAD_Q)) && a.U) {  // the unary is fixed during inference
+        load_row<MP>(a.U + s * MP, x);
 #pragma unroll
-            for (int m = 0; m < MP; m++)
-                if (m < M) x[m] = a.Qin[(size_t)m * ns + s];
-        }
-    } else {
-#pragma unroll
-        for (int m = 0; m < MP; m++) x[m] = (valid && m < M && a.U) ? -a.U[(size_t)m * ns + s] : 0.f;
+        for (int m = 0; m < MP; m++) x[m] = -x[m];
     }
-
-    // ---- 3. wait for the copies (bounded; a timeout is reported, never a hang)
+    pdl_wait();
+    if (valid) {
+        if (mode & PP_ONES)
+            x[0] = 1.f;
+        else if (mode & PP_LOAD_Q)
+            load_row<MP>(a.Qin + s * MP, x);
+    }
+    // ---- 2. wait for the copies (bounded; a timeout is reported, never a hang)
     if (any_staged) {
         const bool ok = mbar_wait_bounded(&mbar, 0);
         if (__syncthreads_or(!ok)) {
@@ -277,14 +371,16 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
             mbar_wait_bounded(&mbar, 0);  // let this CTA's own copies land before it exits
             return;
         }
+    } else {
+        __syncthreads();
     }
 
-    // ---- 4. messages of every term
-    if (mode & PP_MSG) {
+    // ---- 3. per point (one thread per point): messages of every term,
+    // softmax, outputs
+    if ((mode & PP_MSG) && valid) {
         for (int k = 0; k < a.ts.n; k++) {
             const TermDev &T = a.ts.t[k];
             const TileBlocks b = sTB[k];
-            if (!valid) continue;
             float acc[MP];
 #pragma unroll
             for (int m = 0; m < MP; m++) acc[m] = 0.f;
@@ -294,16 +390,15 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
             const float *vps = reinterpret_cast<const float *>(smem + T.sm_vp);
             const bool rows_smem = T.staged && b.vp_staged;
             const float alpha = T.alpha;
-            const bool seq = T.seq;
             for (int r = 0; r <= T.d; r++) {
                 const int loc = locs[r * SPLAT_TILE + li];
                 const float bw = ws[r * SPLAT_TILE + li];
                 float v[MP];
                 if (rows_smem)
-                    load_row_smem<MP>(vps + loc * MP, v);
+                    load_row_s<MP>(vps + loc * MP, v);
                 else
                     load_row<MP>(T.pv + (size_t)(b.pb + loc) * MP, v);
-                if (seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
+                if (T.seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
 #pragma unroll
                     for (int m = 0; m < MP; m++) acc[m] = fmaf(fmul(bw, v[m]), alpha, acc[m]);
                 } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
@@ -319,12 +414,11 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
             }
             // with given marginals this is the pairwise part of klDivergence
             // (densecrf.cpp:229-233): sum Q * compat(K Q)
-            fold_compat<MP>(T, acc, x, M, given, kl);
+            fold_compat<MP>(T, T.sm_cmp >= 0 ? reinterpret_cast<const float *>(smem + T.sm_cmp) : nullptr, acc, x, M,
+                            given, kl);
         }
     }
-
-    // ---- 5. softmax and outputs
-    if (valid && !given) {
+    if (valid && !given) {  // softmax (densecrf.cpp:98-106)
         float mx = x[0];
 #pragma unroll
         for (int m = 1; m < MP; m++)
@@ -344,19 +438,19 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
     if (valid) {
         if (mode & PP_KL) {
             // entropy and unary parts (densecrf.cpp:216-226); log() there is the double overload
+            float u[MP];
+#pragma unroll
+            for (int m = 0; m < MP; m++) u[m] = 0.f;
+            if (a.U) load_row<MP>(a.U + s * MP, u);
 #pragma unroll
             for (int m = 0; m < MP; m++)
                 if (m < M) {
                     kl += (double)q[m] * log((double)fmaxf(q[m], 1e-20f));
-                    if (a.U) kl += (double)fmul(a.U[(size_t)m * ns + s], q[m]);
+                    kl += (double)fmul(u[m], q[m]);
                 }
         }
-        if (mode & PP_WRITE_Q) {
-#pragma unroll
-            for (int m = 0; m < MP; m++)
-                if (m < M) a.Qout[(size_t)m * ns + s] = q[m];
-        }
-        if (mode & PP_MAP) {
+        if (mode & PP_WRITE_Q) store_row<MP>(a.Qout + s * MP, q);
+        if (mode & PP_MAP) {  // first maximum (densecrf.cpp:132-137)
             int best = 0;
             float bv = q[0];
 #pragma unroll
@@ -371,7 +465,7 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
     if (mode & PP_KL) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) kl += __shfl_down_sync(0xffffffffu, kl, o);
-        if ((li & 31) == 0) sKL[li >> 5] = kl;
+        if (lane == 0) sKL[warp] = kl;
         __syncthreads();
         if (li == 0) {
             double ssum = 0.0;
@@ -380,15 +474,15 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
         }
     }
 
-    // ---- 6. splat the tile's q into each term's partials (every thread takes part)
-    // Each task sums at most SPLAT_TASK members of one partial (fixed order);
-    // a partial made of several tasks adds the task sums in task order.
+    // ---- 4. splat the tile's q into each term's partials.  Each task sums at
+    // most SPLAT_TASK members of one partial in member order; a partial made of
+    // several tasks adds the task sums in task order.  A group of lanes takes
+    // one task at a time, each lane its own labels.
     if (mode & PP_SPLAT) {
         float *sQ = reinterpret_cast<float *>(smem + a.sm_q);
         float *sRes = reinterpret_cast<float *>(smem + a.sm_res);
-        __syncthreads();  // the slice phase is done with the regions sQ aliases
-#pragma unroll
-        for (int m = 0; m < MP; m++) sQ[li * MP + m] = q[m];
+        __syncthreads();  // the message phase is done with the regions sQ aliases
+        store_row<MP>(sQ + li * MP, q);
         __syncthreads();
         for (int k = 0; k < a.ts.n; k++) {
             // the normalisation before the filter (pairwise.cpp:65-66) is folded into
@@ -400,49 +494,43 @@ __global__ void __launch_bounds__(SPLAT_TILE, (MP <= 20 ? 3 : 2)) pointpass_kern
                                              : T.task + b.tb;
             const uint16_t *mpt = T.staged ? reinterpret_cast<const uint16_t *>(smem + T.sm_mpt) : T.mem_pt + tbm;
             const float *mw = T.staged ? reinterpret_cast<const float *>(smem + T.sm_mw) : T.mem_w + tbm;
-            for (int j = li; j < b.nt; j += SPLAT_TILE) {
-                const uint32_t tk = tasks[j];
-                const int pl = (int)(tk >> 19), e0 = (int)((tk >> 6) & 0x1FFFu), len = (int)(tk & 63u);
-                float acc[MP];
+            if (gactive) {
+                for (int j = gid; j < b.nt; j += NG) {
+                    const uint32_t tk = tasks[j];
+                    const int pl = (int)(tk >> 19), e0 = (int)((tk >> 6) & 0x1FFFu), len = (int)(tk & 63u);
+                    float acc[VW];
 #pragma unroll
-                for (int m = 0; m < MP; m++) acc[m] = 0.f;
-                for (int e = e0; e < e0 + len; e++) {
-                    const float w = mw[e];
-                    float v[MP];
-                    load_row_smem<MP>(sQ + mpt[e] * MP, v);
+                    for (int e = 0; e < VW; e++) acc[e] = 0.f;
+                    for (int e = e0; e < e0 + len; e++) {
+                        const float w = mw[e];
+                        float v[VW];
+                        vload<VW>(sQ + mpt[e] * MP + m0, v);
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fmaf(w, v[m], acc[m]);
-                }
-                const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
-                const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
-                float *dst = (first && last) ? T.pv + (size_t)(b.pb + pl) * MP : sRes + (size_t)j * MP;
-                if constexpr (MP % 4 == 0) {
-#pragma unroll
-                    for (int c = 0; c < MP / 4; c++)
-                        reinterpret_cast<float4 *>(dst)[c] =
-                            make_float4(acc[4 * c], acc[4 * c + 1], acc[4 * c + 2], acc[4 * c + 3]);
-                } else {
-#pragma unroll
-                    for (int m = 0; m < MP; m++) dst[m] = acc[m];
+                        for (int f = 0; f < VW; f++) acc[f] = fmaf(w, v[f], acc[f]);
+                    }
+                    const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
+                    const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
+                    float *dst = (first && last) ? T.pv + (size_t)(b.pb + pl) * MP : sRes + (size_t)j * MP;
+                    vstore<VW>(dst + m0, acc);
                 }
             }
             __syncthreads();
-            for (int j = li; j < b.nt; j += SPLAT_TILE) {
-                const int pl = (int)(tasks[j] >> 19);
-                const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
-                const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
-                if (!first || last) continue;
-                float acc[MP];
-                load_row_smem<MP>(sRes + (size_t)j * MP, acc);
-                for (int jj = j + 1; jj < b.nt && (int)(tasks[jj] >> 19) == pl; jj++) {
-                    float v[MP];
-                    load_row_smem<MP>(sRes + (size_t)jj * MP, v);
+            if (gactive) {
+                for (int j = gid; j < b.nt; j += NG) {
+                    const int pl = (int)(tasks[j] >> 19);
+                    const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
+                    const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
+                    if (!first || last) continue;
+                    float acc[VW];
+                    vload<VW>(sRes + (size_t)j * MP + m0, acc);
+                    for (int jj = j + 1; jj < b.nt && (int)(tasks[jj] >> 19) == pl; jj++) {
+                        float v[VW];
+                        vload<VW>(sRes + (size_t)jj * MP + m0, v);
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], v[m]);
+                        for (int f = 0; f < VW; f++) acc[f] = fadd(acc[f], v[f]);
+                    }
+                    vstore<VW>(T.pv + (size_t)(b.pb + pl) * MP + m0, acc);
                 }
-                float *dst = T.pv + (size_t)(b.pb + pl) * MP;
-#pragma unroll
-                for (int m = 0; m < MP; m++) dst[m] = acc[m];
             }
             __syncthreads();
         }
@@ -456,7 +544,7 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
     const size_t s = (size_t)blockIdx.x * SPLAT_TILE + threadIdx.x;
     const int i = a.slot_pt[s];
     if (i < 0) return;
-    const int N = a.N, M = a.M, ns = a.nslots;
+    const int N = a.N, M = a.M;
     if (a.mode & PP_NORM) {
         // value size 1, seqCompute slice: out += (w * v) * alpha (permutohedral.cpp:513-521)
         for (int k = 0; k < a.ts.n; k++) {
@@ -497,14 +585,15 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
             for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
         }
     }
+    float *dst = a.Qout + s * MP;
 #pragma unroll
-    for (int m = 0; m < MP; m++)
-        if (m < M) a.Qout[(size_t)m * ns + s] = acc[m];
+    for (int m = 0; m < MP; m++) dst[m] = m < M ? acc[m] : 0.f;
 }
 
 template <int MP>
 __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ ReduceArgs a) {
     constexpr int G = Grp<MP>::G, CH = Grp<MP>::CH;
+    pdl_trigger();
     const long long gidx = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
     const int lgi = threadIdx.x % G;
     if (gidx >= a.begin[a.n]) return;
@@ -519,6 +608,7 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
     // the group's lanes fetch G partial indices at a time; the rows are then
     // read back to back (independent loads), added in list order
     const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
+    pdl_wait();  // the partials come from the previous kernel
     for (int b = s0; b < s1; b += G) {
         const int mine = (b + lgi < s1) ? T.red_list[b + lgi] : 0;
         const int cnt = min(G, s1 - b);
@@ -545,6 +635,7 @@ template <int MP, bool SEQ>
 __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurArgs a) {
     constexpr int VEC = (MP % 4 == 0) ? 4 : (MP % 2 == 0) ? 2 : 1;
     constexpr int NV = MP / VEC;
+    pdl_trigger();
     const long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= a.begin[a.n]) return;
     int k = 0;
@@ -555,6 +646,7 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
     const int c = (int)(local - (long long)v * NV);
     const int2 nb = __ldg(T.nbr + (size_t)T.axis * T.L + v);
     const size_t o0 = (size_t)(v + 1) * MP + c * VEC, o1 = (size_t)nb.x * MP + c * VEC, o2 = (size_t)nb.y * MP + c * VEC;
+    pdl_wait();  // the values come from the previous kernel
     float x0[VEC], x1[VEC], x2[VEC], y[VEC];
     if constexpr (VEC == 4) {
         float4 p = *reinterpret_cast<const float4 *>(T.Vin + o0), q1 = *reinterpret_cast<const float4 *>(T.Vin + o1),
@@ -625,8 +717,9 @@ __device__ __forceinline__ size_t user_offset(int point_major, int M, int N, con
     return (size_t)s0 * M + (size_t)m * nb + (p - s0);
 }
 
-// out[m][slot] = in(m, slot_pt[slot]) or 0
-__global__ void to_slots_kernel(const float *__restrict__ in, int point_major, int M, int N,
+// out[slot][m] = in(m, slot_pt[slot]) for m < M; 0 for padding labels m < ld
+// and for empty slots
+__global__ void to_slots_kernel(const float *__restrict__ in, int point_major, int M, int ld, int N,
                                 const int *__restrict__ seg, int nseg, const int *__restrict__ slot_pt, int nslots,
                                 float *__restrict__ out) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -637,19 +730,20 @@ __global__ void to_slots_kernel(const float *__restrict__ in, int point_major, i
         o0 = user_offset(point_major, M, N, seg, nseg, pt, 0);
         step = M > 1 ? user_offset(point_major, M, N, seg, nseg, pt, 1) - o0 : 0;
     }
-    for (int m = 0; m < M; m++) out[(size_t)m * nslots + s] = pt >= 0 ? in[o0 + m * step] : 0.f;
+    float *dst = out + s * ld;
+    for (int m = 0; m < ld; m++) dst[m] = (pt >= 0 && m < M) ? in[o0 + m * step] : 0.f;
 }
 
-// out(m, pt) = in[m][pt_slot[pt]]
-__global__ void from_slots_kernel(const float *__restrict__ in, int M, int N, const int *__restrict__ seg, int nseg,
-                                  int nslots, const int *__restrict__ pt_slot, int point_major,
+// out(m, pt) = in[pt_slot[pt]][m]
+__global__ void from_slots_kernel(const float *__restrict__ in, int M, int ld, int N, const int *__restrict__ seg,
+                                  int nseg, const int *__restrict__ pt_slot, int point_major,
                                   float *__restrict__ out) {
     const int pt = blockIdx.x * blockDim.x + threadIdx.x;
     if (pt >= N) return;
-    const size_t s = (size_t)pt_slot[pt];
+    const float *src = in + (size_t)pt_slot[pt] * ld;
     const size_t o0 = user_offset(point_major, M, N, seg, nseg, pt, 0);
     const size_t step = M > 1 ? user_offset(point_major, M, N, seg, nseg, pt, 1) - o0 : 0;
-    for (int m = 0; m < M; m++) out[o0 + m * step] = in[(size_t)m * nslots + s];
+    for (int m = 0; m < M; m++) out[o0 + m * step] = src[m];
 }
 
 // DenseCRF2D features (densecrf.cpp:61-81) of every image of the handle:
@@ -706,7 +800,7 @@ static cudaError_t pp_launch(const PPArgs &a, cudaStream_t s) {
     if (a.mode & (PP_NORM | PP_FILTER)) {
         DCRF_LAUNCH(slice_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
     } else {
-        DCRF_LAUNCH(pointpass_kernel<MP><<<a.ntiles, SPLAT_TILE, a.smem_bytes, s>>>(a));
+        return launch_pdl(pointpass_kernel<MP>, dim3(a.ntiles), dim3(SPLAT_TILE), a.smem_bytes, s, a);
     }
     return cudaGetLastError();
 }
@@ -748,7 +842,7 @@ cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s) {
 template <int MP>
 static cudaError_t red_launch(const ReduceArgs &a, cudaStream_t s) {
     long long threads = a.begin[a.n] * Grp<MP>::G;
-    if (threads > 0) DCRF_LAUNCH(reduce_kernel<MP><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a));
+    if (threads > 0) return launch_pdl(reduce_kernel<MP>, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, s, a);
     return cudaGetLastError();
 }
 
@@ -771,7 +865,7 @@ cudaError_t launch_reduce(const ReduceArgs &a, int MP, cudaStream_t s) {
 template <int MP, bool SEQ>
 static cudaError_t blur_launch(const BlurArgs &a, cudaStream_t s) {
     long long threads = a.begin[a.n];
-    if (threads > 0) DCRF_LAUNCH(blur_kernel<MP, SEQ><<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(a));
+    if (threads > 0) return launch_pdl(blur_kernel<MP, SEQ>, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, s, a);
     return cudaGetLastError();
 }
 
@@ -787,19 +881,19 @@ cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s) {
 #undef DCRF_BL
 }
 
-cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *seg, int nseg,
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,
                             const int *slot_pt, int nslots, float *out, cudaStream_t s) {
     if (nslots > 0)
-        DCRF_LAUNCH(to_slots_kernel<<<(nslots + 255) / 256, 256, 0, s>>>(in, point_major, M, N, seg, nseg, slot_pt,
+        DCRF_LAUNCH(to_slots_kernel<<<(nslots + 255) / 256, 256, 0, s>>>(in, point_major, M, ld, N, seg, nseg, slot_pt,
                                                                          nslots, out));
     return cudaGetLastError();
 }
 
-cudaError_t launch_from_slots(const float *in, int M, int N, const int *seg, int nseg, int nslots,
-                              const int *pt_slot, int point_major, float *out, cudaStream_t s) {
+cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *pt_slot,
+                              int point_major, float *out, cudaStream_t s) {
     if (N > 0)
-        DCRF_LAUNCH(from_slots_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, N, seg, nseg, nslots, pt_slot,
-                                                                      point_major, out));
+        DCRF_LAUNCH(from_slots_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, ld, N, seg, nseg, pt_slot, point_major,
+                                                                      out));
     return cudaGetLastError();
 }
 

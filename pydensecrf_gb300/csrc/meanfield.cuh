@@ -22,9 +22,9 @@ struct PPArgs {
     int N, M, mode;
     int ntiles, nslots;
     const int *slot_pt;  // [nslots] point of each tile slot, -1 = empty
-    const float *U;      // [M][nslots] or nullptr (no unary: zero)
-    const float *Qin;    // [M][nslots]
-    float *Qout;         // [M][nslots]
+    const float *U;      // [nslots][MP] slot rows, or nullptr (no unary: zero)
+    const float *Qin;    // [nslots][MP]
+    float *Qout;         // [nslots][MP]
     int16_t *map_out;    // [N] (point order)
     double *kl_part;     // [ntiles]
     DevStatus *status;
@@ -71,12 +71,12 @@ cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s);
 
 // Layout conversions between user layouts (point-major [N][M], or label-major:
 // per image an M x N_b block, images one after another -- [M][N] for one image)
-// and the slot-major [M][nslots] device layout.  seg[0..nseg] are the images'
-// point offsets on the device.
-cudaError_t launch_to_slots(const float *in, int point_major, int M, int N, const int *seg, int nseg,
+// and the device slot rows [nslots][ld] (ld >= M; padding labels and empty
+// slots hold 0).  seg[0..nseg] are the images' point offsets on the device.
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,
                             const int *slot_pt, int nslots, float *out, cudaStream_t s);
-cudaError_t launch_from_slots(const float *in, int M, int N, const int *seg, int nseg, int nslots,
-                              const int *pt_slot, int point_major, float *out, cudaStream_t s);
+cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *pt_slot,
+                              int point_major, float *out, cudaStream_t s);
 // 2D features of DenseCRF2D (densecrf.cpp:61-81) of every image into [d][N]
 cudaError_t launch_features_2d(int N, const int *seg, const int *imgW, int nseg, float sx, float sy,
                                const uint8_t *rgb, float sr, float sg, float sb, float *feat, cudaStream_t s);
