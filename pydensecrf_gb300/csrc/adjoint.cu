@@ -13,9 +13,48 @@ namespace dcrf {
 // count); labels m >= M and empty slots are written as 0.
 
 // b = Q * sum(x .* Q) - x .* Q  per point: the softmax adjoint with the
-// reference's sign (sumAndNormalize, densecrf.cpp:107-114, applied to x .* Q).
-__global__ void softmax_adjoint_kernel(const float *__restrict__ Q, const float *__restrict__ x, float *__restrict__ b,
-                                       int M, int ld, int ns, const int *__restrict__ slot_pt) {
+// reference's sign (sumAndNormalize, densecrf.cpp:107-114, applied to x .* Q);
+// with du, also du += b.  Rows are read and written as float4 vectors.
+template <int MP>
+__global__ void __launch_bounds__(256) softmax_adjoint_kernel(const float *__restrict__ Q, const float *__restrict__ x,
+                                                              float *__restrict__ b, float *__restrict__ du, int M,
+                                                              int ns, const int *__restrict__ slot_pt) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)ns) return;
+    float q[MP], xx[MP], o[MP];
+    const bool ok = slot_pt[s] >= 0;
+#pragma unroll
+    for (int c = 0; c < MP / 4; c++) {
+        float4 a4 = make_float4(0.f, 0.f, 0.f, 0.f), b4 = a4;
+        if (ok) {
+            a4 = reinterpret_cast<const float4 *>(Q + s * MP)[c];
+            b4 = reinterpret_cast<const float4 *>(x + s * MP)[c];
+        }
+        q[4 * c] = a4.x, q[4 * c + 1] = a4.y, q[4 * c + 2] = a4.z, q[4 * c + 3] = a4.w;
+        xx[4 * c] = b4.x, xx[4 * c + 1] = b4.y, xx[4 * c + 2] = b4.z, xx[4 * c + 3] = b4.w;
+    }
+    float dot = 0.f;
+#pragma unroll
+    for (int m = 0; m < MP; m++)
+        if (m < M) dot = fmaf(xx[m], q[m], dot);
+#pragma unroll
+    for (int m = 0; m < MP; m++) o[m] = (ok && m < M) ? fmaf(q[m], dot, -xx[m] * q[m]) : 0.f;
+#pragma unroll
+    for (int c = 0; c < MP / 4; c++) {
+        const float4 v = make_float4(o[4 * c], o[4 * c + 1], o[4 * c + 2], o[4 * c + 3]);
+        reinterpret_cast<float4 *>(b + s * MP)[c] = v;
+        if (du) {
+            float4 u = reinterpret_cast<const float4 *>(du + s * MP)[c];
+            u.x += v.x, u.y += v.y, u.z += v.z, u.w += v.w;
+            reinterpret_cast<float4 *>(du + s * MP)[c] = u;
+        }
+    }
+}
+
+// The same for M <= 2 (rows of M floats).
+__global__ void softmax_adjoint_small_kernel(const float *__restrict__ Q, const float *__restrict__ x,
+                                             float *__restrict__ b, float *__restrict__ du, int M, int ld, int ns,
+                                             const int *__restrict__ slot_pt) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
     const float *q = Q + s * ld, *xx = x + s * ld;
@@ -26,61 +65,115 @@ __global__ void softmax_adjoint_kernel(const float *__restrict__ Q, const float 
     }
     float dot = 0.f;
     for (int m = 0; m < M; m++) dot = fmaf(xx[m], q[m], dot);
-    for (int m = 0; m < ld; m++) o[m] = m < M ? fmaf(q[m], dot, -xx[m] * q[m]) : 0.f;
+    for (int m = 0; m < ld; m++) {
+        o[m] = m < M ? fmaf(q[m], dot, -xx[m] * q[m]) : 0.f;
+        if (du) du[s * ld + m] += o[m];
+    }
 }
 
-// y (+)= C x, or C^T x, per point (labelcompatibility.cpp:46-48,66-68,82-87)
-__global__ void compat_kernel(const float *__restrict__ x, float *__restrict__ y, int M, int ld, int ns, int kind,
-                              float potts_w, const float *__restrict__ C, int transpose, int accumulate) {
+// y (+)= C x, or C^T x, per point (labelcompatibility.cpp:46-48,66-68,82-87).
+// One thread per row; the row is read and written as float4 vectors and the
+// Matrix is staged in shared memory (transposed when applying C).
+template <int MP>
+__global__ void __launch_bounds__(256) compat_kernel(const float *__restrict__ x, float *__restrict__ y, int M, int ns,
+                                                     int kind, float potts_w, const float *__restrict__ C,
+                                                     int transpose, int accumulate) {
+    __shared__ float sC[MP * MP];  // sC[k][m]: weight of x_k in y_m
+    if (kind == DCRF_COMPAT_MATRIX) {
+        for (int e = threadIdx.x; e < MP * MP; e += blockDim.x) {
+            const int k = e / MP, m = e - k * MP;
+            sC[e] = (k < M && m < M) ? (transpose ? C[k * M + m] : C[m * M + k]) : 0.f;
+        }
+        __syncthreads();
+    }
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)ns) return;
+    float xv[MP], v[MP];
+#pragma unroll
+    for (int c = 0; c < MP / 4; c++) {
+        const float4 q = reinterpret_cast<const float4 *>(x + s * MP)[c];
+        xv[4 * c] = q.x, xv[4 * c + 1] = q.y, xv[4 * c + 2] = q.z, xv[4 * c + 3] = q.w;
+    }
+    if (kind == DCRF_COMPAT_POTTS) {
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = m < M ? -potts_w * xv[m] : 0.f;
+    } else if (kind == DCRF_COMPAT_DIAGONAL) {
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = m < M ? __ldg(C + m) * xv[m] : 0.f;
+    } else {
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = 0.f;
+#pragma unroll
+        for (int k = 0; k < MP; k++) {
+            if (k >= M) continue;
+#pragma unroll
+            for (int m = 0; m < MP; m++) v[m] = fmaf(sC[k * MP + m], xv[k], v[m]);
+        }
+    }
+    float4 *yr = reinterpret_cast<float4 *>(y + s * MP);
+#pragma unroll
+    for (int c = 0; c < MP / 4; c++) {
+        float4 o = make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
+        if (accumulate) {
+            const float4 p = yr[c];
+            o.x += p.x, o.y += p.y, o.z += p.z, o.w += p.w;
+        }
+        yr[c] = o;
+    }
+}
+
+// Labels M <= 2 (rows of 1 or 2 floats): the scalar form of the same.
+__global__ void compat_small_kernel(const float *__restrict__ x, float *__restrict__ y, int M, int ld, int ns, int kind,
+                                    float potts_w, const float *__restrict__ C, int transpose, int accumulate) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
     const float *xx = x + s * ld;
     float *yy = y + s * ld;
-    for (int m = 0; m < ld; m++) {
-        float v = 0.f;
-        if (m < M) {
-            if (kind == DCRF_COMPAT_POTTS) {
-                v = -potts_w * xx[m];
-            } else if (kind == DCRF_COMPAT_DIAGONAL) {
-                v = C[m] * xx[m];
-            } else {
-                for (int k = 0; k < M; k++) v = fmaf(transpose ? C[k * M + m] : C[m * M + k], xx[k], v);
-            }
-        }
-        if (accumulate)
-            yy[m] += v;
+    float v[2] = {0.f, 0.f};
+    for (int m = 0; m < M; m++) {
+        if (kind == DCRF_COMPAT_POTTS)
+            v[m] = -potts_w * xx[m];
+        else if (kind == DCRF_COMPAT_DIAGONAL)
+            v[m] = C[m] * xx[m];
         else
-            yy[m] = v;
+            for (int k = 0; k < M; k++) v[m] = fmaf(transpose ? C[k * M + m] : C[m * M + k], xx[k], v[m]);
     }
+    for (int m = 0; m < ld; m++) yy[m] = accumulate ? yy[m] + v[m] : v[m];
 }
 
-// y = x .* norm^pw per point (pw in 1..3)
+// y = x .* norm^pw per point (pw in 1..3), one thread per float4 of a row (ld % 4 == 0)
+// or per row (ld < 4)
 __global__ void scale_norm_kernel(const float *__restrict__ x, float *__restrict__ y, const float *__restrict__ norm,
                                   int ld, int ns, int pw) {
-    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= (size_t)ns) return;
+    const int nv = ld % 4 == 0 ? ld / 4 : 1;
+    const size_t gi = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= (size_t)ns * nv) return;
+    const size_t s = gi / nv;
     const float n = norm[s];
     const float f = pw == 1 ? n : pw == 2 ? n * n : n * n * n;
-    for (int m = 0; m < ld; m++) y[s * ld + m] = x[s * ld + m] * f;
+    if (ld % 4 == 0) {
+        float4 q = reinterpret_cast<const float4 *>(x)[gi];
+        q.x *= f, q.y *= f, q.z *= f, q.w *= f;
+        reinterpret_cast<float4 *>(y)[gi] = q;
+    } else {
+        for (int m = 0; m < ld; m++) y[s * ld + m] = x[s * ld + m] * f;
+    }
 }
 
 // y = scale * (x1 .* x2 + x3 .* x4) .* norm^pw per point (x3/x4 may be null; norm null: pw ignored)
 __global__ void prod_kernel(const float *__restrict__ x1, const float *__restrict__ x2, const float *__restrict__ x3,
                             const float *__restrict__ x4, float scale, const float *__restrict__ norm, int pw,
                             float *__restrict__ y, int ld, int ns) {
-    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= (size_t)ns) return;
+    const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= (size_t)ns * ld) return;
     float f = scale;
     if (norm) {
-        const float n = norm[s];
+        const float n = norm[o / ld];
         f *= pw == 1 ? n : pw == 2 ? n * n : n * n * n;
     }
-    for (int m = 0; m < ld; m++) {
-        const size_t o = s * ld + m;
-        float v = x1[o] * x2[o];
-        if (x3) v = fmaf(x3[o], x4[o], v);
-        y[o] = v * f;
-    }
+    float v = x1[o] * x2[o];
+    if (x3) v = fmaf(x3[o], x4[o], v);
+    y[o] = v * f;
 }
 
 __global__ void add_kernel(const float *__restrict__ x, float *__restrict__ y, size_t n) {
@@ -95,41 +188,75 @@ __global__ void fill_kernel(float *__restrict__ y, float v, int M, int ld, int n
     for (int m = 0; m < ld; m++) y[s * ld + m] = m < M ? val : 0.f;
 }
 
-// Per-block partial sums of the label products over the occupied slots:
-//  mode 0 (per label):  part[blk][m]      = sum_s a[m][s] * b[m][s]
-//  mode 1 (outer):      part[blk][m*M+k]  = sum_s a[m][s] * b[k][s]
-// Padding slots (slot_pt < 0) hold no point and are left out whatever they contain.
+// out[s] = sum over labels of x (one value per slot)
+__global__ void row_sum_kernel(const float *__restrict__ x, float *__restrict__ out, int M, int ld, int ns) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)ns) return;
+    float t = 0.f;
+    for (int m = 0; m < M; m++) t = fadd(t, x[s * ld + m]);
+    out[s] = t;
+}
+
+// Per-block partial sums of the label products over the occupied slots, a
+// tall-skinny product of two [rows][ld] blocks staged in shared memory:
+//  mode 0 (per label):  part[blk][m]      = sum_s a[s][m] * b[s][m]
+//  mode 1 (outer):      part[blk][m*M+k]  = sum_s a[s][m] * b[s][k]
+// Each block takes LP_ROWS slots; each thread owns outputs threadIdx.x + 256 j
+// and accumulates them over the block's rows in slot order (float), the block
+// result is stored as double.  Padding slots (slot_pt < 0) are left out
+// whatever they contain.
+constexpr int LP_ROWS = 128;
+
 __global__ void __launch_bounds__(256) label_products_kernel(const float *__restrict__ a, const float *__restrict__ b,
                                                              int M, int ld, int ns, const int *__restrict__ slot_pt,
                                                              int mode, double *__restrict__ part) {
-    extern __shared__ double sred[];  // [8 warps][K]
+    extern __shared__ float sab[];  // [LP_ROWS][ld] of a, then of b
+    float *sa = sab, *sb = sab + LP_ROWS * ld;
     const int K = mode == 0 ? M : M * M;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool ok = s < (size_t)ns && slot_pt[s] >= 0;
-    for (int kk = 0; kk < K; kk++) {
-        const int m = mode == 0 ? kk : kk / M, k = mode == 0 ? kk : kk % M;
-        double v = ok ? (double)a[s * ld + m] * (double)b[s * ld + k] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) sred[warp * K + kk] = v;
+    const size_t r0 = (size_t)blockIdx.x * LP_ROWS;
+    for (int e = threadIdx.x; e < LP_ROWS * ld; e += blockDim.x) {
+        const int r = e / ld;
+        const size_t sl = r0 + r;
+        const bool ok = sl < (size_t)ns && slot_pt[sl] >= 0;
+        sa[e] = ok ? a[r0 * ld + e] : 0.f;
+        sb[e] = ok ? b[r0 * ld + e] : 0.f;
     }
     __syncthreads();
     for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); w++) t += sred[w * K + kk];
-        part[(size_t)blockIdx.x * K + kk] = t;
+        const int m = mode == 0 ? kk : kk / M, k = mode == 0 ? kk : kk % M;
+        float t = 0.f;
+        for (int r = 0; r < LP_ROWS; r++) t = fmaf(sa[r * ld + m], sb[r * ld + k], t);
+        part[(size_t)kk * gridDim.x + blockIdx.x] = (double)t;
     }
 }
 
-// out[k] = sum over blocks (in block order) of part[blk][k]
+// out[k] (+)= sum over blocks of part[k][blk] (output-major partials): one
+// warp per output, lanes striding over the blocks, then a fixed shuffle tree
 __global__ void sum_parts_kernel(const double *__restrict__ part, int nblk, int K, double *__restrict__ out,
                                  int accumulate) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    const int k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
     if (k >= K) return;
     double t = 0.0;
-    for (int b = 0; b < nblk; b++) t += part[(size_t)b * K + k];
-    out[k] = accumulate ? out[k] + t : t;
+    for (int b = lane; b < nblk; b += 32) t += part[(size_t)k * nblk + b];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) out[k] = accumulate ? out[k] + t : t;
+}
+
+// A row of MP floats from global memory (float4 loads when MP % 4 == 0).
+template <int MP>
+__device__ __forceinline__ void row_load(const float *__restrict__ p, float (&v)[MP]) {
+    if constexpr (MP % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < MP / 4; c++) {
+            const float4 q = __ldg(reinterpret_cast<const float4 *>(p) + c);
+            v[4 * c] = q.x, v[4 * c + 1] = q.y, v[4 * c + 2] = q.z, v[4 * c + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = __ldg(p + m);
+    }
 }
 
 // Feature gradient of the slice (the per-point part of Permutohedral::gradient,
@@ -145,16 +272,19 @@ __global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
     if (i < 0) return;
     const int d = a.d, N = a.N, M = a.M;
     float z[MP];
+    row_load<MP>(a.z + s * MP, z);
 #pragma unroll
-    for (int m = 0; m < MP; m++) z[m] = m < M ? a.z[s * MP + m] : 0.f;
+    for (int m = 0; m < MP; m++)
+        if (m >= M) z[m] = 0.f;
     float sm[MP];
 #pragma unroll
     for (int m = 0; m < MP; m++) sm[m] = 0.f;
     for (int j = 0; j <= d; j++) {
         const int r0 = d - (int)a.rank[(size_t)j * N + i];
         const int r1 = r0 + 1 > d ? 0 : r0 + 1;
-        const float *v0 = a.V + (size_t)(a.off[(size_t)r0 * N + i] + 1) * MP;
-        const float *v1 = a.V + (size_t)(a.off[(size_t)r1 * N + i] + 1) * MP;
+        float v0[MP], v1[MP];
+        row_load<MP>(a.V + (size_t)(a.off[(size_t)r0 * N + i] + 1) * MP, v0);
+        row_load<MP>(a.V + (size_t)(a.off[(size_t)r1 * N + i] + 1) * MP, v1);
         float grad = 0.f;
 #pragma unroll
         for (int m = 0; m < MP; m++) {
@@ -186,34 +316,63 @@ __global__ void __launch_bounds__(256) kernel_param_grad_kernel(const float *__r
     for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x / 32); w++) t += sred[w * K + kk];
-        part[(size_t)blockIdx.x * K + kk] = t;
+        part[(size_t)kk * gridDim.x + blockIdx.x] = t;
     }
 }
 
 // ---------------------------------------------------------------------------
 static unsigned blocks(size_t n) { return (unsigned)((n + 255) / 256); }
 
-cudaError_t launch_softmax_adjoint(const float *Q, const float *x, float *b, int M, int ns, const int *slot_pt,
-                                   cudaStream_t s) {
-    DCRF_LAUNCH(softmax_adjoint_kernel<<<blocks(ns), 256, 0, s>>>(Q, x, b, M, pad_labels(M), ns, slot_pt));
+cudaError_t launch_softmax_adjoint(const float *Q, const float *x, float *b, float *du, int M, int ns,
+                                   const int *slot_pt, cudaStream_t s) {
+    switch (pad_labels(M)) {
+#define DCRF_SA(X) \
+    case X: DCRF_LAUNCH(softmax_adjoint_kernel<X><<<blocks(ns), 256, 0, s>>>(Q, x, b, du, M, ns, slot_pt)); break;
+        DCRF_SA(4) DCRF_SA(8) DCRF_SA(12) DCRF_SA(16) DCRF_SA(20) DCRF_SA(24) DCRF_SA(28) DCRF_SA(32)
+#undef DCRF_SA
+        default:
+            DCRF_LAUNCH(softmax_adjoint_small_kernel<<<blocks(ns), 256, 0, s>>>(Q, x, b, du, M, pad_labels(M), ns,
+                                                                                slot_pt));
+    }
+    return cudaGetLastError();
+}
+
+template <int MP>
+static cudaError_t compat_launch(const float *x, float *y, int M, int ns, int kind, float potts_w, const float *C,
+                                 int transpose, int accumulate, cudaStream_t s) {
+    DCRF_LAUNCH(compat_kernel<MP><<<blocks(ns), 256, 0, s>>>(x, y, M, ns, kind, potts_w, C, transpose, accumulate));
     return cudaGetLastError();
 }
 
 cudaError_t launch_compat(const float *x, float *y, int M, int ns, int kind, float potts_w, const float *C,
                           int transpose, int accumulate, cudaStream_t s) {
-    DCRF_LAUNCH(compat_kernel<<<blocks(ns), 256, 0, s>>>(x, y, M, pad_labels(M), ns, kind, potts_w, C, transpose,
-                                                         accumulate));
-    return cudaGetLastError();
+    switch (pad_labels(M)) {
+        case 4: return compat_launch<4>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 8: return compat_launch<8>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 12: return compat_launch<12>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 16: return compat_launch<16>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 20: return compat_launch<20>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 24: return compat_launch<24>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 28: return compat_launch<28>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        case 32: return compat_launch<32>(x, y, M, ns, kind, potts_w, C, transpose, accumulate, s);
+        default:
+            DCRF_LAUNCH(compat_small_kernel<<<blocks(ns), 256, 0, s>>>(x, y, M, pad_labels(M), ns, kind, potts_w, C,
+                                                                       transpose, accumulate));
+            return cudaGetLastError();
+    }
 }
 
 cudaError_t launch_scale_norm(const float *x, float *y, const float *norm, int M, int ns, int pw, cudaStream_t s) {
-    DCRF_LAUNCH(scale_norm_kernel<<<blocks(ns), 256, 0, s>>>(x, y, norm, pad_labels(M), ns, pw));
+    const int ld = pad_labels(M);
+    const size_t n = (size_t)ns * (ld % 4 == 0 ? ld / 4 : 1);
+    DCRF_LAUNCH(scale_norm_kernel<<<blocks(n), 256, 0, s>>>(x, y, norm, ld, ns, pw));
     return cudaGetLastError();
 }
 
 cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const float *x4, float scale,
                         const float *norm, int pw, float *y, int M, int ns, cudaStream_t s) {
-    DCRF_LAUNCH(prod_kernel<<<blocks(ns), 256, 0, s>>>(x1, x2, x3, x4, scale, norm, pw, y, pad_labels(M), ns));
+    const int ld = pad_labels(M);
+    DCRF_LAUNCH(prod_kernel<<<blocks((size_t)ns * ld), 256, 0, s>>>(x1, x2, x3, x4, scale, norm, pw, y, ld, ns));
     return cudaGetLastError();
 }
 
@@ -227,21 +386,26 @@ cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cu
     return cudaGetLastError();
 }
 
-int label_products_blocks(int ns) { return (int)blocks(ns); }
+cudaError_t launch_row_sum(const float *x, float *out, int M, int ns, cudaStream_t s) {
+    DCRF_LAUNCH(row_sum_kernel<<<blocks(ns), 256, 0, s>>>(x, out, M, pad_labels(M), ns));
+    return cudaGetLastError();
+}
+
+int label_products_blocks(int ns) { return (ns + LP_ROWS - 1) / LP_ROWS; }
+
+static cudaError_t sum_parts(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s) {
+    DCRF_LAUNCH(sum_parts_kernel<<<(K + 7) / 8, 256, 0, s>>>(part, nblk, K, out, accumulate));
+    return cudaGetLastError();
+}
 
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
                                   double *part, double *out, int accumulate, cudaStream_t s) {
     const int K = mode == 0 ? M : M * M;
-    const unsigned nb = blocks(ns);
-    const size_t smem = 8 * (size_t)K * sizeof(double);  // up to 64 KB for 32 x 32 labels
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(label_products_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
-        if (e != cudaSuccess) return e;
-    }
-    DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, pad_labels(M), ns, slot_pt, mode, part));
-    DCRF_LAUNCH(sum_parts_kernel<<<blocks(K), 256, 0, s>>>(part, (int)nb, K, out, accumulate));
-    return cudaGetLastError();
+    const int ld = pad_labels(M);
+    const unsigned nb = (unsigned)label_products_blocks(ns);
+    const size_t smem = 2 * (size_t)LP_ROWS * ld * sizeof(float);  // at most 32 KB
+    DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, ld, ns, slot_pt, mode, part));
+    return sum_parts(part, (int)nb, K, out, accumulate, s);
 }
 
 template <int MP>
@@ -273,8 +437,7 @@ cudaError_t launch_kernel_param_grad(const float *f, const float *fg, int d, int
     const int K = full ? d * d : d;
     const unsigned nb = blocks(N);
     DCRF_LAUNCH(kernel_param_grad_kernel<<<nb, 256, 8 * K * sizeof(double), s>>>(f, fg, d, N, full, part));
-    DCRF_LAUNCH(sum_parts_kernel<<<blocks(K), 256, 0, s>>>(part, (int)nb, K, out, accumulate));
-    return cudaGetLastError();
+    return sum_parts(part, (int)nb, K, out, accumulate, s);
 }
 
 }  // namespace dcrf

@@ -18,8 +18,9 @@ struct SliceGradArgs {
     float *df;            // [N][d] accumulated feature gradient
 };
 
-cudaError_t launch_softmax_adjoint(const float *Q, const float *x, float *b, int M, int ns, const int *slot_pt,
-                                   cudaStream_t s);
+// b = softmax adjoint of x at Q (slot rows); du += b when du is not null
+cudaError_t launch_softmax_adjoint(const float *Q, const float *x, float *b, float *du, int M, int ns,
+                                   const int *slot_pt, cudaStream_t s);
 cudaError_t launch_compat(const float *x, float *y, int M, int ns, int kind, float potts_w, const float *C,
                           int transpose, int accumulate, cudaStream_t s);
 cudaError_t launch_scale_norm(const float *x, float *y, const float *norm, int M, int ns, int pw, cudaStream_t s);
@@ -27,6 +28,7 @@ cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const
                         const float *norm, int pw, float *y, int M, int ns, cudaStream_t s);
 cudaError_t launch_add(const float *x, float *y, size_t n, cudaStream_t s);
 cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cudaStream_t s);
+cudaError_t launch_row_sum(const float *x, float *out, int M, int ns, cudaStream_t s);
 int label_products_blocks(int ns);
 // mode 0: out[m] (+)= sum a[m].*b[m]; mode 1: out[m*M+k] (+)= sum a[m].*b[k]; part: [blocks][K] doubles
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,

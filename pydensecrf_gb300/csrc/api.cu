@@ -120,6 +120,10 @@ struct Term {
     float *compat = nullptr;  // device compat (Diagonal M / Matrix M*M symmetrised)
     float *mem_wn = nullptr;  // splat member weights times the members' norm (forward pre-normalisation)
     float *df = nullptr;      // [N][d] accumulated feature gradient (adjoint)
+    // adjoint work lattices, vertex order with a zero row 0: [L+1][MP] x 3, [L+1] x 3
+    float *bv[3] = {nullptr, nullptr, nullptr};
+    float *b1[3] = {nullptr, nullptr, nullptr};
+    bool r1_valid = false;  // b1[2] holds the reverse-blurred splat of ones
     std::vector<float> compat_h;
     std::vector<float> params;  // kernel parameters (DIAG d, FULL d*d row-major)
     bool params_set = false;    // the lattice uses params (else the features as given)
@@ -157,9 +161,15 @@ struct dcrf_crf {
     // the per-iteration checkpoints of the last dcrf_inference_checkpointed
     unsigned long long version = 0, ckpt_version = ~0ull;
     int ckpt_T = -1;
-    float *ckpt = nullptr;  // [(T+1)][M][nslots]
+    float *ckpt = nullptr;  // [(T+1)][nslots][MP]
     size_t ckpt_cap = 0;
-    float *bw[14] = {};     // adjoint work buffers, [M][nslots] each
+    // per iteration t < T and term k: the forward's splat S and blurred lattice
+    // B of Q_t, each [L_k+1][MP], at ckv + t * ckv_iter + ckv_off[k] (+ (L_k+1)*MP for B)
+    float *ckv = nullptr;
+    size_t ckv_cap = 0, ckv_iter = 0;
+    std::vector<size_t> ckv_off, ckv_layout;
+    float *bw[14] = {};     // adjoint work buffers, [nslots][MP] each
+    float *bw1[2] = {};     // adjoint work buffers, [nslots] each
     double *dpart = nullptr, *dacc = nullptr;
     size_t dpart_cap = 0, dacc_cap = 0;
     // CUDA graph of the last inference launch sequence (re-used through
@@ -548,7 +558,8 @@ std::vector<int> all_terms(dcrf_crf *h) {
 // partial_order: the last pass writes the result in tile-partial order (pv,
 // input of the mean-field point pass) instead of vertex order (V, input of the
 // point-order slice).
-int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, bool value1, bool partial_order) {
+int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, bool value1, bool partial_order,
+                 float *const *S_out = nullptr, float *const *B_out = nullptr) {
     int MP = value1 ? 1 : h->MP;
     bool seq = value1 || h->M <= 2;
     ReduceArgs ra{};
@@ -557,7 +568,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
     int maxd = 0;
     for (size_t k = 0; k < which.size(); k++) {
         Term &T = h->terms[which[k]];
-        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.pv, T.V[0], T.lat.L};
+        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.pv, S_out ? S_out[k] : T.V[0], T.lat.L};
         ra.begin[k + 1] = ra.begin[k] + T.lat.L;
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
@@ -577,8 +588,8 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
             if (pass > T.d) continue;
             const bool last = pass == T.d;
             BlurArgs::T &bt = ba.t[ba.n];
-            bt.Vin = T.V[pass & 1];
-            bt.Vout = (last && partial_order) ? nullptr : T.V[(pass + 1) & 1];
+            bt.Vin = (pass == 0 && S_out) ? S_out[k] : T.V[pass & 1];
+            bt.Vout = (last && B_out) ? B_out[k] : (last && partial_order) ? nullptr : T.V[(pass + 1) & 1];
             bt.nbr = T.lat.nbr;
             bt.L = T.lat.L;
             bt.axis = transpose ? T.d - pass : pass;  // reverse blur order for the transpose (permutohedral.cpp:556)
@@ -621,6 +632,12 @@ void free_term_lattice(dcrf_crf *h, Term &T) {
     dev_free_async(T.mem_wn, h->stream);
     dev_free_async(T.df, h->stream);
     T.norm = T.V[0] = T.V[1] = T.pv = T.mem_wn = T.df = nullptr;
+    for (int j = 0; j < 3; j++) {
+        dev_free_async(T.bv[j], h->stream);
+        dev_free_async(T.b1[j], h->stream);
+        T.bv[j] = T.b1[j] = nullptr;
+    }
+    T.r1_valid = false;
     lattice_free(&T.lat, h->stream);
 }
 
@@ -792,7 +809,16 @@ int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
         CU(pp(h, a, h->MP));
     }
     for (int it = 1; it <= T; it++) {
-        if ((rc = filter_phase(h, w, false, false, true))) return rc;
+        if (ckpt && h->ckv) {  // keep S and B of Q_{it-1} for the adjoint
+            float *S[DCRF_MAX_TERMS], *B[DCRF_MAX_TERMS];
+            for (size_t k = 0; k < w.size(); k++) {
+                S[k] = h->ckv + (size_t)(it - 1) * h->ckv_iter + h->ckv_off[w[k]];
+                B[k] = S[k] + ((size_t)h->terms[w[k]].lat.L + 1) * h->MP;
+            }
+            if ((rc = filter_phase(h, w, false, false, true, S, B))) return rc;
+        } else if ((rc = filter_phase(h, w, false, false, true))) {
+            return rc;
+        }
         int mode = PP_MSG | (it < T ? PP_SPLAT : final_mode) | (ckpt ? PP_WRITE_Q : 0);
         PPArgs a = pp_args(h, mode, w, false, false);
         if (ckpt) a.Qout = ckpt + it * qsz;
@@ -850,96 +876,107 @@ bool fwd_post(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.n
 bool tr_pre(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_AFTER; }
 bool tr_post(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_BEFORE; }
 
-// Splat of in_s (plain or norm-folded member weights) and the d+1 blur passes
-// (reverse order for the transpose); the result is the term's vertex-order V.
-int splat_blur(dcrf_crf *h, int k, const float *in_s, bool transpose, bool fold_norm) {
-    Term &T = h->terms[k];
-    std::vector<int> one{k};
-    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, transpose, false);
-    a.ts.t[0].mem_w = fold_norm ? T.mem_wn : T.lat.mem_w;
-    a.Qin = in_s;
-    CU(pp(h, a, h->MP));
-    return filter_phase(h, one, transpose, false, false);
-}
-
-// out_s = K in_s (raw lattice filter; the transpose uses the reverse blur),
-// optionally with the term's normalisation on either side.
-int filter_into(dcrf_crf *h, int k, const float *in_s, float *out_s, bool transpose, bool pre, bool post) {
-    Term &T = h->terms[k];
-    int rc = splat_blur(h, k, in_s, transpose, pre);
-    if (rc) return rc;
-    std::vector<int> one{k};
-    PPArgs f = pp_args(h, PP_FILTER, one, transpose, false);
-    f.Qout = out_s;
-    CU(pp(h, f, h->MP));
-    if (post) CU(launch_scale_norm(out_s, out_s, T.norm, h->M, h->nslots, 1, h->stream));
+// Adjoint work lattices of a term, allocated on first use; row 0 of each is
+// the zero sentinel the blur reads for missing neighbours.
+int ensure_adjoint_bufs(dcrf_crf *h, Term &T) {
+    const size_t rows = (size_t)T.lat.L + 1;
+    int rc;
+    for (int j = 0; j < 3; j++) {
+        if (!T.bv[j]) {
+            if ((rc = dev_alloc_async(&T.bv[j], rows * h->MP, h->stream))) return rc;
+            CU(cudaMemsetAsync(T.bv[j], 0, sizeof(float) * rows * h->MP, h->stream));
+        }
+        if (!T.b1[j]) {
+            if ((rc = dev_alloc_async(&T.b1[j], rows, h->stream))) return rc;
+            CU(cudaMemsetAsync(T.b1[j], 0, sizeof(float) * rows, h->stream));
+        }
+    }
     return DCRF_OK;
 }
 
-// T.df += sign * d/dfeatures (x^T K y) (Permutohedral::gradient, permutohedral.cpp:612-695):
-// direction 0 slices the forward-blurred splat of x against y, direction 1 the
-// reverse-blurred splat of y against x.
-int lattice_grad(dcrf_crf *h, int k, const float *x, const float *y, float sign) {
+// S (vertex rows) = splat of the slot rows x with the plain barycentric weights
+// (the splat of Permutohedral::compute, permutohedral.cpp:545-553).
+int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1) {
+    Term &T = h->terms[k];
+    const int MP = value1 ? 1 : h->MP;
+    std::vector<int> one{k};
+    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, false, value1);
+    a.ts.t[0].pre_norm = 0;
+    a.ts.t[0].mem_w = T.lat.mem_w;
+    a.Qin = x;
+    CU(pp(h, a, MP));
+    ReduceArgs ra{};
+    ra.n = 1;
+    ra.begin[0] = 0;
+    ra.begin[1] = T.lat.L;
+    ra.t[0] = {T.lat.red_beg, T.lat.red_list, T.pv, S, T.lat.L};
+    ProfScope ps(h, DCRF_KCLASS_REDUCE);
+    CU(launch_reduce(ra, MP, h->stream));
+    return DCRF_OK;
+}
+
+// Out = the d+1 blur passes of S, axes 0..d or d..0 for the transpose
+// (permutohedral.cpp:556); S is kept, the term's V buffers are the ping-pong.
+int blur_into(dcrf_crf *h, int k, const float *S, float *Out, bool reverse, bool value1) {
+    Term &T = h->terms[k];
+    const int MP = value1 ? 1 : h->MP;
+    const bool seq = value1 || h->M <= 2 || T.variant == DCRF_VARIANT_SCALAR;
+    const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
+    for (int pass = 0; pass <= T.d; pass++) {
+        BlurArgs ba{};
+        ba.n = 1;
+        ba.begin[0] = 0;
+        ba.begin[1] = (long long)T.lat.L * NV;
+        ba.t[0].Vin = pass == 0 ? S : T.V[pass & 1];
+        ba.t[0].Vout = pass == T.d ? Out : T.V[(pass + 1) & 1];
+        ba.t[0].nbr = T.lat.nbr;
+        ba.t[0].L = T.lat.L;
+        ba.t[0].axis = reverse ? T.d - pass : pass;
+        ba.t[0].pv = nullptr;
+        ProfScope ps(h, DCRF_KCLASS_BLUR);
+        CU(launch_blur(ba, MP, seq, h->stream));
+    }
+    if (value1) return zero_sentinels(h, T);
+    return DCRF_OK;
+}
+
+// out (slot rows) = slice of the vertex rows V (permutohedral.cpp:574-584);
+// with post, also Fpost = [norm .*] out (norm when post_norm) and
+// Gacc += compat(Fpost) (either may be null).
+int slice_from(dcrf_crf *h, int k, const float *V, float *out, bool value1, bool post_norm = false,
+               float *Fpost = nullptr, float *Gacc = nullptr) {
+    std::vector<int> one{k};
+    PPArgs f = pp_args(h, PP_FILTER, one, false, value1);
+    f.ts.t[0].V = V;
+    f.ts.t[0].post_norm = post_norm ? 1 : 0;
+    f.Qout = out;
+    f.Fpost = Fpost;
+    f.Gacc = Gacc;
+    CU(pp(h, f, value1 ? 1 : h->MP));
+    return DCRF_OK;
+}
+
+// T.df += sign * sum over labels of z . d(slice of V)/d(features): the
+// per-point part of Permutohedral::gradient (permutohedral.cpp:612-695).
+int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float sign, bool value1) {
     Term &T = h->terms[k];
     SliceGradArgs g{};
     g.N = h->N;
-    g.M = h->M;
+    g.M = value1 ? 1 : h->M;
     g.d = T.d;
     g.nslots = h->nslots;
     g.slot_pt = h->slot_pt;
     g.off = T.lat.off;
     g.rank = T.lat.rank;
-    g.V = T.V[(T.d + 1) & 1];
-    {
-        float inv_std_dev = (float)(std::sqrt(2.0 / 3.0) * (T.d + 1));
-        for (int i = 0; i < T.d; i++)
-            g.sf[i] = (float)(1.0 / std::sqrt((double)((i + 2) * (i + 1))) * (double)inv_std_dev);
-        g.alpha = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1);
-    }
+    g.V = V;
+    g.z = z;
+    const float inv_std_dev = (float)(std::sqrt(2.0 / 3.0) * (T.d + 1));
+    for (int i = 0; i < T.d; i++)
+        g.sf[i] = (float)(1.0 / std::sqrt((double)((i + 2) * (i + 1))) * (double)inv_std_dev);
+    g.alpha = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1) * sign;
     g.df = T.df;
-    for (int dir = 0; dir < 2; dir++) {
-        int rc = splat_blur(h, k, dir ? y : x, dir == 1, false);
-        if (rc) return rc;
-        g.z = dir ? x : y;
-        // sign folded into the contraction values would need a copy; scale the
-        // alpha instead (the gradient is linear in the sliced values)
-        g.alpha = (1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1)) * sign;
-        CU(launch_slice_grad(g, h->MP, h->stream));
-    }
+    CU(launch_slice_grad(g, value1 ? 1 : h->MP, h->stream));
     return DCRF_OK;
-}
-
-// Feature gradient of a^T C K(Q) with the normalisation's own dependence on
-// the features (DenseKernel::featureGradient, pairwise.cpp:87-114), added to T.df.
-int feature_grad(dcrf_crf *h, int k, const float *a, const float *bb) {
-    Term &T = h->terms[k];
-    const int M = h->M, ns = h->nslots;
-    float *an = h->bw[7], *bn = h->bw[8], *fa = h->bw[9], *fb = h->bw[10], *c1 = h->bw[11], *ones = h->bw[12];
-    int rc;
-    switch (T.ntype) {
-        case DCRF_NORMALIZE_SYMMETRIC:
-            CU(launch_scale_norm(a, an, T.norm, M, ns, 1, h->stream));
-            CU(launch_scale_norm(bb, bn, T.norm, M, ns, 1, h->stream));
-            if ((rc = filter_into(h, k, an, fa, true, false, false))) return rc;
-            if ((rc = filter_into(h, k, bn, fb, false, false, false))) return rc;
-            CU(launch_prod(a, fb, fa, bb, 0.5f, T.norm, 3, c1, M, ns, h->stream));
-            if ((rc = lattice_grad(h, k, c1, ones, -1.f))) return rc;
-            return lattice_grad(h, k, an, bn, 1.f);
-        case DCRF_NORMALIZE_AFTER:
-            if ((rc = filter_into(h, k, bb, fb, false, false, false))) return rc;
-            CU(launch_prod(a, fb, nullptr, nullptr, 1.f, T.norm, 2, c1, M, ns, h->stream));
-            if ((rc = lattice_grad(h, k, c1, ones, -1.f))) return rc;
-            CU(launch_scale_norm(a, an, T.norm, M, ns, 1, h->stream));
-            return lattice_grad(h, k, an, bb, 1.f);
-        case DCRF_NORMALIZE_BEFORE:
-            if ((rc = filter_into(h, k, a, fa, true, false, false))) return rc;
-            CU(launch_prod(fa, bb, nullptr, nullptr, 1.f, T.norm, 2, c1, M, ns, h->stream));
-            if ((rc = lattice_grad(h, k, c1, ones, -1.f))) return rc;
-            CU(launch_scale_norm(bb, bn, T.norm, M, ns, 1, h->stream));
-            return lattice_grad(h, k, a, bn, 1.f);
-        default:
-            return lattice_grad(h, k, a, bb, 1.f);
-    }
 }
 
 int compat_count(const dcrf_crf *h, const Term &T) {
@@ -1006,7 +1043,9 @@ int dcrf_destroy(dcrf_crf *h) {
     h->event_pool.clear();
     for (Term &T : h->terms) free_term(h, T);
     dev_free_async(h->ckpt, h->stream);
+    dev_free_async(h->ckv, h->stream);
     for (float *&b : h->bw) dev_free_async(b, h->stream);
+    for (float *&b : h->bw1) dev_free_async(b, h->stream);
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
@@ -1421,6 +1460,29 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
         if ((rc = dev_alloc_async(&h->ckpt, need, h->stream))) return rc;
         h->ckpt_cap = need;
     }
+    // the forward's splat S and blurred lattice B of every iterate, per term
+    h->ckv_off.assign(h->terms.size(), 0);
+    size_t per_it = 0;
+    for (size_t k = 0; k < h->terms.size(); k++) {
+        h->ckv_off[k] = per_it;
+        per_it += 2 * ((size_t)h->terms[k].lat.L + 1) * h->MP;
+    }
+    const size_t vneed = std::max<size_t>(per_it * (size_t)n_iterations, 1);
+    bool fresh = per_it != h->ckv_iter;
+    h->ckv_iter = per_it;
+    if (vneed > h->ckv_cap) {
+        dev_free_async(h->ckv, h->stream);
+        h->ckv = nullptr;
+        h->ckv_cap = 0;
+        if ((rc = dev_alloc_async(&h->ckv, vneed, h->stream))) return rc;
+        h->ckv_cap = vneed;
+        fresh = true;
+    }
+    // row 0 of every S and B is the zero sentinel and is never written afterwards
+    std::vector<size_t> sig = h->ckv_off;
+    for (const Term &Tk : h->terms) sig.push_back((size_t)Tk.lat.L);
+    if (fresh || h->ckv_layout != sig) CU(cudaMemsetAsync(h->ckv, 0, sizeof(float) * vneed, h->stream));
+    h->ckv_layout = sig;
     if ((rc = run_inference(h, n_iterations, 0, h->ckpt))) return rc;
     if ((rc = store_mn(h, h->ckpt + (size_t)n_iterations * qsz, Q, layout, where))) return rc;
     if ((rc = sync_check(h))) return rc;
@@ -1440,6 +1502,10 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
     const bool want_compat = dcompat != nullptr, want_kernel = dkernel != nullptr;
     for (float *&b : h->bw)
         if (!b && (rc = dev_alloc_async(&b, qsz, h->stream))) return rc;
+    for (float *&b : h->bw1)
+        if (!b && (rc = dev_alloc_async(&b, (size_t)ns, h->stream))) return rc;
+    if (!h->ckv || h->ckv_off.size() != h->terms.size())
+        return set_err(DCRF_ERR_STATE, "dcrf_backward needs a dcrf_inference_checkpointed of the current model");
     // reduction space: per term compat (M or M*M) and kernel (d*d) accumulators
     std::vector<size_t> coff(nt), koff(nt);
     size_t nacc = 0;
@@ -1473,35 +1539,93 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
                 if (!Tk.df && (rc = dev_alloc_async(&Tk.df, (size_t)h->N * Tk.d, h->stream))) return rc;
                 CU(cudaMemsetAsync(Tk.df, 0, sizeof(float) * (size_t)h->N * Tk.d, h->stream));
             }
-    float *b = h->bw[0], *g = h->bw[1], *du = h->bw[2], *kq = h->bw[3], *a = h->bw[4], *xt = h->bw[5],
-          *bb = h->bw[6];
-    CU(launch_fill(h->bw[12], 1.f, M, ns, h->slot_pt, h->stream));
-    // seed: b = -dL/dA_{T-1} from dL/dQ_T (densecrf.cpp:256-258)
+    // slot-row work buffers
+    float *b = h->bw[0], *g = h->bw[1], *du = h->bw[2], *xn = h->bw[3], *F = h->bw[4], *Fn = h->bw[5],
+          *y = h->bw[6], *cq = h->bw[8], *yn = h->bw[9], *fb = h->bw[10], *c1 = h->bw[11];
+    float *x1 = h->bw1[0], *ones1 = h->bw1[1];
+    CU(launch_fill(ones1, 1.f, 1, ns, h->slot_pt, h->stream));
+    for (int k = 0; k < nt; k++) {
+        Term &Tk = h->terms[k];
+        if ((rc = ensure_adjoint_bufs(h, Tk))) return rc;
+        // R1: the reverse-blurred splat of ones (fixed per lattice), for the
+        // normalisation's dependence on the features
+        if (want_kernel && Tk.ktype != DCRF_CONST_KERNEL && Tk.ntype != DCRF_NO_NORMALIZATION && !Tk.r1_valid) {
+            if ((rc = splat_into(h, k, ones1, Tk.b1[0], true))) return rc;
+            if ((rc = blur_into(h, k, Tk.b1[0], Tk.b1[2], true, true))) return rc;
+            Tk.r1_valid = true;
+        }
+    }
+    // seed: b = -dL/dA_T from dL/dQ_T (densecrf.cpp:256-258)
     if ((rc = load_mn(h, dQ, layout, where, g))) return rc;
-    CU(launch_softmax_adjoint(h->ckpt + (size_t)T * qsz, g, b, M, ns, h->slot_pt, h->stream));
+    CU(launch_softmax_adjoint(h->ckpt + (size_t)T * qsz, g, b, nullptr, M, ns, h->slot_pt, h->stream));
     CU(cudaMemcpyAsync(du, b, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
     for (int it = T - 1; it >= 0; it--) {
         const float *Qt = h->ckpt + (size_t)it * qsz;
         CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];
-            if (want_compat) {  // PairwisePotential::gradient, pairwise.cpp:190-195
-                if ((rc = filter_into(h, k, Qt, kq, false, fwd_pre(Tk), fwd_post(Tk)))) return rc;
-                CU(launch_label_products(b, kq, M, ns, h->slot_pt, Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0, h->dpart,
+            const size_t rows = (size_t)Tk.lat.L + 1;
+            const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];  // forward splat of Q_t
+            const float *Bt = St + rows * h->MP;                                   // and its blurred lattice
+            const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
+            // x~ = b with the transpose's first normalisation; S_b = its splat
+            const float *xs = b;
+            if (tr_pre(Tk)) {
+                CU(launch_scale_norm(b, xn, Tk.norm, M, ns, 1, h->stream));
+                xs = xn;
+            }
+            if ((rc = splat_into(h, k, xs, Tk.bv[0], false))) return rc;
+            // F = K_raw^T x~ (reverse blur) and Fp = K^T b = [norm .*] F; g += C^T Fp
+            // (applyTranspose, pairwise.cpp:179-183; the compatibilities are symmetric)
+            if ((rc = blur_into(h, k, Tk.bv[0], Tk.bv[1], true, false))) return rc;
+            const bool need_F =
+                kgrad && (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_BEFORE);
+            if ((rc = slice_from(h, k, Tk.bv[1], need_F ? F : nullptr, false, tr_post(Tk), want_compat ? Fn : nullptr,
+                                 g)))
+                return rc;
+            if (want_compat) {  // PairwisePotential::gradient (pairwise.cpp:190-195): sum b (K Q_t)^T = sum (K^T b) Q_t^T
+                CU(launch_label_products(Fn, Qt, M, ns, h->slot_pt, Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0, h->dpart,
                                          h->dacc + coff[k], 1, h->stream));
             }
-            if (want_kernel && Tk.ktype != DCRF_CONST_KERNEL) {  // pairwise.cpp:202-207
-                CU(launch_compat(Qt, bb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
-                if ((rc = feature_grad(h, k, b, bb))) return rc;
+            // y = K_raw [norm] Q_t, sliced from the forward's blurred lattice
+            const bool need_y = kgrad && (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER);
+            if (need_y && (rc = slice_from(h, k, Bt, y, false))) return rc;
+            if (kgrad) {  // kernelGradient (pairwise.cpp:202-207) through featureGradient (87-114)
+                CU(launch_compat(Qt, cq, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                const float *ys = cq;  // y~ = C Q_t with the forward's first normalisation
+                if (fwd_pre(Tk)) {
+                    CU(launch_scale_norm(cq, yn, Tk.norm, M, ns, 1, h->stream));
+                    ys = yn;
+                }
+                // d/df x~^T K_raw y~: the forward-blurred S_b against y~, and the
+                // reverse-blurred splat of y~ (= C S_t) against x~
+                if ((rc = blur_into(h, k, Tk.bv[0], Tk.bv[1], false, false))) return rc;
+                if ((rc = slice_grad_into(h, k, Tk.bv[1], ys, 1.f, false))) return rc;
+                CU(launch_compat(St, Tk.bv[2], M, (int)rows, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                if ((rc = blur_into(h, k, Tk.bv[2], Tk.bv[1], true, false))) return rc;
+                if ((rc = slice_grad_into(h, k, Tk.bv[1], xs, 1.f, false))) return rc;
+                if (Tk.ntype != DCRF_NO_NORMALIZATION) {
+                    // - d/df c1^T K_raw 1 with c1 the normalisation's coefficients; the
+                    // contraction with ones reduces to one value per point
+                    if (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC) {
+                        CU(launch_compat(y, fb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                        CU(launch_prod(b, fb, F, cq, 0.5f, Tk.norm, 3, c1, M, ns, h->stream));
+                    } else if (Tk.ntype == DCRF_NORMALIZE_AFTER) {
+                        CU(launch_compat(y, fb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                        CU(launch_prod(b, fb, nullptr, nullptr, 1.f, Tk.norm, 2, c1, M, ns, h->stream));
+                    } else {
+                        CU(launch_prod(F, cq, nullptr, nullptr, 1.f, Tk.norm, 2, c1, M, ns, h->stream));
+                    }
+                    CU(launch_row_sum(c1, x1, M, ns, h->stream));
+                    if ((rc = splat_into(h, k, x1, Tk.b1[0], true))) return rc;
+                    if ((rc = blur_into(h, k, Tk.b1[0], Tk.b1[1], false, true))) return rc;
+                    if ((rc = slice_grad_into(h, k, Tk.b1[1], ones1, -1.f, true))) return rc;
+                    if ((rc = slice_grad_into(h, k, Tk.b1[2], x1, -1.f, true))) return rc;
+                }
             }
-            // g += K^T C^T b (applyTranspose, pairwise.cpp:179-183)
-            CU(launch_compat(b, a, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 1, 0, h->stream));
-            if ((rc = filter_into(h, k, a, xt, true, tr_pre(Tk), tr_post(Tk)))) return rc;
-            CU(launch_add(xt, g, qsz, h->stream));
         }
-        // b = -dL/dA_{it-1} (densecrf.cpp:290)
-        CU(launch_softmax_adjoint(Qt, g, b, M, ns, h->slot_pt, h->stream));
-        CU(launch_add(b, du, qsz, h->stream));
+        // b = -dL/dA_t (densecrf.cpp:290)
+        CU(launch_softmax_adjoint(Qt, g, b, du, M, ns, h->slot_pt, h->stream));
     }
     if (dU && (rc = store_mn(h, du, dU, layout, where))) return rc;
     if (want_kernel)

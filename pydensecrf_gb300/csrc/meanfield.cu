@@ -541,6 +541,15 @@ __global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_c
 // from the vertex-order blurred values; used off the iteration loop).
 template <int MP>
 __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPArgs a) {
+    __shared__ __align__(16) float sCT[(MP % 4 == 0) ? MP * MP : 4];
+    const bool stage = a.Gacc && a.ts.t[0].ckind == DCRF_COMPAT_MATRIX && MP % 4 == 0;
+    if (stage) {  // the adjoint epilogue's Matrix, [k][MP] (its transpose equals it)
+        for (int e = threadIdx.x; e < MP * MP; e += blockDim.x) {
+            const int k = e / MP, m = e - k * MP;
+            sCT[e] = (k < a.M && m < a.M) ? a.ts.t[0].compat[(size_t)m * a.M + k] : 0.f;
+        }
+        __syncthreads();
+    }
     const size_t s = (size_t)blockIdx.x * SPLAT_TILE + threadIdx.x;
     const int i = a.slot_pt[s];
     if (i < 0) return;
@@ -585,9 +594,29 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
             for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
         }
     }
-    float *dst = a.Qout + s * MP;
 #pragma unroll
-    for (int m = 0; m < MP; m++) dst[m] = m < M ? acc[m] : 0.f;
+    for (int m = 0; m < MP; m++)
+        if (m >= M) acc[m] = 0.f;
+    if (a.Qout) store_row<MP>(a.Qout + s * MP, acc);
+    if (!a.Fpost && !a.Gacc) return;
+    if (T.post_norm) {
+        const float nn = T.norm[s];
+#pragma unroll
+        for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
+    }
+    if (a.Fpost) store_row<MP>(a.Fpost + s * MP, acc);
+    if (a.Gacc) {  // Gacc += compat(F'); the compatibilities are symmetric (W = (m + m^T) / 2)
+        float gv[MP];
+        load_row<MP>(a.Gacc + s * MP, gv);
+        double unused = 0.0;
+        float neg[MP];
+#pragma unroll
+        for (int m = 0; m < MP; m++) neg[m] = -gv[m];
+        fold_compat<MP>(T, stage ? sCT : nullptr, acc, neg, M, false, unused);  // neg -= compat(F')
+#pragma unroll
+        for (int m = 0; m < MP; m++) gv[m] = m < M ? -neg[m] : 0.f;
+        store_row<MP>(a.Gacc + s * MP, gv);
+    }
 }
 
 template <int MP>

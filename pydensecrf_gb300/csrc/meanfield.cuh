@@ -31,6 +31,11 @@ struct PPArgs {
     int smem_bytes;      // dynamic shared memory of the point pass
     int sm_q;            // offset of the splat's q rows (aliases the slice-phase regions)
     int sm_res;          // offset of the splat's per-task results (after the q rows)
+    // PP_FILTER epilogue (adjoint): with F the raw filter of term 0 and
+    // F' = F .* norm when term 0's post_norm is set (else F): Fpost = F' and
+    // Gacc += compat(F') (rows; null to skip).  Qout (raw F) may be null.
+    float *Fpost;
+    float *Gacc;
     // PP_NORM outputs, per term ([nslots] each)
     float *norm_out[DCRF_MAX_TERMS];
     int ntype[DCRF_MAX_TERMS];
