@@ -211,6 +211,7 @@ def learning_step_times(lib, _lib, dev, stream, reps: int = 2):
     h = ctypes.c_void_p()
     _lib.check(lib.dcrf_create_2d(Wt, Ht, Mt, ctypes.byref(h)))
     _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    _lib.check(lib.dcrf_set_autotune(h, 1))
     cols = torch.arange(Nt, device=dev)
     grads = {}
 
@@ -306,6 +307,7 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
     hb = ctypes.c_void_p()
     _lib.check(lib.dcrf_create_batch_2d(len(sizes), Wa.ctypes.data, Ha.ctypes.data, Mb, ctypes.byref(hb)))
     _lib.check(lib.dcrf_set_stream(hb, ctypes.c_void_p(stream.cuda_stream)))
+    _lib.check(lib.dcrf_set_autotune(hb, 1))
 
     def timed(fn):
         fn()
@@ -320,19 +322,25 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
             ms.append(a.elapsed_time(b))
         return float(np.median(ms))
 
+    batch_ms = timed(lambda: solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all)))
     c0, c1 = ctypes.c_ulonglong(), ctypes.c_ulonglong()
     lib.dcrf_launch_count(ctypes.byref(c0))
-    batch_ms = timed(lambda: solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all)))
+    solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all))
+    torch.cuda.synchronize()
     lib.dcrf_launch_count(ctypes.byref(c1))
-    batch_launches = (c1.value - c0.value) // (reps + 1)
+    batch_launches = c1.value - c0.value
     Qb = Q_all.clone()
+    knobs = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()]
+    _lib.check(lib.dcrf_get_tuning(hb, *[ctypes.byref(k) for k in knobs]))
     lib.dcrf_destroy(hb)
 
+    # the per-image handles run with the batch's tuned knobs (same arithmetic)
     hs = []
     for w, h_ in sizes:
         h = ctypes.c_void_p()
         _lib.check(lib.dcrf_create_2d(w, h_, Mb, ctypes.byref(h)))
         _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+        _lib.check(lib.dcrf_set_tuning(h, *[k.value for k in knobs]))
         hs.append(h)
 
     def loop():
@@ -349,7 +357,9 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
             "speedup": round(loop_ms / batch_ms, 3),
             "batched_value": round(units / (batch_ms / 1e3), 1), "loop_value": round(units / (loop_ms / 1e3), 1),
             "unit": "MPix*label*iter/s", "batched_launches": int(batch_launches),
-            "batched_equals_loop": same}
+            "batched_equals_loop": same,
+            "tuning": {"split": knobs[0].value, "smem_kb": knobs[1].value, "task_len": knobs[2].value,
+                       "hash_load": round(knobs[3].value, 2)}}
 
 
 def run_gpu(args):
@@ -377,6 +387,7 @@ def run_gpu(args):
     _lib.check(lib.dcrf_create_2d(W, H, M, ctypes.byref(h)))
     stream = torch.cuda.current_stream(dev)
     _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    _lib.check(lib.dcrf_set_autotune(h, 1))  # tuned during the first warm-up step
     cg = np.array([3.0], np.float32)
     cb = np.array([10.0], np.float32)
 
@@ -418,6 +429,10 @@ def run_gpu(args):
         total_ms = float(t.item())
     value = world * args.steps * UNITS_PER_STEP / (total_ms / 1e3)
     launches = int(cnt1.value - cnt0.value)
+
+    tk = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()]
+    _lib.check(lib.dcrf_get_tuning(h, *[ctypes.byref(k) for k in tk]))
+    tuning = {"split": tk[0].value, "smem_kb": tk[1].value, "task_len": tk[2].value, "hash_load": round(tk[3].value, 2)}
 
     # ---- breakdown and roofline: a profiled pass (events around every launch)
     _lib.check(lib.dcrf_set_profiling(h, 1))
@@ -507,6 +522,7 @@ def run_gpu(args):
             "iteration_ms": round((prof["point"]["ms_per_step"] + prof["reduce"]["ms_per_step"]
                                    + prof["blur"]["ms_per_step"]) / T, 4),
             "lattice": {"L": Ls, "partials": Ps},
+            "tuning": tuning,
             "roofline": roofline,
             "cpu_baseline": cpu,
             "learning": learning,

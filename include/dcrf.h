@@ -210,6 +210,27 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
  * (permutohedral.cpp:556). */
 int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU, double *dcompat, double *dkernel);
 
+/* ---- autotuning (no reference counterpart) --------------------------------
+ * The engine's launch and build knobs -- threads per point of the mean-field
+ * point pass (1 or 2), its shared-memory budget per CTA (KB), the splat task
+ * length (members per task, 1..63) and the lattice hash-table load factor --
+ * are picked per configuration (labels, per-term d / compatibility kind /
+ * normalisation / arithmetic variant, one image or a batch, size class
+ * log2 N) by timing candidates on the handle's own lattices.  Choices are
+ * remembered for the process.  Only the task length changes results (the
+ * grouping of the splat sums, at the 1e-7 level). */
+
+/* Tune at the first inference of every new configuration (or take the
+ * remembered choice). Off by default. */
+int dcrf_set_autotune(dcrf_crf *h, int on);
+/* Tune now for the current terms (rebuilds the lattices while trying). */
+int dcrf_autotune(dcrf_crf *h);
+/* The knobs in effect (any pointer may be NULL). */
+int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float *hash_load);
+/* Set the knobs (split 0 = rule of thumb, smem_kb 0 = default); rebuilds the
+ * lattices when the task length or load factor changes. */
+int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load);
+
 /* ---- measurement -------------------------------------------------------- */
 
 /* Number of kernels this library has launched in the process so far. */

@@ -20,7 +20,7 @@ from numbers import Number
 import numpy as np
 
 from . import _lib
-from .densecrf import DIAG_KERNEL, NORMALIZE_SYMMETRIC, _check_enum, _labelcomp, _ptr
+from .densecrf import DIAG_KERNEL, NORMALIZE_SYMMETRIC, DenseCRF, _check_enum, _labelcomp, _ptr
 
 __all__ = ["DenseCRFBatch", "DenseCRF2DBatch"]
 
@@ -112,6 +112,12 @@ class DenseCRFBatch:
         n = ctypes.c_int()
         _lib.check(_lib.load().dcrf_info(self._h, None, None, ctypes.byref(n)))
         return n.value
+
+    # -- autotuning --------------------------------------------------------------------
+    set_autotune = DenseCRF.set_autotune
+    autotune = DenseCRF.autotune
+    tuning = DenseCRF.tuning
+    set_tuning = DenseCRF.set_tuning
 
     # -- inference ------------------------------------------------------------------
     def _flat(self) -> np.ndarray:

@@ -1,6 +1,8 @@
 // api.cu -- the C ABI of include/dcrf.h: handles, device memory, and the
 // launch sequences of lattice build, normalisation and mean-field inference.
 #include <algorithm>
+#include <chrono>
+#include <map>
 #include <atomic>
 #include <cmath>
 #include <mutex>
@@ -129,6 +131,14 @@ struct Term {
     bool params_set = false;    // the lattice uses params (else the features as given)
 };
 
+// Knobs of the launch sequence that the autotuner picks per configuration.
+struct TuneCfg {
+    int split = 0;           // threads per point in the point pass (0: by rule, see pick_split)
+    int smem_kb = 0;         // point-pass shared-memory budget per CTA (0: the default for MP)
+    int task = SPLAT_TASK;   // most members of one splat task (lattice build)
+    float hash_load = 2.0f;  // hash-table capacity factor (lattice build)
+};
+
 }  // namespace
 
 struct dcrf_crf {
@@ -155,7 +165,6 @@ struct dcrf_crf {
     int ntiles = 0;
     int *slot_pt = nullptr;
     int *tile_vbase = nullptr;
-    float hash_load = 2.0f;
     std::vector<Term> terms;
     // model version (bumped by every change of unary, terms or parameters) and
     // the per-iteration checkpoints of the last dcrf_inference_checkpointed
@@ -175,6 +184,9 @@ struct dcrf_crf {
     // CUDA graph of the last inference launch sequence (re-used through
     // cudaGraphExecUpdate while its topology stays the same)
     bool use_graphs = true;
+    // launch and build knobs (see the autotuner below)
+    TuneCfg tune;
+    bool autotune = false, tuned = false;
     cudaStream_t capture = nullptr;
     cudaGraphExec_t gexec = nullptr;
     // profiling: events bracketing launches, by kernel class
@@ -436,7 +448,8 @@ size_t align128(size_t x) { return (x + 127) & ~(size_t)127; }
 // alias them).  Tiles with more partials than a term's vcap read their rows
 // from global memory; terms whose fixed blocks do not fit are not staged.
 void plan_smem(dcrf_crf *h, PPArgs &a, const std::vector<int> &which, bool msg, int MP) {
-    const int budget = pointpass_smem_budget(MP);
+    const int budget = h->tune.smem_kb > 0 ? std::min(h->tune.smem_kb * 1024, POINTPASS_SMEM_MAX)
+                                           : pointpass_smem_budget(MP);
     const int n = (int)which.size();
     int max_nt = 0;
     for (int k = 0; k < n; k++) max_nt = std::max(max_nt, h->terms[which[k]].lat.max_nt);
@@ -524,6 +537,18 @@ cudaError_t pp(dcrf_crf *h, const PPArgs &a, int MP) {
     return launch_pointpass(a, MP, h->stream);
 }
 
+// Threads per point of the point pass: the tuned value, else two for label
+// rows of 8k floats without a Matrix compatibility (measured: two threads win
+// for Potts/Diagonal, one for Matrix, whose products then need the partner's
+// labels).
+int pick_split(const dcrf_crf *h, bool value1) {
+    if (value1 || h->MP % 8 != 0) return 1;
+    if (h->tune.split == 1 || h->tune.split == 2) return h->tune.split;
+    for (const Term &T : h->terms)
+        if (T.ckind == DCRF_COMPAT_MATRIX) return 1;
+    return 2;
+}
+
 PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transpose, bool value1) {
     PPArgs a{};
     a.N = h->N;
@@ -544,6 +569,7 @@ PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transp
         a.ntype[k] = h->terms[which[k]].ntype;
         a.norm_out[k] = h->terms[which[k]].norm;
     }
+    a.split = pick_split(h, value1);
     plan_smem(h, a, which, (mode & PP_MSG) != 0, value1 ? 1 : h->MP);
     return a;
 }
@@ -704,10 +730,10 @@ int build_term(dcrf_crf *h, int k) {
     tm.ntiles = h->ntiles;
     tm.slot_pt = h->slot_pt;
     tm.tile_vbase = h->tile_vbase;
-    float load = h->hash_load;
+    float load = h->tune.hash_load;
     for (int attempt = 0;; attempt++) {
         ProfScope ps(h, DCRF_KCLASS_LATTICE);
-        rc = lattice_build(feat, T.d, h->N, seg, tm, T.variant, load, h->stream, h->status, &T.lat);
+        rc = lattice_build(feat, T.d, h->N, seg, tm, T.variant, load, h->tune.task, h->stream, h->status, &T.lat);
         if (rc == DCRF_ERR_HASH_FULL && attempt < 3) {
             load *= 4.f;
             continue;
@@ -764,6 +790,7 @@ int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, c
         return rc;
     }
     h->terms.push_back(T);
+    h->tuned = false;  // a new configuration for the autotuner
     const int k = (int)h->terms.size() - 1;
     if ((rc = build_term(h, k))) {
         free_term(h, h->terms[k]);
@@ -831,7 +858,148 @@ int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
 // stream, instantiated once and afterwards updated in place (same kernels,
 // new arguments), launched on the handle's stream.  Profiling launches the
 // kernels directly so that the per-launch events can be recorded.
+// ---- autotuner ----------------------------------------------------------------
+// Picks the launch and build knobs per configuration -- labels, per-term (d,
+// compatibility kind, normalisation, arithmetic variant), one image or a batch,
+// and the size class log2(N) -- by timing candidates on the handle's own
+// lattices, and remembers the choice for the process.  Build knobs: hash load
+// factor (1.5, 2, 3) and splat task length (8, 16, 32), scored as one build
+// plus ten iterations; launch knobs: threads per point (1, 2) and the point
+// pass's shared-memory budget (default, or 72 KB for three CTAs per SM).
+// Only the task length changes results (the grouping of the splat sums).
+
+std::mutex g_tune_mu;
+std::map<std::string, TuneCfg> g_tune_cache;
+
+std::string tune_key(const dcrf_crf *h) {
+    int lg = 0;
+    while ((1ll << (lg + 1)) <= (long long)h->N) lg++;
+    std::string k = "M" + std::to_string(h->M) + (h->seg.size() > 2 ? "/batch" : "/one") + "/N2^" + std::to_string(lg);
+    for (const Term &T : h->terms)
+        k += "/d" + std::to_string(T.d) + "c" + std::to_string(T.ckind) + "n" + std::to_string(T.ntype) + "v" +
+             std::to_string(T.variant);
+    return k;
+}
+
+int rebuild_terms(dcrf_crf *h) {
+    for (size_t k = 0; k < h->terms.size(); k++) {
+        int rc = build_term(h, (int)k);
+        if (rc) return rc;
+    }
+    return DCRF_OK;
+}
+
+// Device time of n mean-field iterations (min of reps), launched directly.
+int time_iterations(dcrf_crf *h, int n, int reps, float *ms_out) {
+    cudaEvent_t a = take_event(h), b = take_event(h);
+    float best = 1e30f;
+    int rc = DCRF_OK;
+    for (int r = 0; r <= reps && !rc; r++) {
+        CU(cudaEventRecord(a, h->stream));
+        rc = issue_inference(h, n, PP_WRITE_Q);
+        CU(cudaEventRecord(b, h->stream));
+        CU(cudaEventSynchronize(b));
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, a, b));
+        if (r > 0) best = std::min(best, ms);  // the first run warms up
+    }
+    h->event_pool.push_back(a);
+    h->event_pool.push_back(b);
+    *ms_out = best;
+    return rc;
+}
+
+int autotune_now(dcrf_crf *h) {
+    if (h->terms.empty()) return DCRF_OK;
+    const bool prof = h->profiling;
+    h->profiling = false;
+    int rc = DCRF_OK;
+    // build knobs: one build plus ten iterations
+    TuneCfg best = h->tune;
+    double best_score = 1e30;
+    const float loads[3] = {1.5f, 2.0f, 3.0f};
+    const int tasks[3] = {8, 16, 32};
+    for (float ld : loads)
+        for (int tk : tasks) {
+            h->tune.hash_load = ld;
+            h->tune.task = tk;
+            auto t0 = std::chrono::steady_clock::now();
+            if ((rc = rebuild_terms(h))) break;
+            const double build_ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            float it_ms = 0.f;
+            if ((rc = time_iterations(h, 2, 2, &it_ms))) break;
+            const double score = build_ms + 5.0 * it_ms;
+            if (score < best_score) {
+                best_score = score;
+                best.hash_load = ld;
+                best.task = tk;
+            }
+        }
+    if (!rc) {
+        h->tune.hash_load = best.hash_load;
+        h->tune.task = best.task;
+        rc = rebuild_terms(h);
+    }
+    // launch knobs on the chosen lattices
+    if (!rc) {
+        float best_ms = 1e30f;
+        const int splits[2] = {1, 2};
+        const int smems[2] = {0, 72};
+        for (int sp : splits) {
+            if (sp == 2 && h->MP % 8 != 0) continue;
+            for (int sm : smems) {
+                h->tune.split = sp;
+                h->tune.smem_kb = sm;
+                float ms = 0.f;
+                if ((rc = time_iterations(h, 2, 3, &ms))) break;
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best.split = sp;
+                    best.smem_kb = sm;
+                }
+            }
+            if (rc) break;
+        }
+        h->tune.split = best.split;
+        h->tune.smem_kb = best.smem_kb;
+    }
+    h->profiling = prof;
+    if (rc) return rc;
+    h->tuned = true;
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache[tune_key(h)] = h->tune;
+    return DCRF_OK;
+}
+
+// Applies knobs; rebuilds the lattices when a build knob changes.
+int apply_tuning(dcrf_crf *h, const TuneCfg &c) {
+    const bool rebuild = c.task != h->tune.task || c.hash_load != h->tune.hash_load;
+    h->tune = c;
+    h->tuned = true;
+    return rebuild ? rebuild_terms(h) : DCRF_OK;
+}
+
+// Automatic mode: tune (or take the remembered choice) before the first
+// inference of a configuration.
+int maybe_autotune(dcrf_crf *h) {
+    if (!h->autotune || h->tuned || h->terms.empty()) return DCRF_OK;
+    TuneCfg c;
+    bool hit = false;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        auto it = g_tune_cache.find(tune_key(h));
+        if (it != g_tune_cache.end()) {
+            c = it->second;
+            hit = true;
+        }
+    }
+    return hit ? apply_tuning(h, c) : autotune_now(h);
+}
+
 int run_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
+    int trc = maybe_autotune(h);
+    if (trc) return trc;
     if (h->profiling || !h->use_graphs) return issue_inference(h, T, final_mode, ckpt);
     cudaStream_t user = h->stream;
     h->stream = h->capture;
@@ -1356,6 +1524,7 @@ int dcrf_clear_pairwise(dcrf_crf *h) {
     if (rc) return rc;
     for (Term &T : h->terms) free_term(h, T);
     h->terms.clear();
+    h->tuned = false;
     h->version++;
     return ok();
 }
@@ -1363,6 +1532,47 @@ int dcrf_clear_pairwise(dcrf_crf *h) {
 int dcrf_launch_count(unsigned long long *count) {
     if (!count) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     *count = g_launches.load();
+    return ok();
+}
+
+int dcrf_set_autotune(dcrf_crf *h, int on) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    h->autotune = on != 0;
+    return ok();
+}
+
+int dcrf_autotune(dcrf_crf *h) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (h->terms.empty()) return set_err(DCRF_ERR_STATE, "autotune needs at least one pairwise term");
+    if ((rc = autotune_now(h))) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float *hash_load) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (split) *split = pick_split(h, false);
+    if (smem_kb) *smem_kb = h->tune.smem_kb > 0 ? h->tune.smem_kb : pointpass_smem_budget(h->MP) / 1024;
+    if (task_len) *task_len = h->tune.task;
+    if (hash_load) *hash_load = h->tune.hash_load;
+    return ok();
+}
+
+int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (split < 0 || split > 2 || smem_kb < 0 || smem_kb > 224 || task_len < 1 || task_len > 63 || !(hash_load >= 1.f))
+        return set_err(DCRF_ERR_INVALID_ARG, "tuning values out of range");
+    TuneCfg c;
+    c.split = split;
+    c.smem_kb = smem_kb;
+    c.task = task_len;
+    c.hash_load = hash_load;
+    if ((rc = apply_tuning(h, c))) return rc;
+    if ((rc = sync_check(h))) return rc;
     return ok();
 }
 
@@ -1422,6 +1632,7 @@ int dcrf_set_compat(dcrf_crf *h, int term, int compat_kind, const float *compat)
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
     if ((rc = validate_compat(compat_kind, compat))) return rc;
+    if (compat_kind != h->terms[term].ckind) h->tuned = false;
     if ((rc = set_term_compat(h, h->terms[term], compat_kind, compat))) return rc;
     h->version++;
     if ((rc = sync_check(h))) return rc;

@@ -445,11 +445,11 @@ __global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long
 }
 
 // Splat tasks of one tile: each partial's member run split into pieces of at
-// most SPLAT_TASK members.  Pass 0 counts, pass 1 writes.
+// most task_len members.  Pass 0 counts, pass 1 writes.
 __global__ void __launch_bounds__(256) tile_tasks_kernel(const int *__restrict__ tile_pbeg,
                                                          const int *__restrict__ part_mend, int pass,
                                                          uint32_t *__restrict__ tile_nt, const uint32_t *tile_tbeg,
-                                                         uint32_t *__restrict__ task) {
+                                                         uint32_t *__restrict__ task, int task_len) {
     __shared__ uint32_t s_warp[8];
     const int t = blockIdx.x;
     const int pb = tile_pbeg[t], np = tile_pbeg[t + 1] - pb;
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(256) tile_tasks_kernel(const int *__restrict__
     uint32_t cnt = 0;
     for (int j = j0; j < j1; j++) {
         const int b = j == 0 ? 0 : part_mend[pb + j - 1], e = part_mend[pb + j];
-        cnt += (uint32_t)((e - b + SPLAT_TASK - 1) / SPLAT_TASK);
+        cnt += (uint32_t)((e - b + task_len - 1) / task_len);
     }
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t x = cnt;
@@ -482,8 +482,8 @@ __global__ void __launch_bounds__(256) tile_tasks_kernel(const int *__restrict__
     uint32_t out = tile_tbeg[t] + before + x - cnt;
     for (int j = j0; j < j1; j++) {
         const int b = j == 0 ? 0 : part_mend[pb + j - 1], e = part_mend[pb + j];
-        for (int q = b; q < e; q += SPLAT_TASK)
-            task[out++] = ((uint32_t)j << 19) | ((uint32_t)q << 6) | (uint32_t)min(SPLAT_TASK, e - q);
+        for (int q = b; q < e; q += task_len)
+            task[out++] = ((uint32_t)j << 19) | ((uint32_t)q << 6) | (uint32_t)min(task_len, e - q);
     }
 }
 
@@ -538,7 +538,7 @@ T *dalloc(size_t n, cudaStream_t s, size_t *acc) {
 
 template <int D>
 int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
-            cudaStream_t s, DevStatus *status, LatticeDev *out) {
+            int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out) {
     constexpr int KW = KeyW<D>::KW;
     LatticeDev L{};
     L.d = D;
@@ -697,7 +697,8 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         uint32_t hT = 0;
         std::vector<uint32_t> htb(L.ntiles + 1, 0);
         if (L.ntiles > 0) {
-            DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 0, tile_nt, nullptr, nullptr));
+            DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 0, tile_nt, nullptr, nullptr,
+                                                                   task_len));
             if (scan_exclusive_u32(tile_nt, (uint32_t *)L.tile_tbeg, L.ntiles, d_T, stemp, s) != cudaSuccess)
                 return bail(DCRF_ERR_CUDA, "scan failed");
             cudaMemcpyAsync(&hT, d_T, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
@@ -713,7 +714,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.tile_tbeg + L.ntiles, (int)hT));
         if (L.ntiles > 0)
             DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 1, nullptr,
-                                                                   (const uint32_t *)L.tile_tbeg, L.task));
+                                                                   (const uint32_t *)L.tile_tbeg, L.task, task_len));
     }
     // ---- reduce lists: partials grouped by vertex, in tile order ------------
     {
@@ -767,13 +768,14 @@ void lattice_free(LatticeDev *L, cudaStream_t s) {
 }
 
 int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
-                  cudaStream_t s, DevStatus *status, LatticeDev *out) {
+                  int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out) {
+    if (task_len < 1 || task_len > 63) return fail(DCRF_ERR_INVALID_ARG, "splat task length must be in [1, 63]");
     if (N < 0 || (seg.start.size() < 2)) return fail(DCRF_ERR_INVALID_ARG, "bad point segmentation");
     if (cudaMemsetAsync(status, 0, sizeof(DevStatus), s) != cudaSuccess) return fail(DCRF_ERR_CUDA, "memset failed");
     switch (d) {
 #define DCRF_CASE(D) \
     case D:          \
-        return build_d<D>(feat, N, seg, tm, variant, load, s, status, out);
+        return build_d<D>(feat, N, seg, tm, variant, load, task_len, s, status, out);
         DCRF_CASE(1) DCRF_CASE(2) DCRF_CASE(3) DCRF_CASE(4) DCRF_CASE(5) DCRF_CASE(6) DCRF_CASE(7) DCRF_CASE(8)
         DCRF_CASE(9) DCRF_CASE(10) DCRF_CASE(11) DCRF_CASE(12) DCRF_CASE(13) DCRF_CASE(14) DCRF_CASE(15)
         DCRF_CASE(16)

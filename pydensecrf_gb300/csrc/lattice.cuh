@@ -9,7 +9,7 @@
 namespace dcrf {
 
 constexpr int SPLAT_TILE = 256;  // points per tile of the in-kernel splat
-constexpr int SPLAT_TASK = 16;   // members per splat task (load balance of the in-kernel splat)
+constexpr int SPLAT_TASK = 16;   // default members per splat task (load balance of the in-kernel splat)
 
 struct LatticeDev {
     int d = 0, N = 0, L = 0, P = 0, ntiles = 0, variant = 0;
@@ -56,10 +56,11 @@ struct TileMapDev {
 // Builds the lattice of `feat` ([d][N], device) on `s`.  `variant` selects the
 // x86 (SSE) or scalar arithmetic of the reference; SSE also inserts the
 // zero-feature padding points of each image (N_img % 4 != 0).  `load` is the
-// hash-table capacity factor (capacity = pow2 >= load * corners).  Returns a
-// DCRF status; on DCRF_ERR_HASH_FULL the caller may retry with a larger load.
+// hash-table capacity factor (capacity = pow2 >= load * corners); `task_len`
+// the most members of one splat task (1..63).  Returns a DCRF status; on
+// DCRF_ERR_HASH_FULL the caller may retry with a larger load.
 int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
-                  cudaStream_t s, DevStatus *status, LatticeDev *out);
+                  int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out);
 
 void lattice_free(LatticeDev *lat, cudaStream_t s);
 

@@ -32,6 +32,8 @@
 // reference uses it.
 #include <math.h>
 
+#include <algorithm>
+
 #include "meanfield.cuh"
 
 namespace dcrf {
@@ -206,6 +208,8 @@ __device__ __forceinline__ void fold_compat(const TermDev &T, const float *sCT, 
     } else {
 #pragma unroll
         for (int m = 0; m < MP; m++) c[m] = 0.f;
+        // products contracted into FMAs, as the reference's aarch64 build (Eigen's
+        // fused multiply-add) computes W Q
         if (sCT && MP % 4 == 0) {
 #pragma unroll
             for (int k = 0; k < MP; k++)
@@ -213,7 +217,7 @@ __device__ __forceinline__ void fold_compat(const TermDev &T, const float *sCT, 
                     float w[MP];
                     load_row_s<MP>(sCT + k * MP, w);
 #pragma unroll
-                    for (int m = 0; m < MP; m++) c[m] = fadd(c[m], fmul(w[m], acc[k]));
+                    for (int m = 0; m < MP; m++) c[m] = fmaf(w[m], acc[k], c[m]);
                 }
         } else {
 #pragma unroll
@@ -222,7 +226,7 @@ __device__ __forceinline__ void fold_compat(const TermDev &T, const float *sCT, 
                     const float *row = T.compat + (size_t)m * M;
 #pragma unroll
                     for (int k = 0; k < MP; k++)
-                        if (k < M) c[m] = fadd(c[m], fmul(__ldg(row + k), acc[k]));
+                        if (k < M) c[m] = fmaf(__ldg(row + k), acc[k], c[m]);
                 }
         }
     }
@@ -257,27 +261,99 @@ __device__ __forceinline__ TileBlocks tile_blocks(const TermDev &T, int t) {
     return b;
 }
 
+// Thread shape of the point pass: SPLIT threads per point (each owning H =
+// MP / SPLIT consecutive labels), SPLAT_TILE * SPLIT threads per tile.  Two
+// threads per point halve the registers a point needs (2 CTAs of 16 warps per
+// SM instead of 2 CTAs of 8).
+template <int MP, int S>
+struct PPT {
+    static constexpr int SPLIT = S;
+    static constexpr int H = MP / SPLIT;
+    static constexpr int NT = SPLAT_TILE * SPLIT;
+    static constexpr int MINB = (SPLIT == 2 && MP > 24) ? 1 : 2;  // 32 labels: registers over CTAs
+};
+
+// x -= compatibility(acc) on the thread's labels l0..l0+H-1 (or kl += q .
+// compatibility(acc) in kl_mode), the point's other labels coming from the
+// partner thread (pair mask pm).  Potts: -w acc; Diagonal: v * acc; Matrix:
+// W acc summed over k in label order with fused multiply-adds (the reference's
+// aarch64 build, Eigen's FMA) (labelcompatibility.cpp:46-48,66-68,82-84).
+template <int MP, int S>
+__device__ __forceinline__ void fold_compat_h(const TermDev &T, const float *sCT, const float (&acc)[PPT<MP, S>::H],
+                                              float (&x)[PPT<MP, S>::H], int M, int l0, int h, unsigned pm,
+                                              bool kl_mode, double &kl) {
+    constexpr int H = PPT<MP, S>::H, SPLIT = PPT<MP, S>::SPLIT;
+    float c[H];
+    if (T.ckind == DCRF_COMPAT_POTTS) {
+        const float nw = -T.potts_w;
+#pragma unroll
+        for (int e = 0; e < H; e++) c[e] = fmul(nw, acc[e]);
+    } else if (T.ckind == DCRF_COMPAT_DIAGONAL) {
+#pragma unroll
+        for (int e = 0; e < H; e++) c[e] = l0 + e < M ? fmul(__ldg(T.compat + l0 + e), acc[e]) : 0.f;
+    } else {
+#pragma unroll
+        for (int e = 0; e < H; e++) c[e] = 0.f;
+#pragma unroll
+        for (int b = 0; b < SPLIT; b++) {
+#pragma unroll
+            for (int j = 0; j < H; j++) {
+                float a = acc[j];
+                if constexpr (SPLIT == 2) {
+                    const float other = __shfl_xor_sync(pm, acc[j], 1);
+                    a = b == h ? acc[j] : other;
+                }
+                const int k = b * H + j;
+                if (k >= M) continue;
+                if (sCT) {
+                    float w[H];
+                    load_row_s<H>(sCT + k * MP + l0, w);
+#pragma unroll
+                    for (int e = 0; e < H; e++) c[e] = fmaf(w[e], a, c[e]);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < H; e++)
+                        if (l0 + e < M) c[e] = fmaf(__ldg(T.compat + (size_t)(l0 + e) * M + k), a, c[e]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int e = 0; e < H; e++) {
+        if (l0 + e >= M) continue;
+        if (kl_mode)
+            kl += (double)fmul(x[e], c[e]);
+        else
+            x[e] = fsub(x[e], c[e]);
+    }
+}
+
 // One CTA per tile of SPLAT_TILE points; marginals and unaries are slot rows
 // of MP floats ([nslots][MP]).
-template <int MP>
-__global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_constant__ PPArgs a) {
+template <int MP, int S>
+__global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_kernel(const __grid_constant__ PPArgs a) {
+    constexpr int SPLIT = PPT<MP, S>::SPLIT, H = PPT<MP, S>::H, NT = PPT<MP, S>::NT;
     using P = PG<MP>;
-    constexpr int VW = P::VW, G = P::G, GPW = P::GPW, NG = P::NG;
+    constexpr int VW = P::VW, G = P::G, GPW = P::GPW;
+    constexpr int NG = (NT / 32) * GPW;  // splat groups per CTA
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ uint64_t mbar;
-    __shared__ double sKL[SPLAT_TILE / 32];
+    __shared__ double sKL[NT / 32];
     __shared__ TileBlocks sTB[DCRF_MAX_TERMS];
 
     const int t = blockIdx.x;
     const int li = threadIdx.x;
     const int lane = li & 31, warp = li >> 5;
-    const int g = lane / G;                  // group within the warp
+    const int pi = li / SPLIT;               // point of the tile
+    const int h = li - pi * SPLIT;           // which labels of it
+    const int l0 = h * H;
+    const unsigned pm = SPLIT == 2 ? (3u << (lane & ~1)) : (1u << lane);
+    const int g = lane / G;                  // splat group within the warp
     const bool gactive = g < GPW;            // lanes past the last full group idle
     const int gc = gactive ? g : GPW - 1;
     const int c = lane - gc * G;             // lane within the group
-    const int gbase = gc * G;                // first lane of the group
     const int gid = warp * GPW + gc;         // group within the CTA
-    const int m0 = c * VW;                   // first label of the lane
+    const int m0 = c * VW;                   // first label of the lane in the splat
     const int M = a.M, mode = a.mode;
     pdl_trigger();
 
@@ -334,34 +410,35 @@ __global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_c
             const TermDev &T = a.ts.t[k];
             if (T.ckind != DCRF_COMPAT_MATRIX || T.sm_cmp < 0) continue;
             float *sCT = reinterpret_cast<float *>(smem + T.sm_cmp);
-            for (int e = li; e < MP * MP; e += SPLAT_TILE) {
+            for (int e = li; e < MP * MP; e += NT) {
                 const int kk = e / MP, m = e - kk * MP;
                 sCT[e] = (kk < M && m < M) ? T.compat[(size_t)m * M + kk] : 0.f;
             }
         }
     }
 
-    // the point's own inputs, overlapping the copies (one thread per point)
-    const size_t s = (size_t)t * SPLAT_TILE + li;
+    // the point's own inputs, overlapping the copies
+    const size_t s = (size_t)t * SPLAT_TILE + pi;
     const int i = a.slot_pt[s];
     const bool valid = i >= 0;
     const bool given = (mode & (PP_LOAD_Q | PP_ONES)) != 0;
     double kl = 0.0;
     // x: the logits of the update, or the given marginals (LOAD_Q / ONES); q after the softmax
-    float x[MP];
+    float x[H];
 #pragma unroll
-    for (int m = 0; m < MP; m++) x[m] = 0.f;
+    for (int e = 0; e < H; e++) x[e] = 0.f;
     if (valid && !(mode & (PP_ONES | PP_LOAD_Q)) && a.U) {  // the unary is fixed during inference
-        load_row<MP>(a.U + s * MP, x);
+        load_row<H>(a.U + s * MP + l0, x);
 #pragma unroll
-        for (int m = 0; m < MP; m++) x[m] = -x[m];
+        for (int e = 0; e < H; e++) x[e] = -x[e];
     }
     pdl_wait();
     if (valid) {
-        if (mode & PP_ONES)
-            x[0] = 1.f;
-        else if (mode & PP_LOAD_Q)
-            load_row<MP>(a.Qin + s * MP, x);
+        if (mode & PP_ONES) {
+            if (h == 0) x[0] = 1.f;
+        } else if (mode & PP_LOAD_Q) {
+            load_row<H>(a.Qin + s * MP + l0, x);
+        }
     }
     // ---- 2. wait for the copies (bounded; a timeout is reported, never a hang)
     if (any_staged) {
@@ -375,15 +452,15 @@ __global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_c
         __syncthreads();
     }
 
-    // ---- 3. per point (one thread per point): messages of every term,
-    // softmax, outputs
+    // ---- 3. per point: messages of every term, softmax, outputs (the two
+    // threads of a point share `valid`, so their pair shuffles converge)
     if ((mode & PP_MSG) && valid) {
         for (int k = 0; k < a.ts.n; k++) {
             const TermDev &T = a.ts.t[k];
             const TileBlocks b = sTB[k];
-            float acc[MP];
+            float acc[H];
 #pragma unroll
-            for (int m = 0; m < MP; m++) acc[m] = 0.f;
+            for (int e = 0; e < H; e++) acc[e] = 0.f;
             const size_t tb = (size_t)t * SPLAT_TILE * (T.d + 1);
             const uint16_t *locs = T.staged ? reinterpret_cast<const uint16_t *>(smem + T.sm_loc) : T.tl_loc + tb;
             const float *ws = T.staged ? reinterpret_cast<const float *>(smem + T.sm_w) : T.tl_w + tb;
@@ -391,75 +468,93 @@ __global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_c
             const bool rows_smem = T.staged && b.vp_staged;
             const float alpha = T.alpha;
             for (int r = 0; r <= T.d; r++) {
-                const int loc = locs[r * SPLAT_TILE + li];
-                const float bw = ws[r * SPLAT_TILE + li];
-                float v[MP];
+                const int loc = locs[r * SPLAT_TILE + pi];
+                const float bw = ws[r * SPLAT_TILE + pi];
+                float v[H];
                 if (rows_smem)
-                    load_row_s<MP>(vps + loc * MP, v);
+                    load_row_s<H>(vps + loc * MP + l0, v);
                 else
-                    load_row<MP>(T.pv + (size_t)(b.pb + loc) * MP, v);
+                    load_row<H>(T.pv + (size_t)(b.pb + loc) * MP + l0, v);
                 if (T.seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fmaf(fmul(bw, v[m]), alpha, acc[m]);
+                    for (int e = 0; e < H; e++) acc[e] = fmaf(fmul(bw, v[e]), alpha, acc[e]);
                 } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
                     const float w = fmul(bw, alpha);
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fmaf(w, v[m], acc[m]);
+                    for (int e = 0; e < H; e++) acc[e] = fmaf(w, v[e], acc[e]);
                 }
             }
             if (T.post_norm) {
-                const float nn = T.staged ? reinterpret_cast<const float *>(smem + T.sm_norm)[li] : T.norm[s];
+                const float nn = T.staged ? reinterpret_cast<const float *>(smem + T.sm_norm)[pi] : T.norm[s];
 #pragma unroll
-                for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
+                for (int e = 0; e < H; e++) acc[e] = fmul(acc[e], nn);
             }
             // with given marginals this is the pairwise part of klDivergence
             // (densecrf.cpp:229-233): sum Q * compat(K Q)
-            fold_compat<MP>(T, T.sm_cmp >= 0 ? reinterpret_cast<const float *>(smem + T.sm_cmp) : nullptr, acc, x, M,
-                            given, kl);
+            fold_compat_h<MP, S>(T, T.sm_cmp >= 0 ? reinterpret_cast<const float *>(smem + T.sm_cmp) : nullptr, acc, x,
+                              M, l0, h, pm, given, kl);
         }
     }
-    if (valid && !given) {  // softmax (densecrf.cpp:98-106)
-        float mx = x[0];
+    if (valid && !given) {  // softmax over the point's labels (densecrf.cpp:98-106)
+        float mx = -INFINITY;
 #pragma unroll
-        for (int m = 1; m < MP; m++)
-            if (m < M) mx = fmaxf(mx, x[m]);
-        float sum = 0.f;
+        for (int e = 0; e < H; e++)
+            if (l0 + e < M) mx = fmaxf(mx, x[e]);
+        if constexpr (SPLIT == 2) mx = fmaxf(mx, __shfl_xor_sync(pm, mx, 1));
+        float part = 0.f;
 #pragma unroll
-        for (int m = 0; m < MP; m++)
-            if (m < M) {
-                x[m] = expf(fsub(x[m], mx));
-                sum = fadd(sum, x[m]);
+        for (int e = 0; e < H; e++)
+            if (l0 + e < M) {
+                x[e] = expf(fsub(x[e], mx));
+                part = fadd(part, x[e]);
             }
+        float sum = part;
+        if constexpr (SPLIT == 2) {
+            // one sum in label order, as with one thread per point: the upper
+            // thread continues from the lower thread's partial sum
+            float full = __shfl_sync(pm, part, lane & ~1);
+            if (h == 1) {
+#pragma unroll
+                for (int e = 0; e < H; e++)
+                    if (l0 + e < M) full = fadd(full, x[e]);
+            }
+            sum = __shfl_sync(pm, full, lane | 1);
+        }
         const float rs = __frcp_rn(sum);
 #pragma unroll
-        for (int m = 0; m < MP; m++) x[m] = m < M ? fmul(x[m], rs) : 0.f;
+        for (int e = 0; e < H; e++) x[e] = l0 + e < M ? fmul(x[e], rs) : 0.f;
     }
-    float(&q)[MP] = x;
+    float(&q)[H] = x;
     if (valid) {
         if (mode & PP_KL) {
             // entropy and unary parts (densecrf.cpp:216-226); log() there is the double overload
-            float u[MP];
+            float u[H];
 #pragma unroll
-            for (int m = 0; m < MP; m++) u[m] = 0.f;
-            if (a.U) load_row<MP>(a.U + s * MP, u);
+            for (int e = 0; e < H; e++) u[e] = 0.f;
+            if (a.U) load_row<H>(a.U + s * MP + l0, u);
 #pragma unroll
-            for (int m = 0; m < MP; m++)
-                if (m < M) {
-                    kl += (double)q[m] * log((double)fmaxf(q[m], 1e-20f));
-                    kl += (double)fmul(u[m], q[m]);
+            for (int e = 0; e < H; e++)
+                if (l0 + e < M) {
+                    kl += (double)q[e] * log((double)fmaxf(q[e], 1e-20f));
+                    kl += (double)fmul(u[e], q[e]);
                 }
         }
-        if (mode & PP_WRITE_Q) store_row<MP>(a.Qout + s * MP, q);
+        if (mode & PP_WRITE_Q) store_row<H>(a.Qout + s * MP + l0, q);
         if (mode & PP_MAP) {  // first maximum (densecrf.cpp:132-137)
-            int best = 0;
+            int best = l0;
             float bv = q[0];
 #pragma unroll
-            for (int m = 1; m < MP; m++)
-                if (m < M && q[m] > bv) {
-                    bv = q[m];
-                    best = m;
+            for (int e = 1; e < H; e++)
+                if (l0 + e < M && q[e] > bv) {
+                    bv = q[e];
+                    best = l0 + e;
                 }
-            a.map_out[i] = (int16_t)best;
+            if constexpr (SPLIT == 2) {
+                const float ov = __shfl_xor_sync(pm, bv, 1);
+                const int ob = __shfl_xor_sync(pm, best, 1);
+                if (h == 0 && ob < M && ov > bv) best = ob;
+            }
+            if (h == 0) a.map_out[i] = (int16_t)best;
         }
     }
     if (mode & PP_KL) {
@@ -469,7 +564,7 @@ __global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_c
         __syncthreads();
         if (li == 0) {
             double ssum = 0.0;
-            for (int w = 0; w < SPLAT_TILE / 32; w++) ssum += sKL[w];
+            for (int w = 0; w < NT / 32; w++) ssum += sKL[w];
             a.kl_part[t] = ssum;
         }
     }
@@ -482,7 +577,7 @@ __global__ void __launch_bounds__(SPLAT_TILE, 2) pointpass_kernel(const __grid_c
         float *sQ = reinterpret_cast<float *>(smem + a.sm_q);
         float *sRes = reinterpret_cast<float *>(smem + a.sm_res);
         __syncthreads();  // the message phase is done with the regions sQ aliases
-        store_row<MP>(sQ + li * MP, q);
+        store_row<H>(sQ + pi * MP + l0, q);
         __syncthreads();
         for (int k = 0; k < a.ts.n; k++) {
             // the normalisation before the filter (pairwise.cpp:65-66) is folded into
@@ -823,20 +918,45 @@ __global__ void scale_members_kernel(const uint16_t *__restrict__ mem_pt, const 
 // ---------------------------------------------------------------------------
 int pointpass_smem_budget(int MP) { return MP <= 20 ? 72 * 1024 : 108 * 1024; }
 
+template <int MP, int S>
+static cudaError_t pp_launch_s(const PPArgs &a, cudaStream_t s) {
+    return launch_pdl(pointpass_kernel<MP, S>, dim3(a.ntiles), dim3(PPT<MP, S>::NT), a.smem_bytes, s, a);
+}
+
 template <int MP>
 static cudaError_t pp_launch(const PPArgs &a, cudaStream_t s) {
     if (a.ntiles <= 0) return cudaSuccess;
     if (a.mode & (PP_NORM | PP_FILTER)) {
         DCRF_LAUNCH(slice_kernel<MP><<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
-    } else {
-        return launch_pdl(pointpass_kernel<MP>, dim3(a.ntiles), dim3(SPLAT_TILE), a.smem_bytes, s, a);
+        return cudaGetLastError();
     }
-    return cudaGetLastError();
+    if constexpr (MP % 8 == 0) {
+        if (a.split == 2) return pp_launch_s<MP, 2>(a, s);
+    }
+    return pp_launch_s<MP, 1>(a, s);
+}
+
+// Opts a point-pass instance into the largest dynamic shared memory a CTA can
+// have next to its static shared memory; each launch asks for what its plan needs.
+template <typename K>
+static void pp_optin(K kernel) {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, kernel) != cudaSuccess || optin <= 0) {
+        cudaGetLastError();
+        return;
+    }
+    const int dyn = std::min<int>(POINTPASS_SMEM_MAX, optin - (int)fa.sharedSizeBytes);
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn) != cudaSuccess)
+        cudaGetLastError();
 }
 
 template <int MP>
 static void pp_prepare() {
-    cudaFuncSetAttribute(pointpass_kernel<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize, pointpass_smem_budget(MP));
+    pp_optin(pointpass_kernel<MP, 1>);
+    if constexpr (MP % 8 == 0) pp_optin(pointpass_kernel<MP, 2>);
 }
 
 void prepare_pointpass_kernels() {

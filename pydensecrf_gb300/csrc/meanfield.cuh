@@ -29,6 +29,7 @@ struct PPArgs {
     double *kl_part;     // [ntiles]
     DevStatus *status;
     int smem_bytes;      // dynamic shared memory of the point pass
+    int split;           // threads per point of the point pass (1, or 2 when MP % 8 == 0)
     int sm_q;            // offset of the splat's q rows (aliases the slice-phase regions)
     int sm_res;          // offset of the splat's per-task results (after the q rows)
     // PP_FILTER epilogue (adjoint): with F the raw filter of term 0 and
@@ -93,6 +94,8 @@ cudaError_t launch_scale_members(const uint16_t *mem_pt, const float *mem_w, con
 // Opts every point-pass instantiation in to its dynamic shared-memory budget.
 void prepare_pointpass_kernels();
 // Largest dynamic shared memory the point pass may use per CTA.
+// default shared-memory budget of a point-pass CTA (two CTAs per SM)
 int pointpass_smem_budget(int MP);
+constexpr int POINTPASS_SMEM_MAX = 224 * 1024;  // dynamic shared memory a point-pass CTA may plan
 
 }  // namespace dcrf

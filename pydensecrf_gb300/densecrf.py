@@ -220,6 +220,26 @@ class DenseCRF:
         _lib.check(_lib.load().dcrf_map(self._h, int(niter), _ptr(out), _lib.HOST))
         return out
 
+    # -- autotuning (no reference counterpart) -----------------------------------
+    def set_autotune(self, on: bool = True) -> None:
+        """Tune the engine's launch and build knobs at the first inference of
+        every new configuration (remembered for the process)."""
+        _lib.check(_lib.load().dcrf_set_autotune(self._h, int(bool(on))))
+
+    def autotune(self) -> dict:
+        """Tune now for the current pairwise terms; returns the chosen knobs."""
+        _lib.check(_lib.load().dcrf_autotune(self._h))
+        return self.tuning()
+
+    def tuning(self) -> dict:
+        sp, sm, tk, hl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        _lib.check(_lib.load().dcrf_get_tuning(self._h, ctypes.byref(sp), ctypes.byref(sm), ctypes.byref(tk),
+                                               ctypes.byref(hl)))
+        return {"split": sp.value, "smem_kb": sm.value, "task_len": tk.value, "hash_load": hl.value}
+
+    def set_tuning(self, split: int = 0, smem_kb: int = 0, task_len: int = 16, hash_load: float = 2.0) -> None:
+        _lib.check(_lib.load().dcrf_set_tuning(self._h, int(split), int(smem_kb), int(task_len), float(hash_load)))
+
     # -- learning (the parameter API and adjoint of densecrf.cpp:238-360) -------
     def setCompatibility(self, term: int, compat) -> None:
         """Replace term ``term``'s label compatibility (Potts number, Diagonal

@@ -124,3 +124,37 @@ def test_batch_shape_errors(engine):
         bt.setUnaryEnergy([np.zeros((3, 32), np.float32), np.zeros((3, 44), np.float32)])
     with pytest.raises(ValueError):
         bt.addPairwiseBilateral(sxy=3, srgb=3, rgbims=[np.zeros((4, 8, 3), np.uint8)] * 2, compat=1)
+
+
+def test_autotune_choices_and_results(engine):
+    """The autotuner's knobs are in range, a handle given the same knobs
+    reproduces the tuned handle exactly, and results stay within 1e-5 of the
+    default knobs (only the splat task length regroups sums)."""
+    rng = np.random.default_rng(14)
+    W, H, M, T = 96, 80, 8, 4
+    img = _images(rng, [(W, H)])[0]
+    U = _unaries(rng, M, [W * H])[0]
+
+    def make():
+        d = engine.DenseCRF2D(W, H, M)
+        d.setUnaryEnergy(U)
+        d.addPairwiseGaussian(sxy=3, compat=3)
+        d.addPairwiseBilateral(sxy=30, srgb=13, rgbim=img, compat=5)
+        return d
+
+    ref = np.array(make().inference(T))
+    tuned = make()
+    knobs = tuned.autotune()
+    assert knobs["split"] in (1, 2) and 8 <= knobs["task_len"] <= 32 and knobs["hash_load"] >= 1.5
+    assert knobs["smem_kb"] > 0
+    Qt = np.array(tuned.inference(T))
+    same = make()
+    same.set_tuning(knobs["split"], knobs["smem_kb"], knobs["task_len"], knobs["hash_load"])
+    assert np.array_equal(np.array(same.inference(T)), Qt)
+    assert np.abs(Qt - ref).max() < 1e-5
+    # automatic mode takes the remembered choice for the same configuration
+    auto = make()
+    auto.set_autotune(True)
+    Qa = np.array(auto.inference(T))
+    assert auto.tuning() == knobs
+    assert np.array_equal(Qa, Qt)
