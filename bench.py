@@ -111,6 +111,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def profiled_traffic():
+    """DRAM bytes (read + write) of one point-pass launch on this workload, from the
+    committed ncu summary (profiles/pointpass_plain_vga.md)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "pointpass_plain_vga.md")) as fh:
+            for line in fh:
+                if line.startswith("traffic_bytes_per_launch:"):
+                    return int(line.split(":")[1])
+    except Exception:
+        pass
+    return None
+
+
 def measured_peak():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
@@ -462,10 +475,11 @@ def run_gpu(args):
     pp_bytes = N * M * 4 + N * 4 + sum(N * (d + 1) * 8 + N * 4 + L * MP * 4 + N * (d + 1) * 6 + P * MP * 4
                                        for d, L, P in zip(d_terms, Ls, Ps))
     peak, peak_kind = measured_peak()
+    traffic = args.traffic if args.traffic is not None else profiled_traffic()
     avg_s = prof["point"]["avg_us"] / 1e6
     achieved = pp_bytes / avg_s / 1e9
     roofline = {"bound": "hbm", "kernel": "pointpass_kernel<24>", "achieved": round(achieved, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3), "traffic": args.traffic,
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3), "traffic": traffic,
                 "algorithmic_bytes_per_launch": int(pp_bytes), "avg_launch_us": round(prof["point"]["avg_us"], 2),
                 "peak_kind": peak_kind}
 
