@@ -17,10 +17,12 @@
 //   5. neighbours thread per (axis, vertex): look up key -1/+1 with +d/-d on
 //                 the axis.
 //   6. tiles      per splat tile (a set of up to SPLAT_TILE points), the
-//                 corners grouped by vertex in point order (block bitonic
-//                 sort): the tile's distinct vertices ("partials"), the member
-//                 lists of the in-kernel splat, and per corner the index of its
-//                 vertex among the tile's partials (the tile-local slice table).
+//                 corners grouped by vertex in corner order without a sort
+//                 (shared-memory hash, first-occurrence numbering, stable
+//                 warp-sequential ranking): the tile's distinct vertices
+//                 ("partials"), the member lists and splat tasks of the
+//                 in-kernel splat, and per corner the index of its vertex among
+//                 the tile's partials (the tile-local slice table).
 //   7. reduce     stable radix sort of the tiles' partials by vertex: the
 //                 order in which a vertex's partial sums are added.
 // Bounded probing everywhere: a full table sets DCRF_ERR_HASH_FULL and the
@@ -345,151 +347,254 @@ __global__ void neighbors_kernel(const uint64_t *__restrict__ keys, const uint32
 
 // Block bitonic sort of one tile's corners by (vertex, corner) and count of
 // distinct vertices.  Corner idx = slot*(D+1) + r of the tile's slot.
+// ---- sort-free tile grouping ---------------------------------------------------
+// A tile's corners c = li*(d+1)+r (point slot li, corner r) are grouped by
+// vertex into "partials" numbered in first-occurrence order; the members of a
+// partial stay in corner order.  tile_group finds the partials with a
+// shared-memory hash (first corner by atomicMin, numbering by a block scan) and
+// counts their members; tile_place, after the tiles' partial and task counts
+// are scanned, lays out the member lists (stable, warp-sequential ranking),
+// the tile-local slice tables and the splat tasks.
+constexpr int TG_THREADS = 256;
+
 template <int D>
-__global__ void __launch_bounds__(256) tile_sort_kernel(const int *__restrict__ off, int N,
-                                                        const int *__restrict__ slot_pt,
-                                                        const int *__restrict__ tile_vbase, int n2max,
-                                                        unsigned long long *__restrict__ sorted,
-                                                        uint32_t *__restrict__ tile_nv) {
-    extern __shared__ unsigned long long s_keys[];
-    __shared__ uint32_t s_cnt;
-    const int t = blockIdx.x;
-    if (threadIdx.x == 0) s_cnt = 0;
-    for (int idx = threadIdx.x; idx < n2max; idx += blockDim.x) {
-        unsigned long long x = ~0ull;
-        if (idx < SPLAT_TILE * (D + 1)) {
-            int li = idx / (D + 1), r = idx - li * (D + 1);
-            int pt = slot_pt[(size_t)t * SPLAT_TILE + li];
-            if (pt >= 0) x = ((unsigned long long)(uint32_t)off[(size_t)r * N + pt] << 16) | (unsigned long long)idx;
-        }
-        s_keys[idx] = x;
-    }
-    __syncthreads();
-    for (int k = 2; k <= n2max; k <<= 1) {
-        for (int j = k >> 1; j > 0; j >>= 1) {
-            for (int i = threadIdx.x; i < n2max; i += blockDim.x) {
-                int ixj = i ^ j;
-                if (ixj > i) {
-                    unsigned long long a = s_keys[i], b = s_keys[ixj];
-                    bool asc = (i & k) == 0;
-                    if ((a > b) == asc) {
-                        s_keys[i] = b;
-                        s_keys[ixj] = a;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-    }
-    const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
-    const size_t base = (size_t)t * SPLAT_TILE * (D + 1);
-    uint32_t cnt = 0;
-    for (int idx = threadIdx.x; idx < n; idx += blockDim.x) {
-        unsigned long long x = s_keys[idx];
-        sorted[base + idx] = x;
-        if (idx == 0 || (x >> 16) != (s_keys[idx - 1] >> 16)) cnt++;
-    }
-    atomicAdd(&s_cnt, cnt);
-    __syncthreads();
-    if (threadIdx.x == 0) tile_nv[t] = s_cnt;
+struct TG {
+    static constexpr int C = SPLAT_TILE * (D + 1);      // corners of a tile
+    static constexpr int HT = C <= 1024 ? 2048 : C <= 2048 ? 4096 : C <= 4096 ? 8192 : 16384;
+    static constexpr int PER = C / TG_THREADS;          // corners per thread (d+1)
+};
+
+__device__ __forceinline__ uint32_t tg_hash(uint32_t v) {
+    v ^= v >> 16;
+    v *= 0x7feb352dU;
+    v ^= v >> 15;
+    v *= 0x846ca68bU;
+    v ^= v >> 16;
+    return v;
 }
 
 template <int D>
-__global__ void __launch_bounds__(256) tile_fill_kernel(const unsigned long long *__restrict__ sorted,
-                                                        const float *__restrict__ bary, int N,
-                                                        const int *__restrict__ slot_pt,
-                                                        const int *__restrict__ tile_vbase,
-                                                        const uint32_t *__restrict__ tile_pbeg,
-                                                        int *__restrict__ part_v, int *__restrict__ part_mend,
-                                                        uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
-                                                        uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w) {
-    __shared__ uint32_t s_warp[8];
-    const int t = blockIdx.x;
-    const int n = (tile_vbase[t + 1] - tile_vbase[t]) * (D + 1);
-    const size_t base = (size_t)t * SPLAT_TILE * (D + 1);
-    const int chunk = (n + blockDim.x - 1) / blockDim.x;
-    const int i0 = min(n, (int)threadIdx.x * chunk), i1 = min(n, i0 + chunk);
-    uint32_t cnt = 0;
-    for (int idx = i0; idx < i1; idx++)
-        if (idx == 0 || (sorted[base + idx] >> 16) != (sorted[base + idx - 1] >> 16)) cnt++;
-    // block exclusive scan of cnt
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = cnt;
+__global__ void __launch_bounds__(TG_THREADS) tile_group_kernel(const int *__restrict__ off, int N,
+                                                               const int *__restrict__ slot_pt, int task_len,
+                                                               uint16_t *__restrict__ cl, int *__restrict__ pvx,
+                                                               int *__restrict__ pcnt, uint32_t *__restrict__ tile_np,
+                                                               uint32_t *__restrict__ tile_nt,
+                                                               uint32_t *__restrict__ maxes, DevStatus *st) {
+    constexpr int C = TG<D>::C, HT = TG<D>::HT, PER = TG<D>::PER;
+    extern __shared__ int tg_smem[];
+    int *hkey = tg_smem;            // [HT] vertex id or -1
+    int *hfirst = hkey + HT;        // [HT] first corner of the vertex, then its partial id
+    int *cnt = hfirst + HT;         // [C] members per partial
+    __shared__ int swarp[TG_THREADS / 32];
+    __shared__ uint32_t s_np, s_nt;
+    const int t = blockIdx.x, tid = threadIdx.x;
+    for (int e = tid; e < HT; e += TG_THREADS) {
+        hkey[e] = -1;
+        hfirst[e] = 0x7FFFFFFF;
+    }
+    for (int e = tid; e < C; e += TG_THREADS) cnt[e] = 0;
+    if (tid == 0) s_nt = 0;
+    __syncthreads();
+    // 1. insert this thread's corners c = tid*PER + k (point li = tid, corners in order)
+    int vtx[PER], hs[PER];
+    const int pt = slot_pt[(size_t)t * SPLAT_TILE + tid];
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        vtx[k] = pt >= 0 ? off[(size_t)k * N + pt] : -1;
+        hs[k] = -1;
+        if (vtx[k] < 0) continue;
+        uint32_t h = tg_hash((uint32_t)vtx[k]) & (HT - 1);
+        for (int probe = 0; probe < HT; probe++, h = (h + 1) & (HT - 1)) {
+            const int prev = atomicCAS(hkey + h, -1, vtx[k]);
+            if (prev == -1 || prev == vtx[k]) {
+                hs[k] = (int)h;
+                break;
+            }
+        }
+        if (hs[k] < 0) {  // cannot happen (HT >= 2 C); reported rather than assumed
+            dcrf_set_error(st, DCRF_ERR_HASH_FULL, t);
+            continue;
+        }
+        atomicMin(hfirst + hs[k], tid * PER + k);
+    }
+    __syncthreads();
+    // 2. number the first occurrences in corner order (block exclusive scan)
+    int nf = 0;
+#pragma unroll
+    for (int k = 0; k < PER; k++) nf += (hs[k] >= 0 && hfirst[hs[k]] == tid * PER + k) ? 1 : 0;
+    const int lane = tid & 31, warp = tid >> 5;
+    int x = nf;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    if (lane == 31) s_warp[warp] = x;
+    if (lane == 31) swarp[warp] = x;
     __syncthreads();
-    uint32_t before = 0;
-    for (int w = 0; w < warp; w++) before += s_warp[w];
-    const uint32_t pbeg = tile_pbeg[t];
-    uint32_t run = pbeg + before + x - cnt;
-    for (int idx = i0; idx < i1; idx++) {
-        unsigned long long s = sorted[base + idx];
-        int el = (int)(s & 0xFFFFull);
-        int li = el / (D + 1), r = el - li * (D + 1);
-        const float w = bary[(size_t)r * N + slot_pt[(size_t)t * SPLAT_TILE + li]];
-        mem_pt[base + idx] = (uint16_t)li;
-        mem_w[base + idx] = w;
-        if (idx == 0 || (s >> 16) != (sorted[base + idx - 1] >> 16)) {
-            part_v[run] = (int)(s >> 16);
+    int before = 0;
+    for (int w = 0; w < warp; w++) before += swarp[w];
+    if (tid == TG_THREADS - 1) s_np = (uint32_t)(before + x);
+    int run = before + x - nf;
+    int firstp[PER];
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        firstp[k] = -1;
+        if (hs[k] >= 0 && hfirst[hs[k]] == tid * PER + k) {
+            firstp[k] = run;
+            pvx[(size_t)t * C + run] = vtx[k];
             run++;
         }
-        if (idx == n - 1 || (s >> 16) != (sorted[base + idx + 1] >> 16)) part_mend[run - 1] = idx + 1;
-        const size_t tl = ((size_t)t * (D + 1) + r) * SPLAT_TILE + li;
-        tl_loc[tl] = (uint16_t)(run - 1 - pbeg);
-        tl_w[tl] = w;
+    }
+    __syncthreads();  // every first corner has been identified: hfirst becomes the partial id
+#pragma unroll
+    for (int k = 0; k < PER; k++)
+        if (firstp[k] >= 0) hfirst[hs[k]] = firstp[k];
+    __syncthreads();
+    // 3. each corner's partial; members per partial
+#pragma unroll
+    for (int k = 0; k < PER; k++) {
+        uint16_t p = 0xFFFF;
+        if (hs[k] >= 0) {
+            p = (uint16_t)hfirst[hs[k]];
+            atomicAdd(cnt + p, 1);
+        }
+        cl[(size_t)t * C + tid * PER + k] = p;
+    }
+    __syncthreads();
+    const int np = (int)s_np;
+    uint32_t ntask = 0;
+    for (int p = tid; p < np; p += TG_THREADS) {
+        const int c = cnt[p];
+        pcnt[(size_t)t * C + p] = c;
+        ntask += (uint32_t)((c + task_len - 1) / task_len);
+    }
+    atomicAdd(&s_nt, ntask);
+    __syncthreads();
+    if (tid == 0) {
+        tile_np[t] = (uint32_t)np;
+        tile_nt[t] = s_nt;
+        atomicMax(maxes + 0, (uint32_t)np);
+        atomicMax(maxes + 1, s_nt);
     }
 }
 
-// Splat tasks of one tile: each partial's member run split into pieces of at
-// most task_len members.  Pass 0 counts, pass 1 writes.
-__global__ void __launch_bounds__(256) tile_tasks_kernel(const int *__restrict__ tile_pbeg,
-                                                         const int *__restrict__ part_mend, int pass,
-                                                         uint32_t *__restrict__ tile_nt, const uint32_t *tile_tbeg,
-                                                         uint32_t *__restrict__ task, int task_len) {
-    __shared__ uint32_t s_warp[8];
-    const int t = blockIdx.x;
-    const int pb = tile_pbeg[t], np = tile_pbeg[t + 1] - pb;
-    const int chunk = (np + blockDim.x - 1) / blockDim.x;
-    const int j0 = min(np, (int)threadIdx.x * chunk), j1 = min(np, j0 + chunk);
-    uint32_t cnt = 0;
-    for (int j = j0; j < j1; j++) {
-        const int b = j == 0 ? 0 : part_mend[pb + j - 1], e = part_mend[pb + j];
-        cnt += (uint32_t)((e - b + task_len - 1) / task_len);
-    }
+// Block exclusive scan of v over 256 threads; returns the prefix, *total the sum.
+__device__ __forceinline__ int block_exscan256(int v, int *swarp, int *total) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    uint32_t x = cnt;
+    int x = v;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
         if (lane >= o) x += y;
     }
-    if (lane == 31) s_warp[warp] = x;
     __syncthreads();
-    if (pass == 0) {
-        if (threadIdx.x == 0) {
-            uint32_t tot = 0;
-            for (int w = 0; w < 8; w++) tot += s_warp[w];
-            tile_nt[t] = tot;
-        }
-        return;
+    if (lane == 31) swarp[warp] = x;
+    __syncthreads();
+    int before = 0, all = 0;
+    for (int w = 0; w < TG_THREADS / 32; w++) {
+        if (w < warp) before += swarp[w];
+        all += swarp[w];
     }
-    uint32_t before = 0;
-    for (int w = 0; w < warp; w++) before += s_warp[w];
-    uint32_t out = tile_tbeg[t] + before + x - cnt;
-    for (int j = j0; j < j1; j++) {
-        const int b = j == 0 ? 0 : part_mend[pb + j - 1], e = part_mend[pb + j];
-        for (int q = b; q < e; q += task_len)
-            task[out++] = ((uint32_t)j << 19) | ((uint32_t)q << 6) | (uint32_t)min(task_len, e - q);
+    *total = all;
+    return before + x - v;
+}
+
+template <int D>
+__global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *__restrict__ cl,
+                                                               const int *__restrict__ pvx,
+                                                               const int *__restrict__ pcnt,
+                                                               const float *__restrict__ bary, int N,
+                                                               const int *__restrict__ slot_pt,
+                                                               const uint32_t *__restrict__ tile_pbeg,
+                                                               const uint32_t *__restrict__ tile_tbeg, int task_len,
+                                                               int *__restrict__ part_v, int *__restrict__ part_mend,
+                                                               uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
+                                                               uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w,
+                                                               uint32_t *__restrict__ task) {
+    constexpr int C = TG<D>::C, PER = TG<D>::PER, NW = TG_THREADS / 32;
+    constexpr int SEG = C / NW;  // corners per warp segment (a multiple of 32)
+    extern __shared__ int tp_smem[];
+    int *moff = tp_smem;            // [C] member offset of each partial
+    int *toff = moff + C;           // [C] task offset of each partial
+    uint16_t *wc = reinterpret_cast<uint16_t *>(toff + C);  // [NW][C] per-warp counts, then bases
+    __shared__ int swarp[NW];
+    const int t = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t pb = tile_pbeg[t], np = tile_pbeg[t + 1] - pb, tb = tile_tbeg[t];
+    const size_t base = (size_t)t * C;
+    // member and task offsets of the partials (partials split among threads in order)
+    const int chunk = ((int)np + TG_THREADS - 1) / TG_THREADS;
+    const int p0 = min((int)np, tid * chunk), p1 = min((int)np, p0 + chunk);
+    int mloc = 0, tloc = 0;
+    for (int p = p0; p < p1; p++) {
+        const int c = pcnt[base + p];
+        mloc += c;
+        tloc += (c + task_len - 1) / task_len;
+    }
+    int mtot, ttot;
+    int mrun = block_exscan256(mloc, swarp, &mtot);
+    int trun = block_exscan256(tloc, swarp, &ttot);
+    for (int p = p0; p < p1; p++) {
+        const int c = pcnt[base + p];
+        moff[p] = mrun;
+        toff[p] = trun;
+        part_v[pb + p] = pvx[base + p];
+        part_mend[pb + p] = mrun + c;  // tile-relative end of the partial's members
+        for (int q = 0; q < c; q += task_len)
+            task[tb + trun++] = ((uint32_t)p << 19) | ((uint32_t)(mrun + q) << 6) | (uint32_t)min(task_len, c - q);
+        mrun += c;
+    }
+    for (int e = tid; e < NW * C; e += TG_THREADS) wc[e] = 0;
+    __syncthreads();
+    // stable member ranks: warps own consecutive corner segments; each warp
+    // counts its segment's corners per partial in order, then ranks them
+    const int s0 = warp * SEG;
+    for (int c0 = s0; c0 < s0 + SEG; c0 += 32) {
+        const uint16_t p = cl[base + c0 + lane];
+        const unsigned peers = __match_any_sync(0xffffffffu, (unsigned)p);
+        if (p != 0xFFFF && (__ffs(peers) - 1) == lane) wc[warp * C + p] += (uint16_t)__popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    for (int p = tid; p < (int)np; p += TG_THREADS) {  // per partial: exclusive prefix over the warps
+        int acc = 0;
+        for (int w = 0; w < NW; w++) {
+            const int c = wc[w * C + p];
+            wc[w * C + p] = (uint16_t)acc;
+            acc += c;
+        }
+    }
+    __syncthreads();
+    const unsigned lt = (1u << lane) - 1u;
+    for (int c0 = s0; c0 < s0 + SEG; c0 += 32) {
+        const int c = c0 + lane;
+        const uint16_t p = cl[base + c];
+        const unsigned peers = __match_any_sync(0xffffffffu, (unsigned)p);
+        if (p != 0xFFFF) {
+            const int li = c / (D + 1), r = c - li * (D + 1);
+            const int pos = moff[p] + (int)wc[warp * C + p] + __popc(peers & lt);
+            const float w = bary[(size_t)r * N + slot_pt[(size_t)t * SPLAT_TILE + li]];
+            mem_pt[base + pos] = (uint16_t)li;
+            mem_w[base + pos] = w;
+            const size_t tl = ((size_t)t * (D + 1) + r) * SPLAT_TILE + li;
+            tl_loc[tl] = p;
+            tl_w[tl] = w;
+        }
+        __syncwarp();
+        if (p != 0xFFFF && (__ffs(peers) - 1) == lane) wc[warp * C + p] += (uint16_t)__popc(peers);
+        __syncwarp();
     }
 }
 
-__global__ void count_kernel(const int *__restrict__ part_v, int P, uint32_t *__restrict__ cnt) {
+
+// Partials per vertex; a vertex id outside [0, L) is reported, never used as an index.
+__global__ void count_kernel(const int *__restrict__ part_v, int P, int L, uint32_t *__restrict__ cnt, DevStatus *st) {
     int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < P) atomicAdd(&cnt[part_v[p]], 1u);
+    if (p >= P) return;
+    const int v = part_v[p];
+    if (v >= 0 && v < L)
+        atomicAdd(&cnt[v], 1u);
+    else
+        dcrf_set_error(st, DCRF_ERR_CUDA, p);
 }
 
 __global__ void iota_kernel(uint32_t *__restrict__ a, int n) {
@@ -639,82 +744,79 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     if (L.L > 0)
         DCRF_LAUNCH(neighbors_kernel<D><<<ceil_div_u((size_t)L.L * (D + 1), 256), 256, 0, s>>>(keys, table, (uint32_t)(cap - 1),
                                                                                   vid, L.vkeys, L.L, L.nbr));
-    // ---- splat tiles --------------------------------------------------------
+    // ---- splat tiles: partials, member lists, slice tables, tasks ----------------
     L.ntiles = tm.ntiles;
     L.tile_pbeg = dalloc<int>(L.ntiles + 1, s, &acc);
+    L.tile_tbeg = dalloc<int>(L.ntiles + 1, s, &acc);
     const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
     L.mem_pt = dalloc<uint16_t>(ntl, s, &acc);
     L.mem_w = dalloc<float>(ntl, s, &acc);
     L.tl_loc = dalloc<uint16_t>(ntl, s, &acc);
     L.tl_w = dalloc<float>(ntl, s, &acc);
-    unsigned long long *sorted = tmp.get<unsigned long long>(ntl);
-    uint32_t *tile_nv = tmp.get<uint32_t>(L.ntiles + 1);
-    uint32_t *d_P = tmp.get<uint32_t>(4);
-    if (!L.tile_pbeg || !L.mem_pt || !L.mem_w || !L.tl_loc || !L.tl_w || tmp.failed)
+    uint16_t *cl = tmp.get<uint16_t>(ntl);
+    int *pvx = tmp.get<int>(ntl);
+    int *pcnt = tmp.get<int>(ntl);
+    uint32_t *tile_np = tmp.get<uint32_t>(L.ntiles + 1);
+    uint32_t *tile_nt = tmp.get<uint32_t>(L.ntiles + 1);
+    uint32_t *maxes = tmp.get<uint32_t>(4);
+    if (!L.tile_pbeg || !L.tile_tbeg || !L.mem_pt || !L.mem_w || !L.tl_loc || !L.tl_w || tmp.failed)
         return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
     // empty slots and padding: local index 0, weight 0
     cudaMemsetAsync(L.tl_loc, 0, ntl * sizeof(uint16_t), s);
     cudaMemsetAsync(L.tl_w, 0, ntl * sizeof(float), s);
     cudaMemsetAsync(L.mem_pt, 0, ntl * sizeof(uint16_t), s);
     cudaMemsetAsync(L.mem_w, 0, ntl * sizeof(float), s);
-    int n2max = 1;
-    while (n2max < SPLAT_TILE * (D + 1)) n2max <<= 1;
-    size_t smem = (size_t)n2max * sizeof(unsigned long long);
-    if (smem > 48 * 1024) cudaFuncSetAttribute(tile_sort_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaMemsetAsync(maxes, 0, 4 * sizeof(uint32_t), s);
+    const size_t smem_g = (2 * (size_t)TG<D>::HT + TG<D>::C) * sizeof(int);
+    const size_t smem_p = 2 * (size_t)TG<D>::C * sizeof(int) + (TG_THREADS / 32) * (size_t)TG<D>::C * sizeof(uint16_t);
+    // opt in to the exact dynamic shared memory (the 48 KB default leaves no room for the
+    // kernels' static shared memory at d = 7, where smem_p is exactly 48 KB)
+    if (cudaFuncSetAttribute(tile_group_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g) !=
+            cudaSuccess ||
+        cudaFuncSetAttribute(tile_place_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p) !=
+            cudaSuccess)
+        return bail(DCRF_ERR_CUDA, "tile kernels: shared-memory opt-in failed");
+    uint32_t hcnt[4] = {0, 0, 0, 0};  // P, T, max partials, max tasks of a tile
     if (L.ntiles > 0) {
-        DCRF_LAUNCH(tile_sort_kernel<D><<<L.ntiles, 256, smem, s>>>(L.off, N, tm.slot_pt, tm.tile_vbase, n2max, sorted, tile_nv));
-        if (scan_exclusive_u32(tile_nv, (uint32_t *)L.tile_pbeg, L.ntiles, d_P, stemp, s) != cudaSuccess)
+        DCRF_LAUNCH(tile_group_kernel<D><<<L.ntiles, TG_THREADS, smem_g, s>>>(L.off, N, tm.slot_pt, task_len, cl, pvx,
+                                                                             pcnt, tile_np, tile_nt, maxes, status));
+        // a launch that did not start must not leave its outputs to the next kernels
+        if ((ce = cudaGetLastError()) != cudaSuccess)
+            return bail(DCRF_ERR_CUDA, std::string("tile grouping launch: ") + cudaGetErrorString(ce));
+        if (scan_exclusive_u32(tile_np, (uint32_t *)L.tile_pbeg, L.ntiles, (uint32_t *)L.tile_pbeg + L.ntiles, stemp,
+                               s) != cudaSuccess ||
+            scan_exclusive_u32(tile_nt, (uint32_t *)L.tile_tbeg, L.ntiles, (uint32_t *)L.tile_tbeg + L.ntiles, stemp,
+                               s) != cudaSuccess)
             return bail(DCRF_ERR_CUDA, "scan failed");
-    }
-    uint32_t hP = 0;
-    std::vector<uint32_t> hpbeg(L.ntiles + 1, 0);
-    if (L.ntiles > 0) {
-        cudaMemcpyAsync(&hP, d_P, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(hpbeg.data(), L.tile_pbeg, sizeof(uint32_t) * L.ntiles, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hcnt, L.tile_pbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hcnt + 1, L.tile_tbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hcnt + 2, maxes, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
         ce = cudaStreamSynchronize(s);
         if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tiles: ") + cudaGetErrorString(ce));
+        if (hst.code != 0) return bail(hst.code, "lattice tile grouping failed");
+    } else {
+        cudaMemsetAsync(L.tile_pbeg, 0, sizeof(int), s);
+        cudaMemsetAsync(L.tile_tbeg, 0, sizeof(int), s);
     }
-    L.P = (int)hP;
-    hpbeg[L.ntiles] = hP;
-    for (int t = 0; t < L.ntiles; t++) L.max_np = std::max(L.max_np, (int)(hpbeg[t + 1] - hpbeg[t]));
+    L.P = (int)hcnt[0];
+    L.max_np = (int)hcnt[2];
+    L.max_nt = (int)hcnt[3];
     L.part_v = dalloc<int>((size_t)L.P + 1, s, &acc);
     L.part_mend = dalloc<int>((size_t)L.P + 8, s, &acc);
     L.red_beg = dalloc<int>((size_t)L.L + 1, s, &acc);
     L.red_list = dalloc<int>((size_t)L.P + 1, s, &acc);
-    if (!L.part_v || !L.part_mend || !L.red_beg || !L.red_list) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
+    L.task = dalloc<uint32_t>((size_t)hcnt[1] + 8, s, &acc);
+    if (!L.part_v || !L.part_mend || !L.red_beg || !L.red_list || !L.task)
+        return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
     cudaMemsetAsync(L.part_mend, 0, sizeof(int) * ((size_t)L.P + 8), s);
-    DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.tile_pbeg + L.ntiles, L.P));
-    if (L.ntiles > 0)
-        DCRF_LAUNCH(tile_fill_kernel<D><<<L.ntiles, 256, 0, s>>>(sorted, L.bary, N, tm.slot_pt, tm.tile_vbase,
-                                                     (const uint32_t *)L.tile_pbeg, L.part_v, L.part_mend, L.mem_pt,
-                                                     L.mem_w, L.tl_loc, L.tl_w));
-    // ---- splat tasks -----------------------------------------------------------
-    {
-        uint32_t *tile_nt = tmp.get<uint32_t>(L.ntiles + 1);
-        uint32_t *d_T = tmp.get<uint32_t>(4);
-        L.tile_tbeg = dalloc<int>(L.ntiles + 1, s, &acc);
-        if (tmp.failed || !L.tile_tbeg) return bail(DCRF_ERR_OOM, "device allocation failed (tasks)");
-        uint32_t hT = 0;
-        std::vector<uint32_t> htb(L.ntiles + 1, 0);
-        if (L.ntiles > 0) {
-            DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 0, tile_nt, nullptr, nullptr,
-                                                                   task_len));
-            if (scan_exclusive_u32(tile_nt, (uint32_t *)L.tile_tbeg, L.ntiles, d_T, stemp, s) != cudaSuccess)
-                return bail(DCRF_ERR_CUDA, "scan failed");
-            cudaMemcpyAsync(&hT, d_T, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-            cudaMemcpyAsync(htb.data(), L.tile_tbeg, sizeof(uint32_t) * L.ntiles, cudaMemcpyDeviceToHost, s);
-            ce = cudaStreamSynchronize(s);
-            if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tasks: ") + cudaGetErrorString(ce));
-        }
-        htb[L.ntiles] = hT;
-        for (int t = 0; t < L.ntiles; t++) L.max_nt = std::max(L.max_nt, (int)(htb[t + 1] - htb[t]));
-        L.task = dalloc<uint32_t>((size_t)hT + 8, s, &acc);
-        if (!L.task) return bail(DCRF_ERR_OOM, "device allocation failed (tasks)");
-        cudaMemsetAsync(L.task, 0, sizeof(uint32_t) * ((size_t)hT + 8), s);
-        DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.tile_tbeg + L.ntiles, (int)hT));
-        if (L.ntiles > 0)
-            DCRF_LAUNCH(tile_tasks_kernel<<<L.ntiles, 256, 0, s>>>(L.tile_pbeg, L.part_mend, 1, nullptr,
-                                                                   (const uint32_t *)L.tile_tbeg, L.task, task_len));
+    cudaMemsetAsync(L.task, 0, sizeof(uint32_t) * ((size_t)hcnt[1] + 8), s);
+    if (L.ntiles > 0) {
+        DCRF_LAUNCH(tile_place_kernel<D><<<L.ntiles, TG_THREADS, smem_p, s>>>(
+            cl, pvx, pcnt, L.bary, N, tm.slot_pt, (const uint32_t *)L.tile_pbeg, (const uint32_t *)L.tile_tbeg,
+            task_len, L.part_v, L.part_mend, L.mem_pt, L.mem_w, L.tl_loc, L.tl_w, L.task));
+        if ((ce = cudaGetLastError()) != cudaSuccess)
+            return bail(DCRF_ERR_CUDA, std::string("tile placement launch: ") + cudaGetErrorString(ce));
     }
     // ---- reduce lists: partials grouped by vertex, in tile order ------------
     {
@@ -724,7 +826,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         uint32_t *rtemp = tmp.get<uint32_t>(radix_temp_words((size_t)L.P) + scan_temp_words((size_t)L.L + 1));
         if (tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (reduce lists)");
         cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ((size_t)L.L + 1), s);
-        if (L.P > 0) DCRF_LAUNCH(count_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, cnt));
+        if (L.P > 0) DCRF_LAUNCH(count_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, L.L, cnt, status));
         if (scan_exclusive_u32(cnt, (uint32_t *)L.red_beg, (size_t)L.L, (uint32_t *)(L.red_beg + L.L), rtemp, s) !=
             cudaSuccess)
             return bail(DCRF_ERR_CUDA, "scan failed");
@@ -750,6 +852,10 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     if (ce != cudaSuccess) {
         lattice_free(&L, s);
         return fail(DCRF_ERR_CUDA, std::string("lattice build launch: ") + cudaGetErrorString(ce));
+    }
+    if (cudaMemcpy(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost) != cudaSuccess || hst.code != 0) {
+        lattice_free(&L, s);
+        return fail(hst.code ? hst.code : DCRF_ERR_CUDA, "lattice build: inconsistent partial tables");
     }
     L.bytes = acc;
     *out = L;
