@@ -343,7 +343,7 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
     lib.dcrf_launch_count(ctypes.byref(c1))
     batch_launches = c1.value - c0.value
     Qb = Q_all.clone()
-    knobs = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()]
+    knobs = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()]
     _lib.check(lib.dcrf_get_tuning(hb, *[ctypes.byref(k) for k in knobs]))
     lib.dcrf_destroy(hb)
 
@@ -372,7 +372,7 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
             "unit": "MPix*label*iter/s", "batched_launches": int(batch_launches),
             "batched_equals_loop": same,
             "tuning": {"split": knobs[0].value, "smem_kb": knobs[1].value, "task_len": knobs[2].value,
-                       "hash_load": round(knobs[3].value, 2)}}
+                       "hash_load": round(knobs[3].value, 2), "coop_blur": knobs[4].value}}
 
 
 def run_gpu(args):
@@ -443,9 +443,10 @@ def run_gpu(args):
     value = world * args.steps * UNITS_PER_STEP / (total_ms / 1e3)
     launches = int(cnt1.value - cnt0.value)
 
-    tk = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()]
+    tk = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()]
     _lib.check(lib.dcrf_get_tuning(h, *[ctypes.byref(k) for k in tk]))
-    tuning = {"split": tk[0].value, "smem_kb": tk[1].value, "task_len": tk[2].value, "hash_load": round(tk[3].value, 2)}
+    tuning = {"split": tk[0].value, "smem_kb": tk[1].value, "task_len": tk[2].value,
+              "hash_load": round(tk[3].value, 2), "coop_blur": tk[4].value}
 
     # ---- breakdown and roofline: a profiled pass (events around every launch)
     _lib.check(lib.dcrf_set_profiling(h, 1))

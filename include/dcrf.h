@@ -213,7 +213,9 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
 /* ---- autotuning (no reference counterpart) --------------------------------
  * The engine's launch and build knobs -- threads per point of the mean-field
  * point pass (1 or 2), its shared-memory budget per CTA (KB), the splat task
- * length (members per task, 1..63) and the lattice hash-table load factor --
+ * length (members per task, 1..63), the lattice hash-table load factor, and
+ * whether the blur runs all axes in one cooperative launch (1) or one launch
+ * per axis (0) --
  * are picked per configuration (labels, per-term d / compatibility kind /
  * normalisation / arithmetic variant, one image or a batch, size class
  * log2 N) by timing candidates on the handle's own lattices.  Choices are
@@ -226,10 +228,10 @@ int dcrf_set_autotune(dcrf_crf *h, int on);
 /* Tune now for the current terms (rebuilds the lattices while trying). */
 int dcrf_autotune(dcrf_crf *h);
 /* The knobs in effect (any pointer may be NULL). */
-int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float *hash_load);
+int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float *hash_load, int *coop_blur);
 /* Set the knobs (split 0 = rule of thumb, smem_kb 0 = default); rebuilds the
  * lattices when the task length or load factor changes. */
-int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load);
+int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load, int coop_blur);
 
 /* ---- measurement -------------------------------------------------------- */
 

@@ -9,6 +9,21 @@
 
 namespace dcrf {
 
+// A row of MP floats from global memory (float4 loads when MP % 4 == 0).
+template <int MP>
+__device__ __forceinline__ void row_load(const float *__restrict__ p, float (&v)[MP]) {
+    if constexpr (MP % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < MP / 4; c++) {
+            const float4 q = __ldg(reinterpret_cast<const float4 *>(p) + c);
+            v[4 * c] = q.x, v[4 * c + 1] = q.y, v[4 * c + 2] = q.z, v[4 * c + 3] = q.w;
+        }
+    } else {
+#pragma unroll
+        for (int m = 0; m < MP; m++) v[m] = __ldg(p + m);
+    }
+}
+
 // All label-valued buffers here are slot rows [ns][ld] (ld = padded label
 // count); labels m >= M and empty slots are written as 0.
 
@@ -188,6 +203,84 @@ __global__ void fill_kernel(float *__restrict__ y, float v, int M, int ld, int n
     for (int m = 0; m < ld; m++) y[s * ld + m] = m < M ? val : 0.f;
 }
 
+// The normalisation's coefficients of the kernel-parameter gradient
+// (DenseKernel::featureGradient, pairwise.cpp:87-114) in one pass per point:
+//   ys = C Q (times norm when the forward filter starts with the norm)
+//   x1 = sum over labels of c1, with
+//     SYMMETRIC c1 = 1/2 (b . C y + F . C Q) norm^3
+//     AFTER     c1 = (b . C y) norm^2
+//     BEFORE    c1 = (F . C Q) norm^2
+// (y = K_raw [norm] Q, F = K_raw^T x~); the compatibilities are symmetric.
+template <int MP>
+__global__ void __launch_bounds__(256) norm_terms_kernel(const float *__restrict__ b, const float *__restrict__ y,
+                                                         const float *__restrict__ F, const float *__restrict__ Q,
+                                                         const float *__restrict__ norm, int M, int ns, int ntype,
+                                                         int kind, float potts_w, const float *__restrict__ C,
+                                                         float *__restrict__ ys, float *__restrict__ x1) {
+    __shared__ float sC[MP * MP];  // sC[k][m]
+    if (kind == DCRF_COMPAT_MATRIX) {
+        for (int e = threadIdx.x; e < MP * MP; e += blockDim.x) {
+            const int k = e / MP, m = e - k * MP;
+            sC[e] = (k < M && m < M) ? C[m * M + k] : 0.f;
+        }
+        __syncthreads();
+    }
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)ns) return;
+    auto apply = [&](const float (&x)[MP], float (&o)[MP]) {
+        if (kind == DCRF_COMPAT_POTTS) {
+#pragma unroll
+            for (int m = 0; m < MP; m++) o[m] = m < M ? -potts_w * x[m] : 0.f;
+        } else if (kind == DCRF_COMPAT_DIAGONAL) {
+#pragma unroll
+            for (int m = 0; m < MP; m++) o[m] = m < M ? __ldg(C + m) * x[m] : 0.f;
+        } else {
+#pragma unroll
+            for (int m = 0; m < MP; m++) o[m] = 0.f;
+#pragma unroll
+            for (int k = 0; k < MP; k++) {
+                if (k >= M) continue;
+#pragma unroll
+                for (int m = 0; m < MP; m++) o[m] = fmaf(sC[k * MP + m], x[k], o[m]);
+            }
+        }
+    };
+    const float n = norm[s];
+    const bool pre = ntype == DCRF_NORMALIZE_SYMMETRIC || ntype == DCRF_NORMALIZE_BEFORE;
+    float q[MP], cq[MP];
+    row_load<MP>(Q + s * MP, q);
+    apply(q, cq);
+    float out[MP];
+#pragma unroll
+    for (int m = 0; m < MP; m++) out[m] = pre ? cq[m] * n : cq[m];
+#pragma unroll
+    for (int c = 0; c < MP / 4; c++)
+        reinterpret_cast<float4 *>(ys + s * MP)[c] = make_float4(out[4 * c], out[4 * c + 1], out[4 * c + 2], out[4 * c + 3]);
+    if (ntype == DCRF_NO_NORMALIZATION) return;
+    float bb[MP], cy[MP], ff[MP];
+    row_load<MP>(b + s * MP, bb);
+    if (ntype != DCRF_NORMALIZE_BEFORE) {
+        float yy[MP];
+        row_load<MP>(y + s * MP, yy);
+        apply(yy, cy);
+    }
+    if (ntype != DCRF_NORMALIZE_AFTER) row_load<MP>(F + s * MP, ff);
+    float t = 0.f;
+#pragma unroll
+    for (int m = 0; m < MP; m++) {
+        if (m >= M) continue;
+        float c1;
+        if (ntype == DCRF_NORMALIZE_SYMMETRIC)
+            c1 = 0.5f * fmaf(ff[m], cq[m], bb[m] * cy[m]) * (n * n * n);
+        else if (ntype == DCRF_NORMALIZE_AFTER)
+            c1 = bb[m] * cy[m] * (n * n);
+        else
+            c1 = ff[m] * cq[m] * (n * n);
+        t = fadd(t, c1);
+    }
+    x1[s] = t;
+}
+
 // out[s] = sum over labels of x (one value per slot)
 __global__ void row_sum_kernel(const float *__restrict__ x, float *__restrict__ out, int M, int ld, int ns) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -244,35 +337,18 @@ __global__ void sum_parts_kernel(const double *__restrict__ part, int nblk, int 
     if (lane == 0) out[k] = accumulate ? out[k] + t : t;
 }
 
-// A row of MP floats from global memory (float4 loads when MP % 4 == 0).
-template <int MP>
-__device__ __forceinline__ void row_load(const float *__restrict__ p, float (&v)[MP]) {
-    if constexpr (MP % 4 == 0) {
-#pragma unroll
-        for (int c = 0; c < MP / 4; c++) {
-            const float4 q = __ldg(reinterpret_cast<const float4 *>(p) + c);
-            v[4 * c] = q.x, v[4 * c + 1] = q.y, v[4 * c + 2] = q.z, v[4 * c + 3] = q.w;
-        }
-    } else {
-#pragma unroll
-        for (int m = 0; m < MP; m++) v[m] = __ldg(p + m);
-    }
-}
-
 // Feature gradient of the slice (the per-point part of Permutohedral::gradient,
 // permutohedral.cpp:660-690): with V the blurred lattice of one direction and
 // z the contraction values, df[i][j-1] += sum_k z[k] * sf[j-1] * (sm_k - j * ra_j[k]),
 // ra_j = alpha/(d+1) * (V[off[r0]] - V[off[r1]]), r0 = d - rank_j, r1 = r0+1 mod (d+1),
 // sm the running sum of ra_0..ra_{j-1}.
+// Contribution of one (V, z) pair to the point's feature gradient grad[j-1].
 template <int MP>
-__global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
-    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= (size_t)a.nslots) return;
-    const int i = a.slot_pt[s];
-    if (i < 0) return;
+__device__ __forceinline__ void slice_grad_pair(const SliceGradArgs &a, const float *V, const float *zrow, float alpha,
+                                                size_t s, int i, float (&grad)[DCRF_MAX_D]) {
     const int d = a.d, N = a.N, M = a.M;
     float z[MP];
-    row_load<MP>(a.z + s * MP, z);
+    row_load<MP>(zrow + s * MP, z);
 #pragma unroll
     for (int m = 0; m < MP; m++)
         if (m >= M) z[m] = 0.f;
@@ -283,17 +359,31 @@ __global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
         const int r0 = d - (int)a.rank[(size_t)j * N + i];
         const int r1 = r0 + 1 > d ? 0 : r0 + 1;
         float v0[MP], v1[MP];
-        row_load<MP>(a.V + (size_t)(a.off[(size_t)r0 * N + i] + 1) * MP, v0);
-        row_load<MP>(a.V + (size_t)(a.off[(size_t)r1 * N + i] + 1) * MP, v1);
-        float grad = 0.f;
+        row_load<MP>(V + (size_t)(a.off[(size_t)r0 * N + i] + 1) * MP, v0);
+        row_load<MP>(V + (size_t)(a.off[(size_t)r1 * N + i] + 1) * MP, v1);
+        float gj = 0.f;
 #pragma unroll
         for (int m = 0; m < MP; m++) {
-            const float ra = a.alpha * (v0[m] - v1[m]);
-            if (j > 0) grad = fmaf(z[m], a.sf[j - 1] * (sm[m] - (float)j * ra), grad);
+            const float ra = alpha * (v0[m] - v1[m]);
+            if (j > 0) gj = fmaf(z[m], a.sf[j - 1] * (sm[m] - (float)j * ra), gj);
             sm[m] += ra;
         }
-        if (j > 0) a.df[(size_t)i * d + (j - 1)] += grad;
+        if (j > 0) grad[j - 1] += gj;
     }
+}
+
+template <int MP>
+__global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)a.nslots) return;
+    const int i = a.slot_pt[s];
+    if (i < 0) return;
+    float grad[DCRF_MAX_D];
+#pragma unroll
+    for (int j = 0; j < DCRF_MAX_D; j++) grad[j] = 0.f;
+    slice_grad_pair<MP>(a, a.V, a.z, a.alpha, s, i, grad);
+    if (a.V2) slice_grad_pair<MP>(a, a.V2, a.z2, a.alpha2, s, i, grad);
+    for (int j = 0; j < a.d; j++) a.df[(size_t)i * a.d + j] += grad[j];
 }
 
 // Kernel-parameter gradient from the feature gradient: DIAG g[j] = sum_n f[j][n] fg[n][j];
@@ -388,6 +478,22 @@ cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cu
 
 cudaError_t launch_row_sum(const float *x, float *out, int M, int ns, cudaStream_t s) {
     DCRF_LAUNCH(row_sum_kernel<<<blocks(ns), 256, 0, s>>>(x, out, M, pad_labels(M), ns));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_norm_terms(const float *b, const float *y, const float *F, const float *Q, const float *norm,
+                              int M, int ns, int ntype, int kind, float potts_w, const float *C, float *ys,
+                              float *x1, cudaStream_t s) {
+    switch (pad_labels(M)) {
+#define DCRF_NT(X)                                                                                               \
+    case X:                                                                                                      \
+        DCRF_LAUNCH(norm_terms_kernel<X><<<blocks(ns), 256, 0, s>>>(b, y, F, Q, norm, M, ns, ntype, kind, potts_w, \
+                                                                    C, ys, x1));                                 \
+        break;
+        DCRF_NT(4) DCRF_NT(8) DCRF_NT(12) DCRF_NT(16) DCRF_NT(20) DCRF_NT(24) DCRF_NT(28) DCRF_NT(32)
+#undef DCRF_NT
+        default: return cudaErrorInvalidValue;  // M <= 2 takes the unfused path
+    }
     return cudaGetLastError();
 }
 

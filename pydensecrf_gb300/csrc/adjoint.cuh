@@ -13,8 +13,11 @@ struct SliceGradArgs {
     const uint8_t *rank;  // [d+1][N]
     const float *V;       // [L+1][MP] blurred values, vertex order
     const float *z;       // [nslots][MP] contraction values (slot rows)
+    const float *V2;      // optional second (V, z) pair, added in the same pass (null: none)
+    const float *z2;
     float sf[DCRF_MAX_D];
-    float alpha;          // 1/(1+2^-d) / (d+1)
+    float alpha;          // sign / (1+2^-d) / (d+1) for the first pair
+    float alpha2;         // and for the second
     float *df;            // [N][d] accumulated feature gradient
 };
 
@@ -29,6 +32,11 @@ cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const
 cudaError_t launch_add(const float *x, float *y, size_t n, cudaStream_t s);
 cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cudaStream_t s);
 cudaError_t launch_row_sum(const float *x, float *out, int M, int ns, cudaStream_t s);
+// ys = [norm .*] C Q and x1 = sum of the normalisation coefficients c1 per point
+// (see adjoint.cu); labels M > 2 only.
+cudaError_t launch_norm_terms(const float *b, const float *y, const float *F, const float *Q, const float *norm,
+                              int M, int ns, int ntype, int kind, float potts_w, const float *C, float *ys,
+                              float *x1, cudaStream_t s);
 int label_products_blocks(int ns);
 // mode 0: out[m] (+)= sum a[m].*b[m]; mode 1: out[m*M+k] (+)= sum a[m].*b[k]; part: [blocks][K] doubles
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,

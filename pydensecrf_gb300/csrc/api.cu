@@ -122,8 +122,8 @@ struct Term {
     float *compat = nullptr;  // device compat (Diagonal M / Matrix M*M symmetrised)
     float *mem_wn = nullptr;  // splat member weights times the members' norm (forward pre-normalisation)
     float *df = nullptr;      // [N][d] accumulated feature gradient (adjoint)
-    // adjoint work lattices, vertex order with a zero row 0: [L+1][MP] x 3, [L+1] x 3
-    float *bv[3] = {nullptr, nullptr, nullptr};
+    // adjoint work lattices, vertex order with a zero row 0: [L+1][MP] x 9, [L+1] x 3
+    float *bv[9] = {};
     float *b1[3] = {nullptr, nullptr, nullptr};
     bool r1_valid = false;  // b1[2] holds the reverse-blurred splat of ones
     std::vector<float> compat_h;
@@ -137,6 +137,7 @@ struct TuneCfg {
     int smem_kb = 0;         // point-pass shared-memory budget per CTA (0: the default for MP)
     int task = SPLAT_TASK;   // most members of one splat task (lattice build)
     float hash_load = 2.0f;  // hash-table capacity factor (lattice build)
+    int coop = 0;            // blur axes in one cooperative launch (1) or one launch per axis (0)
 };
 
 }  // namespace
@@ -176,9 +177,15 @@ struct dcrf_crf {
     // B of Q_t, each [L_k+1][MP], at ckv + t * ckv_iter + ckv_off[k] (+ (L_k+1)*MP for B)
     float *ckv = nullptr;
     size_t ckv_cap = 0, ckv_iter = 0;
+    // per term with kernel parameters (and a post-normalised forward): the
+    // sliced values y_t = K_raw [norm] Q_t of every iterate, [T][nslots][MP]
+    float *cky = nullptr;
+    size_t cky_cap = 0;
+    std::vector<long long> cky_off;  // per term, -1: not kept
     std::vector<size_t> ckv_off, ckv_layout;
     float *bw[14] = {};     // adjoint work buffers, [nslots][MP] each
     float *bw1[2] = {};     // adjoint work buffers, [nslots] each
+    unsigned *bar = nullptr;  // grid-barrier state of the single-launch blur
     double *dpart = nullptr, *dacc = nullptr;
     size_t dpart_cap = 0, dacc_cap = 0;
     // CUDA graph of the last inference launch sequence (re-used through
@@ -359,6 +366,7 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
     prepare_kernels();
     h->stream = h->own;
     if ((rc = dev_alloc(&h->status, 1))) return fail(rc);
+    if ((rc = dev_alloc(&h->bar, 2))) return fail(rc);
     if ((rc = build_tiles(h))) return fail(rc);
     if ((rc = dev_alloc(&h->U, (size_t)h->nslots * h->MP))) return fail(rc);
     if ((rc = dev_alloc(&h->Q, (size_t)h->nslots * h->MP))) return fail(rc);
@@ -604,6 +612,31 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
         ProfScope ps(h, DCRF_KCLASS_REDUCE);
         CU(launch_reduce(ra, MP, h->stream));
     }
+    if (h->tune.coop) {  // every axis pass of every term in one launch
+        BlurChainArgs ca{};
+        ca.n = (int)which.size();
+        ca.npass = maxd + 1;
+        ca.bar = h->bar;
+        ca.status = h->status;
+        for (size_t k = 0; k < which.size(); k++) {
+            Term &T = h->terms[which[k]];
+            BlurChainArgs::C &c = ca.c[k];
+            c.S = S_out ? S_out[k] : T.V[0];
+            c.buf[0] = T.V[1];
+            c.buf[1] = T.V[0];
+            c.Out = B_out ? B_out[k] : partial_order ? nullptr : T.V[(T.d + 1) & 1];
+            c.nbr = T.lat.nbr;
+            c.L = T.lat.L;
+            c.d = T.d;
+            c.reverse = transpose ? 1 : 0;
+            c.red_beg = T.lat.red_beg;
+            c.red_list = T.lat.red_list;
+            c.pv = partial_order ? T.pv : nullptr;
+        }
+        ProfScope ps(h, DCRF_KCLASS_BLUR);
+        CU(launch_blur_chains(ca, MP, seq, h->stream));
+        return DCRF_OK;
+    }
     const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
     for (int pass = 0; pass <= maxd; pass++) {
         BlurArgs ba{};
@@ -658,10 +691,13 @@ void free_term_lattice(dcrf_crf *h, Term &T) {
     dev_free_async(T.mem_wn, h->stream);
     dev_free_async(T.df, h->stream);
     T.norm = T.V[0] = T.V[1] = T.pv = T.mem_wn = T.df = nullptr;
-    for (int j = 0; j < 3; j++) {
-        dev_free_async(T.bv[j], h->stream);
-        dev_free_async(T.b1[j], h->stream);
-        T.bv[j] = T.b1[j] = nullptr;
+    for (float *&b : T.bv) {
+        dev_free_async(b, h->stream);
+        b = nullptr;
+    }
+    for (float *&b : T.b1) {
+        dev_free_async(b, h->stream);
+        b = nullptr;
     }
     T.r1_valid = false;
     lattice_free(&T.lat, h->stream);
@@ -849,6 +885,9 @@ int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
         int mode = PP_MSG | (it < T ? PP_SPLAT : final_mode) | (ckpt ? PP_WRITE_Q : 0);
         PPArgs a = pp_args(h, mode, w, false, false);
         if (ckpt) a.Qout = ckpt + it * qsz;
+        if (ckpt && h->cky)
+            for (size_t k = 0; k < w.size(); k++)
+                if (h->cky_off[w[k]] >= 0) a.ckY[k] = h->cky + h->cky_off[w[k]] + (size_t)(it - 1) * qsz;
         CU(pp(h, a, h->MP));
     }
     return DCRF_OK;
@@ -946,23 +985,27 @@ int autotune_now(dcrf_crf *h) {
         float best_ms = 1e30f;
         const int splits[2] = {1, 2};
         const int smems[2] = {0, 72};
-        for (int sp : splits) {
-            if (sp == 2 && h->MP % 8 != 0) continue;
-            for (int sm : smems) {
-                h->tune.split = sp;
-                h->tune.smem_kb = sm;
-                float ms = 0.f;
-                if ((rc = time_iterations(h, 2, 3, &ms))) break;
-                if (ms < best_ms) {
-                    best_ms = ms;
-                    best.split = sp;
-                    best.smem_kb = sm;
+        for (int co = 0; co < 2 && !rc; co++)
+            for (int sp : splits) {
+                if (sp == 2 && h->MP % 8 != 0) continue;
+                for (int sm : smems) {
+                    h->tune.split = sp;
+                    h->tune.smem_kb = sm;
+                    h->tune.coop = co;
+                    float ms = 0.f;
+                    if ((rc = time_iterations(h, 2, 3, &ms))) break;
+                    if (ms < best_ms) {
+                        best_ms = ms;
+                        best.split = sp;
+                        best.smem_kb = sm;
+                        best.coop = co;
+                    }
                 }
+                if (rc) break;
             }
-            if (rc) break;
-        }
         h->tune.split = best.split;
         h->tune.smem_kb = best.smem_kb;
+        h->tune.coop = best.coop;
     }
     h->profiling = prof;
     if (rc) return rc;
@@ -1049,16 +1092,16 @@ bool tr_post(const Term &T) { return T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.nt
 int ensure_adjoint_bufs(dcrf_crf *h, Term &T) {
     const size_t rows = (size_t)T.lat.L + 1;
     int rc;
-    for (int j = 0; j < 3; j++) {
-        if (!T.bv[j]) {
-            if ((rc = dev_alloc_async(&T.bv[j], rows * h->MP, h->stream))) return rc;
-            CU(cudaMemsetAsync(T.bv[j], 0, sizeof(float) * rows * h->MP, h->stream));
+    for (float *&b : T.bv)
+        if (!b) {
+            if ((rc = dev_alloc_async(&b, rows * h->MP, h->stream))) return rc;
+            CU(cudaMemsetAsync(b, 0, sizeof(float) * rows * h->MP, h->stream));
         }
-        if (!T.b1[j]) {
-            if ((rc = dev_alloc_async(&T.b1[j], rows, h->stream))) return rc;
-            CU(cudaMemsetAsync(T.b1[j], 0, sizeof(float) * rows, h->stream));
+    for (float *&b : T.b1)
+        if (!b) {
+            if ((rc = dev_alloc_async(&b, rows, h->stream))) return rc;
+            CU(cudaMemsetAsync(b, 0, sizeof(float) * rows, h->stream));
         }
-    }
     return DCRF_OK;
 }
 
@@ -1083,29 +1126,90 @@ int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1) {
     return DCRF_OK;
 }
 
+// Independent blur chains advanced together, one launch per axis pass: chain c
+// blurs S along axes 0..d (d..0 when reverse, permutohedral.cpp:556) through
+// the ping-pong pair b[0], b[1] into Out.  Chains of one launch must not share
+// buffers; chains whose arithmetic flavour differs (scalar build) go in
+// separate launches.
+struct Chain {
+    int k;
+    const float *S;
+    float *b[2];
+    float *Out;
+    bool reverse;
+};
+
+int blur_chains(dcrf_crf *h, const std::vector<Chain> &chains, bool value1) {
+    const int MP = value1 ? 1 : h->MP;
+    const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
+    for (int flavour = 0; flavour < 2; flavour++) {
+        std::vector<const Chain *> cs;
+        for (const Chain &c : chains) {
+            const bool seq = value1 || h->M <= 2 || h->terms[c.k].variant == DCRF_VARIANT_SCALAR;
+            if ((int)seq == flavour) cs.push_back(&c);
+        }
+        for (size_t g0 = 0; g0 < cs.size(); g0 += DCRF_MAX_TERMS) {
+            const size_t g1 = std::min(cs.size(), g0 + DCRF_MAX_TERMS);
+            int maxd = 0;
+            for (size_t q = g0; q < g1; q++) maxd = std::max(maxd, h->terms[cs[q]->k].d);
+            for (int pass = 0; pass <= maxd; pass++) {
+                BlurArgs ba{};
+                ba.n = 0;
+                ba.begin[0] = 0;
+                for (size_t q = g0; q < g1; q++) {
+                    const Chain &c = *cs[q];
+                    const Term &T = h->terms[c.k];
+                    if (pass > T.d) continue;
+                    BlurArgs::T &bt = ba.t[ba.n];
+                    bt.Vin = pass == 0 ? c.S : c.b[(pass - 1) & 1];
+                    bt.Vout = pass == T.d ? c.Out : c.b[pass & 1];
+                    bt.nbr = T.lat.nbr;
+                    bt.L = T.lat.L;
+                    bt.axis = c.reverse ? T.d - pass : pass;
+                    bt.pv = nullptr;
+                    ba.begin[ba.n + 1] = ba.begin[ba.n] + (long long)T.lat.L * NV;
+                    ba.n++;
+                }
+                ProfScope ps(h, DCRF_KCLASS_BLUR);
+                CU(launch_blur(ba, MP, flavour == 1, h->stream));
+            }
+        }
+    }
+    return DCRF_OK;
+}
+
 // Out = the d+1 blur passes of S, axes 0..d or d..0 for the transpose
 // (permutohedral.cpp:556); S is kept, the term's V buffers are the ping-pong.
 int blur_into(dcrf_crf *h, int k, const float *S, float *Out, bool reverse, bool value1) {
     Term &T = h->terms[k];
     const int MP = value1 ? 1 : h->MP;
     const bool seq = value1 || h->M <= 2 || T.variant == DCRF_VARIANT_SCALAR;
-    const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
-    for (int pass = 0; pass <= T.d; pass++) {
-        BlurArgs ba{};
-        ba.n = 1;
-        ba.begin[0] = 0;
-        ba.begin[1] = (long long)T.lat.L * NV;
-        ba.t[0].Vin = pass == 0 ? S : T.V[pass & 1];
-        ba.t[0].Vout = pass == T.d ? Out : T.V[(pass + 1) & 1];
-        ba.t[0].nbr = T.lat.nbr;
-        ba.t[0].L = T.lat.L;
-        ba.t[0].axis = reverse ? T.d - pass : pass;
-        ba.t[0].pv = nullptr;
-        ProfScope ps(h, DCRF_KCLASS_BLUR);
-        CU(launch_blur(ba, MP, seq, h->stream));
+    if (!h->tune.coop) {
+        int rc = blur_chains(h, {Chain{k, S, {T.V[1], T.V[0]}, Out, reverse}}, value1);
+        if (rc) return rc;
+        if (value1) return zero_sentinels(h, T);
+        return DCRF_OK;
     }
-    if (value1) return zero_sentinels(h, T);
-    return DCRF_OK;
+    {
+        BlurChainArgs ca{};
+        ca.n = 1;
+        ca.npass = T.d + 1;
+        ca.bar = h->bar;
+        ca.status = h->status;
+        BlurChainArgs::C &c = ca.c[0];
+        c.S = S;
+        c.buf[0] = T.V[1];
+        c.buf[1] = T.V[0];
+        c.Out = Out;
+        c.nbr = T.lat.nbr;
+        c.L = T.lat.L;
+        c.d = T.d;
+        c.reverse = reverse ? 1 : 0;
+        ProfScope ps(h, DCRF_KCLASS_BLUR);
+        CU(launch_blur_chains(ca, MP, seq, h->stream));
+        if (value1) return zero_sentinels(h, T);
+        return DCRF_OK;
+    }
 }
 
 // out (slot rows) = slice of the vertex rows V (permutohedral.cpp:574-584);
@@ -1126,9 +1230,12 @@ int slice_from(dcrf_crf *h, int k, const float *V, float *out, bool value1, bool
 
 // T.df += sign * sum over labels of z . d(slice of V)/d(features): the
 // per-point part of Permutohedral::gradient (permutohedral.cpp:612-695).
-int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float sign, bool value1) {
+int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float sign, bool value1,
+                    const float *V2 = nullptr, const float *z2 = nullptr, float sign2 = 1.f) {
     Term &T = h->terms[k];
     SliceGradArgs g{};
+    g.V2 = V2;
+    g.z2 = z2;
     g.N = h->N;
     g.M = value1 ? 1 : h->M;
     g.d = T.d;
@@ -1142,6 +1249,7 @@ int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float si
     for (int i = 0; i < T.d; i++)
         g.sf[i] = (float)(1.0 / std::sqrt((double)((i + 2) * (i + 1))) * (double)inv_std_dev);
     g.alpha = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1) * sign;
+    g.alpha2 = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1) * sign2;
     g.df = T.df;
     CU(launch_slice_grad(g, value1 ? 1 : h->MP, h->stream));
     return DCRF_OK;
@@ -1212,12 +1320,14 @@ int dcrf_destroy(dcrf_crf *h) {
     for (Term &T : h->terms) free_term(h, T);
     dev_free_async(h->ckpt, h->stream);
     dev_free_async(h->ckv, h->stream);
+    dev_free_async(h->cky, h->stream);
     for (float *&b : h->bw) dev_free_async(b, h->stream);
     for (float *&b : h->bw1) dev_free_async(b, h->stream);
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
     if (h->stream) cudaStreamSynchronize(h->stream);
     dev_free(h->status);
+    dev_free(h->bar);
     dev_free(h->U);
     dev_free(h->Q);
     dev_free(h->tmp);
@@ -1551,9 +1661,10 @@ int dcrf_autotune(dcrf_crf *h) {
     return ok();
 }
 
-int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float *hash_load) {
+int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float *hash_load, int *coop_blur) {
     int rc = check_handle(h);
     if (rc) return rc;
+    if (coop_blur) *coop_blur = h->tune.coop;
     if (split) *split = pick_split(h, false);
     if (smem_kb) *smem_kb = h->tune.smem_kb > 0 ? h->tune.smem_kb : pointpass_smem_budget(h->MP) / 1024;
     if (task_len) *task_len = h->tune.task;
@@ -1561,12 +1672,14 @@ int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float 
     return ok();
 }
 
-int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load) {
+int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load, int coop_blur) {
     int rc = check_handle(h);
     if (rc) return rc;
-    if (split < 0 || split > 2 || smem_kb < 0 || smem_kb > 224 || task_len < 1 || task_len > 63 || !(hash_load >= 1.f))
+    if (split < 0 || split > 2 || smem_kb < 0 || smem_kb > 224 || task_len < 1 || task_len > 63 ||
+        !(hash_load >= 1.f) || coop_blur < 0 || coop_blur > 1)
         return set_err(DCRF_ERR_INVALID_ARG, "tuning values out of range");
     TuneCfg c;
+    c.coop = coop_blur;
     c.split = split;
     c.smem_kb = smem_kb;
     c.task = task_len;
@@ -1690,6 +1803,25 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
         fresh = true;
     }
     // row 0 of every S and B is the zero sentinel and is never written afterwards
+    // y checkpoints of the terms whose kernel gradient needs them
+    h->cky_off.assign(h->terms.size(), -1);
+    size_t ny = 0;
+    for (size_t k = 0; k < h->terms.size(); k++) {
+        const Term &Tk = h->terms[k];
+        if (Tk.ktype != DCRF_CONST_KERNEL &&
+            (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER)) {
+            h->cky_off[k] = (long long)ny;
+            ny += qsz * (size_t)n_iterations;
+        }
+    }
+    if (ny > h->cky_cap) {
+        dev_free_async(h->cky, h->stream);
+        h->cky = nullptr;
+        h->cky_cap = 0;
+        if ((rc = dev_alloc_async(&h->cky, ny, h->stream))) return rc;
+        h->cky_cap = ny;
+    }
+    if (ny == 0) h->cky_off.assign(h->terms.size(), -1);
     std::vector<size_t> sig = h->ckv_off;
     for (const Term &Tk : h->terms) sig.push_back((size_t)Tk.lat.L);
     if (fresh || h->ckv_layout != sig) CU(cudaMemsetAsync(h->ckv, 0, sizeof(float) * vneed, h->stream));
@@ -1773,22 +1905,41 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
     for (int it = T - 1; it >= 0; it--) {
         const float *Qt = h->ckpt + (size_t)it * qsz;
         CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
+        // x~ = b with the transpose's first normalisation (per term)
+        auto xtilde = [&](Term &Tk) -> const float * {
+            if (!tr_pre(Tk)) return b;
+            if (launch_scale_norm(b, xn, Tk.norm, M, ns, 1, h->stream) != cudaSuccess) return nullptr;
+            return xn;
+        };
+        // phase 1, per term: S_b = splat of x~; for kernel gradients also C S_t.
+        // Then all blur chains of all terms advance together: A = K_raw^T
+        // (reverse) of S_b, B = forward blur of S_b, C = reverse blur of C S_t.
+        std::vector<Chain> chains;
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];
             const size_t rows = (size_t)Tk.lat.L + 1;
             const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];  // forward splat of Q_t
-            const float *Bt = St + rows * h->MP;                                   // and its blurred lattice
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
-            // x~ = b with the transpose's first normalisation; S_b = its splat
-            const float *xs = b;
-            if (tr_pre(Tk)) {
-                CU(launch_scale_norm(b, xn, Tk.norm, M, ns, 1, h->stream));
-                xs = xn;
-            }
+            const float *xs = xtilde(Tk);
+            if (!xs) return set_err(DCRF_ERR_CUDA, "scale launch failed");
             if ((rc = splat_into(h, k, xs, Tk.bv[0], false))) return rc;
-            // F = K_raw^T x~ (reverse blur) and Fp = K^T b = [norm .*] F; g += C^T Fp
+            chains.push_back(Chain{k, Tk.bv[0], {Tk.V[1], Tk.V[0]}, Tk.bv[1], true});
+            if (kgrad) {
+                CU(launch_compat(St, Tk.bv[2], M, (int)rows, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                chains.push_back(Chain{k, Tk.bv[0], {Tk.bv[3], Tk.bv[4]}, Tk.bv[5], false});
+                chains.push_back(Chain{k, Tk.bv[2], {Tk.bv[6], Tk.bv[7]}, Tk.bv[8], true});
+            }
+        }
+        if ((rc = blur_chains(h, chains, false))) return rc;
+        // phase 2, per term: slices and gradient contractions
+        for (int k = 0; k < nt; k++) {
+            Term &Tk = h->terms[k];
+            const size_t rows = (size_t)Tk.lat.L + 1;
+            const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];
+            const float *Bt = St + rows * h->MP;  // the forward's blurred lattice of Q_t
+            const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
+            // F = K_raw^T x~ and Fp = K^T b = [norm .*] F; g += C^T Fp
             // (applyTranspose, pairwise.cpp:179-183; the compatibilities are symmetric)
-            if ((rc = blur_into(h, k, Tk.bv[0], Tk.bv[1], true, false))) return rc;
             const bool need_F =
                 kgrad && (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_BEFORE);
             if ((rc = slice_from(h, k, Tk.bv[1], need_F ? F : nullptr, false, tr_post(Tk), want_compat ? Fn : nullptr,
@@ -1798,41 +1949,57 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
                 CU(launch_label_products(Fn, Qt, M, ns, h->slot_pt, Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0, h->dpart,
                                          h->dacc + coff[k], 1, h->stream));
             }
-            // y = K_raw [norm] Q_t, sliced from the forward's blurred lattice
-            const bool need_y = kgrad && (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER);
-            if (need_y && (rc = slice_from(h, k, Bt, y, false))) return rc;
-            if (kgrad) {  // kernelGradient (pairwise.cpp:202-207) through featureGradient (87-114)
-                CU(launch_compat(Qt, cq, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
-                const float *ys = cq;  // y~ = C Q_t with the forward's first normalisation
-                if (fwd_pre(Tk)) {
-                    CU(launch_scale_norm(cq, yn, Tk.norm, M, ns, 1, h->stream));
-                    ys = yn;
-                }
-                // d/df x~^T K_raw y~: the forward-blurred S_b against y~, and the
-                // reverse-blurred splat of y~ (= C S_t) against x~
-                if ((rc = blur_into(h, k, Tk.bv[0], Tk.bv[1], false, false))) return rc;
-                if ((rc = slice_grad_into(h, k, Tk.bv[1], ys, 1.f, false))) return rc;
-                CU(launch_compat(St, Tk.bv[2], M, (int)rows, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
-                if ((rc = blur_into(h, k, Tk.bv[2], Tk.bv[1], true, false))) return rc;
-                if ((rc = slice_grad_into(h, k, Tk.bv[1], xs, 1.f, false))) return rc;
+            if (!kgrad) continue;
+            // kernelGradient (pairwise.cpp:202-207) through featureGradient (87-114)
+            // y = K_raw [norm] Q_t: kept by the forward, else sliced from its blurred lattice
+            const bool need_y = Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER;
+            const float *yt = y;
+            if (need_y) {
+                if (h->cky && h->cky_off[k] >= 0)
+                    yt = h->cky + h->cky_off[k] + (size_t)it * qsz;
+                else if ((rc = slice_from(h, k, Bt, y, false)))
+                    return rc;
+            }
+            const float *xs = xtilde(Tk);
+            if (!xs) return set_err(DCRF_ERR_CUDA, "scale launch failed");
+            if (h->MP % 4 == 0) {
+                // y~ = [norm] C Q_t and the normalisation's coefficients in one pass
+                CU(launch_norm_terms(b, yt, F, Qt, Tk.norm, M, ns, Tk.ntype, Tk.ckind, Tk.potts_w, Tk.compat, yn, x1,
+                                     h->stream));
+                // d/df x~^T K_raw y~: the forward-blurred S_b against y~ plus the
+                // reverse-blurred splat of y~ (= C S_t) against x~, in one pass
+                if ((rc = slice_grad_into(h, k, Tk.bv[5], yn, 1.f, false, Tk.bv[8], xs, 1.f))) return rc;
                 if (Tk.ntype != DCRF_NO_NORMALIZATION) {
-                    // - d/df c1^T K_raw 1 with c1 the normalisation's coefficients; the
-                    // contraction with ones reduces to one value per point
-                    if (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC) {
-                        CU(launch_compat(y, fb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
-                        CU(launch_prod(b, fb, F, cq, 0.5f, Tk.norm, 3, c1, M, ns, h->stream));
-                    } else if (Tk.ntype == DCRF_NORMALIZE_AFTER) {
-                        CU(launch_compat(y, fb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
-                        CU(launch_prod(b, fb, nullptr, nullptr, 1.f, Tk.norm, 2, c1, M, ns, h->stream));
-                    } else {
-                        CU(launch_prod(F, cq, nullptr, nullptr, 1.f, Tk.norm, 2, c1, M, ns, h->stream));
-                    }
-                    CU(launch_row_sum(c1, x1, M, ns, h->stream));
                     if ((rc = splat_into(h, k, x1, Tk.b1[0], true))) return rc;
                     if ((rc = blur_into(h, k, Tk.b1[0], Tk.b1[1], false, true))) return rc;
-                    if ((rc = slice_grad_into(h, k, Tk.b1[1], ones1, -1.f, true))) return rc;
-                    if ((rc = slice_grad_into(h, k, Tk.b1[2], x1, -1.f, true))) return rc;
+                    if ((rc = slice_grad_into(h, k, Tk.b1[1], ones1, -1.f, true, Tk.b1[2], x1, -1.f))) return rc;
                 }
+                continue;
+            }
+            const float *y_ = yt;
+            CU(launch_compat(Qt, cq, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+            const float *ys = cq;  // y~ = C Q_t with the forward's first normalisation
+            if (fwd_pre(Tk)) {
+                CU(launch_scale_norm(cq, yn, Tk.norm, M, ns, 1, h->stream));
+                ys = yn;
+            }
+            if ((rc = slice_grad_into(h, k, Tk.bv[5], ys, 1.f, false, Tk.bv[8], xs, 1.f))) return rc;
+            if (Tk.ntype != DCRF_NO_NORMALIZATION) {
+                // - d/df c1^T K_raw 1 with c1 the normalisation's coefficients; the
+                // contraction with ones reduces to one value per point
+                if (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC) {
+                    CU(launch_compat(y_, fb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                    CU(launch_prod(b, fb, F, cq, 0.5f, Tk.norm, 3, c1, M, ns, h->stream));
+                } else if (Tk.ntype == DCRF_NORMALIZE_AFTER) {
+                    CU(launch_compat(y_, fb, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
+                    CU(launch_prod(b, fb, nullptr, nullptr, 1.f, Tk.norm, 2, c1, M, ns, h->stream));
+                } else {
+                    CU(launch_prod(F, cq, nullptr, nullptr, 1.f, Tk.norm, 2, c1, M, ns, h->stream));
+                }
+                CU(launch_row_sum(c1, x1, M, ns, h->stream));
+                if ((rc = splat_into(h, k, x1, Tk.b1[0], true))) return rc;
+                if ((rc = blur_into(h, k, Tk.b1[0], Tk.b1[1], false, true))) return rc;
+                if ((rc = slice_grad_into(h, k, Tk.b1[1], ones1, -1.f, true, Tk.b1[2], x1, -1.f))) return rc;
             }
         }
         // b = -dL/dA_t (densecrf.cpp:290)

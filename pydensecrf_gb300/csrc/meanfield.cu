@@ -484,6 +484,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                     for (int e = 0; e < H; e++) acc[e] = fmaf(w, v[e], acc[e]);
                 }
             }
+            if (a.ckY[k]) store_row<H>(a.ckY[k] + s * MP + l0, acc);
             if (T.post_norm) {
                 const float nn = T.staged ? reinterpret_cast<const float *>(smem + T.sm_norm)[pi] : T.norm[s];
 #pragma unroll
@@ -816,6 +817,120 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
     }
 }
 
+// Bounded grid barrier of a cooperative launch: the last CTA to arrive resets
+// the arrival count and advances the generation; the others wait for the new
+// generation at most ~2^22 polls, then record DCRF_ERR_TIMEOUT and report
+// failure (the caller returns; the barrier of the next launch starts from a
+// cleared state).
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned nblocks, DevStatus *st) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = bar + 1;
+        const unsigned gen = *vgen;
+        __threadfence();
+        const unsigned arrived = atomicAdd(bar, 1u) + 1u;
+        int ok = 1;
+        if (arrived == nblocks) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicAdd(bar + 1, 1u);
+        } else {
+            ok = 0;
+            for (int it = 0; it < (1 << 22); it++) {
+                if (*vgen != gen) {
+                    ok = 1;
+                    break;
+                }
+                if (it > 32) __nanosleep(64);
+            }
+            if (!ok) dcrf_set_error(st, DCRF_ERR_TIMEOUT, (int)blockIdx.x);
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+template <int MP, bool SEQ>
+__global__ void __launch_bounds__(256) blur_chains_kernel(const __grid_constant__ BlurChainArgs a) {
+    constexpr int VEC = (MP % 4 == 0) ? 4 : (MP % 2 == 0) ? 2 : 1;
+    constexpr int NV = MP / VEC;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int p = 0; p < a.npass; p++) {
+        long long total = 0;
+        for (int k = 0; k < a.n; k++)
+            if (p <= a.c[k].d) total += (long long)a.c[k].L * NV;
+        for (long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x; g < total; g += stride) {
+            int k = 0;
+            long long local = g;
+            for (;; k++) {
+                if (p > a.c[k].d) continue;
+                const long long w = (long long)a.c[k].L * NV;
+                if (local < w) break;
+                local -= w;
+            }
+            const BlurChainArgs::C &C = a.c[k];
+            const int v = (int)(local / NV);
+            const int c = (int)(local - (long long)v * NV);
+            const int axis = C.reverse ? C.d - p : p;
+            const float *Vin = p == 0 ? C.S : C.buf[(p - 1) & 1];
+            const bool last = p == C.d;
+            float *Vout = last ? C.Out : C.buf[p & 1];
+            const int2 nb = __ldg(C.nbr + (size_t)axis * C.L + v);
+            const size_t o0 = (size_t)(v + 1) * MP + c * VEC, o1 = (size_t)nb.x * MP + c * VEC,
+                         o2 = (size_t)nb.y * MP + c * VEC;
+            float x0[VEC], x1[VEC], x2[VEC], y[VEC];
+            // values written by other CTAs in the previous pass: read through L2 (ld.global.cg)
+            if constexpr (VEC == 4) {
+                const float4 q0 = __ldcg(reinterpret_cast<const float4 *>(Vin + o0));
+                const float4 q1 = __ldcg(reinterpret_cast<const float4 *>(Vin + o1));
+                const float4 q2 = __ldcg(reinterpret_cast<const float4 *>(Vin + o2));
+                x0[0] = q0.x, x0[1] = q0.y, x0[2] = q0.z, x0[3] = q0.w;
+                x1[0] = q1.x, x1[1] = q1.y, x1[2] = q1.z, x1[3] = q1.w;
+                x2[0] = q2.x, x2[1] = q2.y, x2[2] = q2.z, x2[3] = q2.w;
+            } else {
+#pragma unroll
+                for (int e = 0; e < VEC; e++) {
+                    x0[e] = __ldcg(Vin + o0 + e);
+                    x1[e] = __ldcg(Vin + o1 + e);
+                    x2[e] = __ldcg(Vin + o2 + e);
+                }
+            }
+#pragma unroll
+            for (int e = 0; e < VEC; e++) {
+                const float sm = fadd(x1[e], x2[e]);
+                if (SEQ)  // seqCompute: old + 0.5*(n1+n2) evaluated in double (permutohedral.cpp:505)
+                    y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)sm));
+                else  // sseCompute: float (permutohedral.cpp:566)
+                    y[e] = fadd(x0[e], fmul(0.5f, sm));
+            }
+            if (Vout) {
+                if constexpr (VEC == 4) {
+                    *reinterpret_cast<float4 *>(Vout + o0) = make_float4(y[0], y[1], y[2], y[3]);
+                } else {
+#pragma unroll
+                    for (int e = 0; e < VEC; e++) Vout[o0 + e] = y[e];
+                }
+            }
+            if (last && C.pv) {
+                const int s0 = C.red_beg[v], s1 = C.red_beg[v + 1];
+                for (int q = s0; q < s1; q++) {
+                    float *dst = C.pv + (size_t)C.red_list[q] * MP + c * VEC;
+                    if constexpr (VEC == 4) {
+                        *reinterpret_cast<float4 *>(dst) = make_float4(y[0], y[1], y[2], y[3]);
+                    } else {
+#pragma unroll
+                        for (int e = 0; e < VEC; e++) dst[e] = y[e];
+                    }
+                }
+            }
+        }
+        if (p + 1 < a.npass && !grid_barrier(a.bar, gridDim.x, a.status)) return;
+    }
+}
+
 // Image of point p: the b with seg[b] <= p < seg[b+1].
 __device__ __forceinline__ int image_of(const int *__restrict__ seg, int nseg, int p) {
     int lo = 0, hi = nseg - 1;
@@ -1028,6 +1143,47 @@ cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s) {
         default: return cudaErrorInvalidValue;
     }
 #undef DCRF_BL
+}
+
+template <int MP, bool SEQ>
+static cudaError_t chains_launch(const BlurChainArgs &a, cudaStream_t s) {
+    static int grid = 0;  // co-resident CTAs of this instance on the device (queried once)
+    if (grid == 0) {
+        int dev = 0, nsm = 0, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, blur_chains_kernel<MP, SEQ>, 256, 0);
+        grid = std::max(1, nsm * std::max(1, per));
+    }
+    long long work = 0;
+    for (int k = 0; k < a.n; k++) work += (long long)a.c[k].L * (MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP);
+    const int blocks = (int)std::max<long long>(1, std::min<long long>(grid, (work + 255) / 256));
+    cudaError_t e = cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned), s);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(blocks);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    note_launch();
+    return cudaLaunchKernelEx(&cfg, blur_chains_kernel<MP, SEQ>, a);
+}
+
+cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStream_t s) {
+    if (a.n <= 0) return cudaSuccess;
+#define DCRF_BC(X) \
+    case X:        \
+        return seq ? chains_launch<X, true>(a, s) : chains_launch<X, false>(a, s);
+    switch (MP) {
+        DCRF_BC(1) DCRF_BC(2) DCRF_BC(4) DCRF_BC(8) DCRF_BC(12) DCRF_BC(16) DCRF_BC(20) DCRF_BC(24) DCRF_BC(28)
+        DCRF_BC(32)
+        default: return cudaErrorInvalidValue;
+    }
+#undef DCRF_BC
 }
 
 cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,

@@ -32,6 +32,9 @@ struct PPArgs {
     int split;           // threads per point of the point pass (1, or 2 when MP % 8 == 0)
     int sm_q;            // offset of the splat's q rows (aliases the slice-phase regions)
     int sm_res;          // offset of the splat's per-task results (after the q rows)
+    // checkpoint (adjoint): per term, the sliced value before the term's
+    // post-normalisation, K_raw [norm] Q, as slot rows (null: not kept)
+    float *ckY[DCRF_MAX_TERMS];
     // PP_FILTER epilogue (adjoint): with F the raw filter of term 0 and
     // F' = F .* norm when term 0's post_norm is set (else F): Fpost = F' and
     // Gacc += compat(F') (rows; null to skip).  Qout (raw F) may be null.
@@ -70,10 +73,33 @@ struct BlurArgs {
     long long begin[DCRF_MAX_TERMS + 1];  // prefix of (vertex, vector) work over terms
 };
 
+// Blur chains for the single-launch blur: each chain runs its d+1 axis passes
+// (d..0 when reverse) from S, ping-ponging through buf[0], buf[1]; the last
+// pass writes Out (may be null) and optionally scatters into pv in partial
+// order.  All chains advance pass by pass together, separated by a bounded grid
+// barrier (cooperative launch, so every CTA is resident).
+struct BlurChainArgs {
+    int n;      // chains
+    int npass;  // max over chains of d+1
+    struct C {
+        const float *S;
+        float *buf[2];
+        float *Out;
+        const int2 *nbr;
+        int L, d, reverse;
+        const int *red_beg;
+        const int *red_list;
+        float *pv;
+    } c[2 * DCRF_MAX_TERMS];
+    unsigned *bar;  // [2] grid-barrier state (arrivals, generation), zero before the launch
+    DevStatus *status;
+};
+
 // Launchers; MP is the padded label count (1, 2, 4, 8, ..., 32).
 cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s);
+cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStream_t s);
 
 // Layout conversions between user layouts (point-major [N][M], or label-major:
 // per image an M x N_b block, images one after another -- [M][N] for one image)

@@ -232,13 +232,16 @@ class DenseCRF:
         return self.tuning()
 
     def tuning(self) -> dict:
-        sp, sm, tk, hl = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float()
+        sp, sm, tk, hl, co = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()
         _lib.check(_lib.load().dcrf_get_tuning(self._h, ctypes.byref(sp), ctypes.byref(sm), ctypes.byref(tk),
-                                               ctypes.byref(hl)))
-        return {"split": sp.value, "smem_kb": sm.value, "task_len": tk.value, "hash_load": hl.value}
+                                               ctypes.byref(hl), ctypes.byref(co)))
+        return {"split": sp.value, "smem_kb": sm.value, "task_len": tk.value, "hash_load": hl.value,
+                "coop_blur": co.value}
 
-    def set_tuning(self, split: int = 0, smem_kb: int = 0, task_len: int = 16, hash_load: float = 2.0) -> None:
-        _lib.check(_lib.load().dcrf_set_tuning(self._h, int(split), int(smem_kb), int(task_len), float(hash_load)))
+    def set_tuning(self, split: int = 0, smem_kb: int = 0, task_len: int = 16, hash_load: float = 2.0,
+                   coop_blur: int = 0) -> None:
+        _lib.check(_lib.load().dcrf_set_tuning(self._h, int(split), int(smem_kb), int(task_len), float(hash_load),
+                                               int(coop_blur)))
 
     # -- learning (the parameter API and adjoint of densecrf.cpp:238-360) -------
     def setCompatibility(self, term: int, compat) -> None:

@@ -146,10 +146,10 @@ def test_autotune_choices_and_results(engine):
     tuned = make()
     knobs = tuned.autotune()
     assert knobs["split"] in (1, 2) and 8 <= knobs["task_len"] <= 32 and knobs["hash_load"] >= 1.5
-    assert knobs["smem_kb"] > 0
+    assert knobs["smem_kb"] > 0 and knobs["coop_blur"] in (0, 1)
     Qt = np.array(tuned.inference(T))
     same = make()
-    same.set_tuning(knobs["split"], knobs["smem_kb"], knobs["task_len"], knobs["hash_load"])
+    same.set_tuning(knobs["split"], knobs["smem_kb"], knobs["task_len"], knobs["hash_load"], knobs["coop_blur"])
     assert np.array_equal(np.array(same.inference(T)), Qt)
     assert np.abs(Qt - ref).max() < 1e-5
     # automatic mode takes the remembered choice for the same configuration
