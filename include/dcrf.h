@@ -166,6 +166,16 @@ int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, doubl
  * by densecrf.pxd:61-62): argmax labels (first maximum) after n iterations. */
 int dcrf_map(dcrf_crf *h, int n_iterations, int16_t *labels, int where);
 
+/* DenseCRF::unaryEnergy (densecrf.cpp:141-153; C++ only, not wrapped by the
+ * reference's Cython): energy[i] = U(l_i, i) for 0 <= l_i < M, else 0.  labels
+ * are N int16 in `where`; energy is N floats in `where_out`. */
+int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *energy, int where_out);
+
+/* DenseCRF::pairwiseEnergy (densecrf.cpp:154-177): energy[i] = -1/2 times the
+ * message of term `term` (-1: the sum over all terms) at l_i for the one-hot
+ * labelling, 0 where l_i is not a label. */
+int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term, float *energy, int where_out);
+
 /* Blocks until the handle's stream is idle. */
 int dcrf_synchronize(dcrf_crf *h);
 

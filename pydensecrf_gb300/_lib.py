@@ -41,6 +41,8 @@ _SIGS = {
     "dcrf_create_batch": ([_i, _vp, _i, ctypes.POINTER(_vp)], _i),
     "dcrf_create_batch_2d": ([_i, _vp, _vp, _i, ctypes.POINTER(_vp)], _i),
     "dcrf_batch_info": ([_vp, _vp, _vp], _i),
+    "dcrf_unary_energy": ([_vp, _vp, _i, _vp, _i], _i),
+    "dcrf_pairwise_energy": ([_vp, _vp, _i, _i, _vp, _i], _i),
     "dcrf_set_autotune": ([_vp, _i], _i),
     "dcrf_autotune": ([_vp], _i),
     "dcrf_get_tuning": ([_vp, _vp, _vp, _vp, _vp, _vp], _i),

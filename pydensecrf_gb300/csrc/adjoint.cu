@@ -281,6 +281,29 @@ __global__ void __launch_bounds__(256) norm_terms_kernel(const float *__restrict
     x1[s] = t;
 }
 
+// One-hot rows of a labelling (densecrf.cpp:165-168): row s gets 1 at the
+// label of its point when 0 <= label < M (else an all-zero row).
+__global__ void onehot_kernel(const int16_t *__restrict__ labels, int M, int ld, int ns,
+                              const int *__restrict__ slot_pt, float *__restrict__ out) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)ns) return;
+    const int pt = slot_pt[s];
+    const int l = pt >= 0 ? (int)labels[pt] : -1;
+    for (int m = 0; m < ld; m++) out[s * ld + m] = (m == l && l < M) ? 1.f : 0.f;
+}
+
+// energy[pt] (+)= scale * x[slot of pt][label of pt] for 0 <= label < M, else
+// (+)= 0 (densecrf.cpp:146-150, 169-174)
+__global__ void label_energy_kernel(const float *__restrict__ x, const int16_t *__restrict__ labels, int M, int ld,
+                                    int N, const int *__restrict__ pt_slot, float scale, int accumulate,
+                                    float *__restrict__ energy) {
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= N) return;
+    const int l = labels[pt];
+    const float v = (x && l >= 0 && l < M) ? scale * x[(size_t)pt_slot[pt] * ld + l] : 0.f;
+    energy[pt] = accumulate ? energy[pt] + v : v;
+}
+
 // out[s] = sum over labels of x (one value per slot)
 __global__ void row_sum_kernel(const float *__restrict__ x, float *__restrict__ out, int M, int ld, int ns) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -494,6 +517,18 @@ cudaError_t launch_norm_terms(const float *b, const float *y, const float *F, co
 #undef DCRF_NT
         default: return cudaErrorInvalidValue;  // M <= 2 takes the unfused path
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_onehot(const int16_t *labels, int M, int ns, const int *slot_pt, float *out, cudaStream_t s) {
+    DCRF_LAUNCH(onehot_kernel<<<blocks(ns), 256, 0, s>>>(labels, M, pad_labels(M), ns, slot_pt, out));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int N, const int *pt_slot, float scale,
+                                int accumulate, float *energy, cudaStream_t s) {
+    DCRF_LAUNCH(label_energy_kernel<<<blocks(N), 256, 0, s>>>(x, labels, M, pad_labels(M), N, pt_slot, scale,
+                                                               accumulate, energy));
     return cudaGetLastError();
 }
 

@@ -1524,6 +1524,78 @@ int dcrf_map(dcrf_crf *h, int n_iterations, int16_t *labels, int where) {
     return ok();
 }
 
+// Labels from the caller into a device buffer of the handle's pool.
+static int load_labels(dcrf_crf *h, const int16_t *labels, int where, int16_t **out) {
+    int rc;
+    if ((rc = dev_alloc_async(out, (size_t)h->N, h->stream))) return rc;
+    CU(cudaMemcpyAsync(*out, labels, sizeof(int16_t) * h->N,
+                       where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    return DCRF_OK;
+}
+
+static int store_energy(dcrf_crf *h, const float *src, float *energy, int where) {
+    CU(cudaMemcpyAsync(energy, src, sizeof(float) * h->N,
+                       where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, h->stream));
+    return DCRF_OK;
+}
+
+int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *energy, int where_out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!labels || !energy) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
+    int16_t *lab = nullptr;
+    float *e = nullptr;
+    if ((rc = load_labels(h, labels, where, &lab))) return rc;
+    if ((rc = dev_alloc_async(&e, (size_t)h->N, h->stream))) return rc;
+    CU(launch_label_energy(h->has_unary ? h->U : nullptr, lab, h->M, h->N, h->pt_slot, 1.f, 0, e, h->stream));
+    rc = store_energy(h, e, energy, where_out);
+    dev_free_async(lab, h->stream);
+    dev_free_async(e, h->stream);
+    if (rc) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term, float *energy, int where_out) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!labels || !energy) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
+    if (term < -1 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    const int M = h->M, ns = h->nslots;
+    const size_t qsz = (size_t)h->MP * ns;
+    for (float *&b : h->bw)
+        if (!b && (rc = dev_alloc_async(&b, qsz, h->stream))) return rc;
+    int16_t *lab = nullptr;
+    float *e = nullptr;
+    if ((rc = load_labels(h, labels, where, &lab))) return rc;
+    if ((rc = dev_alloc_async(&e, (size_t)h->N, h->stream))) return rc;
+    float *q = h->bw[0], *qn = h->bw[1], *g = h->bw[2];
+    CU(launch_onehot(lab, M, ns, h->slot_pt, q, h->stream));
+    CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
+    // g = sum over the terms of PairwisePotential::apply(one-hot) (pairwise.cpp:173-178)
+    for (int k = 0; k < (int)h->terms.size(); k++) {
+        if (term >= 0 && k != term) continue;
+        Term &Tk = h->terms[k];
+        if ((rc = ensure_adjoint_bufs(h, Tk))) return rc;
+        const float *xs = q;
+        if (fwd_pre(Tk)) {
+            CU(launch_scale_norm(q, qn, Tk.norm, M, ns, 1, h->stream));
+            xs = qn;
+        }
+        if ((rc = splat_into(h, k, xs, Tk.bv[0], false))) return rc;
+        if ((rc = blur_into(h, k, Tk.bv[0], Tk.bv[1], false, false))) return rc;
+        if ((rc = slice_from(h, k, Tk.bv[1], nullptr, false, fwd_post(Tk), nullptr, g))) return rc;
+    }
+    // r = -0.5 * message at the point's own label (densecrf.cpp:169-174)
+    CU(launch_label_energy(g, lab, M, h->N, h->pt_slot, -0.5f, 0, e, h->stream));
+    rc = store_energy(h, e, energy, where_out);
+    dev_free_async(lab, h->stream);
+    dev_free_async(e, h->stream);
+    if (rc) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
 int dcrf_synchronize(dcrf_crf *h) {
     int rc = check_handle(h);
     if (rc) return rc;

@@ -39,6 +39,15 @@ class KernelType(int):
     FULL_KERNEL = FULL_KERNEL
 
 
+def _cuda_tensor(x) -> bool:
+    """A torch tensor on a CUDA device (used in place, no host copy)."""
+    try:
+        import torch
+    except ImportError:
+        return False
+    return isinstance(x, torch.Tensor) and x.is_cuda
+
+
 def _ptr(a: np.ndarray):
     return ctypes.c_void_p(a.ctypes.data)
 
@@ -136,13 +145,42 @@ class DenseCRF:
                 pass
             h.value = None
 
+    def _bind_torch_stream(self) -> None:
+        """Order the handle's work on torch's current stream, so device tensors
+        written by torch are complete when the engine reads them."""
+        import torch
+        st = torch.cuda.current_stream().cuda_stream
+        if getattr(self, "_stream", None) != st:
+            _lib.check(_lib.load().dcrf_set_stream(self._h, ctypes.c_void_p(st)))
+            self._stream = st
+
+    def _device_matrix(self, t, rows: int, what: str):
+        import torch
+        if t.dtype != torch.float32 or t.dim() != 2 or t.shape[0] != rows or t.shape[1] != self._nvar:
+            raise ValueError(f"{what}: need a float32 CUDA tensor of shape {(rows, self._nvar)}, got "
+                             f"{tuple(t.shape)} {t.dtype}")
+        self._bind_torch_stream()
+        return t.contiguous()
+
     # -- configuration ------------------------------------------------------
     def set_variant(self, variant: int) -> None:
         """Lattice arithmetic of the x86 (0, default) or scalar (1) reference build."""
         _lib.check(_lib.load().dcrf_set_variant(self._h, int(variant)))
 
     def addPairwiseEnergy(self, features, compat, kernel=DIAG_KERNEL, normalization=NORMALIZE_SYMMETRIC):
-        """densecrf.pyx:71-75."""
+        """densecrf.pyx:71-75.  ``features`` may be a (d, N) float32 CUDA tensor."""
+        if _cuda_tensor(features):
+            t = features
+            if t.dim() != 2 or t.shape[1] != self._nvar:
+                raise ValueError("Bad shape for pairwise energy (Need (?, {}), got {})".format(self._nvar,
+                                                                                         tuple(t.shape)))
+            t = self._device_matrix(t, t.shape[0], "features")
+            kernel = _check_enum(kernel, 0, 2, "KernelType")
+            normalization = _check_enum(normalization, 0, 3, "NormalizationType")
+            kind, c = _labelcomp(compat, self._nlabel)
+            _lib.check(_lib.load().dcrf_add_pairwise(self._h, ctypes.c_void_p(t.data_ptr()), t.shape[0],
+                                                     _lib.DEVICE, kind, _ptr(c), kernel, normalization, None))
+            return
         feat = as_float_buffer(features, 2, "features")
         kernel = _check_enum(kernel, 0, 2, "KernelType")
         normalization = _check_enum(normalization, 0, 3, "NormalizationType")
@@ -160,7 +198,13 @@ class DenseCRF:
         self._set_unary_matrix(u._matrix(self._nlabel, self._nvar))
 
     def setUnaryEnergy(self, u, f=None) -> None:
-        """densecrf.pyx:80-89; with ``f`` the unary is logistic, U = u f."""
+        """densecrf.pyx:80-89; with ``f`` the unary is logistic, U = u f.  ``u``
+        may be an (M, N) float32 CUDA tensor (used in place)."""
+        if f is None and _cuda_tensor(u):
+            t = self._device_matrix(u, self._nlabel, "unary")
+            _lib.check(_lib.load().dcrf_set_unary(self._h, ctypes.c_void_p(t.data_ptr()), _lib.LAYOUT_LM,
+                                                  _lib.DEVICE))
+            return
         u = as_float_buffer(u, 2, "u")
         if u.shape[0] != self._nlabel or (f is None and u.shape[1] != self._nvar):
             raise ValueError("Bad shape for unary energy (Need {}, got {})".format(
@@ -187,6 +231,15 @@ class DenseCRF:
         Q = self._new_q()
         _lib.check(_lib.load().dcrf_inference(self._h, int(niter), _ptr(Q), _lib.LAYOUT_PM, _lib.HOST))
         return MatrixXf().wrap_colmajor(Q)
+
+    def inference_tensor(self, niter: int):
+        """inference(niter) into a new (M, N) float32 CUDA tensor on torch's current stream."""
+        import torch
+        self._bind_torch_stream()
+        Q = torch.empty((self._nlabel, self._nvar), dtype=torch.float32, device="cuda")
+        _lib.check(_lib.load().dcrf_inference(self._h, int(niter), ctypes.c_void_p(Q.data_ptr()), _lib.LAYOUT_LM,
+                                              _lib.DEVICE))
+        return Q
 
     def startInference(self):
         """densecrf.pyx:94-95: (Q, tmp1, tmp2)."""
@@ -218,6 +271,27 @@ class DenseCRF:
         """DenseCRF::map (densecrf.cpp:132-137): argmax labels after niter iterations."""
         out = np.empty(self._nvar, np.int16)
         _lib.check(_lib.load().dcrf_map(self._h, int(niter), _ptr(out), _lib.HOST))
+        return out
+
+    # -- debug energies (densecrf.cpp:141-177; C++ only in the reference) --------
+    def _labels(self, labels) -> np.ndarray:
+        lab = np.ascontiguousarray(np.asarray(labels).reshape(-1), np.int16)
+        if lab.size != self._nvar:
+            raise ValueError(f"labels must have {self._nvar} entries, got {lab.size}")
+        return lab
+
+    def unaryEnergy(self, labels) -> np.ndarray:
+        """U(l_i, i) per variable (0 where l_i is not a label)."""
+        lab = self._labels(labels)
+        out = np.empty(self._nvar, np.float32)
+        _lib.check(_lib.load().dcrf_unary_energy(self._h, _ptr(lab), _lib.HOST, _ptr(out), _lib.HOST))
+        return out
+
+    def pairwiseEnergy(self, labels, term: int = -1) -> np.ndarray:
+        """-1/2 the pairwise message of the one-hot labelling at l_i (term -1: all terms)."""
+        lab = self._labels(labels)
+        out = np.empty(self._nvar, np.float32)
+        _lib.check(_lib.load().dcrf_pairwise_energy(self._h, _ptr(lab), _lib.HOST, int(term), _ptr(out), _lib.HOST))
         return out
 
     # -- autotuning (no reference counterpart) -----------------------------------
@@ -352,6 +426,20 @@ class DenseCRF2D(DenseCRF):
             srgb = (srgb, srgb, srgb)
         if rgbim is None:
             raise TypeError("rgbim must not be None")
+        if _cuda_tensor(rgbim):
+            import torch
+            if rgbim.dtype != torch.uint8 or tuple(rgbim.shape) != (self._h2, self._w, 3):
+                raise ValueError("Bad shape for pairwise bilateral (Need {}, got {} {})".format(
+                    (self._h2, self._w, 3), tuple(rgbim.shape), rgbim.dtype))
+            self._bind_torch_stream()
+            img = rgbim.contiguous()
+            kernel = _check_enum(kernel, 0, 2, "KernelType")
+            normalization = _check_enum(normalization, 0, 3, "NormalizationType")
+            kind, c = _labelcomp(compat, self._nlabel)
+            _lib.check(_lib.load().dcrf_add_pairwise_bilateral(
+                self._h, float(sxy[0]), float(sxy[1]), float(srgb[0]), float(srgb[1]), float(srgb[2]),
+                ctypes.c_void_p(img.data_ptr()), _lib.DEVICE, kind, _ptr(c), kernel, normalization, None))
+            return
         mv = memoryview(rgbim)
         if mv.format not in ("B", "=B", "<B", "@B"):
             raise ValueError(f"Buffer dtype mismatch, expected 'unsigned char' but got '{mv.format}'")
