@@ -73,7 +73,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "20"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -375,6 +375,76 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
                        "hash_load": round(knobs[3].value, 2), "coop_blur": knobs[4].value}}
 
 
+def volumes_fwd_bwd(lib, _lib, dev, stream, reps: int = 2):
+    """Generic (non-2D) batched forward + backward on 8 volumes of 96^3 voxels:
+    features (x/5, y/5, z/5, I/0.1) with a FULL kernel and a random symmetric
+    4x4 Matrix compatibility, plus a DIAG Gaussian on (x/3, y/3, z/3) with
+    Potts 1; M=4, T=8; gradients w.r.t. unary and compatibility.  One batched
+    handle, inputs resident in HBM."""
+    import torch
+
+    from pydensecrf_gb300 import synthetic as S
+
+    cfg = S.volume_96(0)
+    Sz, Mv, Tv = cfg["S"], cfg["M"], cfg["T"]
+    B = len(cfg["U"])
+    n = Sz ** 3
+    Ntot = B * n
+    zz, yy, xx = np.mgrid[0:Sz, 0:Sz, 0:Sz].astype(np.float32)
+    pos = np.ascontiguousarray(np.stack([xx / np.float32(3), yy / np.float32(3), zz / np.float32(3)]).reshape(3, -1))
+    U_all = torch.from_numpy(np.concatenate([u.reshape(-1) for u in cfg["U"]])).to(dev)
+    F4 = torch.from_numpy(np.ascontiguousarray(np.concatenate(cfg["feat"], axis=1))).to(dev)
+    F3 = torch.from_numpy(np.ascontiguousarray(np.concatenate([pos] * B, axis=1))).to(dev)
+    Q = torch.empty(Mv * Ntot, dtype=torch.float32, device=dev)
+    dQ = torch.randn(Mv * Ntot, generator=torch.Generator(device=dev).manual_seed(0), device=dev) / Ntot
+    dU = torch.empty_like(Q)
+    cm = np.ascontiguousarray(cfg["compat"], np.float32)
+    cp = np.array([1.0], np.float32)
+    Ns = np.full(B, n, np.int32)
+    h = ctypes.c_void_p()
+    _lib.check(lib.dcrf_create_batch(B, Ns.ctypes.data, Mv, ctypes.byref(h)))
+    _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
+    _lib.check(lib.dcrf_set_autotune(h, 1))
+    dc = np.zeros(Mv * Mv + 1, np.float64)
+
+    def fwd():
+        _lib.check(lib.dcrf_clear_pairwise(h))
+        _lib.check(lib.dcrf_set_unary(h, ctypes.c_void_p(U_all.data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE))
+        _lib.check(lib.dcrf_add_pairwise(h, ctypes.c_void_p(F4.data_ptr()), 4, _lib.DEVICE, _lib.COMPAT_MATRIX,
+                                         cm.ctypes.data, 2, 3, None))
+        _lib.check(lib.dcrf_add_pairwise(h, ctypes.c_void_p(F3.data_ptr()), 3, _lib.DEVICE, _lib.COMPAT_POTTS,
+                                         cp.ctypes.data, 1, 3, None))
+        _lib.check(lib.dcrf_inference_checkpointed(h, Tv, ctypes.c_void_p(Q.data_ptr()), _lib.LAYOUT_LM,
+                                                   _lib.DEVICE))
+
+    def bwd():
+        _lib.check(lib.dcrf_backward(h, ctypes.c_void_p(dQ.data_ptr()), _lib.LAYOUT_LM, _lib.DEVICE,
+                                     ctypes.c_void_p(dU.data_ptr()), dc.ctypes.data, None))
+
+    fwd()
+    bwd()
+    torch.cuda.synchronize()
+    f_ms, b_ms = [], []
+    for _ in range(reps):
+        e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+        e0.record(stream)
+        fwd()
+        e1.record(stream)
+        bwd()
+        e2.record(stream)
+        torch.cuda.synchronize()
+        f_ms.append(e0.elapsed_time(e1))
+        b_ms.append(e1.elapsed_time(e2))
+    lib.dcrf_destroy(h)
+    f, b = float(np.median(f_ms)), float(np.median(b_ms))
+    units = Ntot * Mv * Tv / 1e6
+    return {"workload": f"{B} volumes of {Sz}^3 (N={Ntot}) M=4 T=8, FULL kernel on (x,y,z,I) + DIAG Gaussian, "
+                        "Matrix compat, one batched handle",
+            "fwd_ms": round(f, 3), "bwd_ms": round(b, 3), "fwd_plus_bwd_over_fwd": round((f + b) / f, 3),
+            "fwd_value": round(units / (f / 1e3), 1), "unit": "MVoxel*label*iter/s (forward incl. lattice builds)",
+            "grads": "dU, dcompat"}
+
+
 def run_gpu(args):
     import torch
 
@@ -521,6 +591,7 @@ def run_gpu(args):
     lib.dcrf_destroy(h)
     learning = learning_step_times(lib, _lib, dev, stream) if (rank == 0 and not args.no_learning) else None
     batched = batched_vs_loop(lib, _lib, dev, stream) if (rank == 0 and not args.no_batch) else None
+    volumes = volumes_fwd_bwd(lib, _lib, dev, stream) if (rank == 0 and not args.no_batch) else None
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "MPix*label*iter/s", "n_gpus": world,
@@ -542,6 +613,7 @@ def run_gpu(args):
             "cpu_baseline": cpu,
             "learning": learning,
             "batched": batched,
+            "volumes": volumes,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

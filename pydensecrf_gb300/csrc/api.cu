@@ -801,6 +801,14 @@ int build_term(dcrf_crf *h, int k) {
     if ((rc = dev_alloc_async(&T.mem_wn, nm, h->stream))) return rc;
     CU(launch_scale_members(T.lat.mem_pt, T.lat.mem_w, T.norm, h->ntiles, T.d + 1, T.mem_wn, h->stream));
     if ((rc = sync_check(h))) return rc;
+    DevStatus st{};
+    CU(cudaMemcpy(&st, h->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
+    if (st.code != 0) {
+        CU(cudaMemset(h->status, 0, sizeof(DevStatus)));
+        free_term_lattice(h, T);
+        return set_err(st.code, "lattice build of term " + std::to_string(k) + " failed on the device (status " +
+                                    std::to_string(st.code) + ", detail " + std::to_string(st.detail) + ")");
+    }
     h->version++;
     return DCRF_OK;
 }

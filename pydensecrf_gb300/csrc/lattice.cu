@@ -842,20 +842,14 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
             cudaMemcpyAsync(L.red_list, in_alt ? v1 : v0, sizeof(uint32_t) * L.P, cudaMemcpyDeviceToDevice, s);
         }
     }
-    ce = cudaStreamSynchronize(s);
+    // no synchronisation here: the temporaries go back to the pool in stream
+    // order, and the caller checks the device status block (count_kernel's
+    // consistency check included) at its next synchronisation
     tmp.release();
-    if (ce != cudaSuccess) {
-        lattice_free(&L, s);
-        return fail(DCRF_ERR_CUDA, std::string("lattice build: ") + cudaGetErrorString(ce));
-    }
     ce = cudaGetLastError();
     if (ce != cudaSuccess) {
         lattice_free(&L, s);
         return fail(DCRF_ERR_CUDA, std::string("lattice build launch: ") + cudaGetErrorString(ce));
-    }
-    if (cudaMemcpy(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost) != cudaSuccess || hst.code != 0) {
-        lattice_free(&L, s);
-        return fail(hst.code ? hst.code : DCRF_ERR_CUDA, "lattice build: inconsistent partial tables");
     }
     L.bytes = acc;
     *out = L;

@@ -58,7 +58,9 @@ struct TileMapDev {
 // zero-feature padding points of each image (N_img % 4 != 0).  `load` is the
 // hash-table capacity factor (capacity = pow2 >= load * corners); `task_len`
 // the most members of one splat task (1..63).  Returns a DCRF status; on
-// DCRF_ERR_HASH_FULL the caller may retry with a larger load.
+// DCRF_ERR_HASH_FULL the caller may retry with a larger load.  Work may still
+// be in flight on return: the caller synchronises and checks `status` (a
+// non-zero code means the lattice is unusable).
 int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
                   int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out);
 
