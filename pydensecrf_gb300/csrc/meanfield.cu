@@ -502,11 +502,14 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
         for (int e = 0; e < H; e++)
             if (l0 + e < M) mx = fmaxf(mx, x[e]);
         if constexpr (SPLIT == 2) mx = fmaxf(mx, __shfl_xor_sync(pm, mx, 1));
+        // exponentials through the fast hardware path: __expf is within a few
+        // ulp for arguments near 0, where the marginals' mass is, and its larger
+        // error at very negative arguments scales values below 1e-30 of the sum
         float part = 0.f;
 #pragma unroll
         for (int e = 0; e < H; e++)
             if (l0 + e < M) {
-                x[e] = expf(fsub(x[e], mx));
+                x[e] = __expf(fsub(x[e], mx));
                 part = fadd(part, x[e]);
             }
         float sum = part;
