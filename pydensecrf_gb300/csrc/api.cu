@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <chrono>
 #include <map>
+#include <memory>
 #include <atomic>
 #include <cmath>
 #include <mutex>
@@ -77,23 +78,9 @@ int ok() {
         if (e_ != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
     } while (0)
 
-template <class T>
-int dev_alloc(T **p, size_t n) {
-    void *q = nullptr;
-    cudaError_t e = cudaMalloc(&q, std::max<size_t>(n * sizeof(T), 16));
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return set_err(DCRF_ERR_OOM, "cudaMalloc of " + std::to_string(n * sizeof(T)) + " bytes failed");
-    }
-    *p = static_cast<T *>(q);
-    return DCRF_OK;
-}
-
-void dev_free(void *p) {
-    if (p) cudaFree(p);
-}
-
-// stream-ordered allocations of per-term buffers: rebuilding terms reuses the pool
+// stream-ordered allocations from the library's pool (released memory stays
+// in the pool): creating, rebuilding and destroying handles does not
+// synchronise the device
 template <class T>
 int dev_alloc_async(T **p, size_t n, cudaStream_t s) {
     void *q = nullptr;
@@ -189,8 +176,11 @@ struct dcrf_crf {
     double *dpart = nullptr, *dacc = nullptr;
     size_t dpart_cap = 0, dacc_cap = 0;
     // CUDA graph of the last inference launch sequence (re-used through
-    // cudaGraphExecUpdate while its topology stays the same)
+    // cudaGraphExecUpdate while its topology stays the same); a handle's first
+    // inference launches directly, since instantiating a graph costs more than
+    // it saves on a one-shot solve
     bool use_graphs = true;
+    int inference_runs = 0;
     // launch and build knobs (see the autotuner below)
     TuneCfg tune;
     bool autotune = false, tuned = false;
@@ -266,8 +256,32 @@ int check_handle(dcrf_crf *h) {
 // images).  A 2D image uses 16x16 pixel blocks (the corners of a block share
 // far more lattice vertices than a raster strip of the same size); a generic
 // point set uses runs of 256 consecutive points.
-int build_tiles(dcrf_crf *h) {
-    std::vector<int> slot, vbase{0};
+struct TileLayout {
+    std::vector<int> slot, inv, vbase;
+};
+
+// Host tables of a tile layout, computed once per image-size list for the
+// process (handles are often created per image; the tables depend only on the
+// sizes) and kept for the few most recent layouts.
+std::shared_ptr<const TileLayout> tile_layout(const dcrf_crf *h) {
+    static std::mutex mu;
+    static std::vector<std::pair<std::vector<int>, std::shared_ptr<const TileLayout>>> cache;
+    std::vector<int> key{h->grid2d ? 1 : 0, h->N};
+    key.insert(key.end(), h->seg.begin(), h->seg.end());
+    key.insert(key.end(), h->imgW.begin(), h->imgW.end());
+    key.insert(key.end(), h->imgH.begin(), h->imgH.end());
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        for (size_t k = 0; k < cache.size(); k++)
+            if (cache[k].first == key) {
+                auto hit = cache[k].second;
+                std::rotate(cache.begin(), cache.begin() + k, cache.begin() + k + 1);
+                return hit;
+            }
+    }
+    auto lay = std::make_shared<TileLayout>();
+    std::vector<int> &slot = lay->slot, &vbase = lay->vbase;
+    vbase.push_back(0);
     const int nimg = (int)h->seg.size() - 1;
     for (int b = 0; b < nimg; b++) {
         const int base = h->seg[b], nb = h->seg[b + 1] - h->seg[b];
@@ -299,23 +313,34 @@ int build_tiles(dcrf_crf *h) {
             }
         }
     }
-    h->ntiles = (int)vbase.size() - 1;
-    h->nslots = h->ntiles * SPLAT_TILE;
-    std::vector<int> inv(h->N, 0);
+    lay->inv.assign(h->N, 0);
     for (size_t sl = 0; sl < slot.size(); sl++)
-        if (slot[sl] >= 0) inv[slot[sl]] = (int)sl;
+        if (slot[sl] >= 0) lay->inv[slot[sl]] = (int)sl;
+    std::lock_guard<std::mutex> lk(mu);
+    cache.insert(cache.begin(), {key, lay});
+    if (cache.size() > 8) cache.pop_back();
+    return lay;
+}
+
+// Device tile tables of the handle (stream-ordered on the handle's own stream).
+int build_tiles(dcrf_crf *h) {
+    const std::shared_ptr<const TileLayout> lay = tile_layout(h);
+    const cudaStream_t s = h->own;
+    h->ntiles = (int)lay->vbase.size() - 1;
+    h->nslots = h->ntiles * SPLAT_TILE;
     int rc;
-    if ((rc = dev_alloc(&h->slot_pt, slot.size() + 1))) return rc;
-    if ((rc = dev_alloc(&h->pt_slot, (size_t)h->N + 1))) return rc;
-    if ((rc = dev_alloc(&h->tile_vbase, vbase.size() + 1))) return rc;
-    if ((rc = dev_alloc(&h->kl_part, (size_t)h->ntiles + 1))) return rc;
-    if ((rc = dev_alloc(&h->d_seg, h->seg.size()))) return rc;
-    if ((rc = dev_alloc(&h->d_imgW, h->seg.size()))) return rc;
-    CU(cudaMemcpy(h->slot_pt, slot.data(), slot.size() * sizeof(int), cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(h->pt_slot, inv.data(), inv.size() * sizeof(int), cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(h->tile_vbase, vbase.data(), vbase.size() * sizeof(int), cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(h->d_seg, h->seg.data(), h->seg.size() * sizeof(int), cudaMemcpyHostToDevice));
-    if (h->grid2d) CU(cudaMemcpy(h->d_imgW, h->imgW.data(), h->imgW.size() * sizeof(int), cudaMemcpyHostToDevice));
+    if ((rc = dev_alloc_async(&h->slot_pt, lay->slot.size() + 1, s))) return rc;
+    if ((rc = dev_alloc_async(&h->pt_slot, (size_t)h->N + 1, s))) return rc;
+    if ((rc = dev_alloc_async(&h->tile_vbase, lay->vbase.size() + 1, s))) return rc;
+    if ((rc = dev_alloc_async(&h->kl_part, (size_t)h->ntiles + 1, s))) return rc;
+    if ((rc = dev_alloc_async(&h->d_seg, h->seg.size(), s))) return rc;
+    if ((rc = dev_alloc_async(&h->d_imgW, h->seg.size(), s))) return rc;
+    CU(cudaMemcpyAsync(h->slot_pt, lay->slot.data(), lay->slot.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(h->pt_slot, lay->inv.data(), lay->inv.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(h->tile_vbase, lay->vbase.data(), lay->vbase.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    CU(cudaMemcpyAsync(h->d_seg, h->seg.data(), h->seg.size() * sizeof(int), cudaMemcpyHostToDevice, s));
+    if (h->grid2d)
+        CU(cudaMemcpyAsync(h->d_imgW, h->imgW.data(), h->imgW.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     return DCRF_OK;
 }
 
@@ -365,15 +390,27 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
         return fail(set_err(DCRF_ERR_CUDA, "cudaStreamCreate failed"));
     prepare_kernels();
     h->stream = h->own;
-    if ((rc = dev_alloc(&h->status, 1))) return fail(rc);
-    if ((rc = dev_alloc(&h->bar, 2))) return fail(rc);
+    // handle memory comes from the stream-ordered pool on the handle's own
+    // stream (no device-wide synchronisation at creation or destruction);
+    // work on another stream starts after dcrf_set_stream's synchronisation
+    const cudaStream_t s = h->own;
+    const size_t rows = (size_t)h->nslots * h->MP;
+    if ((rc = dev_alloc_async(&h->status, 1, s))) return fail(rc);
+    if ((rc = dev_alloc_async(&h->bar, 2, s))) return fail(rc);
     if ((rc = build_tiles(h))) return fail(rc);
-    if ((rc = dev_alloc(&h->U, (size_t)h->nslots * h->MP))) return fail(rc);
-    if ((rc = dev_alloc(&h->Q, (size_t)h->nslots * h->MP))) return fail(rc);
-    if ((rc = dev_alloc(&h->tmp, (size_t)h->nslots * h->MP))) return fail(rc);
-    if ((rc = dev_alloc(&h->stage, (size_t)N * M))) return fail(rc);
-    if ((rc = dev_alloc(&h->map, (size_t)N))) return fail(rc);
-    CU(cudaMemset(h->status, 0, sizeof(DevStatus)));
+    if ((rc = dev_alloc_async(&h->U, (size_t)h->nslots * h->MP, s))) return fail(rc);
+    if ((rc = dev_alloc_async(&h->Q, (size_t)h->nslots * h->MP, s))) return fail(rc);
+    if ((rc = dev_alloc_async(&h->tmp, (size_t)h->nslots * h->MP, s))) return fail(rc);
+    if ((rc = dev_alloc_async(&h->stage, (size_t)N * M, s))) return fail(rc);
+    if ((rc = dev_alloc_async(&h->map, (size_t)N, s))) return fail(rc);
+    // pooled memory may hold an earlier handle's data: status, the grid
+    // barrier and the slot rows (padding slots and labels included) start at 0
+    if (cudaMemsetAsync(h->status, 0, sizeof(DevStatus), s) != cudaSuccess ||
+        cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), s) != cudaSuccess ||
+        cudaMemsetAsync(h->U, 0, rows * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(h->Q, 0, rows * sizeof(float), s) != cudaSuccess ||
+        cudaMemsetAsync(h->tmp, 0, rows * sizeof(float), s) != cudaSuccess)
+        return fail(set_err(DCRF_ERR_CUDA, "cudaMemsetAsync failed"));
     *out = h;
     return ok();
 }
@@ -1051,7 +1088,7 @@ int maybe_autotune(dcrf_crf *h) {
 int run_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
     int trc = maybe_autotune(h);
     if (trc) return trc;
-    if (h->profiling || !h->use_graphs) return issue_inference(h, T, final_mode, ckpt);
+    if (h->profiling || !h->use_graphs || h->inference_runs++ == 0) return issue_inference(h, T, final_mode, ckpt);
     cudaStream_t user = h->stream;
     h->stream = h->capture;
     CU(cudaStreamBeginCapture(h->capture, cudaStreamCaptureModeThreadLocal));
@@ -1333,20 +1370,10 @@ int dcrf_destroy(dcrf_crf *h) {
     for (float *&b : h->bw1) dev_free_async(b, h->stream);
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
-    if (h->stream) cudaStreamSynchronize(h->stream);
-    dev_free(h->status);
-    dev_free(h->bar);
-    dev_free(h->U);
-    dev_free(h->Q);
-    dev_free(h->tmp);
-    dev_free(h->stage);
-    dev_free(h->pt_slot);
-    dev_free(h->map);
-    dev_free(h->kl_part);
-    dev_free(h->slot_pt);
-    dev_free(h->tile_vbase);
-    dev_free(h->d_seg);
-    dev_free(h->d_imgW);
+    for (void *p : {(void *)h->status, (void *)h->bar, (void *)h->U, (void *)h->Q, (void *)h->tmp,
+                    (void *)h->stage, (void *)h->pt_slot, (void *)h->map, (void *)h->kl_part, (void *)h->slot_pt,
+                    (void *)h->tile_vbase, (void *)h->d_seg, (void *)h->d_imgW})
+        dev_free_async(p, h->stream);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->capture) cudaStreamDestroy(h->capture);
     if (h->own) cudaStreamDestroy(h->own);
