@@ -635,12 +635,10 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
     bool seq = value1 || h->M <= 2;
     ReduceArgs ra{};
     ra.n = (int)which.size();
-    ra.begin[0] = 0;
     int maxd = 0;
     for (size_t k = 0; k < which.size(); k++) {
         Term &T = h->terms[which[k]];
-        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.pv, S_out ? S_out[k] : T.V[0], T.lat.L};
-        ra.begin[k + 1] = ra.begin[k] + T.lat.L;
+        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.pv, S_out ? S_out[k] : T.V[0], T.lat.L, T.lat.P};
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
     }
@@ -712,11 +710,21 @@ int zero_sentinels(dcrf_crf *h, Term &T) {
     return DCRF_OK;
 }
 
+// Waits for the handle's stream and reports CUDA errors and the device status
+// block (set by kernels whose bounded waits ran out or whose inputs failed a
+// consistency check); a reported status is cleared.
 int sync_check(dcrf_crf *h) {
-    cudaError_t e = cudaStreamSynchronize(h->stream);
+    DevStatus st{};
+    cudaError_t e = cudaMemcpyAsync(&st, h->status, sizeof(DevStatus), cudaMemcpyDeviceToHost, h->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string("device error: ") + cudaGetErrorString(e));
     e = cudaGetLastError();
     if (e != cudaSuccess) return set_err(DCRF_ERR_CUDA, std::string("launch error: ") + cudaGetErrorString(e));
+    if (st.code != 0) {
+        cudaMemsetAsync(h->status, 0, sizeof(DevStatus), h->stream);
+        return set_err(st.code, "device status " + std::to_string(st.code) + " (detail " + std::to_string(st.detail) +
+                                    ")");
+    }
     return DCRF_OK;
 }
 
@@ -837,14 +845,12 @@ int build_term(dcrf_crf *h, int k) {
     const size_t nm = (size_t)h->ntiles * SPLAT_TILE * (T.d + 1);
     if ((rc = dev_alloc_async(&T.mem_wn, nm, h->stream))) return rc;
     CU(launch_scale_members(T.lat.mem_pt, T.lat.mem_w, T.norm, h->ntiles, T.d + 1, T.mem_wn, h->stream));
-    if ((rc = sync_check(h))) return rc;
-    DevStatus st{};
-    CU(cudaMemcpy(&st, h->status, sizeof(DevStatus), cudaMemcpyDeviceToHost));
-    if (st.code != 0) {
-        CU(cudaMemset(h->status, 0, sizeof(DevStatus)));
-        free_term_lattice(h, T);
-        return set_err(st.code, "lattice build of term " + std::to_string(k) + " failed on the device (status " +
-                                    std::to_string(st.code) + ", detail " + std::to_string(st.detail) + ")");
+    if ((rc = sync_check(h))) {
+        if (rc != DCRF_ERR_CUDA) {
+            free_term_lattice(h, T);
+            return set_err(rc, "lattice build of term " + std::to_string(k) + " failed on the device: " + g_err);
+        }
+        return rc;
     }
     h->version++;
     return DCRF_OK;
@@ -1163,9 +1169,7 @@ int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1) {
     CU(pp(h, a, MP));
     ReduceArgs ra{};
     ra.n = 1;
-    ra.begin[0] = 0;
-    ra.begin[1] = T.lat.L;
-    ra.t[0] = {T.lat.red_beg, T.lat.red_list, T.pv, S, T.lat.L};
+    ra.t[0] = {T.lat.red_beg, T.lat.red_list, T.pv, S, T.lat.L, T.lat.P};
     ProfScope ps(h, DCRF_KCLASS_REDUCE);
     CU(launch_reduce(ra, MP, h->stream));
     return DCRF_OK;
@@ -2218,9 +2222,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     CU(launch_pointpass(a, MPv, s));
     ReduceArgs ra{};
     ra.n = 1;
-    ra.begin[0] = 0;
-    ra.begin[1] = T.lat.L;
-    ra.t[0] = {T.lat.red_beg, T.lat.red_list, pv, V0, T.lat.L};
+    ra.t[0] = {T.lat.red_beg, T.lat.red_list, pv, V0, T.lat.L, T.lat.P};
     CU(launch_reduce(ra, MPv, s));
     const int NV = MPv % 4 == 0 ? MPv / 4 : MPv % 2 == 0 ? MPv / 2 : MPv;
     const bool seq = v1 || h->M <= 2 || T.variant == DCRF_VARIANT_SCALAR;

@@ -28,6 +28,7 @@
 // Bounded probing everywhere: a full table sets DCRF_ERR_HASH_FULL and the
 // host retries with a larger table; no kernel waits on another thread.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -511,7 +512,7 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
                                                                uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
                                                                uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w,
                                                                uint32_t *__restrict__ task) {
-    constexpr int C = TG<D>::C, PER = TG<D>::PER, NW = TG_THREADS / 32;
+    constexpr int C = TG<D>::C, NW = TG_THREADS / 32;
     constexpr int SEG = C / NW;  // corners per warp segment (a multiple of 32)
     extern __shared__ int tp_smem[];
     int *moff = tp_smem;            // [C] member offset of each partial
@@ -597,48 +598,91 @@ __global__ void count_kernel(const int *__restrict__ part_v, int P, int L, uint3
         dcrf_set_error(st, DCRF_ERR_CUDA, p);
 }
 
-__global__ void iota_kernel(uint32_t *__restrict__ a, int n) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p < n) a[p] = (uint32_t)p;
-}
-
 __global__ void set_int_kernel(int *p, int v) { *p = v; }
 
 // ---------------------------------------------------------------------------
 namespace {
 
-struct Pool {
+// Stream-ordered bump allocation from a few pool blocks.  reserve(b) takes one
+// block for the buffers that follow; get() carves 256-byte aligned pieces from
+// it and falls back to a block of its own when the reservation is used up (a
+// reservation that is too small costs an allocation, never correctness).
+struct Arena {
     cudaStream_t s;
-    std::vector<void *> ptrs;
+    std::vector<void *> blocks;
+    char *cur = nullptr;
+    size_t left = 0, bytes = 0;
     bool failed = false;
+    static size_t rnd(size_t b) { return (std::max<size_t>(b, 16) + 255) & ~(size_t)255; }
     template <class T>
-    T *get(size_t n) {
+    static size_t sz(size_t n) {
+        return rnd(n * sizeof(T));
+    }
+    void *block(size_t b) {
         void *p = nullptr;
-        if (pool_malloc_async(&p, std::max<size_t>(n * sizeof(T), 16), s) != cudaSuccess) {
+        if (pool_malloc_async(&p, b, s) != cudaSuccess) {
             failed = true;
             return nullptr;
         }
-        ptrs.push_back(p);
-        return static_cast<T *>(p);
+        blocks.push_back(p);
+        bytes += b;
+        return p;
+    }
+    void reserve(size_t b) {
+        cur = static_cast<char *>(block(b));
+        left = cur ? b : 0;
+    }
+    template <class T>
+    T *get(size_t n) {
+        const size_t b = rnd(n * sizeof(T));
+        if (b > left) return static_cast<T *>(block(b));
+        T *p = reinterpret_cast<T *>(cur);
+        cur += b;
+        left -= b;
+        return p;
     }
     void release() {
-        for (void *p : ptrs) cudaFreeAsync(p, s);
-        ptrs.clear();
+        for (void *p : blocks) cudaFreeAsync(p, s);
+        blocks.clear();
+        cur = nullptr;
+        left = bytes = 0;
     }
 };
+
+// Zeroes n1 elements at p1 and n2 at p2 (and the alignment gap between them)
+// with one memset when the second directly follows the first.
+template <class A, class B>
+void zero_pair(A *p1, size_t n1, B *p2, size_t n2, cudaStream_t s) {
+    const size_t b1 = Arena::sz<A>(n1);
+    if (reinterpret_cast<char *>(p1) + b1 == reinterpret_cast<char *>(p2)) {
+        cudaMemsetAsync(p1, 0, b1 + n2 * sizeof(B), s);
+    } else {
+        cudaMemsetAsync(p1, 0, n1 * sizeof(A), s);
+        cudaMemsetAsync(p2, 0, n2 * sizeof(B), s);
+    }
+}
+
+// The tile kernels' exact dynamic shared memory, set once per device (the 48 KB
+// default leaves no room for their static shared memory at d = 7, where the
+// placement kernel's dynamic part is exactly 48 KB).
+template <int D>
+cudaError_t tile_kernels_optin(size_t smem_g, size_t smem_p) {
+    static std::atomic<uint64_t> done{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const uint64_t bit = dev < 64 ? (1ull << dev) : 0;
+    if (bit && (done.load() & bit)) return cudaSuccess;
+    e = cudaFuncSetAttribute(tile_group_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(tile_place_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p);
+    if (e == cudaSuccess && bit) done.fetch_or(bit);
+    return e;
+}
 
 int fail(int code, const std::string &m) {
     g_msg = m;
     return code;
-}
-
-template <class T>
-T *dalloc(size_t n, cudaStream_t s, size_t *acc) {
-    void *p = nullptr;
-    size_t b = std::max<size_t>(n * sizeof(T), 16);
-    if (pool_malloc_async(&p, b, s) != cudaSuccess) return nullptr;
-    *acc += b;
-    return static_cast<T *>(p);
 }
 
 template <int D>
@@ -663,17 +707,22 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     const size_t Ereal = (size_t)N * (D + 1);
     if (E >= 0xFFFFFFF0ull) return fail(DCRF_ERR_INVALID_ARG, "lattice too large (more than 2^32 simplex corners)");
 
-    Pool tmp{s};
+    size_t cap = 1024;
+    while ((double)cap < (double)load * (double)E && cap < (1ull << 31)) cap <<= 1;
+    const size_t scan_words = scan_temp_words(E);
+    // temporaries and the lattice's own tables come from one block per build
+    // stage (sizes known at the start of each stage)
+    Arena tmp{s}, per{s};
+    tmp.reserve(Arena::sz<uint64_t>(E * KW) + 2 * Arena::sz<uint32_t>(E) + Arena::sz<uint32_t>(4) +
+                Arena::sz<int>(nseg + 1) + Arena::sz<int>(n_ph + 1) + Arena::sz<uint32_t>(cap) +
+                Arena::sz<uint32_t>(scan_words));
     uint64_t *keys = tmp.get<uint64_t>(E * KW);
     uint32_t *slot = tmp.get<uint32_t>(E);
     uint32_t *vid = tmp.get<uint32_t>(E);
     uint32_t *d_L = tmp.get<uint32_t>(4);
     int *d_seg = tmp.get<int>(nseg + 1);
     int *d_ph = tmp.get<int>(n_ph + 1);
-    size_t cap = 1024;
-    while ((double)cap < (double)load * (double)E && cap < (1ull << 31)) cap <<= 1;
     uint32_t *table = tmp.get<uint32_t>(cap);
-    size_t scan_words = scan_temp_words(E);
     uint32_t *stemp = tmp.get<uint32_t>(scan_words);
     if (tmp.failed) {
         tmp.release();
@@ -681,19 +730,19 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     }
     auto bail = [&](int code, const std::string &m) {
         tmp.release();
-        lattice_free(&L, s);
+        per.release();
         return fail(code, m);
     };
     cudaMemcpyAsync(d_seg, seg.start.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, s);
     if (n_ph) cudaMemcpyAsync(d_ph, ph_img.data(), sizeof(int) * n_ph, cudaMemcpyHostToDevice, s);
     cudaMemsetAsync(table, 0xFF, cap * sizeof(uint32_t), s);
 
-    size_t acc = 0;
-    L.off = dalloc<int>(Ereal, s, &acc);
-    L.bary = dalloc<float>(Ereal, s, &acc);
-    L.wslice = dalloc<float>(Ereal, s, &acc);
-    L.rank = dalloc<uint8_t>(Ereal, s, &acc);
-    if (!L.off || !L.bary || !L.wslice || !L.rank) return bail(DCRF_ERR_OOM, "device allocation failed (lattice)");
+    per.reserve(Arena::sz<int>(Ereal) + 2 * Arena::sz<float>(Ereal) + Arena::sz<uint8_t>(Ereal));
+    L.off = per.get<int>(Ereal);
+    L.bary = per.get<float>(Ereal);
+    L.wslice = per.get<float>(Ereal);
+    L.rank = per.get<uint8_t>(Ereal);
+    if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (lattice)");
 
     EmbedArgs ea{};
     ea.feat = feat;
@@ -736,9 +785,14 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     if (hst.code != 0) return bail(hst.code, "lattice build failed");
     L.L = (int)hL;
 
-    L.nbr = dalloc<int2>((size_t)L.L * (D + 1), s, &acc);
-    L.vkeys = dalloc<uint16_t>((size_t)L.L * (D + 1), s, &acc);
-    if (!L.nbr || !L.vkeys) return bail(DCRF_ERR_OOM, "device allocation failed (neighbours)");
+    const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
+    per.reserve(Arena::sz<int2>((size_t)L.L * (D + 1)) + Arena::sz<uint16_t>((size_t)L.L * (D + 1)) +
+                2 * Arena::sz<int>(tm.ntiles + 1) + 2 * (Arena::sz<uint16_t>(ntl) + Arena::sz<float>(ntl)));
+    tmp.reserve(Arena::sz<uint16_t>(ntl) + 2 * Arena::sz<int>(ntl) + 2 * Arena::sz<uint32_t>(tm.ntiles + 1) +
+                Arena::sz<uint32_t>(4));
+    L.nbr = per.get<int2>((size_t)L.L * (D + 1));
+    L.vkeys = per.get<uint16_t>((size_t)L.L * (D + 1));
+    if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (neighbours)");
     if (E > 0)
         DCRF_LAUNCH(offsets_kernel<D><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, table, slot, vid, E, N, L.off, L.vkeys));
     if (L.L > 0)
@@ -746,35 +800,27 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
                                                                                   vid, L.vkeys, L.L, L.nbr));
     // ---- splat tiles: partials, member lists, slice tables, tasks ----------------
     L.ntiles = tm.ntiles;
-    L.tile_pbeg = dalloc<int>(L.ntiles + 1, s, &acc);
-    L.tile_tbeg = dalloc<int>(L.ntiles + 1, s, &acc);
-    const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
-    L.mem_pt = dalloc<uint16_t>(ntl, s, &acc);
-    L.mem_w = dalloc<float>(ntl, s, &acc);
-    L.tl_loc = dalloc<uint16_t>(ntl, s, &acc);
-    L.tl_w = dalloc<float>(ntl, s, &acc);
+    L.tile_pbeg = per.get<int>(L.ntiles + 1);
+    L.tile_tbeg = per.get<int>(L.ntiles + 1);
+    // member and slice tables side by side: zeroed as two memsets
+    L.mem_pt = per.get<uint16_t>(ntl);
+    L.mem_w = per.get<float>(ntl);
+    L.tl_loc = per.get<uint16_t>(ntl);
+    L.tl_w = per.get<float>(ntl);
     uint16_t *cl = tmp.get<uint16_t>(ntl);
     int *pvx = tmp.get<int>(ntl);
     int *pcnt = tmp.get<int>(ntl);
     uint32_t *tile_np = tmp.get<uint32_t>(L.ntiles + 1);
     uint32_t *tile_nt = tmp.get<uint32_t>(L.ntiles + 1);
     uint32_t *maxes = tmp.get<uint32_t>(4);
-    if (!L.tile_pbeg || !L.tile_tbeg || !L.mem_pt || !L.mem_w || !L.tl_loc || !L.tl_w || tmp.failed)
-        return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
+    if (per.failed || tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
     // empty slots and padding: local index 0, weight 0
-    cudaMemsetAsync(L.tl_loc, 0, ntl * sizeof(uint16_t), s);
-    cudaMemsetAsync(L.tl_w, 0, ntl * sizeof(float), s);
-    cudaMemsetAsync(L.mem_pt, 0, ntl * sizeof(uint16_t), s);
-    cudaMemsetAsync(L.mem_w, 0, ntl * sizeof(float), s);
+    zero_pair(L.mem_pt, ntl, L.mem_w, ntl, s);
+    zero_pair(L.tl_loc, ntl, L.tl_w, ntl, s);
     cudaMemsetAsync(maxes, 0, 4 * sizeof(uint32_t), s);
     const size_t smem_g = (2 * (size_t)TG<D>::HT + TG<D>::C) * sizeof(int);
     const size_t smem_p = 2 * (size_t)TG<D>::C * sizeof(int) + (TG_THREADS / 32) * (size_t)TG<D>::C * sizeof(uint16_t);
-    // opt in to the exact dynamic shared memory (the 48 KB default leaves no room for the
-    // kernels' static shared memory at d = 7, where smem_p is exactly 48 KB)
-    if (cudaFuncSetAttribute(tile_group_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_g) !=
-            cudaSuccess ||
-        cudaFuncSetAttribute(tile_place_kernel<D>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_p) !=
-            cudaSuccess)
+    if (tile_kernels_optin<D>(smem_g, smem_p) != cudaSuccess)
         return bail(DCRF_ERR_CUDA, "tile kernels: shared-memory opt-in failed");
     uint32_t hcnt[4] = {0, 0, 0, 0};  // P, T, max partials, max tasks of a tile
     if (L.ntiles > 0) {
@@ -802,15 +848,18 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     L.P = (int)hcnt[0];
     L.max_np = (int)hcnt[2];
     L.max_nt = (int)hcnt[3];
-    L.part_v = dalloc<int>((size_t)L.P + 1, s, &acc);
-    L.part_mend = dalloc<int>((size_t)L.P + 8, s, &acc);
-    L.red_beg = dalloc<int>((size_t)L.L + 1, s, &acc);
-    L.red_list = dalloc<int>((size_t)L.P + 1, s, &acc);
-    L.task = dalloc<uint32_t>((size_t)hcnt[1] + 8, s, &acc);
-    if (!L.part_v || !L.part_mend || !L.red_beg || !L.red_list || !L.task)
-        return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
-    cudaMemsetAsync(L.part_mend, 0, sizeof(int) * ((size_t)L.P + 8), s);
-    cudaMemsetAsync(L.task, 0, sizeof(uint32_t) * ((size_t)hcnt[1] + 8), s);
+    per.reserve(2 * Arena::sz<int>((size_t)L.P + 1) + Arena::sz<int>((size_t)L.P + 8) + Arena::sz<int>((size_t)L.L + 1) +
+                Arena::sz<uint32_t>((size_t)hcnt[1] + 8));
+    const size_t radix_words = radix_temp_words((size_t)L.P) + scan_temp_words((size_t)L.L + 1);
+    tmp.reserve(Arena::sz<uint32_t>((size_t)L.L + 1) + 4 * Arena::sz<uint32_t>((size_t)L.P + 1) +
+                Arena::sz<uint32_t>(radix_words));
+    L.part_v = per.get<int>((size_t)L.P + 1);
+    L.red_beg = per.get<int>((size_t)L.L + 1);
+    L.red_list = per.get<int>((size_t)L.P + 1);
+    L.part_mend = per.get<int>((size_t)L.P + 8);
+    L.task = per.get<uint32_t>((size_t)hcnt[1] + 8);
+    if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
+    zero_pair(L.part_mend, (size_t)L.P + 8, L.task, (size_t)hcnt[1] + 8, s);
     if (L.ntiles > 0) {
         DCRF_LAUNCH(tile_place_kernel<D><<<L.ntiles, TG_THREADS, smem_p, s>>>(
             cl, pvx, pcnt, L.bary, N, tm.slot_pt, (const uint32_t *)L.tile_pbeg, (const uint32_t *)L.tile_tbeg,
@@ -823,7 +872,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         uint32_t *cnt = tmp.get<uint32_t>((size_t)L.L + 1);
         uint32_t *k0 = tmp.get<uint32_t>((size_t)L.P + 1), *v0 = tmp.get<uint32_t>((size_t)L.P + 1);
         uint32_t *k1 = tmp.get<uint32_t>((size_t)L.P + 1), *v1 = tmp.get<uint32_t>((size_t)L.P + 1);
-        uint32_t *rtemp = tmp.get<uint32_t>(radix_temp_words((size_t)L.P) + scan_temp_words((size_t)L.L + 1));
+        uint32_t *rtemp = tmp.get<uint32_t>(radix_words);
         if (tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (reduce lists)");
         cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ((size_t)L.L + 1), s);
         if (L.P > 0) DCRF_LAUNCH(count_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, L.L, cnt, status));
@@ -832,14 +881,11 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
             return bail(DCRF_ERR_CUDA, "scan failed");
         if (L.L == 0) DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.red_beg, 0));
         if (L.P > 0) {
-            cudaMemcpyAsync(k0, L.part_v, sizeof(uint32_t) * L.P, cudaMemcpyDeviceToDevice, s);
-            DCRF_LAUNCH(iota_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(v0, L.P));
             int bits = 1;
             while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)L.L) bits++;
-            int in_alt = 0;
-            if (radix_sort_pairs_u32(k0, v0, k1, v1, (size_t)L.P, bits, rtemp, s, &in_alt) != cudaSuccess)
+            if (radix_argsort_u32((const uint32_t *)L.part_v, (size_t)L.P, bits, (uint32_t *)L.red_list, k0, v0, k1,
+                                  v1, rtemp, s) != cudaSuccess)
                 return bail(DCRF_ERR_CUDA, "radix sort failed");
-            cudaMemcpyAsync(L.red_list, in_alt ? v1 : v0, sizeof(uint32_t) * L.P, cudaMemcpyDeviceToDevice, s);
         }
     }
     // no synchronisation here: the temporaries go back to the pool in stream
@@ -848,10 +894,11 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     tmp.release();
     ce = cudaGetLastError();
     if (ce != cudaSuccess) {
-        lattice_free(&L, s);
+        per.release();
         return fail(DCRF_ERR_CUDA, std::string("lattice build launch: ") + cudaGetErrorString(ce));
     }
-    L.bytes = acc;
+    L.bytes = per.bytes;
+    L.blocks = per.blocks;
     *out = L;
     return DCRF_OK;
 }
@@ -859,11 +906,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
 }  // namespace
 
 void lattice_free(LatticeDev *L, cudaStream_t s) {
-    void *ps[] = {L->off,       L->bary,   L->wslice,  L->rank,    L->nbr,      L->vkeys,  L->part_v, L->part_mend,
-                  L->tile_pbeg, L->mem_pt, L->mem_w,   L->red_beg, L->red_list, L->tl_loc, L->tl_w,
-                  L->task,      L->tile_tbeg};
-    for (void *p : ps)
-        if (p) cudaFreeAsync(p, s);
+    for (void *p : L->blocks) cudaFreeAsync(p, s);
     *L = LatticeDev{};
 }
 

@@ -37,6 +37,7 @@ struct LatticeDev {
     uint16_t *tl_loc = nullptr;  // index of the corner's vertex among the tile's partials
     float *tl_w = nullptr;       // the corner's barycentric weight
     size_t bytes = 0;
+    std::vector<void *> blocks;  // the pool blocks the tables above are carved from
 };
 
 // Image segmentation of the point set (a single image: nseg = 1).

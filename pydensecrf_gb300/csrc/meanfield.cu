@@ -600,6 +600,9 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                     float acc[VW];
 #pragma unroll
                     for (int e = 0; e < VW; e++) acc[e] = 0.f;
+                    // two members per trip: their loads overlap (measured 4% on
+                    // the point pass at 21 labels; wider unrolls lose it again)
+#pragma unroll 2
                     for (int e = e0; e < e0 + len; e++) {
                         const float w = mw[e];
                         float v[VW];
@@ -631,7 +634,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                     vstore<VW>(T.pv + (size_t)(b.pb + pl) * MP + m0, acc);
                 }
             }
-            __syncthreads();
+            if (k + 1 < a.ts.n) __syncthreads();  // the next term reuses sRes
         }
     }
 }
@@ -718,32 +721,41 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
     }
 }
 
+// Sum of each vertex's tile partials.  A vertex gets G lanes per row (CH
+// labels each) times R row slots; slot r sums list positions r*G..r*G+G-1 of
+// every batch of G*R positions in list order (independent loads), and the
+// slots' sums combine in a fixed pairwise tree, so the result depends only on
+// the vertex's own list.  Terms whose vertices average many partials (large
+// spatial bandwidths) take R = 32/G to shorten their longest chains.
 template <int MP>
 __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ ReduceArgs a) {
     constexpr int G = Grp<MP>::G, CH = Grp<MP>::CH;
     pdl_trigger();
-    const long long gidx = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / G;
-    const int lgi = threadIdx.x % G;
-    if (gidx >= a.begin[a.n]) return;
+    const long long gt = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (gt >= a.begin[a.n]) return;
     int k = 0;
-    while (gidx >= a.begin[k + 1]) k++;
+    while (gt >= a.begin[k + 1]) k++;
     const ReduceArgs::T &T = a.t[k];
-    const int v = (int)(gidx - a.begin[k]);
+    const int GR = G * a.rs[k];
+    const long long loc = gt - a.begin[k];
+    const int v = (int)(loc / GR);
+    if (v >= T.L) return;  // the whole group: groups never straddle terms or warps
+    const int l = (int)(loc - (long long)v * GR);
+    const int lgi = l % G, r0 = l - lgi;  // r0 = slot * G
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned gmask = GR == 32 ? 0xffffffffu : (((1u << GR) - 1u) << (lane & ~(unsigned)(GR - 1)));
     const int s0 = T.red_beg[v], s1 = T.red_beg[v + 1];
     float acc[CH];
 #pragma unroll
     for (int c = 0; c < CH; c++) acc[c] = 0.f;
-    // the group's lanes fetch G partial indices at a time; the rows are then
-    // read back to back (independent loads), added in list order
-    const unsigned gmask = (G == 32) ? 0xffffffffu : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
     pdl_wait();  // the partials come from the previous kernel
-    for (int b = s0; b < s1; b += G) {
-        const int mine = (b + lgi < s1) ? T.red_list[b + lgi] : 0;
-        const int cnt = min(G, s1 - b);
+    for (int b = s0; b < s1; b += GR) {
+        const int mine = (b + l < s1) ? T.red_list[b + l] : 0;
+        const int cnt = min(GR, s1 - b) - r0;  // rows of this slot in the batch (may be <= 0)
         float rowv[G][CH];
 #pragma unroll
         for (int j = 0; j < G; j++) {
-            const int p = __shfl_sync(gmask, mine, j, G);
+            const int p = __shfl_sync(gmask, mine, r0 + j, GR);
 #pragma unroll
             for (int c = 0; c < CH; c++) rowv[j][c] = j < cnt ? T.partial[(size_t)p * MP + lgi + c * G] : 0.f;
         }
@@ -754,6 +766,10 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
                 for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], rowv[j][c]);
             }
     }
+    for (int o = G; o < GR; o <<= 1)
+#pragma unroll
+        for (int c = 0; c < CH; c++) acc[c] = fadd(acc[c], __shfl_xor_sync(gmask, acc[c], o, GR));
+    if (r0 != 0) return;
     float *dst = T.V + (size_t)(v + 1) * MP + lgi;
 #pragma unroll
     for (int c = 0; c < CH; c++) dst[c * G] = acc[c];
@@ -1107,8 +1123,17 @@ cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s) {
 }
 
 template <int MP>
-static cudaError_t red_launch(const ReduceArgs &a, cudaStream_t s) {
-    long long threads = a.begin[a.n] * Grp<MP>::G;
+static cudaError_t red_launch(ReduceArgs a, cudaStream_t s) {
+    constexpr int G = Grp<MP>::G;
+    long long threads = 0;
+    for (int k = 0; k < a.n; k++) {
+        // more than 4 partials per vertex on average: a full warp per vertex
+        const bool wide = a.t[k].L > 0 && a.t[k].P > 4ll * a.t[k].L;
+        a.rs[k] = wide ? 32 / G : 1;
+        a.begin[k] = threads;
+        threads += ((long long)a.t[k].L * G * a.rs[k] + 31) / 32 * 32;
+    }
+    a.begin[a.n] = threads;
     if (threads > 0) return launch_pdl(reduce_kernel<MP>, dim3((unsigned)((threads + 255) / 256)), dim3(256), 0, s, a);
     return cudaGetLastError();
 }

@@ -53,9 +53,12 @@ struct ReduceArgs {
         const int *red_list;  // [P]
         const float *partial; // [P][MP]
         float *V;             // [L+1][MP]
-        int L;
+        int L, P;
     } t[DCRF_MAX_TERMS];
-    long long begin[DCRF_MAX_TERMS + 1];  // prefix of vertex work over terms
+    // set by launch_reduce: row slots of a vertex's lane group, and the prefix
+    // of threads over terms (each term's range starts on a warp boundary)
+    int rs[DCRF_MAX_TERMS];
+    long long begin[DCRF_MAX_TERMS + 1];
 };
 
 struct BlurArgs {

@@ -75,6 +75,56 @@ __global__ void scan_tile_kernel(const uint32_t *in, uint32_t *out, size_t n, co
     if (d_total && threadIdx.x == 0) *d_total = off + total;
 }
 
+// Exclusive scan of up to a few 16384-element chunks by one block of 1024
+// threads (16 consecutive items each), carrying the running total across
+// chunks: one launch instead of the three of the multi-block scan.
+constexpr int SMALL_THREADS = 1024, SMALL_ITEMS = 16, SMALL_CHUNK = SMALL_THREADS * SMALL_ITEMS;
+constexpr size_t SCAN_SMALL_MAX = 4 * (size_t)SMALL_CHUNK;
+
+__global__ void __launch_bounds__(SMALL_THREADS) scan_small_kernel(const uint32_t *in, uint32_t *out, size_t n,
+                                                                   uint32_t *__restrict__ d_total) {
+    __shared__ uint32_t s_warp[SMALL_THREADS / 32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t carry = 0;
+    for (size_t c0 = 0; c0 < n; c0 += SMALL_CHUNK) {
+        const size_t base = c0 + (size_t)threadIdx.x * SMALL_ITEMS;
+        uint32_t v[SMALL_ITEMS];
+        uint32_t sum = 0;
+#pragma unroll
+        for (int k = 0; k < SMALL_ITEMS; k++) {
+            v[k] = base + k < n ? in[base + k] : 0u;
+            sum += v[k];
+        }
+        uint32_t x = sum;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (warp == 0) {
+            uint32_t w = s_warp[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+                if (lane >= o) w += y;
+            }
+            s_warp[lane] = w;
+        }
+        __syncthreads();
+        uint32_t run = carry + (warp ? s_warp[warp - 1] : 0u) + x - sum;
+#pragma unroll
+        for (int k = 0; k < SMALL_ITEMS; k++) {
+            if (base + k < n) out[base + k] = run;
+            run += v[k];
+        }
+        carry += s_warp[SMALL_THREADS / 32 - 1];
+        __syncthreads();  // s_warp is rewritten by the next chunk
+    }
+    if (d_total && threadIdx.x == 0) *d_total = carry;
+}
+
 size_t scan_temp_words(size_t n) {
     size_t w = 0;
     while (n > (size_t)SCAN_TILE) {
@@ -89,6 +139,10 @@ static cudaError_t scan_rec(const uint32_t *in, uint32_t *out, size_t n, uint32_
     size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
     if (nb <= 1) {
         DCRF_LAUNCH(scan_tile_kernel<<<1, SCAN_THREADS, 0, s>>>(in, out, n, nullptr, d_total));
+        return cudaGetLastError();
+    }
+    if (n <= SCAN_SMALL_MAX) {
+        DCRF_LAUNCH(scan_small_kernel<<<1, SMALL_THREADS, 0, s>>>(in, out, n, d_total));
         return cudaGetLastError();
     }
     uint32_t *sums = temp;
@@ -132,6 +186,7 @@ __global__ void radix_hist_kernel(const uint32_t *__restrict__ keys, size_t n, i
     hist[(size_t)threadIdx.x * nblocks + blockIdx.x] = cnt[threadIdx.x];
 }
 
+// vals == nullptr: the value of item i is i (first pass of an argsort)
 __global__ void radix_scatter_kernel(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals, size_t n,
                                      int shift, const uint32_t *__restrict__ hist, unsigned nblocks,
                                      uint32_t *__restrict__ keys_out, uint32_t *__restrict__ vals_out) {
@@ -148,7 +203,7 @@ __global__ void radix_scatter_kernel(const uint32_t *__restrict__ keys, const ui
         size_t i = base + (size_t)r * RADIX_THREADS + threadIdx.x;
         bool valid = i < n;
         uint32_t key = valid ? keys[i] : 0u;
-        uint32_t val = valid ? vals[i] : 0u;
+        uint32_t val = valid ? (vals ? vals[i] : (uint32_t)i) : 0u;
         uint32_t digit = valid ? ((key >> shift) & 255u) : 256u;
         uint32_t peers = __match_any_sync(0xffffffffu, digit);
         int leader = __ffs(peers) - 1;
@@ -182,32 +237,29 @@ size_t radix_temp_words(size_t n) {
     return (h + 63) / 64 * 64 + scan_temp_words(h);
 }
 
-cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
-                                 int bits, uint32_t *temp, cudaStream_t s, int *result_in_alt) {
-    *result_in_alt = 0;
+cudaError_t radix_argsort_u32(const uint32_t *keys, size_t n, int bits, uint32_t *vals_out, uint32_t *k0, uint32_t *v0,
+                              uint32_t *k1, uint32_t *v1, uint32_t *temp, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     unsigned nb = (unsigned)((n + RADIX_TILE - 1) / RADIX_TILE);
     size_t h = 256 * (size_t)nb;
     uint32_t *hist = temp;
     uint32_t *stemp = temp + (h + 63) / 64 * 64;
-    uint32_t *kin = keys, *vin = vals, *kout = keys_alt, *vout = vals_alt;
     int passes = (bits + 7) / 8;
     if (passes < 1) passes = 1;
+    const uint32_t *kin = keys, *vin = nullptr;
     for (int p = 0; p < passes; p++) {
-        int shift = 8 * p;
+        const int shift = 8 * p;
+        // ping-pong between (k1, v1) and (k0, v0); the last pass writes the values out
+        uint32_t *kout = (p & 1) ? k0 : k1;
+        uint32_t *vout = p == passes - 1 ? vals_out : (p & 1) ? v0 : v1;
         DCRF_LAUNCH(radix_hist_kernel<<<nb, RADIX_THREADS, 0, s>>>(kin, n, shift, hist, nb));
         cudaError_t e = scan_exclusive_u32(hist, hist, h, nullptr, stemp, s);
         if (e != cudaSuccess) return e;
         DCRF_LAUNCH(radix_scatter_kernel<<<nb, RADIX_THREADS, 0, s>>>(kin, vin, n, shift, hist, nb, kout, vout));
         e = cudaGetLastError();
         if (e != cudaSuccess) return e;
-        uint32_t *t = kin;
         kin = kout;
-        kout = t;
-        t = vin;
         vin = vout;
-        vout = t;
-        *result_in_alt ^= 1;
     }
     return cudaSuccess;
 }

@@ -14,9 +14,10 @@ cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, size_t n, uint
 
 // Workspace (in 32-bit words) needed by radix_sort_pairs_u32 for n elements.
 size_t radix_temp_words(size_t n);
-// Stable sort of (keys, vals) by the low `bits` bits of keys, ping-ponging with
-// (keys_alt, vals_alt); *result_in_alt tells which pair holds the result.
-cudaError_t radix_sort_pairs_u32(uint32_t *keys, uint32_t *vals, uint32_t *keys_alt, uint32_t *vals_alt, size_t n,
-                                 int bits, uint32_t *temp, cudaStream_t s, int *result_in_alt);
+// Stable argsort by the low `bits` bits of keys[0..n): vals_out[j] = the index
+// of the j-th item in key order (ties in index order).  k0, v0, k1, v1 are n-word
+// work arrays; keys is only read.
+cudaError_t radix_argsort_u32(const uint32_t *keys, size_t n, int bits, uint32_t *vals_out, uint32_t *k0, uint32_t *v0,
+                              uint32_t *k1, uint32_t *v1, uint32_t *temp, cudaStream_t s);
 
 }  // namespace dcrf
