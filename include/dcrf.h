@@ -324,6 +324,17 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
 int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out,
                                 void *stream);
 
+/* Failure-detection check of the device-side bounded waits.  Launches, on the
+ * handle's stream, one warp that waits on a device flag nothing sets, giving up
+ * after `spins` polls (1..1048576, each followed by a ~256 ns sleep) the way the
+ * point pass's copy barrier and the cooperative blur's grid barrier give up: it
+ * records DCRF_ERR_TIMEOUT in the handle's device status block and returns.
+ * The call synchronises and returns that status (DCRF_ERR_TIMEOUT expected;
+ * anything else means the wait or the status path is broken); the status is
+ * cleared and the handle stays usable.
+ * No counterpart in the reference (a diagnostic of this engine). */
+int dcrf_check_bounded_wait(dcrf_crf *h, int spins);
+
 #ifdef __cplusplus
 }
 #endif

@@ -47,6 +47,7 @@ _SIGS = {
     "dcrf_autotune": ([_vp], _i),
     "dcrf_get_tuning": ([_vp, _vp, _vp, _vp, _vp, _vp], _i),
     "dcrf_set_tuning": ([_vp, _i, _i, _i, ctypes.c_float, _i], _i),
+    "dcrf_check_bounded_wait": ([_vp, _i], _i),
     "dcrf_destroy": ([_vp], _i),
     "dcrf_set_stream": ([_vp, _vp], _i),
     "dcrf_set_variant": ([_vp, _i], _i),

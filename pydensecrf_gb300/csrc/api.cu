@@ -953,7 +953,7 @@ int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
 // compatibility kind, normalisation, arithmetic variant), one image or a batch,
 // and the size class log2(N) -- by timing candidates on the handle's own
 // lattices, and remembers the choice for the process.  Build knobs: hash load
-// factor (1.5, 2, 3) and splat task length (8, 16, 32), scored as one build
+// factor (1.5, 2, 3) and splat task length (16, 24, 32), scored as one build
 // plus ten iterations; launch knobs: threads per point (1, 2) and the point
 // pass's shared-memory budget (default, or 72 KB for three CTAs per SM).
 // Only the task length changes results (the grouping of the splat sums).
@@ -1008,7 +1008,7 @@ int autotune_now(dcrf_crf *h) {
     TuneCfg best = h->tune;
     double best_score = 1e30;
     const float loads[3] = {1.5f, 2.0f, 3.0f};
-    const int tasks[3] = {8, 16, 32};
+    const int tasks[3] = {16, 24, 32};
     for (float ld : loads)
         for (int tk : tasks) {
             h->tune.hash_load = ld;
@@ -1314,6 +1314,17 @@ int kernel_count(const Term &T) {
 
 }  // namespace
 
+// A wait on a flag that nothing sets, bounded like the library's other device
+// waits (poll, sleep, give up): it must end in the status block, not hang.
+__global__ void bounded_wait_probe_kernel(const volatile unsigned *flag, int spins, DevStatus *st) {
+    if (threadIdx.x != 0) return;
+    for (int it = 0; it < spins; it++) {
+        if (*flag != 0u) return;
+        __nanosleep(256);
+    }
+    dcrf_set_error(st, DCRF_ERR_TIMEOUT, -1);
+}
+
 extern "C" {
 
 int dcrf_abi_version(void) { return DCRF_ABI_VERSION; }
@@ -1383,6 +1394,20 @@ int dcrf_destroy(dcrf_crf *h) {
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
     return ok();
+}
+
+int dcrf_check_bounded_wait(dcrf_crf *h, int spins) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (spins < 1 || spins > (1 << 20)) return set_err(DCRF_ERR_INVALID_ARG, "spins must be in [1, 1048576]");
+    unsigned *flag = nullptr;
+    if ((rc = dev_alloc_async(&flag, 1, h->stream))) return rc;
+    CU(cudaMemsetAsync(flag, 0, sizeof(unsigned), h->stream));
+    DCRF_LAUNCH(bounded_wait_probe_kernel<<<1, 32, 0, h->stream>>>(flag, spins, h->status));
+    dev_free_async(flag, h->stream);
+    rc = sync_check(h);
+    if (rc == DCRF_ERR_TIMEOUT) set_err(rc, "bounded device wait gave up as expected (" + g_err + ")");
+    return rc;
 }
 
 int dcrf_set_stream(dcrf_crf *h, void *s) {
