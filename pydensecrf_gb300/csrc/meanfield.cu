@@ -775,6 +775,34 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
     for (int c = 0; c < CH; c++) dst[c * G] = acc[c];
 }
 
+// Copies a vertex's VEC values y into its partial rows pv[list[q]] for q in
+// [s0, s1) (the scatter of the filter's last blur pass).  Eight indices are
+// fetched before their stores, so a vertex with many partials (a large
+// spatial bandwidth: over a hundred) costs a few load round trips, not one
+// per partial.
+template <int MP, int VEC>
+__device__ __forceinline__ void scatter_partials(float *__restrict__ pv, const int *__restrict__ list, int s0, int s1,
+                                                 int col, const float (&y)[VEC]) {
+    auto put = [&](int p) {
+        float *dst = pv + (size_t)p * MP + col;
+        if constexpr (VEC == 4) {
+            *reinterpret_cast<float4 *>(dst) = make_float4(y[0], y[1], y[2], y[3]);
+        } else {
+#pragma unroll
+            for (int e = 0; e < VEC; e++) dst[e] = y[e];
+        }
+    };
+    int q = s0;
+    for (; q + 8 <= s1; q += 8) {
+        int idx[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) idx[u] = __ldg(list + q + u);
+#pragma unroll
+        for (int u = 0; u < 8; u++) put(idx[u]);
+    }
+    for (; q < s1; q++) put(__ldg(list + q));
+}
+
 template <int MP, bool SEQ>
 __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurArgs a) {
     constexpr int VEC = (MP % 4 == 0) ? 4 : (MP % 2 == 0) ? 2 : 1;
@@ -822,18 +850,7 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
             for (int e = 0; e < VEC; e++) T.Vout[o0 + e] = y[e];
         }
     }
-    if (T.pv) {
-        const int s0 = T.red_beg[v], s1 = T.red_beg[v + 1];
-        for (int q = s0; q < s1; q++) {
-            float *dst = T.pv + (size_t)T.red_list[q] * MP + c * VEC;
-            if constexpr (VEC == 4) {
-                *reinterpret_cast<float4 *>(dst) = make_float4(y[0], y[1], y[2], y[3]);
-            } else {
-#pragma unroll
-                for (int e = 0; e < VEC; e++) dst[e] = y[e];
-            }
-        }
-    }
+    if (T.pv) scatter_partials<MP, VEC>(T.pv, T.red_list, T.red_beg[v], T.red_beg[v + 1], c * VEC, y);
 }
 
 // Bounded grid barrier of a cooperative launch: the last CTA to arrive resets
@@ -933,18 +950,7 @@ __global__ void __launch_bounds__(256) blur_chains_kernel(const __grid_constant_
                     for (int e = 0; e < VEC; e++) Vout[o0 + e] = y[e];
                 }
             }
-            if (last && C.pv) {
-                const int s0 = C.red_beg[v], s1 = C.red_beg[v + 1];
-                for (int q = s0; q < s1; q++) {
-                    float *dst = C.pv + (size_t)C.red_list[q] * MP + c * VEC;
-                    if constexpr (VEC == 4) {
-                        *reinterpret_cast<float4 *>(dst) = make_float4(y[0], y[1], y[2], y[3]);
-                    } else {
-#pragma unroll
-                        for (int e = 0; e < VEC; e++) dst[e] = y[e];
-                    }
-                }
-            }
+            if (last && C.pv) scatter_partials<MP, VEC>(C.pv, C.red_list, C.red_beg[v], C.red_beg[v + 1], c * VEC, y);
         }
         if (p + 1 < a.npass && !grid_barrier(a.bar, gridDim.x, a.status)) return;
     }
@@ -975,33 +981,87 @@ __device__ __forceinline__ size_t user_offset(int point_major, int M, int N, con
     return (size_t)s0 * M + (size_t)m * nb + (p - s0);
 }
 
-// out[slot][m] = in(m, slot_pt[slot]) for m < M; 0 for padding labels m < ld
-// and for empty slots
-__global__ void to_slots_kernel(const float *__restrict__ in, int point_major, int M, int ld, int N,
-                                const int *__restrict__ seg, int nseg, const int *__restrict__ slot_pt, int nslots,
-                                float *__restrict__ out) {
-    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (s >= (size_t)nslots) return;
-    const int pt = slot_pt[s];
+// Caller-layout <-> slot-row copies, one tile of SPLAT_TILE slots per block.
+// The tile passes through shared memory (row pitch ld + 1, conflict-free), so
+// that the caller's buffer is read or written with consecutive threads on
+// consecutive addresses -- labels of a point for point-major buffers, points
+// of a label for label-major ones -- and the tile's slot rows, one contiguous
+// block of SPLAT_TILE * ld floats, with coalesced stores or loads.
+constexpr int SLOT_PITCH_MAX = DCRF_MAX_MP + 1;
+
+struct SlotTile {
+    float rows[SPLAT_TILE * SLOT_PITCH_MAX];
+    size_t o0[SPLAT_TILE], step[SPLAT_TILE];  // caller offset of label 0, stride between labels
+    int pt[SPLAT_TILE];
+};
+
+__device__ __forceinline__ void slot_tile_points(SlotTile &st, int point_major, int M, int N, const int *seg, int nseg,
+                                                 const int *slot_pt) {
+    const int li = threadIdx.x;
+    const int p = slot_pt[(size_t)blockIdx.x * SPLAT_TILE + li];
     size_t o0 = 0, step = 0;
-    if (pt >= 0) {
-        o0 = user_offset(point_major, M, N, seg, nseg, pt, 0);
-        step = M > 1 ? user_offset(point_major, M, N, seg, nseg, pt, 1) - o0 : 0;
+    if (p >= 0) {
+        o0 = user_offset(point_major, M, N, seg, nseg, p, 0);
+        step = M > 1 ? user_offset(point_major, M, N, seg, nseg, p, 1) - o0 : 0;
     }
-    float *dst = out + s * ld;
-    for (int m = 0; m < ld; m++) dst[m] = (pt >= 0 && m < M) ? in[o0 + m * step] : 0.f;
+    st.pt[li] = p;
+    st.o0[li] = o0;
+    st.step[li] = step;
 }
 
-// out(m, pt) = in[pt_slot[pt]][m]
-__global__ void from_slots_kernel(const float *__restrict__ in, int M, int ld, int N, const int *__restrict__ seg,
-                                  int nseg, const int *__restrict__ pt_slot, int point_major,
-                                  float *__restrict__ out) {
-    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
-    if (pt >= N) return;
-    const float *src = in + (size_t)pt_slot[pt] * ld;
-    const size_t o0 = user_offset(point_major, M, N, seg, nseg, pt, 0);
-    const size_t step = M > 1 ? user_offset(point_major, M, N, seg, nseg, pt, 1) - o0 : 0;
-    for (int m = 0; m < M; m++) out[o0 + m * step] = src[m];
+// element f of the tile's caller-side walk: (slot q, label m)
+__device__ __forceinline__ void slot_tile_elem(int f, int point_major, int M, int &q, int &m) {
+    if (point_major) {
+        q = f / M;
+        m = f - q * M;
+    } else {
+        m = f / SPLAT_TILE;
+        q = f - m * SPLAT_TILE;
+    }
+}
+
+// out[slot][m] = in(m, slot_pt[slot]) for m < M; 0 for padding labels m < ld
+// and for empty slots
+__global__ void __launch_bounds__(SPLAT_TILE) to_slots_kernel(const float *__restrict__ in, int point_major, int M,
+                                                              int ld, int N, const int *__restrict__ seg, int nseg,
+                                                              const int *__restrict__ slot_pt,
+                                                              float *__restrict__ out) {
+    __shared__ SlotTile st;
+    const int li = threadIdx.x, pitch = ld + 1;
+    slot_tile_points(st, point_major, M, N, seg, nseg, slot_pt);
+    __syncthreads();
+    for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE) {
+        int q, m;
+        slot_tile_elem(f, point_major, M, q, m);
+        st.rows[q * pitch + m] = st.pt[q] >= 0 ? in[st.o0[q] + (size_t)m * st.step[q]] : 0.f;
+    }
+    __syncthreads();
+    float *dst = out + (size_t)blockIdx.x * SPLAT_TILE * ld;
+    for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE) {
+        const int q = f / ld, m = f - q * ld;
+        dst[f] = m < M ? st.rows[q * pitch + m] : 0.f;
+    }
+}
+
+// out(m, pt) = in[slot of pt][m]
+__global__ void __launch_bounds__(SPLAT_TILE) from_slots_kernel(const float *__restrict__ in, int M, int ld, int N,
+                                                                const int *__restrict__ seg, int nseg,
+                                                                const int *__restrict__ slot_pt, int point_major,
+                                                                float *__restrict__ out) {
+    __shared__ SlotTile st;
+    const int li = threadIdx.x, pitch = ld + 1;
+    slot_tile_points(st, point_major, M, N, seg, nseg, slot_pt);
+    const float *src = in + (size_t)blockIdx.x * SPLAT_TILE * ld;
+    for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE) {
+        const int q = f / ld, m = f - q * ld;
+        if (m < M) st.rows[q * pitch + m] = src[f];
+    }
+    __syncthreads();
+    for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE) {
+        int q, m;
+        slot_tile_elem(f, point_major, M, q, m);
+        if (st.pt[q] >= 0) out[st.o0[q] + (size_t)m * st.step[q]] = st.rows[q * pitch + m];
+    }
 }
 
 // DenseCRF2D features (densecrf.cpp:61-81) of every image of the handle:
@@ -1216,17 +1276,19 @@ cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStr
 
 cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,
                             const int *slot_pt, int nslots, float *out, cudaStream_t s) {
+    if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0) return cudaErrorInvalidValue;
     if (nslots > 0)
-        DCRF_LAUNCH(to_slots_kernel<<<(nslots + 255) / 256, 256, 0, s>>>(in, point_major, M, ld, N, seg, nseg, slot_pt,
-                                                                         nslots, out));
+        DCRF_LAUNCH(to_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, point_major, M, ld, N, seg, nseg,
+                                                                               slot_pt, out));
     return cudaGetLastError();
 }
 
-cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *pt_slot,
-                              int point_major, float *out, cudaStream_t s) {
-    if (N > 0)
-        DCRF_LAUNCH(from_slots_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, ld, N, seg, nseg, pt_slot, point_major,
-                                                                      out));
+cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *slot_pt,
+                              int nslots, int point_major, float *out, cudaStream_t s) {
+    if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0) return cudaErrorInvalidValue;
+    if (nslots > 0 && N > 0)
+        DCRF_LAUNCH(from_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, M, ld, N, seg, nseg, slot_pt,
+                                                                                 point_major, out));
     return cudaGetLastError();
 }
 
