@@ -105,7 +105,8 @@ struct Term {
     float *feat = nullptr;  // [d][N] features as given (kernel parameters at identity)
     float *norm = nullptr;  // [N]
     float *V[2] = {nullptr, nullptr};  // [L+1][MP] blurred values, vertex order (ping-pong)
-    float *pv = nullptr;               // [P][MP] blurred values in partial order / splat partials
+    float *pv = nullptr;               // [P][MP] blurred values in partial order (slice input)
+    float *pout = nullptr;             // [P][MP] splat partials grouped by vertex (reduce input)
     float *compat = nullptr;  // device compat (Diagonal M / Matrix M*M symmetrised)
     float *mem_wn = nullptr;  // splat member weights times the members' norm (forward pre-normalisation)
     float *df = nullptr;      // [N][d] accumulated feature gradient (adjoint)
@@ -477,6 +478,8 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.task = T.lat.task;
     t.tile_tbeg = T.lat.tile_tbeg;
     t.pv = T.pv;
+    t.pout = T.pout;
+    t.ppos = T.lat.ppos;
     t.norm = T.norm;
     t.compat = T.compat;
     t.staged = 0;
@@ -638,7 +641,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
     int maxd = 0;
     for (size_t k = 0; k < which.size(); k++) {
         Term &T = h->terms[which[k]];
-        ra.t[k] = {T.lat.red_beg, T.lat.red_list, T.pv, S_out ? S_out[k] : T.V[0], T.lat.L, T.lat.P};
+        ra.t[k] = {T.lat.red_beg, T.pout, S_out ? S_out[k] : T.V[0], T.lat.L, T.lat.P};
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
     }
@@ -733,9 +736,10 @@ void free_term_lattice(dcrf_crf *h, Term &T) {
     dev_free_async(T.V[0], h->stream);
     dev_free_async(T.V[1], h->stream);
     dev_free_async(T.pv, h->stream);
+    dev_free_async(T.pout, h->stream);
     dev_free_async(T.mem_wn, h->stream);
     dev_free_async(T.df, h->stream);
-    T.norm = T.V[0] = T.V[1] = T.pv = T.mem_wn = T.df = nullptr;
+    T.norm = T.V[0] = T.V[1] = T.pv = T.pout = T.mem_wn = T.df = nullptr;
     for (float *&b : T.bv) {
         dev_free_async(b, h->stream);
         b = nullptr;
@@ -827,6 +831,7 @@ int build_term(dcrf_crf *h, int k) {
     if ((rc = dev_alloc_async(&T.V[0], vrows * h->MP, h->stream))) return rc;
     if ((rc = dev_alloc_async(&T.V[1], vrows * h->MP, h->stream))) return rc;
     if ((rc = dev_alloc_async(&T.pv, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return rc;
+    if ((rc = dev_alloc_async(&T.pout, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return rc;
     if ((rc = dev_alloc_async(&T.norm, (size_t)h->nslots, h->stream))) return rc;
     CU(cudaMemsetAsync(T.norm, 0, sizeof(float) * (size_t)h->nslots, h->stream));
     // the zero sentinel rows (row 0) are never written afterwards
@@ -1169,7 +1174,7 @@ int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1) {
     CU(pp(h, a, MP));
     ReduceArgs ra{};
     ra.n = 1;
-    ra.t[0] = {T.lat.red_beg, T.lat.red_list, T.pv, S, T.lat.L, T.lat.P};
+    ra.t[0] = {T.lat.red_beg, T.pout, S, T.lat.L, T.lat.P};
     ProfScope ps(h, DCRF_KCLASS_REDUCE);
     CU(launch_reduce(ra, MP, h->stream));
     return DCRF_OK;
@@ -2243,11 +2248,12 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     a.ts.t[0].pre_norm = 0;
     a.ts.t[0].mem_w = T.lat.mem_w;
     a.ts.t[0].pv = pv;
+    a.ts.t[0].pout = pv;  // splat-only pass: the scratch takes the vertex-grouped partials
     a.Qin = in_s;
     CU(launch_pointpass(a, MPv, s));
     ReduceArgs ra{};
     ra.n = 1;
-    ra.t[0] = {T.lat.red_beg, T.lat.red_list, pv, V0, T.lat.L, T.lat.P};
+    ra.t[0] = {T.lat.red_beg, pv, V0, T.lat.L, T.lat.P};
     CU(launch_reduce(ra, MPv, s));
     const int NV = MPv % 4 == 0 ? MPv / 4 : MPv % 2 == 0 ? MPv / 2 : MPv;
     const bool seq = v1 || h->M <= 2 || T.variant == DCRF_VARIANT_SCALAR;

@@ -118,7 +118,9 @@ struct TermDev {
     const float *tl_w;       // [ntiles][d+1][SPLAT_TILE] corner barycentric weight
     const uint32_t *task;    // splat tasks (see LatticeDev::task)
     const int *tile_tbeg;    // [ntiles+1] task range of each tile
-    float *pv;               // [P][MP] blurred values in partial order (read), splat partials (written)
+    float *pv;               // [P][MP] blurred values in partial order (slice input)
+    float *pout;             // [P][MP] splat partials, grouped by vertex (row ppos[p] for partial p)
+    const int *ppos;         // [P] row of each partial in pout
     const float *norm;       // [nslots]
     const float *compat;     // Diagonal [M] / Matrix [M][M] (symmetrised)
     // shared-memory plan of the point pass (byte offsets; staged = 0: global reads)

@@ -600,6 +600,12 @@ __global__ void count_kernel(const int *__restrict__ part_v, int P, int L, uint3
 
 __global__ void set_int_kernel(int *p, int v) { *p = v; }
 
+// inv[list[i]] = i for a permutation list of [0, n)
+__global__ void invert_kernel(const int *__restrict__ list, int n, int *__restrict__ inv) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) inv[list[i]] = i;
+}
+
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -848,7 +854,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     L.P = (int)hcnt[0];
     L.max_np = (int)hcnt[2];
     L.max_nt = (int)hcnt[3];
-    per.reserve(2 * Arena::sz<int>((size_t)L.P + 1) + Arena::sz<int>((size_t)L.P + 8) + Arena::sz<int>((size_t)L.L + 1) +
+    per.reserve(3 * Arena::sz<int>((size_t)L.P + 1) + Arena::sz<int>((size_t)L.P + 8) + Arena::sz<int>((size_t)L.L + 1) +
                 Arena::sz<uint32_t>((size_t)hcnt[1] + 8));
     const size_t radix_words = radix_temp_words((size_t)L.P) + scan_temp_words((size_t)L.L + 1);
     tmp.reserve(Arena::sz<uint32_t>((size_t)L.L + 1) + 4 * Arena::sz<uint32_t>((size_t)L.P + 1) +
@@ -856,6 +862,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     L.part_v = per.get<int>((size_t)L.P + 1);
     L.red_beg = per.get<int>((size_t)L.L + 1);
     L.red_list = per.get<int>((size_t)L.P + 1);
+    L.ppos = per.get<int>((size_t)L.P + 1);
     L.part_mend = per.get<int>((size_t)L.P + 8);
     L.task = per.get<uint32_t>((size_t)hcnt[1] + 8);
     if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
@@ -886,6 +893,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
             if (radix_argsort_u32((const uint32_t *)L.part_v, (size_t)L.P, bits, (uint32_t *)L.red_list, k0, v0, k1,
                                   v1, rtemp, s) != cudaSuccess)
                 return bail(DCRF_ERR_CUDA, "radix sort failed");
+            DCRF_LAUNCH(invert_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.red_list, L.P, L.ppos));
         }
     }
     // no synchronisation here: the temporaries go back to the pool in stream

@@ -35,7 +35,9 @@ struct LatticeDev {
     uint32_t *task = nullptr;     // [T+8]
     int *tile_tbeg = nullptr;     // [ntiles+1] task range of tile t
     int *red_beg = nullptr;      // [L+1]
-    int *red_list = nullptr;     // [P]
+    int *red_list = nullptr;     // [P] partials grouped by vertex (each vertex's in tile order)
+    int *ppos = nullptr;         // [P+1] position of partial p in red_list (its inverse): the row
+                                 // of p in the vertex-grouped splat output that the reduce reads
     // tile-ordered slice tables: corner r of slot li of tile t at (t*(d+1)+r)*SPLAT_TILE+li
     uint16_t *tl_loc = nullptr;  // index of the corner's vertex among the tile's partials
     float *tl_w = nullptr;       // the corner's barycentric weight

@@ -597,6 +597,8 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                 for (int j = gid; j < b.nt; j += NG) {
                     const uint32_t tk = tasks[j];
                     const int pl = (int)(tk >> 19), e0 = (int)((tk >> 6) & 0x1FFFu), len = (int)(tk & 63u);
+                    // the partial's output row, fetched before the member loop hides its latency
+                    const int prow = __ldg(T.ppos + b.pb + pl);
                     float acc[VW];
 #pragma unroll
                     for (int e = 0; e < VW; e++) acc[e] = 0.f;
@@ -612,7 +614,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                     }
                     const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
                     const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
-                    float *dst = (first && last) ? T.pv + (size_t)(b.pb + pl) * MP : sRes + (size_t)j * MP;
+                    float *dst = (first && last) ? T.pout + (size_t)prow * MP : sRes + (size_t)j * MP;
                     vstore<VW>(dst + m0, acc);
                 }
             }
@@ -623,6 +625,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                     const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
                     const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
                     if (!first || last) continue;
+                    const int prow = __ldg(T.ppos + b.pb + pl);
                     float acc[VW];
                     vload<VW>(sRes + (size_t)j * MP + m0, acc);
                     for (int jj = j + 1; jj < b.nt && (int)(tasks[jj] >> 19) == pl; jj++) {
@@ -631,7 +634,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
 #pragma unroll
                         for (int f = 0; f < VW; f++) acc[f] = fadd(acc[f], v[f]);
                     }
-                    vstore<VW>(T.pv + (size_t)(b.pb + pl) * MP + m0, acc);
+                    vstore<VW>(T.pout + (size_t)prow * MP + m0, acc);
                 }
             }
             if (k + 1 < a.ts.n) __syncthreads();  // the next term reuses sRes
@@ -721,12 +724,13 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
     }
 }
 
-// Sum of each vertex's tile partials.  A vertex gets G lanes per row (CH
-// labels each) times R row slots; slot r sums list positions r*G..r*G+G-1 of
-// every batch of G*R positions in list order (independent loads), and the
-// slots' sums combine in a fixed pairwise tree, so the result depends only on
-// the vertex's own list.  Terms whose vertices average many partials (large
-// spatial bandwidths) take R = 32/G to shorten their longest chains.
+// Sum of each vertex's tile partials, which the splat wrote as one contiguous
+// run of rows per vertex (in tile order).  A vertex gets G lanes per row (CH
+// labels each) times R row slots; slot r sums rows r*G..r*G+G-1 of every batch
+// of G*R rows in order (independent loads), and the slots' sums combine in a
+// fixed pairwise tree, so the result depends only on the vertex's own rows.
+// Terms whose vertices average many partials (large spatial bandwidths) take
+// R = 32/G to shorten their longest chains.
 template <int MP>
 __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ ReduceArgs a) {
     constexpr int G = Grp<MP>::G, CH = Grp<MP>::CH;
@@ -750,15 +754,13 @@ __global__ void __launch_bounds__(256) reduce_kernel(const __grid_constant__ Red
     for (int c = 0; c < CH; c++) acc[c] = 0.f;
     pdl_wait();  // the partials come from the previous kernel
     for (int b = s0; b < s1; b += GR) {
-        const int mine = (b + l < s1) ? T.red_list[b + l] : 0;
         const int cnt = min(GR, s1 - b) - r0;  // rows of this slot in the batch (may be <= 0)
+        const float *rows = T.partial + (size_t)(b + r0) * MP + lgi;
         float rowv[G][CH];
 #pragma unroll
-        for (int j = 0; j < G; j++) {
-            const int p = __shfl_sync(gmask, mine, r0 + j, GR);
+        for (int j = 0; j < G; j++)
 #pragma unroll
-            for (int c = 0; c < CH; c++) rowv[j][c] = j < cnt ? T.partial[(size_t)p * MP + lgi + c * G] : 0.f;
-        }
+            for (int c = 0; c < CH; c++) rowv[j][c] = j < cnt ? rows[(size_t)j * MP + c * G] : 0.f;
 #pragma unroll
         for (int j = 0; j < G; j++)
             if (j < cnt) {

@@ -49,9 +49,8 @@ struct PPArgs {
 struct ReduceArgs {
     int n;  // number of terms
     struct T {
-        const int *red_beg;   // [L+1]
-        const int *red_list;  // [P]
-        const float *partial; // [P][MP]
+        const int *red_beg;   // [L+1] vertex v's partials are rows [red_beg[v], red_beg[v+1]) of partial
+        const float *partial; // [P][MP] splat partials grouped by vertex
         float *V;             // [L+1][MP]
         int L, P;
     } t[DCRF_MAX_TERMS];
