@@ -441,7 +441,7 @@ int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where, i
     float *ddst = where == DCRF_DEVICE ? dst : h->stage;
     {
         ProfScope ps(h, DCRF_KCLASS_OTHER);
-        CU(launch_from_slots(src, M, ld, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots,
+        CU(launch_from_slots(src, M, ld, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, h->pt_slot,
                              layout == DCRF_LAYOUT_PM, ddst, h->stream));
     }
     if (where != DCRF_DEVICE)
@@ -2274,7 +2274,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     f.ts.t[0].V = Vb[(T.d + 1) & 1];
     f.Qout = in_s;
     CU(launch_pointpass(f, MPv, s));
-    CU(launch_from_slots(in_s, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, 0, out,
-                         s));
+    CU(launch_from_slots(in_s, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots,
+                         h->pt_slot, 0, out, s));
     return ok();
 }

@@ -1032,6 +1032,8 @@ __global__ void __launch_bounds__(SPLAT_TILE) to_slots_kernel(const float *__res
     const int li = threadIdx.x, pitch = ld + 1;
     slot_tile_points(st, point_major, M, N, seg, nseg, slot_pt);
     __syncthreads();
+    // eight independent loads in flight per thread
+#pragma unroll 8
     for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE) {
         int q, m;
         slot_tile_elem(f, point_major, M, q, m);
@@ -1045,7 +1047,20 @@ __global__ void __launch_bounds__(SPLAT_TILE) to_slots_kernel(const float *__res
     }
 }
 
-// out(m, pt) = in[slot of pt][m]
+// out(m, pt) = in[pt_slot[pt]][m], one thread per point: label-major output is
+// written a whole image row at a time (consecutive points on consecutive
+// addresses for every label)
+__global__ void from_slots_lm_kernel(const float *__restrict__ in, int M, int ld, int N, const int *__restrict__ seg,
+                                     int nseg, const int *__restrict__ pt_slot, float *__restrict__ out) {
+    const int pt = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pt >= N) return;
+    const float *src = in + (size_t)pt_slot[pt] * ld;
+    const size_t o0 = user_offset(0, M, N, seg, nseg, pt, 0);
+    const size_t step = M > 1 ? user_offset(0, M, N, seg, nseg, pt, 1) - o0 : 0;
+    for (int m = 0; m < M; m++) out[o0 + m * step] = src[m];
+}
+
+// out(m, pt) = in[slot of pt][m] through a shared-memory tile (point-major output)
 __global__ void __launch_bounds__(SPLAT_TILE) from_slots_kernel(const float *__restrict__ in, int M, int ld, int N,
                                                                 const int *__restrict__ seg, int nseg,
                                                                 const int *__restrict__ slot_pt, int point_major,
@@ -1054,6 +1069,7 @@ __global__ void __launch_bounds__(SPLAT_TILE) from_slots_kernel(const float *__r
     const int li = threadIdx.x, pitch = ld + 1;
     slot_tile_points(st, point_major, M, N, seg, nseg, slot_pt);
     const float *src = in + (size_t)blockIdx.x * SPLAT_TILE * ld;
+#pragma unroll 8
     for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE) {
         const int q = f / ld, m = f - q * ld;
         if (m < M) st.rows[q * pitch + m] = src[f];
@@ -1286,11 +1302,16 @@ cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int
 }
 
 cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *slot_pt,
-                              int nslots, int point_major, float *out, cudaStream_t s) {
+                              int nslots, const int *pt_slot, int point_major, float *out, cudaStream_t s) {
     if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0) return cudaErrorInvalidValue;
-    if (nslots > 0 && N > 0)
-        DCRF_LAUNCH(from_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, M, ld, N, seg, nseg, slot_pt,
-                                                                                 point_major, out));
+    if (N <= 0) return cudaGetLastError();
+    if (point_major) {
+        if (nslots > 0)
+            DCRF_LAUNCH(from_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, M, ld, N, seg, nseg, slot_pt,
+                                                                                     point_major, out));
+    } else {
+        DCRF_LAUNCH(from_slots_lm_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, ld, N, seg, nseg, pt_slot, out));
+    }
     return cudaGetLastError();
 }
 

@@ -110,7 +110,7 @@ cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStr
 cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,
                             const int *slot_pt, int nslots, float *out, cudaStream_t s);
 cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *slot_pt,
-                              int nslots, int point_major, float *out, cudaStream_t s);
+                              int nslots, const int *pt_slot, int point_major, float *out, cudaStream_t s);
 // 2D features of DenseCRF2D (densecrf.cpp:61-81) of every image into [d][N]
 cudaError_t launch_features_2d(int N, const int *seg, const int *imgW, int nseg, float sx, float sy,
                                const uint8_t *rgb, float sr, float sg, float sb, float *feat, cudaStream_t s);
