@@ -636,12 +636,30 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
                  float *const *S_out = nullptr, float *const *B_out = nullptr) {
     int MP = value1 ? 1 : h->MP;
     bool seq = value1 || h->M <= 2;
+    // Blur launches per term: passes 2i and 2i+1 share launch i (the last pass
+    // alone when d+1 is odd).  Buffers are planned backwards from the final
+    // output, alternating the term's two lattice buffers launch by launch, so
+    // that no launch reads the buffer it writes; the reduce fills the first
+    // launch's input.  (The cooperative blur keeps its pass-by-pass chain from
+    // V[0].)
+    struct Chain2 {
+        int n;
+        float *fin;
+        float *x[DCRF_MAX_D + 2];
+    };
+    std::vector<Chain2> plan(which.size());
     ReduceArgs ra{};
     ra.n = (int)which.size();
     int maxd = 0;
     for (size_t k = 0; k < which.size(); k++) {
         Term &T = h->terms[which[k]];
-        ra.t[k] = {T.lat.red_beg, T.pout, S_out ? S_out[k] : T.V[0], T.lat.L, T.lat.P};
+        Chain2 &c = plan[k];
+        c.n = (T.d + 2) / 2;
+        c.fin = B_out ? B_out[k] : partial_order ? nullptr : T.V[(T.d + 1) & 1];
+        c.x[c.n - 1] = c.fin == T.V[0] ? T.V[1] : T.V[0];
+        for (int i = c.n - 2; i >= 0; i--) c.x[i] = c.x[i + 1] == T.V[0] ? T.V[1] : T.V[0];
+        float *red_out = S_out ? S_out[k] : h->tune.coop ? T.V[0] : c.x[0];
+        ra.t[k] = {T.lat.red_beg, T.pout, red_out, T.lat.L, T.lat.P};
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
     }
@@ -676,20 +694,23 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
         return DCRF_OK;
     }
     const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
-    for (int pass = 0; pass <= maxd; pass++) {
+    for (int i = 0; 2 * i <= maxd; i++) {
         BlurArgs ba{};
         ba.n = 0;
         ba.begin[0] = 0;
         for (size_t k = 0; k < which.size(); k++) {
             Term &T = h->terms[which[k]];
-            if (pass > T.d) continue;
-            const bool last = pass == T.d;
+            const Chain2 &c = plan[k];
+            if (i >= c.n) continue;
+            const bool last = i == c.n - 1;
+            const int p = 2 * i;
             BlurArgs::T &bt = ba.t[ba.n];
-            bt.Vin = (pass == 0 && S_out) ? S_out[k] : T.V[pass & 1];
-            bt.Vout = (last && B_out) ? B_out[k] : (last && partial_order) ? nullptr : T.V[(pass + 1) & 1];
+            bt.Vin = (i == 0 && S_out) ? S_out[k] : c.x[i];
+            bt.Vout = last ? c.fin : c.x[i + 1];
             bt.nbr = T.lat.nbr;
             bt.L = T.lat.L;
-            bt.axis = transpose ? T.d - pass : pass;  // reverse blur order for the transpose (permutohedral.cpp:556)
+            bt.axis = transpose ? T.d - p : p;  // reverse blur order for the transpose (permutohedral.cpp:556)
+            bt.axis2 = p + 1 > T.d ? -1 : transpose ? T.d - (p + 1) : p + 1;
             bt.red_beg = T.lat.red_beg;
             bt.red_list = T.lat.red_list;
             bt.pv = (last && partial_order) ? T.pv : nullptr;
@@ -1220,6 +1241,7 @@ int blur_chains(dcrf_crf *h, const std::vector<Chain> &chains, bool value1) {
                     bt.nbr = T.lat.nbr;
                     bt.L = T.lat.L;
                     bt.axis = c.reverse ? T.d - pass : pass;
+                    bt.axis2 = -1;
                     bt.pv = nullptr;
                     ba.begin[ba.n + 1] = ba.begin[ba.n] + (long long)T.lat.L * NV;
                     ba.n++;
@@ -2267,6 +2289,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
         ba.t[0].nbr = T.lat.nbr;
         ba.t[0].L = T.lat.L;
         ba.t[0].axis = reverse ? T.d - pass : pass;
+        ba.t[0].axis2 = -1;
         ba.t[0].pv = nullptr;
         CU(launch_blur(ba, MPv, seq, s));
     }

@@ -805,6 +805,50 @@ __device__ __forceinline__ void scatter_partials(float *__restrict__ pv, const i
     for (; q < s1; q++) put(__ldg(list + q));
 }
 
+// One blur step at a vertex: y = x0 + 0.5 * (x1 + x2) over VEC labels, in
+// float (sseCompute, permutohedral.cpp:566) or evaluated in double
+// (seqCompute, permutohedral.cpp:505).
+template <int VEC, bool SEQ>
+__device__ __forceinline__ void blur_step(const float (&x0)[VEC], const float (&x1)[VEC], const float (&x2)[VEC],
+                                          float (&y)[VEC]) {
+#pragma unroll
+    for (int e = 0; e < VEC; e++) {
+        const float sm = fadd(x1[e], x2[e]);
+        if (SEQ)
+            y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)sm));
+        else
+            y[e] = fadd(x0[e], fmul(0.5f, sm));
+    }
+}
+
+template <int VEC>
+__device__ __forceinline__ void load_vec(const float *p, float (&x)[VEC]) {
+    if constexpr (VEC == 4) {
+        const float4 q = *reinterpret_cast<const float4 *>(p);
+        x[0] = q.x, x[1] = q.y, x[2] = q.z, x[3] = q.w;
+    } else {
+#pragma unroll
+        for (int e = 0; e < VEC; e++) x[e] = p[e];
+    }
+}
+
+// One pass along an axis at lattice row `row` (1-based; its neighbours nb are
+// rows, 0 = the zero sentinel), VEC labels from column col.
+template <int MP, int VEC, bool SEQ>
+__device__ __forceinline__ void blur_at(const float *Vin, int row, int2 nb, int col, float (&y)[VEC]) {
+    float x0[VEC], x1[VEC], x2[VEC];
+    load_vec<VEC>(Vin + (size_t)row * MP + col, x0);
+    load_vec<VEC>(Vin + (size_t)nb.x * MP + col, x1);
+    load_vec<VEC>(Vin + (size_t)nb.y * MP + col, x2);
+    blur_step<VEC, SEQ>(x0, x1, x2, y);
+}
+
+// One launch = one or two consecutive axis passes for every listed term.  Two
+// passes (axis2 >= 0) recompute the first pass at the vertex and at its two
+// neighbours along axis2 (a missing neighbour is the zero sentinel row of the
+// intermediate buffer, so 0) and apply the second: the same arithmetic as two
+// launches through an intermediate buffer, one launch and one global round
+// trip fewer.
 template <int MP, bool SEQ>
 __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurArgs a) {
     constexpr int VEC = (MP % 4 == 0) ? 4 : (MP % 2 == 0) ? 2 : 1;
@@ -818,32 +862,30 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
     const long long local = g - a.begin[k];
     const int v = (int)(local / NV);
     const int c = (int)(local - (long long)v * NV);
+    const int col = c * VEC;
+    // neighbour tables are fixed since the build: read before the wait
     const int2 nb = __ldg(T.nbr + (size_t)T.axis * T.L + v);
-    const size_t o0 = (size_t)(v + 1) * MP + c * VEC, o1 = (size_t)nb.x * MP + c * VEC, o2 = (size_t)nb.y * MP + c * VEC;
+    int2 nb2 = make_int2(0, 0), na = make_int2(0, 0), nbb = make_int2(0, 0);
+    const bool two = T.axis2 >= 0;
+    if (two) {
+        nb2 = __ldg(T.nbr + (size_t)T.axis2 * T.L + v);
+        if (nb2.x) na = __ldg(T.nbr + (size_t)T.axis * T.L + (nb2.x - 1));
+        if (nb2.y) nbb = __ldg(T.nbr + (size_t)T.axis * T.L + (nb2.y - 1));
+    }
     pdl_wait();  // the values come from the previous kernel
-    float x0[VEC], x1[VEC], x2[VEC], y[VEC];
-    if constexpr (VEC == 4) {
-        float4 p = *reinterpret_cast<const float4 *>(T.Vin + o0), q1 = *reinterpret_cast<const float4 *>(T.Vin + o1),
-               q2 = *reinterpret_cast<const float4 *>(T.Vin + o2);
-        x0[0] = p.x, x0[1] = p.y, x0[2] = p.z, x0[3] = p.w;
-        x1[0] = q1.x, x1[1] = q1.y, x1[2] = q1.z, x1[3] = q1.w;
-        x2[0] = q2.x, x2[1] = q2.y, x2[2] = q2.z, x2[3] = q2.w;
-    } else {
+    float y[VEC];
+    blur_at<MP, VEC, SEQ>(T.Vin, v + 1, nb, col, y);
+    if (two) {
+        float ya[VEC], yb[VEC], y2[VEC];
 #pragma unroll
-        for (int e = 0; e < VEC; e++) {
-            x0[e] = T.Vin[o0 + e];
-            x1[e] = T.Vin[o1 + e];
-            x2[e] = T.Vin[o2 + e];
-        }
-    }
+        for (int e = 0; e < VEC; e++) ya[e] = yb[e] = 0.f;
+        if (nb2.x) blur_at<MP, VEC, SEQ>(T.Vin, nb2.x, na, col, ya);
+        if (nb2.y) blur_at<MP, VEC, SEQ>(T.Vin, nb2.y, nbb, col, yb);
+        blur_step<VEC, SEQ>(y, ya, yb, y2);
 #pragma unroll
-    for (int e = 0; e < VEC; e++) {
-        const float sm = fadd(x1[e], x2[e]);
-        if (SEQ)  // seqCompute: old + 0.5*(n1+n2) evaluated in double (permutohedral.cpp:505)
-            y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)sm));
-        else  // sseCompute: float (permutohedral.cpp:566)
-            y[e] = fadd(x0[e], fmul(0.5f, sm));
+        for (int e = 0; e < VEC; e++) y[e] = y2[e];
     }
+    const size_t o0 = (size_t)(v + 1) * MP + col;
     if (T.Vout) {
         if constexpr (VEC == 4) {
             *reinterpret_cast<float4 *>(T.Vout + o0) = make_float4(y[0], y[1], y[2], y[3]);
@@ -852,7 +894,7 @@ __global__ void __launch_bounds__(256) blur_kernel(const __grid_constant__ BlurA
             for (int e = 0; e < VEC; e++) T.Vout[o0 + e] = y[e];
         }
     }
-    if (T.pv) scatter_partials<MP, VEC>(T.pv, T.red_list, T.red_beg[v], T.red_beg[v + 1], c * VEC, y);
+    if (T.pv) scatter_partials<MP, VEC>(T.pv, T.red_list, T.red_beg[v], T.red_beg[v + 1], col, y);
 }
 
 // Bounded grid barrier of a cooperative launch: the last CTA to arrive resets

@@ -68,6 +68,8 @@ struct BlurArgs {
         const int2 *nbr;      // [d+1][L]
         int L;
         int axis;
+        int axis2;            // >= 0: a second pass along axis2 in the same launch (the first
+                              // pass recomputed at the second's neighbours); -1: one pass
         const int *red_beg;   // scatter of the result into partial order (last pass of the
         const int *red_list;  // mean-field filter): pv[red_list[s]] = out[v], s in red_beg[v..v+1)
         float *pv;            // null: no scatter
