@@ -1214,6 +1214,47 @@ struct Chain {
     bool reverse;
 };
 
+// Launch plan of a chain: launch i runs passes pass[i] (and pass[i] + 1 when
+// two[i]) from in[i] into out[i].  Passes go two per launch with the
+// intermediate buffers planned backwards from Out, alternating b[0] and b[1];
+// a chain whose S would be overwritten by its first launch keeps one pass per
+// launch (the original ping-pong).
+struct ChainPlan {
+    int n = 0;
+    int pass[DCRF_MAX_D + 1];
+    bool two[DCRF_MAX_D + 1];
+    const float *in[DCRF_MAX_D + 1];
+    float *out[DCRF_MAX_D + 1];
+};
+
+ChainPlan plan_chain(const Chain &c, int d) {
+    ChainPlan p;
+    const int n2 = (d + 2) / 2;
+    float *x[DCRF_MAX_D + 2];
+    x[n2] = c.Out;
+    x[n2 - 1] = c.Out == c.b[0] ? c.b[1] : c.b[0];
+    for (int i = n2 - 2; i >= 1; i--) x[i] = x[i + 1] == c.b[0] ? c.b[1] : c.b[0];
+    const bool clash = (n2 >= 2 && x[1] == c.S) || (n2 == 1 && c.Out == c.S);
+    if (!clash) {
+        p.n = n2;
+        for (int i = 0; i < n2; i++) {
+            p.pass[i] = 2 * i;
+            p.two[i] = 2 * i + 1 <= d;
+            p.in[i] = i == 0 ? c.S : x[i];
+            p.out[i] = x[i + 1];
+        }
+        return p;
+    }
+    p.n = d + 1;
+    for (int q = 0; q <= d; q++) {
+        p.pass[q] = q;
+        p.two[q] = false;
+        p.in[q] = q == 0 ? c.S : c.b[(q - 1) & 1];
+        p.out[q] = q == d ? c.Out : c.b[q & 1];
+    }
+    return p;
+}
+
 int blur_chains(dcrf_crf *h, const std::vector<Chain> &chains, bool value1) {
     const int MP = value1 ? 1 : h->MP;
     const int NV = MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP;
@@ -1225,23 +1266,29 @@ int blur_chains(dcrf_crf *h, const std::vector<Chain> &chains, bool value1) {
         }
         for (size_t g0 = 0; g0 < cs.size(); g0 += DCRF_MAX_TERMS) {
             const size_t g1 = std::min(cs.size(), g0 + DCRF_MAX_TERMS);
-            int maxd = 0;
-            for (size_t q = g0; q < g1; q++) maxd = std::max(maxd, h->terms[cs[q]->k].d);
-            for (int pass = 0; pass <= maxd; pass++) {
+            std::vector<ChainPlan> plans;
+            int steps = 0;
+            for (size_t q = g0; q < g1; q++) {
+                plans.push_back(plan_chain(*cs[q], h->terms[cs[q]->k].d));
+                steps = std::max(steps, plans.back().n);
+            }
+            for (int i = 0; i < steps; i++) {
                 BlurArgs ba{};
                 ba.n = 0;
                 ba.begin[0] = 0;
                 for (size_t q = g0; q < g1; q++) {
                     const Chain &c = *cs[q];
+                    const ChainPlan &pl = plans[q - g0];
                     const Term &T = h->terms[c.k];
-                    if (pass > T.d) continue;
+                    if (i >= pl.n) continue;
+                    const int p = pl.pass[i];
                     BlurArgs::T &bt = ba.t[ba.n];
-                    bt.Vin = pass == 0 ? c.S : c.b[(pass - 1) & 1];
-                    bt.Vout = pass == T.d ? c.Out : c.b[pass & 1];
+                    bt.Vin = pl.in[i];
+                    bt.Vout = pl.out[i];
                     bt.nbr = T.lat.nbr;
                     bt.L = T.lat.L;
-                    bt.axis = c.reverse ? T.d - pass : pass;
-                    bt.axis2 = -1;
+                    bt.axis = c.reverse ? T.d - p : p;
+                    bt.axis2 = !pl.two[i] ? -1 : c.reverse ? T.d - (p + 1) : p + 1;
                     bt.pv = nullptr;
                     ba.begin[ba.n + 1] = ba.begin[ba.n] + (long long)T.lat.L * NV;
                     ba.n++;
