@@ -244,32 +244,46 @@ __device__ __forceinline__ bool key_eq(const uint64_t *__restrict__ a, const uin
     return eq;
 }
 
+// Lanes of a warp holding the same key insert it once: the lowest such lane
+// (the smallest corner index among them, the only one that can matter to the
+// first-occurrence minimum) probes, the others take its slot.  Neighbouring
+// points share most lattice vertices, so a warp of 32 corners holds only a
+// few distinct keys.
 template <int KW>
 __global__ void insert_kernel(const uint64_t *__restrict__ keys, size_t E, uint32_t *table, uint32_t mask,
                               uint32_t *__restrict__ slot, DevStatus *st) {
-    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned active = __ballot_sync(0xffffffffu, k < E);
     if (k >= E) return;
     uint64_t key[KW];
 #pragma unroll
     for (int w = 0; w < KW; w++) key[w] = keys[k * KW + w];
+    unsigned peers = active;
+#pragma unroll
+    for (int w = 0; w < KW; w++) peers &= __match_any_sync(active, key[w]);
+    const int lane = (int)(threadIdx.x & 31u), leader = __ffs(peers) - 1;
     uint32_t h = key_hash<KW>(key) & mask;
-    for (uint32_t probe = 0; probe <= mask; probe++) {
-        uint32_t e = __ldcg(&table[h]);
-        if (e == EMPTY) {
-            e = atomicCAS(&table[h], EMPTY, (uint32_t)k);
+    if (lane == leader) {
+        bool done = false;
+        for (uint32_t probe = 0; probe <= mask && !done; probe++) {
+            uint32_t e = __ldcg(&table[h]);
             if (e == EMPTY) {
-                slot[k] = h;
-                return;
+                e = atomicCAS(&table[h], EMPTY, (uint32_t)k);
+                if (e == EMPTY) {
+                    done = true;
+                    break;
+                }
             }
+            if (key_eq<KW>(keys + (size_t)e * KW, key)) {
+                atomicMin(&table[h], (uint32_t)k);
+                done = true;
+                break;
+            }
+            h = (h + 1) & mask;
         }
-        if (key_eq<KW>(keys + (size_t)e * KW, key)) {
-            atomicMin(&table[h], (uint32_t)k);
-            slot[k] = h;
-            return;
-        }
-        h = (h + 1) & mask;
+        if (!done) dcrf_set_error(st, DCRF_ERR_HASH_FULL, 0);
     }
-    dcrf_set_error(st, DCRF_ERR_HASH_FULL, 0);
+    slot[k] = __shfl_sync(peers, h, leader);
 }
 
 __global__ void first_flag_kernel(const uint32_t *__restrict__ table, const uint32_t *__restrict__ slot, size_t E,
