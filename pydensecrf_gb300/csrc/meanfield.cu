@@ -154,9 +154,12 @@ struct PG {
 
 template <int VW>
 __device__ __forceinline__ void vload(const float *p, float (&v)[VW]) {
-    if constexpr (VW == 4) {
-        const float4 x = *reinterpret_cast<const float4 *>(p);
-        v[0] = x.x, v[1] = x.y, v[2] = x.z, v[3] = x.w;
+    if constexpr (VW % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < VW / 4; c++) {
+            const float4 x = *reinterpret_cast<const float4 *>(p + 4 * c);
+            v[4 * c] = x.x, v[4 * c + 1] = x.y, v[4 * c + 2] = x.z, v[4 * c + 3] = x.w;
+        }
     } else if constexpr (VW == 2) {
         const float2 x = *reinterpret_cast<const float2 *>(p);
         v[0] = x.x, v[1] = x.y;
@@ -180,8 +183,10 @@ __device__ __forceinline__ void vload_g(const float *__restrict__ p, float (&v)[
 
 template <int VW>
 __device__ __forceinline__ void vstore(float *p, const float (&v)[VW]) {
-    if constexpr (VW == 4) {
-        *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+    if constexpr (VW % 4 == 0) {
+#pragma unroll
+        for (int c = 0; c < VW / 4; c++)
+            *reinterpret_cast<float4 *>(p + 4 * c) = make_float4(v[4 * c], v[4 * c + 1], v[4 * c + 2], v[4 * c + 3]);
     } else if constexpr (VW == 2) {
         *reinterpret_cast<float2 *>(p) = make_float2(v[0], v[1]);
     } else {
