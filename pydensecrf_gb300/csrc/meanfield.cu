@@ -3,15 +3,16 @@
 // One iteration of DenseCRF::inference (pydensecrf/densecrf/src/densecrf.cpp:
 // 122-129) for all pairwise terms at once is three phases:
 //
-//   reduce  per vertex: sum the per-tile splat partials (in tile order) into
-//           V[v] -- the end of the splat of Permutohedral::compute
-//           (permutohedral.cpp:545-553);
+//   reduce  per vertex: sum its per-tile splat partials (which the splat
+//           wrote as one contiguous run of rows per vertex) into V[v] -- the
+//           end of the splat of Permutohedral::compute (permutohedral.cpp:
+//           545-553);
 //   blur    per axis j = 0..d (d..0 for the transpose): V' = V + 1/2 (V[n1] +
-//           V[n2]) with the zero sentinel row (permutohedral.cpp:556-569);
-//           terms of smaller d drop out of the later axis launches.  The last
-//           axis also scatters every vertex's value to the partials that
-//           reference it (tile-partial order), so each tile's inputs of the
-//           next phase are one contiguous block;
+//           V[n2]) with the zero sentinel row (permutohedral.cpp:556-569), two
+//           axes per launch; terms of smaller d drop out of the later
+//           launches.  The last axis also scatters every vertex's value to the
+//           partials that reference it (tile-partial order), so each tile's
+//           inputs of the next phase are one contiguous block;
 //   point   one CTA per tile of 256 points (a 16x16 pixel block of a
 //           DenseCRF2D): an elected thread prefetches the tile's tables and
 //           blurred values with cp.async.bulk (TMA bulk copies) behind one
@@ -26,7 +27,7 @@
 //
 // Deterministic: a tile's corners are grouped by vertex at lattice-build time
 // (point order), every partial is a fixed-order sum, and the reduce adds a
-// vertex's partials in tile order; no float atomics.  Products and sums are
+// vertex's partials in an order fixed by its own list; no float atomics.  Products and sums are
 // rounded separately like the reference's x86 build; the value-size <= 2
 // arithmetic of seqCompute (double blur, (w*v)*alpha slice) is kept where the
 // reference uses it.
