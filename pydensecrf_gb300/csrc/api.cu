@@ -128,6 +128,48 @@ struct TuneCfg {
     int coop = 0;            // blur axes in one cooperative launch (1) or one launch per axis (0)
 };
 
+// Tile tables of one image-size list: slot -> point, point -> slot, and the
+// prefix of valid slots per tile, on the host and -- made on first use, one
+// allocation per device -- on the device, shared read-only by every handle of
+// that size list and freed with the layout.
+struct TileLayout {
+    std::vector<int> slot, inv, vbase;
+    mutable std::mutex dmu;
+    mutable std::vector<std::pair<int, int *>> dev;  // (device, [slot | inv | vbase])
+    int *device_tables(int device) const {
+        std::lock_guard<std::mutex> lk(dmu);
+        for (auto &d : dev)
+            if (d.first == device) return d.second;
+        std::vector<int> all(slot);
+        all.push_back(0);
+        all.insert(all.end(), inv.begin(), inv.end());
+        all.push_back(0);
+        all.insert(all.end(), vbase.begin(), vbase.end());
+        all.push_back(0);
+        int *p = nullptr;
+        if (cudaMalloc(&p, all.size() * sizeof(int)) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        if (cudaMemcpy(p, all.data(), all.size() * sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(p);
+            return nullptr;
+        }
+        dev.push_back({device, p});
+        return p;
+    }
+    ~TileLayout() {
+        int cur = 0;
+        if (cudaGetDevice(&cur) != cudaSuccess) return;
+        for (auto &d : dev) {
+            cudaSetDevice(d.first);
+            cudaFree(d.second);  // synchronises: no handle's work still reads the tables
+        }
+        cudaSetDevice(cur);
+    }
+};
+
 }  // namespace
 
 struct dcrf_crf {
@@ -154,6 +196,7 @@ struct dcrf_crf {
     int ntiles = 0;
     int *slot_pt = nullptr;
     int *tile_vbase = nullptr;
+    std::shared_ptr<const TileLayout> layout;  // owns slot_pt, pt_slot, tile_vbase
     std::vector<Term> terms;
     // model version (bumped by every change of unary, terms or parameters) and
     // the per-iteration checkpoints of the last dcrf_inference_checkpointed
@@ -257,9 +300,6 @@ int check_handle(dcrf_crf *h) {
 // images).  A 2D image uses 16x16 pixel blocks (the corners of a block share
 // far more lattice vertices than a raster strip of the same size); a generic
 // point set uses runs of 256 consecutive points.
-struct TileLayout {
-    std::vector<int> slot, inv, vbase;
-};
 
 // Host tables of a tile layout, computed once per image-size list for the
 // process (handles are often created per image; the tables depend only on the
@@ -330,15 +370,15 @@ int build_tiles(dcrf_crf *h) {
     h->ntiles = (int)lay->vbase.size() - 1;
     h->nslots = h->ntiles * SPLAT_TILE;
     int rc;
-    if ((rc = dev_alloc_async(&h->slot_pt, lay->slot.size() + 1, s))) return rc;
-    if ((rc = dev_alloc_async(&h->pt_slot, (size_t)h->N + 1, s))) return rc;
-    if ((rc = dev_alloc_async(&h->tile_vbase, lay->vbase.size() + 1, s))) return rc;
+    int *tables = lay->device_tables(h->device);
+    if (!tables) return set_err(DCRF_ERR_OOM, "device allocation of the tile tables failed");
+    h->layout = lay;
+    h->slot_pt = tables;
+    h->pt_slot = tables + lay->slot.size() + 1;
+    h->tile_vbase = h->pt_slot + lay->inv.size() + 1;
     if ((rc = dev_alloc_async(&h->kl_part, (size_t)h->ntiles + 1, s))) return rc;
     if ((rc = dev_alloc_async(&h->d_seg, h->seg.size(), s))) return rc;
     if ((rc = dev_alloc_async(&h->d_imgW, h->seg.size(), s))) return rc;
-    CU(cudaMemcpyAsync(h->slot_pt, lay->slot.data(), lay->slot.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(h->pt_slot, lay->inv.data(), lay->inv.size() * sizeof(int), cudaMemcpyHostToDevice, s));
-    CU(cudaMemcpyAsync(h->tile_vbase, lay->vbase.data(), lay->vbase.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     CU(cudaMemcpyAsync(h->d_seg, h->seg.data(), h->seg.size() * sizeof(int), cudaMemcpyHostToDevice, s));
     if (h->grid2d)
         CU(cudaMemcpyAsync(h->d_imgW, h->imgW.data(), h->imgW.size() * sizeof(int), cudaMemcpyHostToDevice, s));
@@ -1460,8 +1500,7 @@ int dcrf_destroy(dcrf_crf *h) {
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
     for (void *p : {(void *)h->status, (void *)h->bar, (void *)h->U, (void *)h->Q, (void *)h->tmp,
-                    (void *)h->stage, (void *)h->pt_slot, (void *)h->map, (void *)h->kl_part, (void *)h->slot_pt,
-                    (void *)h->tile_vbase, (void *)h->d_seg, (void *)h->d_imgW})
+                    (void *)h->stage, (void *)h->map, (void *)h->kl_part, (void *)h->d_seg, (void *)h->d_imgW})
         dev_free_async(p, h->stream);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
     if (h->capture) cudaStreamDestroy(h->capture);
