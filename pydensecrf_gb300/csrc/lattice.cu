@@ -849,10 +849,9 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         // a launch that did not start must not leave its outputs to the next kernels
         if ((ce = cudaGetLastError()) != cudaSuccess)
             return bail(DCRF_ERR_CUDA, std::string("tile grouping launch: ") + cudaGetErrorString(ce));
-        if (scan_exclusive_u32(tile_np, (uint32_t *)L.tile_pbeg, L.ntiles, (uint32_t *)L.tile_pbeg + L.ntiles, stemp,
-                               s) != cudaSuccess ||
-            scan_exclusive_u32(tile_nt, (uint32_t *)L.tile_tbeg, L.ntiles, (uint32_t *)L.tile_tbeg + L.ntiles, stemp,
-                               s) != cudaSuccess)
+        if (scan_exclusive_u32_pair(tile_np, (uint32_t *)L.tile_pbeg, (uint32_t *)L.tile_pbeg + L.ntiles, tile_nt,
+                                    (uint32_t *)L.tile_tbeg, (uint32_t *)L.tile_tbeg + L.ntiles, L.ntiles, stemp,
+                                    s) != cudaSuccess)
             return bail(DCRF_ERR_CUDA, "scan failed");
         cudaMemcpyAsync(hcnt, L.tile_pbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hcnt + 1, L.tile_tbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);

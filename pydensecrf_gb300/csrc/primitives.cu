@@ -81,8 +81,18 @@ __global__ void scan_tile_kernel(const uint32_t *in, uint32_t *out, size_t n, co
 constexpr int SMALL_THREADS = 1024, SMALL_ITEMS = 16, SMALL_CHUNK = SMALL_THREADS * SMALL_ITEMS;
 constexpr size_t SCAN_SMALL_MAX = 4 * (size_t)SMALL_CHUNK;
 
-__global__ void __launch_bounds__(SMALL_THREADS) scan_small_kernel(const uint32_t *in, uint32_t *out, size_t n,
-                                                                   uint32_t *__restrict__ d_total) {
+// Up to two independent arrays of the same length per launch: block b scans
+// array b.
+struct SmallScan {
+    const uint32_t *in[2];
+    uint32_t *out[2];
+    uint32_t *total[2];
+};
+
+__global__ void __launch_bounds__(SMALL_THREADS) scan_small_kernel(const __grid_constant__ SmallScan a, size_t n) {
+    const uint32_t *in = a.in[blockIdx.x];
+    uint32_t *out = a.out[blockIdx.x];
+    uint32_t *d_total = a.total[blockIdx.x];
     __shared__ uint32_t s_warp[SMALL_THREADS / 32];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     uint32_t carry = 0;
@@ -142,7 +152,8 @@ static cudaError_t scan_rec(const uint32_t *in, uint32_t *out, size_t n, uint32_
         return cudaGetLastError();
     }
     if (n <= SCAN_SMALL_MAX) {
-        DCRF_LAUNCH(scan_small_kernel<<<1, SMALL_THREADS, 0, s>>>(in, out, n, d_total));
+        const SmallScan a = {{in, nullptr}, {out, nullptr}, {d_total, nullptr}};
+        DCRF_LAUNCH(scan_small_kernel<<<1, SMALL_THREADS, 0, s>>>(a, n));
         return cudaGetLastError();
     }
     uint32_t *sums = temp;
@@ -161,6 +172,18 @@ cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, size_t n, uint
         return cudaSuccess;
     }
     return scan_rec(in, out, n, d_total, temp, s);
+}
+
+cudaError_t scan_exclusive_u32_pair(const uint32_t *in0, uint32_t *out0, uint32_t *total0, const uint32_t *in1,
+                                    uint32_t *out1, uint32_t *total1, size_t n, uint32_t *temp, cudaStream_t s) {
+    if (n > 1024 && n <= SCAN_SMALL_MAX) {
+        const SmallScan a = {{in0, in1}, {out0, out1}, {total0, total1}};
+        DCRF_LAUNCH(scan_small_kernel<<<2, SMALL_THREADS, 0, s>>>(a, n));
+        return cudaGetLastError();
+    }
+    cudaError_t e = scan_exclusive_u32(in0, out0, n, total0, temp, s);
+    if (e != cudaSuccess) return e;
+    return scan_exclusive_u32(in1, out1, n, total1, temp, s);
 }
 
 // ---------------------------------------------------------------------------
