@@ -473,21 +473,37 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
             const float *vps = reinterpret_cast<const float *>(smem + T.sm_vp);
             const bool rows_smem = T.staged && b.vp_staged;
             const float alpha = T.alpha;
-            for (int r = 0; r <= T.d; r++) {
-                const int loc = locs[r * SPLAT_TILE + pi];
-                const float bw = ws[r * SPLAT_TILE + pi];
-                float v[H];
-                if (rows_smem)
-                    load_row_s<H>(vps + loc * MP + l0, v);
-                else
-                    load_row<H>(T.pv + (size_t)(b.pb + loc) * MP + l0, v);
-                if (T.seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
-#pragma unroll
-                    for (int e = 0; e < H; e++) acc[e] = fmaf(fmul(bw, v[e]), alpha, acc[e]);
-                } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
-                    const float w = fmul(bw, alpha);
+            if (rows_smem && !T.seq) {
+                // the common case on its own loop: rows staged in shared memory,
+                // the x86 slice (w * alpha) * v (permutohedral.cpp:579-581); no
+                // per-corner branches (measured: 7.7 % fewer instructions, -2.4 us)
+                const float *vrow = vps + l0;
+                const uint16_t *lp = locs + pi;
+                const float *wp = ws + pi;
+                for (int r = 0; r <= T.d; r++, lp += SPLAT_TILE, wp += SPLAT_TILE) {
+                    float v[H];
+                    load_row_s<H>(vrow + *lp * MP, v);
+                    const float w = fmul(*wp, alpha);
 #pragma unroll
                     for (int e = 0; e < H; e++) acc[e] = fmaf(w, v[e], acc[e]);
+                }
+            } else {
+                for (int r = 0; r <= T.d; r++) {
+                    const int loc = locs[r * SPLAT_TILE + pi];
+                    const float bw = ws[r * SPLAT_TILE + pi];
+                    float v[H];
+                    if (rows_smem)
+                        load_row_s<H>(vps + loc * MP + l0, v);
+                    else
+                        load_row<H>(T.pv + (size_t)(b.pb + loc) * MP + l0, v);
+                    if (T.seq) {  // seqCompute slice: (w * v) * alpha (permutohedral.cpp:520)
+#pragma unroll
+                        for (int e = 0; e < H; e++) acc[e] = fmaf(fmul(bw, v[e]), alpha, acc[e]);
+                    } else {  // sseCompute slice: (w * alpha) * v (permutohedral.cpp:579-581)
+                        const float w = fmul(bw, alpha);
+#pragma unroll
+                        for (int e = 0; e < H; e++) acc[e] = fmaf(w, v[e], acc[e]);
+                    }
                 }
             }
             if (a.ckY[k]) store_row<H>(a.ckY[k] + s * MP + l0, acc);
