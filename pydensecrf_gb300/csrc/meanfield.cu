@@ -519,21 +519,24 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
         }
     }
     if (valid && !given) {  // softmax over the point's labels (densecrf.cpp:98-106)
-        float mx = -INFINITY;
+        // padding labels at -inf: their exponentials are exact zeros, so the
+        // loops below need no label masks and the sums are unchanged
 #pragma unroll
         for (int e = 0; e < H; e++)
-            if (l0 + e < M) mx = fmaxf(mx, x[e]);
+            if (l0 + e >= M) x[e] = -INFINITY;
+        float mx = -INFINITY;
+#pragma unroll
+        for (int e = 0; e < H; e++) mx = fmaxf(mx, x[e]);
         if constexpr (SPLIT == 2) mx = fmaxf(mx, __shfl_xor_sync(pm, mx, 1));
         // exponentials through the fast hardware path: __expf is within a few
         // ulp for arguments near 0, where the marginals' mass is, and its larger
         // error at very negative arguments scales values below 1e-30 of the sum
         float part = 0.f;
 #pragma unroll
-        for (int e = 0; e < H; e++)
-            if (l0 + e < M) {
-                x[e] = __expf(fsub(x[e], mx));
-                part = fadd(part, x[e]);
-            }
+        for (int e = 0; e < H; e++) {
+            x[e] = __expf(fsub(x[e], mx));
+            part = fadd(part, x[e]);
+        }
         float sum = part;
         if constexpr (SPLIT == 2) {
             // one sum in label order, as with one thread per point: the upper
@@ -541,14 +544,13 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
             float full = __shfl_sync(pm, part, lane & ~1);
             if (h == 1) {
 #pragma unroll
-                for (int e = 0; e < H; e++)
-                    if (l0 + e < M) full = fadd(full, x[e]);
+                for (int e = 0; e < H; e++) full = fadd(full, x[e]);
             }
             sum = __shfl_sync(pm, full, lane | 1);
         }
         const float rs = __frcp_rn(sum);
 #pragma unroll
-        for (int e = 0; e < H; e++) x[e] = l0 + e < M ? fmul(x[e], rs) : 0.f;
+        for (int e = 0; e < H; e++) x[e] = fmul(x[e], rs);
     }
     float(&q)[H] = x;
     if (valid) {
