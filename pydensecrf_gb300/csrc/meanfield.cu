@@ -324,9 +324,10 @@ __device__ __forceinline__ void fold_compat_h(const TermDev &T, const float *sCT
             }
         }
     }
+    // padding labels have c = 0 (their filtered values and compatibility
+    // entries are 0), so no label mask is needed here
 #pragma unroll
     for (int e = 0; e < H; e++) {
-        if (l0 + e >= M) continue;
         if (kl_mode)
             kl += (double)fmul(x[e], c[e]);
         else
