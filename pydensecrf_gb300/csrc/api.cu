@@ -281,12 +281,21 @@ void release_marks(dcrf_crf *h) {
     h->marks.clear();
 }
 
-// Sets kernel attributes (dynamic shared memory opt-in) outside any capture.
+// Sets kernel attributes (dynamic shared memory opt-in) outside any capture,
+// once per device (function attributes belong to the device's context).
 void prepare_kernels() {
-    static bool done = false;
-    if (done) return;
+    static std::mutex mu;
+    static uint64_t done = 0;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) {
+        cudaGetLastError();
+        return;
+    }
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    std::lock_guard<std::mutex> lk(mu);
+    if (bit && (done & bit)) return;
     prepare_pointpass_kernels();
-    done = true;
+    done |= bit;
 }
 
 int check_handle(dcrf_crf *h) {

@@ -34,6 +34,7 @@
 #include <math.h>
 
 #include <algorithm>
+#include <atomic>
 
 #include "meanfield.cuh"
 
@@ -1320,13 +1321,17 @@ cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s) {
 
 template <int MP, bool SEQ>
 static cudaError_t chains_launch(const BlurChainArgs &a, cudaStream_t s) {
-    static int grid = 0;  // co-resident CTAs of this instance on the device (queried once)
+    // co-resident CTAs of this instance, queried once per device
+    static std::atomic<int> grids[64];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    int grid = dev >= 0 && dev < 64 ? grids[dev].load() : 0;
     if (grid == 0) {
-        int dev = 0, nsm = 0, per = 0;
-        cudaGetDevice(&dev);
+        int nsm = 0, per = 0;
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, blur_chains_kernel<MP, SEQ>, 256, 0);
         grid = std::max(1, nsm * std::max(1, per));
+        if (dev >= 0 && dev < 64) grids[dev].store(grid);
     }
     long long work = 0;
     for (int k = 0; k < a.n; k++) work += (long long)a.c[k].L * (MP % 4 == 0 ? MP / 4 : MP % 2 == 0 ? MP / 2 : MP);
