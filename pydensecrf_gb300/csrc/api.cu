@@ -920,13 +920,10 @@ int build_term(dcrf_crf *h, int k) {
     const size_t nm = (size_t)h->ntiles * SPLAT_TILE * (T.d + 1);
     if ((rc = dev_alloc_async(&T.mem_wn, nm, h->stream))) return rc;
     CU(launch_scale_members(T.lat.mem_pt, T.lat.mem_w, T.norm, h->ntiles, T.d + 1, T.mem_wn, h->stream));
-    if ((rc = sync_check(h))) {
-        if (rc != DCRF_ERR_CUDA) {
-            free_term_lattice(h, T);
-            return set_err(rc, "lattice build of term " + std::to_string(k) + " failed on the device: " + g_err);
-        }
-        return rc;
-    }
+    // No synchronisation: the normalisation runs on while the caller goes on
+    // (the next term's build, or the inference) in stream order; a device
+    // status it leaves is reported by the next synchronising call.
+    CU(cudaGetLastError());
     h->version++;
     return DCRF_OK;
 }

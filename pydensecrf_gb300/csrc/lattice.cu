@@ -301,6 +301,9 @@ __global__ void offsets_kernel(const uint64_t *__restrict__ keys, const uint32_t
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= E) return;
     uint32_t rep = table[slot[k]];
+    // a corner whose insert failed (hash table full, reported by the insert)
+    // maps to vertex 0 until the host sees the status and drops the build
+    if (rep >= (uint32_t)E) rep = (uint32_t)k;
     uint32_t v = vid[rep];
     if (k < (size_t)N * (D + 1)) {
         size_t i = k / (D + 1);
@@ -332,14 +335,12 @@ __device__ __forceinline__ int lookup(const uint64_t *__restrict__ keys, const u
     return -1;
 }
 
+// Neighbours of vertex v along axis j: the keys one step down and
+// up the axis; nbr = (index + 1) of each, 0 when absent.
 template <int D>
-__global__ void neighbors_kernel(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table, uint32_t mask,
-                                 const uint32_t *__restrict__ vid, const uint16_t *__restrict__ vkeys, int L,
-                                 int2 *__restrict__ nbr) {
-    size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (size_t)L * (D + 1)) return;
-    int j = (int)(t / L);
-    int v = (int)(t - (size_t)j * L);
+__device__ __forceinline__ void neighbors_of(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table,
+                                             uint32_t mask, const uint32_t *__restrict__ vid,
+                                             const uint16_t *__restrict__ vkeys, int v, int j, int2 *out) {
     uint16_t kf[D + 1], n1[D + 1], n2[D + 1];
 #pragma unroll
     for (int q = 0; q <= D; q++) kf[q] = vkeys[(size_t)v * (D + 1) + q];
@@ -355,10 +356,26 @@ __global__ void neighbors_kernel(const uint64_t *__restrict__ keys, const uint32
         n1[q + 1] = (uint16_t)a;
         n2[q + 1] = (uint16_t)b;
     }
-    int i1 = lookup<D>(keys, table, mask, vid, n1);
-    int i2 = lookup<D>(keys, table, mask, vid, n2);
-    nbr[t] = make_int2(i1 + 1, i2 + 1);
+    const int i1 = lookup<D>(keys, table, mask, vid, n1);
+    const int i2 = lookup<D>(keys, table, mask, vid, n2);
+    *out = make_int2(i1 + 1, i2 + 1);
 }
+
+// The vertex count L is read on the device (the host learns it later), so the
+// launch covers an upper bound with a grid-stride loop.
+template <int D>
+__global__ void neighbors_kernel(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table, uint32_t mask,
+                                 const uint32_t *__restrict__ vid, const uint16_t *__restrict__ vkeys,
+                                 const uint32_t *__restrict__ d_L, int2 *__restrict__ nbr) {
+    const int L = (int)*d_L;
+    for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < (size_t)L * (D + 1);
+         t += (size_t)gridDim.x * blockDim.x) {
+        const int j = (int)(t / L);
+        const int v = (int)(t - (size_t)j * L);
+        neighbors_of<D>(keys, table, mask, vid, vkeys, v, j, nbr + t);
+    }
+}
+
 
 // Block bitonic sort of one tile's corners by (vertex, corner) and count of
 // distinct vertices.  Corner idx = slot*(D+1) + r of the tile's slot.
@@ -751,7 +768,18 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     auto bail = [&](int code, const std::string &m) {
         tmp.release();
         per.release();
+        cudaMemsetAsync(status, 0, sizeof(DevStatus), s);  // the reported status is consumed
         return fail(code, m);
+    };
+    // device status of the build after a synchronisation: 0, or the error to return
+    auto status_error = [&](const DevStatus &st) -> int {
+        if (st.code == DCRF_ERR_KEY_OVERFLOW)
+            return bail(DCRF_ERR_KEY_OVERFLOW,
+                        "a lattice coordinate of point " + std::to_string(st.detail) +
+                            " leaves the int16 key range of the reference (features too large)");
+        if (st.code == DCRF_ERR_HASH_FULL) return bail(DCRF_ERR_HASH_FULL, "lattice hash table full");
+        if (st.code != 0) return bail(st.code, "lattice build failed");
+        return 0;
     };
     cudaMemcpyAsync(d_seg, seg.start.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, s);
     if (n_ph) cudaMemcpyAsync(d_ph, ph_img.data(), sizeof(int) * n_ph, cudaMemcpyHostToDevice, s);
@@ -791,33 +819,38 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     if (E > 0) DCRF_LAUNCH(insert_kernel<KW><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, E, table, (uint32_t)(cap - 1), slot, status));
     if (E > 0) DCRF_LAUNCH(first_flag_kernel<<<ceil_div_u(E, 256), 256, 0, s>>>(table, slot, E, vid));
     if (scan_exclusive_u32(vid, vid, E, d_L, stemp, s) != cudaSuccess) return bail(DCRF_ERR_CUDA, "scan failed");
+    // The vertex count L is needed on the host only to size the neighbour and
+    // key tables.  When their upper bound (L <= E) is small, they are reserved
+    // at that size and the build runs on to its single synchronisation (L comes
+    // back with the tile counts); otherwise the host waits for L here.
     uint32_t hL = 0;
     DevStatus hst{};
-    cudaMemcpyAsync(&hL, d_L, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-    cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
-    cudaError_t ce = cudaStreamSynchronize(s);
-    if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice build: ") + cudaGetErrorString(ce));
-    if (hst.code == DCRF_ERR_KEY_OVERFLOW)
-        return bail(DCRF_ERR_KEY_OVERFLOW,
-                    "a lattice coordinate of point " + std::to_string(hst.detail) +
-                        " leaves the int16 key range of the reference (features too large)");
-    if (hst.code == DCRF_ERR_HASH_FULL) return bail(DCRF_ERR_HASH_FULL, "lattice hash table full");
-    if (hst.code != 0) return bail(hst.code, "lattice build failed");
-    L.L = (int)hL;
+    cudaError_t ce = cudaSuccess;
+    const bool learn_L_first = (size_t)10 * E * (D + 1) > ((size_t)256 << 20);
+    if (learn_L_first) {
+        cudaMemcpyAsync(&hL, d_L, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+        ce = cudaStreamSynchronize(s);
+        if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice build: ") + cudaGetErrorString(ce));
+        if (int rc = status_error(hst)) return rc;
+        L.L = (int)hL;
+    }
+    const size_t Lcap = learn_L_first ? (size_t)L.L : E;  // rows reserved for the neighbour and key tables
 
     const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
-    per.reserve(Arena::sz<int2>((size_t)L.L * (D + 1)) + Arena::sz<uint16_t>((size_t)L.L * (D + 1)) +
+    per.reserve(Arena::sz<int2>(Lcap * (D + 1)) + Arena::sz<uint16_t>(Lcap * (D + 1)) +
                 2 * Arena::sz<int>(tm.ntiles + 1) + 2 * (Arena::sz<uint16_t>(ntl) + Arena::sz<float>(ntl)));
     tmp.reserve(Arena::sz<uint16_t>(ntl) + 2 * Arena::sz<int>(ntl) + 2 * Arena::sz<uint32_t>(tm.ntiles + 1) +
                 Arena::sz<uint32_t>(4));
-    L.nbr = per.get<int2>((size_t)L.L * (D + 1));
-    L.vkeys = per.get<uint16_t>((size_t)L.L * (D + 1));
+    L.nbr = per.get<int2>(Lcap * (D + 1));
+    L.vkeys = per.get<uint16_t>(Lcap * (D + 1));
     if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (neighbours)");
     if (E > 0)
         DCRF_LAUNCH(offsets_kernel<D><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, table, slot, vid, E, N, L.off, L.vkeys));
-    if (L.L > 0)
-        DCRF_LAUNCH(neighbors_kernel<D><<<ceil_div_u((size_t)L.L * (D + 1), 256), 256, 0, s>>>(keys, table, (uint32_t)(cap - 1),
-                                                                                  vid, L.vkeys, L.L, L.nbr));
+    if (Lcap > 0) {
+        const unsigned nb = (unsigned)std::min<size_t>(ceil_div_u(Lcap * (D + 1), 256), 4096);
+        DCRF_LAUNCH(neighbors_kernel<D><<<nb, 256, 0, s>>>(keys, table, (uint32_t)(cap - 1), vid, L.vkeys, d_L, L.nbr));
+    }
     // ---- splat tiles: partials, member lists, slice tables, tasks ----------------
     L.ntiles = tm.ntiles;
     L.tile_pbeg = per.get<int>(L.ntiles + 1);
@@ -856,14 +889,16 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         cudaMemcpyAsync(hcnt, L.tile_pbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hcnt + 1, L.tile_tbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(hcnt + 2, maxes, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
-        ce = cudaStreamSynchronize(s);
-        if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tiles: ") + cudaGetErrorString(ce));
-        if (hst.code != 0) return bail(hst.code, "lattice tile grouping failed");
     } else {
         cudaMemsetAsync(L.tile_pbeg, 0, sizeof(int), s);
         cudaMemsetAsync(L.tile_tbeg, 0, sizeof(int), s);
     }
+    if (!learn_L_first) cudaMemcpyAsync(&hL, d_L, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
+    ce = cudaStreamSynchronize(s);
+    if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tiles: ") + cudaGetErrorString(ce));
+    if (int rc = status_error(hst)) return rc;
+    if (!learn_L_first) L.L = (int)hL;
     L.P = (int)hcnt[0];
     L.max_np = (int)hcnt[2];
     L.max_nt = (int)hcnt[3];
@@ -935,7 +970,6 @@ int lattice_build(const float *feat, int d, int N, const Segments &seg, const Ti
                   int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out) {
     if (task_len < 1 || task_len > 63) return fail(DCRF_ERR_INVALID_ARG, "splat task length must be in [1, 63]");
     if (N < 0 || (seg.start.size() < 2)) return fail(DCRF_ERR_INVALID_ARG, "bad point segmentation");
-    if (cudaMemsetAsync(status, 0, sizeof(DevStatus), s) != cudaSuccess) return fail(DCRF_ERR_CUDA, "memset failed");
     switch (d) {
 #define DCRF_CASE(D) \
     case D:          \
