@@ -57,6 +57,21 @@ def dist_env():
     return rank, world, local
 
 
+def whole_job_rate(local_time, steps, world, dist=None, device="cpu", per_second=1.0):
+    """Whole-job throughput of `world` replicas that each ran `steps` solves:
+    every rank's work over the slowest rank's time (max over ranks; `dist`
+    None on one rank).  `local_time` is this rank's time in units of
+    1/per_second seconds (per_second=1e3 for milliseconds).  Returns (rate,
+    slowest time)."""
+    import torch
+
+    t = torch.tensor([float(local_time)], dtype=torch.float64, device=device)
+    if dist is not None:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    slowest = float(t.item())
+    return world * steps * UNITS_PER_STEP / (slowest / per_second), slowest
+
+
 class ClockSampler:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -505,12 +520,7 @@ def run_gpu(args):
         barrier()
     lib.dcrf_launch_count(ctypes.byref(cnt1))
     step_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = float(sum(step_ms))
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world * args.steps * UNITS_PER_STEP / (total_ms / 1e3)
+    value, total_ms = whole_job_rate(float(sum(step_ms)), args.steps, world, dist, dev, per_second=1e3)
     launches = int(cnt1.value - cnt0.value)
 
     tk = [ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_float(), ctypes.c_int()]
@@ -573,12 +583,7 @@ def run_gpu(args):
     for _ in range(args.steps):
         Q = step_e2e()
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = world * args.steps * UNITS_PER_STEP / e2e_s
+    e2e_value, e2e_s = whole_job_rate(time.perf_counter() - t0, args.steps, world, dist, dev)
 
     # ---- CPU baseline (rank 0, single GPU runs only)
     cpu = None

@@ -1,0 +1,81 @@
+"""The N > 1 path of bench.py on CPU: two ranks over gloo.
+
+Each rank is an independent replica (no data-path collective); the only
+cross-rank operation is the max over ranks of the timed region, from which
+the whole-job throughput is formed.  The reference arm runs on rank 0 only;
+the other ranks exit 0 without work or output."""
+import os
+import socket
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, times, queue):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank), WORLD_SIZE=str(world),
+                      LOCAL_RANK=str(rank))
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    try:
+        sys.path.insert(0, ROOT)
+        import bench
+
+        env = bench.dist_env()
+        rate, slowest = bench.whole_job_rate(times[rank], 3, world, dist)
+        queue.put((rank, env, rate, slowest))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_whole_job_rate_over_two_gloo_ranks():
+    import torch.multiprocessing as mp
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    ctx = mp.get_context("spawn")
+    queue = ctx.Queue()
+    port = _free_port()
+    times = [2.0, 3.5]  # seconds of the timed region on ranks 0 and 1
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, times, queue)) for r in range(2)]
+    for p in procs:
+        p.start()
+    results = sorted(queue.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    for rank, env, rate, slowest in results:
+        assert env == (rank, 2, rank)
+        assert slowest == 3.5  # the slowest rank's time, on every rank
+        assert rate == pytest.approx(2 * 3 * bench.UNITS_PER_STEP / 3.5)
+
+
+def test_single_rank_rate_needs_no_process_group():
+    sys.path.insert(0, ROOT)
+    import bench
+
+    rate, slowest = bench.whole_job_rate(250.0, 4, 1, None, per_second=1e3)
+    assert slowest == 250.0
+    assert rate == pytest.approx(4 * bench.UNITS_PER_STEP / 0.25)
+
+
+def test_reference_arm_other_ranks_exit_quietly(monkeypatch, capsys):
+    sys.path.insert(0, ROOT)
+    import bench
+
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    monkeypatch.setenv("LOCAL_RANK", "1")
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--gpus", "2", "--steps", "1",
+                                      "--warmup", "0"])
+    assert bench.main() == 0
+    assert capsys.readouterr().out == ""
