@@ -312,7 +312,7 @@ class DenseCRF:
         return {"split": sp.value, "smem_kb": sm.value, "task_len": tk.value, "hash_load": hl.value,
                 "coop_blur": co.value}
 
-    def set_tuning(self, split: int = 0, smem_kb: int = 0, task_len: int = 16, hash_load: float = 2.0,
+    def set_tuning(self, split: int = 0, smem_kb: int = 0, task_len: int = 24, hash_load: float = 2.0,
                    coop_blur: int = 0) -> None:
         _lib.check(_lib.load().dcrf_set_tuning(self._h, int(split), int(smem_kb), int(task_len), float(hash_load),
                                                int(coop_blur)))

@@ -200,3 +200,33 @@ def test_volume_batch_fwd_bwd_matches_per_volume(engine):
             dk_sum[k] += dk[k]
     for k in range(len(dkb)):
         assert np.allclose(dkb[k], dk_sum[k], rtol=1e-4, atol=1e-7), (k, dkb[k], dk_sum[k])
+
+
+def test_two_axis_blur_launches_match_pass_by_pass(engine):
+    """The launched blur runs two axes per launch (the first recomputed at the
+    second's neighbours); the cooperative blur runs one axis per grid-barrier
+    step through a buffer.  Same arithmetic: marginals and gradients agree bit
+    for bit."""
+    rng = np.random.default_rng(16)
+    W, H, M, T = 48, 40, 6, 4
+    img = _images(rng, [(W, H)])[0]
+    U = _unaries(rng, M, [W * H])[0]
+    dQ = rng.normal(0, 1, size=(M, W * H)).astype(np.float32)
+
+    def run(coop):
+        d = engine.DenseCRF2D(W, H, M)
+        d.set_tuning(2 if M % 8 == 0 else 1, 0, 24, 2.0, coop)
+        d.setUnaryEnergy(U)
+        d.addPairwiseGaussian(sxy=3, compat=3)
+        d.addPairwiseBilateral(sxy=30, srgb=13, rgbim=img, compat=np.float32(np.eye(M) + 1))
+        Q = np.array(d.inferenceCheckpointed(T))
+        dU, dc, dk = d.backward(dQ, want_compat=True, want_kernel=True)
+        return Q, dU, dc, dk
+
+    Qa, dUa, dca, dka = run(0)
+    Qb, dUb, dcb, dkb = run(1)
+    assert np.array_equal(Qa, Qb)
+    assert np.array_equal(dUa, dUb)
+    for x, y in zip(dca + dka, dcb + dkb):
+        if x is not None:
+            assert np.array_equal(x, y)
