@@ -180,6 +180,78 @@ def cpu_oracle_rate(cfg, threads: int, solves_per_thread: int = 1):
     return n * UNITS_PER_STEP / dt, dt, n
 
 
+def _oracle():
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    return O
+
+
+def cpu_oracle_problems(problems, threads: int):
+    """Wall-clock throughput of the CPU oracle on full solves of `problems`, one
+    per host thread (`threads` at a time).  A problem is (N, M, T, unary as
+    (N, M), [(features as (N, d), compatibility, kernel type)]); the oracle's C
+    calls release the GIL, so the threads run in parallel.  Returns (MPix * label
+    * iter/s, seconds, solves)."""
+    O = _oracle()
+
+    def solve(p):
+        N, Mp, Tp, U, terms = p
+        c = O.OracleCRF(N, Mp)
+        c.set_unary(U)
+        for f, compat, ktype in terms:
+            c.add_pairwise(f, compat, ktype=ktype)
+        c.inference(Tp)
+
+    import concurrent.futures as cf
+
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=max(1, threads)) as ex:
+        list(ex.map(solve, problems))
+    dt = time.perf_counter() - t0
+    units = sum(p[0] * p[1] * p[2] for p in problems) / 1e6
+    return units / dt, dt, len(problems)
+
+
+def cpu_batched_baseline(threads: int):
+    """The batched workload's CPU reference point: the oracle on the first
+    `threads` images of the 64-image batch, one per host thread."""
+    from pydensecrf_gb300 import synthetic as S
+
+    O = _oracle()
+    # the generator's first images are those of the 64-image batch (only the
+    # shared compatibility, drawn after the images, differs)
+    cfg = S.batch_uneven(0, B=min(threads, 64))
+    probs = []
+    for b in range(len(cfg["sizes"])):
+        Wb, Hb = cfg["sizes"][b]
+        probs.append((Wb * Hb, cfg["M"], cfg["T"], np.ascontiguousarray(cfg["U"][b].T),
+                      [(O.features_gaussian_2d(Wb, Hb, 3.0, 3.0), cfg["compat"], 1),
+                       (O.features_bilateral_2d(cfg["img"][b], 80, 80, 13, 13, 13), cfg["compat"], 1)]))
+    rate, dt, n = cpu_oracle_problems(probs, threads)
+    px = sum(p[0] for p in probs)
+    return {"value": round(rate, 3), "unit": "MPix*label*iter/s", "cores": threads, "kind": "port",
+            "sample": f"{n} of the 64 images ({px} px), one full solve per host thread, {dt:.1f} s"}
+
+
+def cpu_volumes_baseline(threads: int):
+    """The volume workload's CPU reference point: the oracle's forward on the 8
+    volumes, one per host thread."""
+    from pydensecrf_gb300 import synthetic as S
+
+    cfg = S.volume_96(0)
+    Sz = cfg["S"]
+    n = Sz ** 3
+    zz, yy, xx = np.mgrid[0:Sz, 0:Sz, 0:Sz].astype(np.float32)
+    pos = np.ascontiguousarray(np.stack([xx / np.float32(3), yy / np.float32(3), zz / np.float32(3)]).reshape(3, -1).T)
+    probs = [(n, cfg["M"], cfg["T"], np.ascontiguousarray(u.T),
+              [(np.ascontiguousarray(f.T), cfg["compat"], 2), (pos, 1.0, 1)]) for u, f in zip(cfg["U"], cfg["feat"])]
+    rate, dt, k = cpu_oracle_problems(probs, threads)
+    return {"value": round(rate, 3), "unit": "MVoxel*label*iter/s (forward incl. lattice builds)", "cores": threads,
+            "kind": "port", "sample": f"the {k} volumes' forward solves, one per host thread, {dt:.1f} s"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -597,6 +669,16 @@ def run_gpu(args):
     learning = learning_step_times(lib, _lib, dev, stream) if (rank == 0 and not args.no_learning) else None
     batched = batched_vs_loop(lib, _lib, dev, stream) if (rank == 0 and not args.no_batch) else None
     volumes = volumes_fwd_bwd(lib, _lib, dev, stream) if (rank == 0 and not args.no_batch) else None
+    # CPU reference points of the batched and volume workloads (the oracle port,
+    # one solve per host thread); reported only, never the target
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        for obj, fn in ((batched, cpu_batched_baseline), (volumes, cpu_volumes_baseline)):
+            if obj is not None:
+                try:
+                    obj["cpu_baseline"] = fn(threads)
+                except Exception as e:  # a baseline that cannot run is reported, not fatal
+                    obj["cpu_baseline"] = {"unavailable": f"{type(e).__name__}: {e}"}
     if rank == 0:
         line = {
             "metric": METRIC, "value": round(value, 3), "unit": "MPix*label*iter/s", "n_gpus": world,

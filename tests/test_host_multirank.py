@@ -79,3 +79,22 @@ def test_reference_arm_other_ranks_exit_quietly(monkeypatch, capsys):
                                       "--warmup", "0"])
     assert bench.main() == 0
     assert capsys.readouterr().out == ""
+
+
+def test_cpu_oracle_problems_rate():
+    """The bench's CPU reference points: the oracle on a list of problems, one
+    per host thread; the rate counts every problem's N * M * T."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    rng = np.random.default_rng(5)
+    probs = []
+    for N, M in ((300, 3), (512, 4)):
+        U = rng.uniform(0.1, 3.0, size=(N, M)).astype(np.float32)
+        f = rng.normal(0, 1.5, size=(N, 3)).astype(np.float32)
+        probs.append((N, M, 4, U, [(f, 2.0, 1), (f[:, :2].copy(), np.eye(M, dtype=np.float32), 1)]))
+    rate, dt, n = bench.cpu_oracle_problems(probs, 2)
+    assert n == 2 and dt > 0
+    assert rate == pytest.approx((300 * 3 * 4 + 512 * 4 * 4) / 1e6 / dt)
