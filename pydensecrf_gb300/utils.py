@@ -76,11 +76,13 @@ def unary_from_softmax(sm, scale=None, clip=1e-5):
     """
     n_cls = sm.shape[0]
     if _is_tensor(sm):
+        # the numpy form's type promotion: a float32 softmax stays float32
+        # unless ``scale`` mixes in the (float64) uniform term
         import torch
-        x = sm.to(torch.float64)
+        x = sm if sm.is_floating_point() else sm.to(torch.float64)
         if scale is not None:
             assert 0 < scale <= 1, "`scale` needs to be in (0,1]"
-            x = scale * x + (1 - scale) / n_cls
+            x = (scale * x).to(torch.float64) + (1 - scale) * (1.0 / n_cls)
         if clip is not None:
             x = x.clamp(clip, 1.0)
         return (-torch.log(x)).reshape(n_cls, -1).to(torch.float32)

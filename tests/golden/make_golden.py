@@ -15,12 +15,16 @@ oracle/Makefile).  Outputs, all small:
                    a logistic unary L*I), compatibility and kernel-parameter
                    gradients, for every normalisation, compatibility and kernel
                    type.
+* utils.npz     -- outputs of the reference's pure-numpy pydensecrf/utils.py
+                   (unary and feature builders) on seeded inputs, imported
+                   from its source file.
 * examples.npz  -- the reference's example images and annotations
                    (examples/im*.png, anno*.png) decoded, with the shipped
                    outputs (out*.png) turned back into label maps, and the
                    reference's MAP of the generic path of examples/inference.py.
 
-Usage: python tests/golden/make_golden.py [REFERENCE_ROOT]
+Usage: python tests/golden/make_golden.py [REFERENCE_ROOT [FIXTURE ...]]
+(FIXTURE: lattice, inference, gradient, utils, examples; default all)
 """
 from __future__ import annotations
 
@@ -215,6 +219,61 @@ def gen_gradient():
     print("gradient.npz", len(cases), "cases")
 
 
+def _ref_utils():
+    """The reference's pydensecrf/utils.py, loaded from its file alone (its
+    package __init__ would import the compiled extension)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("ref_utils", os.path.join(REF_ROOT, "pydensecrf", "utils.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def gen_utils():
+    R = _ref_utils()
+    rng = np.random.default_rng(515)
+    out = {}
+    # unary_from_labels: 1-based labels with unknowns, and 0-based labels
+    lab = rng.integers(0, 6, size=(13, 17)).astype(np.int32)
+    out["lab"] = lab
+    for gt in (0.5, 0.7, 0.95):
+        out[f"labels_unsure/{gt}"] = R.unary_from_labels(lab, 5, gt, zero_unsure=True)
+        out[f"labels_sure/{gt}"] = R.unary_from_labels(lab, 6, gt, zero_unsure=False)
+    out["compute_unary"] = R.compute_unary(lab, 5, GT_PROB=0.6)
+    # unary_from_softmax / softmax_to_unary on float64 and float32 probabilities
+    logits = rng.normal(0, 3, size=(4, 9, 11))
+    sm = np.exp(logits - logits.max(0))
+    sm /= sm.sum(0)
+    sm[0, 0, :3] = 0.0
+    out["sm64"] = sm
+    out["sm32"] = sm.astype(np.float32)
+    for name in ("sm64", "sm32"):
+        x = out[name]
+        out[f"softmax/{name}/default"] = R.unary_from_softmax(x)
+        out[f"softmax/{name}/scale"] = R.unary_from_softmax(x, scale=0.8)
+        out[f"softmax/{name}/noclip"] = R.unary_from_softmax(np.maximum(x, 1e-30), clip=None)
+        out[f"softmax/{name}/scale_noclip"] = R.unary_from_softmax(x, scale=0.6, clip=None)
+        out[f"softmax/{name}/to_unary"] = R.softmax_to_unary(np.maximum(x, 1e-30))
+        out[f"softmax/{name}/to_unary_gt"] = R.softmax_to_unary(x, GT_PROB=0.7)
+    # feature builders: 2-D and 3-D grids, RGB / single-channel / channels-first images
+    out["gauss2"] = R.create_pairwise_gaussian(sdims=(3, 5), shape=(19, 23))
+    out["gauss2_frac"] = R.create_pairwise_gaussian(sdims=(0.7, 13.3), shape=(7, 29))
+    out["gauss3"] = R.create_pairwise_gaussian(sdims=(2, 3, 7), shape=(5, 6, 7))
+    img = rng.integers(0, 256, size=(15, 18, 3)).astype(np.uint8)
+    vol = rng.integers(0, 4096, size=(2, 5, 6, 4)).astype(np.uint16)
+    gray = rng.random(size=(12, 10)).astype(np.float32)
+    out["img"], out["vol"], out["gray"] = img, vol, gray
+    out["bilat_rgb"] = R.create_pairwise_bilateral(sdims=(80, 80), schan=(13, 13, 13), img=img, chdim=2)
+    out["bilat_rgb_mixed"] = R.create_pairwise_bilateral(sdims=(3.3, 7), schan=(5, 11.5, 0.9), img=img, chdim=2)
+    out["bilat_rgb_scalar"] = R.create_pairwise_bilateral(sdims=(4, 4), schan=20, img=img, chdim=2)
+    out["bilat_gray"] = R.create_pairwise_bilateral(sdims=(2, 9), schan=0.3, img=gray, chdim=-1)
+    out["bilat_vol"] = R.create_pairwise_bilateral(sdims=(1, 2, 3), schan=(100, 250.0), img=vol, chdim=0)
+    out["gauss2_loop"] = R._create_pairwise_gaussian_2d(3, 5, (9, 8))
+    out["bilat2_loop"] = R._create_pairwise_bilateral_2d(3, 5, 13, 11, 7, img[:9, :8])
+    np.savez_compressed(os.path.join(HERE, "utils.npz"), **out)
+    print("utils.npz", len(out), "arrays")
+
+
 def gen_examples():
     ex = os.path.join(REF_ROOT, "examples")
     out = {}
@@ -259,7 +318,7 @@ if __name__ == "__main__":
     O.build()
     if not (O.ref_available(O.VARIANT_SSE) and O.ref_available(O.VARIANT_SCALAR)):
         sys.exit("the reference could not be built from " + REF_ROOT)
-    gen_lattice()
-    gen_inference()
-    gen_gradient()
-    gen_examples()
+    gens = {"lattice": gen_lattice, "inference": gen_inference, "gradient": gen_gradient, "utils": gen_utils,
+            "examples": gen_examples}
+    for name in (sys.argv[2:] or gens):
+        gens[name]()
