@@ -229,6 +229,10 @@ def test_shape_errors(engine):
     d = engine.DenseCRF2D(10, 10, 2)
     with pytest.raises(ValueError):
         d.setUnaryEnergy(np.ones((3, 100), np.float32))
+    # a unary with the right labels but the wrong pixel count raises at
+    # setUnaryEnergy, not later (the reference's tests/issue29.py)
+    with pytest.raises(ValueError):
+        d.setUnaryEnergy(np.ones((2, 99), np.float32))
     with pytest.raises(ValueError):
         d.addPairwiseEnergy(np.ones((2, 99), np.float32), compat=1.0)
     with pytest.raises(ValueError):
