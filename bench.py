@@ -188,6 +188,33 @@ def _oracle():
     return O
 
 
+def cpu_single_core(cfg, reps: int = 1):
+    """The reference's own setting: one solve on one host thread (its sources
+    have no threading), with the lattice builds (the two addPairwise calls)
+    and the T iterations timed apart; the fastest of `reps` solves."""
+    O = _oracle()
+    U = np.ascontiguousarray(cfg["U"].T)
+    fg = O.features_gaussian_2d(W, H, 3.0, 3.0)
+    fb = O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13)
+    best = None
+    for _ in range(max(1, reps)):
+        t0 = time.perf_counter()
+        c = O.OracleCRF(W * H, M)
+        c.set_unary(U)
+        c.add_pairwise(fg, 3.0)
+        c.add_pairwise(fb, 10.0)
+        t1 = time.perf_counter()
+        c.inference(T)
+        t2 = time.perf_counter()
+        del c
+        if best is None or t2 - t0 < best[0] + best[1]:
+            best = (t1 - t0, t2 - t1)
+    build_s, inf_s = best
+    return {"value": round(UNITS_PER_STEP / (build_s + inf_s), 3), "unit": "MPix*label*iter/s", "cores": 1,
+            "kind": "port", "build_ms": round(1e3 * build_s, 1), "iteration_ms": round(1e3 * inf_s / T, 2),
+            "sample": f"one full solve on one thread (fastest of {max(1, reps)})"}
+
+
 def cpu_oracle_problems(problems, threads: int):
     """Wall-clock throughput of the CPU oracle on full solves of `problems`, one
     per host thread (`threads` at a time).  A problem is (N, M, T, unary as
@@ -664,6 +691,10 @@ def run_gpu(args):
         rate, dt, n = cpu_oracle_rate(cfg, threads)
         cpu = {"value": round(rate, 3), "unit": "MPix*label*iter/s", "cores": threads, "kind": "port",
                "sample": f"{n} full solves of the same workload, one per thread, {dt:.1f} s"}
+        try:
+            cpu["single_core"] = cpu_single_core(cfg)
+        except Exception as e:  # reported, not fatal
+            cpu["single_core"] = {"unavailable": f"{type(e).__name__}: {e}"}
 
     lib.dcrf_destroy(h)
     learning = learning_step_times(lib, _lib, dev, stream) if (rank == 0 and not args.no_learning) else None
