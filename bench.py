@@ -148,6 +148,22 @@ def measured_peak():
 
 
 # ----------------------------------------------------------------------------
+def host_variant(O) -> int:
+    """The lattice build the reference compiles on this host: its SSE path on
+    x86-64, its scalar path elsewhere (e.g. aarch64), selected by the
+    reference's own #ifdef __SSE__ (permutohedral.cpp:36-39)."""
+    import platform
+
+    return O.VARIANT_SSE if platform.machine().lower() in ("x86_64", "amd64", "i686", "i386") else O.VARIANT_SCALAR
+
+
+def host_variant_name() -> str:
+    import platform
+
+    x86 = platform.machine().lower() in ("x86_64", "amd64", "i686", "i386")
+    return "SSE lattice build and filter (x86)" if x86 else "scalar lattice build and filter (non-x86)"
+
+
 def cpu_oracle_rate(cfg, threads: int, solves_per_thread: int = 1):
     """Throughput of the CPU oracle on full solves of the workload, `threads` in parallel."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -159,7 +175,7 @@ def cpu_oracle_rate(cfg, threads: int, solves_per_thread: int = 1):
     fb = O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13)
 
     def solve():
-        c = O.OracleCRF(W * H, M)
+        c = O.OracleCRF(W * H, M, host_variant(O))
         c.set_unary(U)
         c.add_pairwise(fg, 3.0)
         c.add_pairwise(fb, 10.0)
@@ -199,7 +215,7 @@ def cpu_single_core(cfg, reps: int = 1):
     best = None
     for _ in range(max(1, reps)):
         t0 = time.perf_counter()
-        c = O.OracleCRF(W * H, M)
+        c = O.OracleCRF(W * H, M, host_variant(O))
         c.set_unary(U)
         c.add_pairwise(fg, 3.0)
         c.add_pairwise(fb, 10.0)
@@ -211,7 +227,8 @@ def cpu_single_core(cfg, reps: int = 1):
             best = (t1 - t0, t2 - t1)
     build_s, inf_s = best
     return {"value": round(UNITS_PER_STEP / (build_s + inf_s), 3), "unit": "MPix*label*iter/s", "cores": 1,
-            "kind": "port", "build_ms": round(1e3 * build_s, 1), "iteration_ms": round(1e3 * inf_s / T, 2),
+            "kind": "port", "variant": host_variant_name(), "build_ms": round(1e3 * build_s, 1),
+            "iteration_ms": round(1e3 * inf_s / T, 2),
             "sample": f"one full solve on one thread (fastest of {max(1, reps)})"}
 
 
@@ -225,7 +242,7 @@ def cpu_oracle_problems(problems, threads: int):
 
     def solve(p):
         N, Mp, Tp, U, terms = p
-        c = O.OracleCRF(N, Mp)
+        c = O.OracleCRF(N, Mp, host_variant(O))
         c.set_unary(U)
         for f, compat, ktype in terms:
             c.add_pairwise(f, compat, ktype=ktype)
@@ -259,6 +276,7 @@ def cpu_batched_baseline(threads: int):
     rate, dt, n = cpu_oracle_problems(probs, threads)
     px = sum(p[0] for p in probs)
     return {"value": round(rate, 3), "unit": "MPix*label*iter/s", "cores": threads, "kind": "port",
+            "variant": host_variant_name(),
             "sample": f"{n} of the 64 images ({px} px), one full solve per host thread, {dt:.1f} s"}
 
 
@@ -276,7 +294,8 @@ def cpu_volumes_baseline(threads: int):
               [(np.ascontiguousarray(f.T), cfg["compat"], 2), (pos, 1.0, 1)]) for u, f in zip(cfg["U"], cfg["feat"])]
     rate, dt, k = cpu_oracle_problems(probs, threads)
     return {"value": round(rate, 3), "unit": "MVoxel*label*iter/s (forward incl. lattice builds)", "cores": threads,
-            "kind": "port", "sample": f"the {k} volumes' forward solves, one per host thread, {dt:.1f} s"}
+            "kind": "port", "variant": host_variant_name(),
+            "sample": f"the {k} volumes' forward solves, one per host thread, {dt:.1f} s"}
 
 
 def run_reference(args):
@@ -302,6 +321,7 @@ def run_reference(args):
         "data": "synthetic (seeded plain_vga generator)", "impl": "reference",
         "config": {"workload": WORKLOAD, "step": f"{cores} full solves in parallel (one per host thread)"},
         "cpu_baseline": {"value": round(value, 3), "unit": "MPix*label*iter/s", "cores": cores, "kind": "port",
+                         "variant": host_variant_name(),
                          "sample": f"{cores} concurrent full solves per step, {args.steps} steps"},
         "e2e": {"value": round(value, 3), "unit": "MPix*label*iter/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
@@ -690,6 +710,7 @@ def run_gpu(args):
         threads = os.cpu_count() or 1
         rate, dt, n = cpu_oracle_rate(cfg, threads)
         cpu = {"value": round(rate, 3), "unit": "MPix*label*iter/s", "cores": threads, "kind": "port",
+               "variant": host_variant_name(),
                "sample": f"{n} full solves of the same workload, one per thread, {dt:.1f} s"}
         try:
             cpu["single_core"] = cpu_single_core(cfg)
