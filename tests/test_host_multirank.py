@@ -98,3 +98,31 @@ def test_cpu_oracle_problems_rate():
     rate, dt, n = bench.cpu_oracle_problems(probs, 2)
     assert n == 2 and dt > 0
     assert rate == pytest.approx((300 * 3 * 4 + 512 * 4 * 4) / 1e6 / dt)
+
+
+def test_cpu_arms_follow_the_host_variant(monkeypatch):
+    """The CPU arms run the lattice path the reference compiles on the host:
+    SSE on x86-64, scalar elsewhere (aarch64)."""
+    import platform
+
+    sys.path.insert(0, ROOT)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import bench
+    import oracle as O
+
+    monkeypatch.setattr(platform, "machine", lambda: "aarch64")
+    assert bench.host_variant(O) == O.VARIANT_SCALAR and "scalar" in bench.host_variant_name()
+    monkeypatch.setattr(platform, "machine", lambda: "x86_64")
+    assert bench.host_variant(O) == O.VARIANT_SSE and "SSE" in bench.host_variant_name()
+
+
+def test_cpu_single_core_point():
+    """One solve of the bench workload on one thread, build and iterations apart."""
+    sys.path.insert(0, ROOT)
+    import bench
+    from pydensecrf_gb300 import synthetic as S
+
+    r = bench.cpu_single_core(S.plain_vga(0))
+    assert r["cores"] == 1 and r["kind"] == "port" and r["build_ms"] > 0 and r["iteration_ms"] > 0
+    total_s = (r["build_ms"] + bench.T * r["iteration_ms"]) / 1e3
+    assert r["value"] == pytest.approx(bench.UNITS_PER_STEP / total_s, rel=0.01)
