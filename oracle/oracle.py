@@ -128,6 +128,8 @@ def ref_lib(variant: int = VARIANT_SSE):
         lib.ref_crf_kl.restype = ctypes.c_double
         lib.ref_crf_kl.argtypes = [_vp, _f32p, ctypes.c_int, ctypes.c_int]
         lib.ref_crf_map.argtypes = [_vp, ctypes.c_int, _i16p]
+        lib.ref_crf_unary_energy.argtypes = [_vp, _i16p, ctypes.c_int, _f32p]
+        lib.ref_crf_pairwise_energy.argtypes = [_vp, _i16p, ctypes.c_int, ctypes.c_int, _f32p]
         lib.ref_crf_compat_param_count.argtypes = [_vp]
         lib.ref_crf_kernel_param_count.argtypes = [_vp]
         lib.ref_crf_unary_param_count.argtypes = [_vp]
@@ -302,6 +304,20 @@ class RefCRF:
     def map(self, T: int) -> np.ndarray:
         out = np.empty(self.N, np.int16)
         self._lib.ref_crf_map(self._h, T, _p(out, _i16p))
+        return out
+
+    def unary_energy(self, labels: np.ndarray) -> np.ndarray:
+        """DenseCRF::unaryEnergy (densecrf.cpp:141-153)."""
+        lab = np.ascontiguousarray(labels, dtype=np.int16)
+        out = np.empty(self.N, np.float32)
+        self._lib.ref_crf_unary_energy(self._h, _p(lab, _i16p), self.N, _p(out, _f32p))
+        return out
+
+    def pairwise_energy(self, labels: np.ndarray, term: int = -1) -> np.ndarray:
+        """DenseCRF::pairwiseEnergy (densecrf.cpp:154-177); term -1 sums all terms."""
+        lab = np.ascontiguousarray(labels, dtype=np.int16)
+        out = np.empty(self.N, np.float32)
+        self._lib.ref_crf_pairwise_energy(self._h, _p(lab, _i16p), self.N, term, _p(out, _f32p))
         return out
 
     def gradient(self, T: int, gt: np.ndarray, want_unary=False, want_compat=True, want_kernel=True):

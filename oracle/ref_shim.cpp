@@ -139,6 +139,21 @@ void ref_crf_map(void *h, int T, short *labels) {
     VectorXs r = static_cast<DenseCRF *>(h)->map(T);
     std::memcpy(labels, r.data(), sizeof(short) * r.size());
 }
+// DenseCRF::unaryEnergy / pairwiseEnergy (densecrf.cpp:141-177): per-point
+// energies of the labelling l (N entries; labels outside [0, M) give 0);
+// term -1 sums every pairwise term.
+void ref_crf_unary_energy(void *h, const short *l, int N, float *out) {
+    VectorXs v(N);
+    for (int i = 0; i < N; i++) v[i] = l[i];
+    VectorXf r = static_cast<DenseCRF *>(h)->unaryEnergy(v);
+    std::memcpy(out, r.data(), sizeof(float) * r.size());
+}
+void ref_crf_pairwise_energy(void *h, const short *l, int N, int term, float *out) {
+    VectorXs v(N);
+    for (int i = 0; i < N; i++) v[i] = l[i];
+    VectorXf r = static_cast<DenseCRF *>(h)->pairwiseEnergy(v, term);
+    std::memcpy(out, r.data(), sizeof(float) * r.size());
+}
 // Parameter vectors: sizes via *_count
 int ref_crf_compat_param_count(void *h) { return (int)static_cast<DenseCRF *>(h)->labelCompatibilityParameters().size(); }
 int ref_crf_kernel_param_count(void *h) { return (int)static_cast<DenseCRF *>(h)->kernelParameters().size(); }

@@ -15,6 +15,10 @@ oracle/Makefile).  Outputs, all small:
                    a logistic unary L*I), compatibility and kernel-parameter
                    gradients, for every normalisation, compatibility and kernel
                    type.
+* energy.npz    -- the reference's own DenseCRF::unaryEnergy / pairwiseEnergy
+                   (debug energies of a labelling) on seeded CRFs covering
+                   every normalisation, compatibility and kernel type, both
+                   builds.
 * utils.npz     -- outputs of the reference's pure-numpy pydensecrf/utils.py
                    (unary and feature builders) on seeded inputs, imported
                    from its source file.
@@ -24,7 +28,7 @@ oracle/Makefile).  Outputs, all small:
                    reference's MAP of the generic path of examples/inference.py.
 
 Usage: python tests/golden/make_golden.py [REFERENCE_ROOT [FIXTURE ...]]
-(FIXTURE: lattice, inference, gradient, utils, examples; default all)
+(FIXTURE: lattice, inference, gradient, energy, utils, examples; default all)
 """
 from __future__ import annotations
 
@@ -219,6 +223,37 @@ def gen_gradient():
     print("gradient.npz", len(cases), "cases")
 
 
+def gen_energy():
+    rng = np.random.default_rng(4242)
+    N, M = 700, 5
+    f = rng.normal(0, 1.5, size=(N, 3)).astype(np.float32)
+    f2 = rng.normal(0, 2.0, size=(N, 2)).astype(np.float32)
+    U = (rng.random((N, M)) * 3).astype(np.float32)  # per point
+    mat = rng.uniform(-1, 1, size=(M, M)).astype(np.float32)
+    diag = rng.uniform(0, 2, size=M).astype(np.float32)
+    lab = rng.integers(-1, M + 1, size=N).astype(np.int16)  # -1 and M: no label
+    out = {"f": f, "f2": f2, "U": U, "mat": mat, "diag": diag, "lab": lab}
+    # name -> terms [(feature key, compat, kernel type, normalisation)]
+    cases = {f"mat_n{nt}": [("f", "mat", 1, nt)] for nt in range(4)}
+    cases["potts_n3"] = [("f", 2.5, 1, 3)]
+    cases["diag_n1"] = [("f", "diag", 1, 1)]
+    cases["full_n3"] = [("f", "mat", 2, 3)]
+    cases["two_terms"] = [("f", 2.0, 1, 3), ("f2", "mat", 1, 2)]
+    out["cases"] = np.array(list(cases))
+    for name, terms in cases.items():
+        for vname, var in (("sse", O.VARIANT_SSE), ("scalar", O.VARIANT_SCALAR)):
+            r = O.RefCRF(N, M, variant=var)
+            r.set_unary(U)
+            for fk, ck, kt, nt in terms:
+                r.add_pairwise(out[fk], out[ck] if isinstance(ck, str) else ck, kt, nt)
+            out[f"{name}/{vname}/unary"] = r.unary_energy(lab)
+            out[f"{name}/{vname}/pairwise"] = r.pairwise_energy(lab, -1)
+            for k in range(len(terms)):
+                out[f"{name}/{vname}/pairwise{k}"] = r.pairwise_energy(lab, k)
+    np.savez_compressed(os.path.join(HERE, "energy.npz"), **out)
+    print("energy.npz", len(cases), "cases")
+
+
 def _ref_utils():
     """The reference's pydensecrf/utils.py, loaded from its file alone (its
     package __init__ would import the compiled extension)."""
@@ -318,7 +353,7 @@ if __name__ == "__main__":
     O.build()
     if not (O.ref_available(O.VARIANT_SSE) and O.ref_available(O.VARIANT_SCALAR)):
         sys.exit("the reference could not be built from " + REF_ROOT)
-    gens = {"lattice": gen_lattice, "inference": gen_inference, "gradient": gen_gradient, "utils": gen_utils,
-            "examples": gen_examples}
+    gens = {"lattice": gen_lattice, "inference": gen_inference, "gradient": gen_gradient, "energy": gen_energy,
+            "utils": gen_utils, "examples": gen_examples}
     for name in (sys.argv[2:] or gens):
         gens[name]()

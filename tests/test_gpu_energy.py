@@ -1,6 +1,7 @@
 """DenseCRF::unaryEnergy / pairwiseEnergy (densecrf.cpp:141-177) on the device
 against the same quantities from the oracle's lattice filter (tolerance 1e-5
-of the largest magnitude)."""
+of the largest magnitude).  That restatement is itself pinned to the
+reference's own energies by tests/test_energy_golden.py."""
 import numpy as np
 import pytest
 
