@@ -243,6 +243,12 @@ class OracleCRF:
         Q = np.ascontiguousarray(Q, dtype=np.float32)
         return self._lib.orc_crf_kl(self._h, _p(Q, _f32p))
 
+    def map(self, T: int) -> np.ndarray:
+        """map (densecrf.cpp:132-137,202-211): labels of the first maximum after T iterations."""
+        out = np.empty(self.N, np.int16)
+        self._lib.orc_crf_map(self._h, T, _p(out, _i16p))
+        return out
+
     def term_norm(self, k: int) -> np.ndarray:
         out = np.empty(self.N, np.float32)
         self._lib.orc_crf_term_norm(self._h, k, _p(out, _f32p))

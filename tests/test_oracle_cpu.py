@@ -121,3 +121,34 @@ def test_oracle_vs_reference_random(oracle_mod, vname, var):
             v = rng.random((N, 3)).astype(np.float32)
             for rev in (False, True):
                 assert np.array_equal(_bits(a.compute(v, rev)), _bits(b.compute(v, rev)))
+
+
+@requires_ref
+@pytest.mark.parametrize("vname,var", VARIANTS)
+def test_oracle_map_matches_reference(oracle_mod, vname, var):
+    """map after T iterations: the first maximum per point, as the reference's
+    DenseCRF::map (densecrf.cpp:132-137,202-211).  A CRF with exactly tied
+    marginals (no unary, so Q is uniform) must give label 0 everywhere; a
+    random one must give the reference's labels (ties are measure-zero there,
+    and Q differs from the reference's only at the ulp level)."""
+    O = oracle_mod
+    if not O.ref_available(var):
+        pytest.skip("variant not built")
+    rng = np.random.default_rng(77 + var)
+    N, M = 900, 6
+    f = rng.normal(0, 1.5, size=(N, 3)).astype(np.float32)
+    o, r = O.OracleCRF(N, M, var), O.RefCRF(N, M, variant=var)
+    for c in (o, r):
+        c.add_pairwise(f, 3.0)
+    assert np.array_equal(o.map(3), np.zeros(N, np.int16))
+    assert np.array_equal(r.map(3), np.zeros(N, np.int16))
+    U = (rng.random((N, M)) * 4).astype(np.float32)
+    mat = rng.uniform(0, 1, (M, M)).astype(np.float32)
+    o, r = O.OracleCRF(N, M, var), O.RefCRF(N, M, variant=var)
+    for c in (o, r):
+        c.set_unary(U)
+        c.add_pairwise(f, 3.0)
+        c.add_pairwise(f[:, :2].copy(), mat)
+    mo, mr = o.map(4), r.map(4)
+    assert mo.dtype == np.int16 and np.array_equal(mo, o.inference(4).argmax(1).astype(np.int16))
+    assert (mo == mr).mean() >= 0.999, (mo == mr).mean()
