@@ -39,6 +39,32 @@ def test_library_errors_without_device_are_explicit():
     _lib.load()
     with pytest.raises(_lib.DenseCRFError):
         densecrf.DenseCRF(100, 2)
+    with pytest.raises(_lib.DenseCRFError):
+        densecrf.DenseCRF2D(10, 10, 2)
+
+
+def test_batch_handles_without_device_are_explicit():
+    """The batched classes have no CPU path either; their host-side argument
+    checks run before any device call."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    from pydensecrf_gb300 import _lib, batch
+    _lib.load()
+    with pytest.raises(_lib.DenseCRFError):
+        batch.DenseCRFBatch([100, 37], 3)
+    with pytest.raises(_lib.DenseCRFError):
+        batch.DenseCRF2DBatch([10, 7], [10, 3], 3)
+    with pytest.raises(ValueError):
+        batch.DenseCRF2DBatch([10, 7], [10], 3)
+
+
+def test_bandwidth_grad_chain_rule():
+    """dL/ds for features x/s from the DIAG parameter gradient at p = 1."""
+    import torch
+    from pydensecrf_gb300 import autograd
+    dp = torch.tensor([1.0, 2.0, 3.0, 4.0], dtype=torch.float64)
+    assert float(autograd.bandwidth_grad(dp, 2.0, (0, 2))) == -(1.0 + 3.0) / 2.0
 
 
 # ---- eigen (reference: pydensecrf/tests/test_eigen.py) -----------------------
