@@ -126,3 +126,27 @@ def test_cpu_single_core_point():
     assert r["cores"] == 1 and r["kind"] == "port" and r["build_ms"] > 0 and r["iteration_ms"] > 0
     total_s = (r["build_ms"] + bench.T * r["iteration_ms"]) / 1e3
     assert r["value"] == pytest.approx(bench.UNITS_PER_STEP / total_s, rel=0.01)
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """The reference arm's JSON line on one rank: the contract's keys, the
+    CPU sample described, and an e2e entry with no host-device traffic."""
+    import json
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK"):
+        monkeypatch.delenv(k, raising=False)
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--steps", "1", "--warmup", "0"])
+    assert bench.main() == 0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    for key in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+                "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+        assert key in line, key
+    assert line["impl"] == "reference" and line["value"] > 0 and line["higher_is_better"] is True
+    assert line["metric"] == bench.METRIC and line["config"]["workload"] == bench.WORKLOAD
+    cb = line["cpu_baseline"]
+    assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
+    assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
+                           "d2h_bytes_per_step": 0}
