@@ -20,6 +20,8 @@ W*H*M*T / step time (higher is better).
 * cpu_baseline -- the CPU oracle (a C restatement of the reference's
   algorithm, oracle/dcrf_oracle.c) on a bounded sample of the same workload,
   one solve per host thread in parallel.
+* accuracy -- the marginals of the last timed end-to-end solve against the
+  oracle on the same inputs, in float and in float64.
 * --impl reference -- the reference's CPU path for this workload on the host
   cores (the oracle port: the reference itself is not built on this machine),
   same metric and step definition.
@@ -230,6 +232,24 @@ def cpu_single_core(cfg, reps: int = 1):
             "kind": "port", "variant": host_variant_name(), "build_ms": round(1e3 * build_s, 1),
             "iteration_ms": round(1e3 * inf_s / T, 2),
             "sample": f"one full solve on one thread (fastest of {max(1, reps)})"}
+
+
+def solve_accuracy(cfg, Q_gpu: np.ndarray):
+    """Error of the benchmarked solve's own marginals (M x N, from the timed
+    end-to-end steps) against the oracle on the same inputs, in float (the
+    reference's arithmetic, x86 lattice variant like the engine's default) and
+    in float64 (the exact-arithmetic limit over the same lattices)."""
+    O = _oracle()
+    c = O.OracleCRF(W * H, M, O.VARIANT_SSE)
+    c.set_unary(np.ascontiguousarray(cfg["U"].T))
+    c.add_pairwise(O.features_gaussian_2d(W, H, 3.0, 3.0), 3.0)
+    c.add_pairwise(O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13), 10.0)
+    q32, q64 = c.inference(T), c.inference_f64(T)
+    q = np.asarray(Q_gpu, np.float32).reshape(M, W * H).T
+    return {"max_abs_vs_oracle": float(np.abs(q - q32).max()), "max_abs_vs_fp64": float(np.abs(q - q64).max()),
+            "oracle_vs_fp64": float(np.abs(q32 - q64).max()),
+            "argmax_agreement_vs_oracle": float((q.argmax(1) == q32.argmax(1)).mean()),
+            "sample": "the marginals of the last timed end-to-end solve"}
 
 
 def cpu_oracle_problems(problems, threads: int):
@@ -721,6 +741,14 @@ def run_gpu(args):
             except Exception as e:
                 cpu["single_core"] = {"unavailable": f"{type(e).__name__}: {e}"}
 
+    # ---- accuracy of the timed solve itself against the oracle (float and FP64)
+    accuracy = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        try:
+            accuracy = solve_accuracy(cfg, np.array(Q))
+        except Exception as e:  # reported, not fatal
+            accuracy = {"unavailable": f"{type(e).__name__}: {e}"}
+
     lib.dcrf_destroy(h)
     learning = learning_step_times(lib, _lib, dev, stream) if (rank == 0 and not args.no_learning) else None
     batched = batched_vs_loop(lib, _lib, dev, stream) if (rank == 0 and not args.no_batch) else None
@@ -754,6 +782,7 @@ def run_gpu(args):
             "tuning": tuning,
             "roofline": roofline,
             "cpu_baseline": cpu,
+            "accuracy": accuracy,
             "learning": learning,
             "batched": batched,
             "volumes": volumes,

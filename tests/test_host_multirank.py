@@ -150,3 +150,24 @@ def test_reference_arm_line(monkeypatch, capsys):
     assert cb["value"] == line["value"] and cb["kind"] == "port" and cb["cores"] >= 1 and cb["sample"]
     assert line["e2e"] == {"value": line["value"], "unit": line["unit"], "h2d_bytes_per_step": 0,
                            "d2h_bytes_per_step": 0}
+
+
+def test_solve_accuracy_figures():
+    """The bench's accuracy entry: given the oracle's own float marginals
+    (M x N, as the API returns them) the float error is 0, and the float64
+    error is the oracle's own, well inside the 1e-4 inference tolerance."""
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    import bench
+    from pydensecrf_gb300 import synthetic as S
+
+    cfg = S.plain_vga(0)
+    O = bench._oracle()
+    c = O.OracleCRF(bench.W * bench.H, bench.M, O.VARIANT_SSE)
+    c.set_unary(np.ascontiguousarray(cfg["U"].T))
+    c.add_pairwise(O.features_gaussian_2d(bench.W, bench.H, 3.0, 3.0), 3.0)
+    c.add_pairwise(O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13), 10.0)
+    r = bench.solve_accuracy(cfg, np.ascontiguousarray(c.inference(bench.T).T))
+    assert r["max_abs_vs_oracle"] == 0.0 and r["argmax_agreement_vs_oracle"] == 1.0
+    assert r["max_abs_vs_fp64"] == r["oracle_vs_fp64"] < 1e-4
