@@ -150,6 +150,16 @@ def measured_peak():
 
 
 # ----------------------------------------------------------------------------
+def _oracle():
+    """The CPU oracle module (test infrastructure: used here only for the CPU
+    reference figures), built on first use."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+
+    O.build()
+    return O
+
+
 def host_variant(O) -> int:
     """The lattice build the reference compiles on this host: its SSE path on
     x86-64, its scalar path elsewhere (e.g. aarch64), selected by the
@@ -168,10 +178,7 @@ def host_variant_name() -> str:
 
 def cpu_oracle_rate(cfg, threads: int, solves_per_thread: int = 1):
     """Throughput of the CPU oracle on full solves of the workload, `threads` in parallel."""
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-
-    O.build()
+    O = _oracle()
     U = np.ascontiguousarray(cfg["U"].T)
     fg = O.features_gaussian_2d(W, H, 3.0, 3.0)
     fb = O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13)
@@ -196,14 +203,6 @@ def cpu_oracle_rate(cfg, threads: int, solves_per_thread: int = 1):
     dt = time.perf_counter() - t0
     n = threads * solves_per_thread
     return n * UNITS_PER_STEP / dt, dt, n
-
-
-def _oracle():
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle as O
-
-    O.build()
-    return O
 
 
 def cpu_single_core(cfg, reps: int = 1):
