@@ -152,3 +152,66 @@ def test_oracle_map_matches_reference(oracle_mod, vname, var):
     mo, mr = o.map(4), r.map(4)
     assert mo.dtype == np.int16 and np.array_equal(mo, o.inference(4).argmax(1).astype(np.int16))
     assert (mo == mr).mean() >= 0.999, (mo == mr).mean()
+
+
+@pytest.mark.parametrize("name", ["potts_n3_k1", "diag_n1_k1", "mat_n3_k1", "mat_n2_k2"])
+def test_reference_gradient_vs_fp64_finite_differences(oracle_mod, golden, name):
+    """The reference's own DenseCRF::gradient (the golden fixture the GPU
+    adjoint is held to) against central differences of the FP64 restatement
+    of the same mean-field: objective = mean log Q(gt) (objective.cpp:37-50;
+    the cases here keep every Q(gt) far above its 1e-20 clamp).  dL/dU, the
+    compatibility of the first term (Potts weight, Diagonal entries, or the
+    Matrix's packed upper triangle, labelcompatibility.cpp:101-107, under a
+    symmetric perturbation) and the second term's Potts weight.  Steps are
+    powers of two, so the perturbed float inputs are exact.  Tolerance 1e-3 of
+    the largest magnitude, like the GPU tests."""
+    g = golden("gradient.npz")
+    O = oracle_mod
+    W, H, M, T = int(g["W"]), int(g["H"]), int(g["M"]), int(g["T"])
+    N = W * H
+    U, gt = g["U"], g["gt"].astype(np.int64)
+    fg = O.features_gaussian_2d(W, H, 2.0, 2.0)
+    fb = O.features_bilateral_2d(g["img"], 5.0, 5.0, 40.0, 40.0, 40.0)
+    ck, rest = name.split("_n")
+    nt, kt = (int(x) for x in rest.split("_k"))
+    compat = {"potts": np.float32(2.0), "diag": g["diag"], "mat": g["mat"]}[ck]
+
+    def obj(Uv, c=compat, w2=3.0):
+        o = O.OracleCRF(N, M)
+        o.set_unary(Uv)
+        o.add_pairwise(fg, float(c) if np.ndim(c) == 0 else c, kt, nt)
+        o.add_pairwise(fb, w2, kt, 3)
+        return float(np.log(o.inference_f64(T)[np.arange(N), gt]).mean())
+
+    assert abs(obj(U) - float(g[f"{name}/obj"])) < 1e-5
+    dU, dc = g[f"{name}/dU"], g[f"{name}/dcompat"]
+    rng = np.random.default_rng(9)
+    du = 2.0 ** -10
+    fd, ref = [], []
+    for n, m in zip(rng.integers(0, N, 10), rng.integers(0, M, 10)):
+        up, dn = U.copy(), U.copy()
+        up[n, m] += np.float32(du)
+        dn[n, m] -= np.float32(du)
+        fd.append((obj(up) - obj(dn)) / (2 * du))
+        ref.append(dU[n, m])
+    assert np.abs(np.array(fd) - ref).max() <= 1e-3 * np.abs(dU).max()
+
+    dw = 2.0 ** -8
+    want = []
+    if ck == "potts":
+        want.append((obj(U, compat + dw) - obj(U, compat - dw)) / (2 * dw))
+    elif ck == "diag":
+        for m in range(M):
+            e = np.zeros(M, np.float32)
+            e[m] = dw
+            want.append((obj(U, compat + e) - obj(U, compat - e)) / (2 * dw))
+    else:
+        for i in range(M):
+            for j in range(i, M):
+                e = np.zeros((M, M), np.float32)
+                e[i, j] = e[j, i] = dw
+                want.append((obj(U, compat + e) - obj(U, compat - e)) / (2 * dw))
+    want.append((obj(U, w2=3.0 + dw) - obj(U, w2=3.0 - dw)) / (2 * dw))
+    want = np.array(want)
+    assert dc.shape == want.shape
+    assert np.abs(dc - want).max() <= 1e-3 * np.abs(want).max(), (dc, want)
