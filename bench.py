@@ -129,16 +129,17 @@ class ClockSampler:
 
 
 def profiled_traffic():
-    """DRAM bytes (read + write) of one point-pass launch on this workload, from the
-    committed ncu summary (profiles/pointpass_plain_vga.md)."""
+    """DRAM bytes (read + write) of one point-pass launch on this workload and
+    where they come from: the ncu capture recorded in
+    profiles/pointpass_plain_vga.json (dram__bytes_read.sum +
+    dram__bytes_write.sum of one launch, with the command that took it).
+    Returns (bytes or None, source text)."""
     try:
-        with open(os.path.join(ROOT, "profiles", "pointpass_plain_vga.md")) as fh:
-            for line in fh:
-                if line.startswith("traffic_bytes_per_launch:"):
-                    return int(line.split(":")[1])
+        with open(os.path.join(ROOT, "profiles", "pointpass_plain_vga.json")) as fh:
+            rec = json.load(fh)
+        return int(rec["traffic_bytes_per_launch"]), rec.get("traffic_source", "ncu capture")
     except Exception:
-        pass
-    return None
+        return None, None
 
 
 def measured_peak():
@@ -694,11 +695,14 @@ def run_gpu(args):
     pp_bytes = N * M * 4 + N * 4 + sum(N * (d + 1) * 8 + N * 4 + L * MP * 4 + N * (d + 1) * 6 + P * MP * 4
                                        for d, L, P in zip(d_terms, Ls, Ps))
     peak, peak_kind = measured_peak()
-    traffic = args.traffic if args.traffic is not None else profiled_traffic()
+    if args.traffic is not None:
+        traffic, traffic_src = args.traffic, "--traffic argument"
+    else:
+        traffic, traffic_src = profiled_traffic()
     avg_s = prof["point"]["avg_us"] / 1e6
     achieved = pp_bytes / avg_s / 1e9
     roofline = {"bound": "hbm", "kernel": "pointpass_kernel<24>", "achieved": round(achieved, 1),
-                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3), "traffic": traffic,
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3), "traffic": traffic, "traffic_source": traffic_src,
                 "algorithmic_bytes_per_launch": int(pp_bytes), "avg_launch_us": round(prof["point"]["avg_us"], 2),
                 "peak_kind": peak_kind}
 

@@ -311,8 +311,17 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
  * one static device array of DCRF_NOALLOC_MAX_FLOATS floats.  Term `term` must
  * already be built (dcrf_add_pairwise*).
  *   in, out: DEVICE pointers, (value_size, N) label-major; value_size is 1 or M.
+ *            `in` must be ready, and both must stay valid, in `stream`'s order.
  *   stream:  cudaStream_t the work is ordered on (NULL: the legacy default
- *            stream); the call returns once the work is enqueued.
+ *            stream); the call returns once the work is enqueued.  The work
+ *            starts after everything already queued on the handle's stream
+ *            (dcrf_set_stream; a term's build finishes there after
+ *            dcrf_add_pairwise* returns), and the handle's stream waits for it
+ *            before its own later work, through an event the handle created at
+ *            dcrf_create*.  Passing the handle's stream is fine.
+ * A bounded device wait that gives up inside this call is recorded in the
+ * handle's status block and returned by the handle's next synchronising call
+ * (dcrf_synchronize, an inference, a build).
  * The first call on a device resolves the array's address on that device
  * (cudaGetSymbolAddress) and should come before any stream capture.  All calls
  * share the one array and it keeps the last call's contents: calls that may

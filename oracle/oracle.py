@@ -37,9 +37,15 @@ def _p(a, t):
     return a.ctypes.data_as(t) if a is not None else None
 
 
-def build(quiet: bool = True) -> None:
-    """Compile liboracle.so (and _ref when the reference sources exist)."""
-    out = subprocess.run(["make", "-C", HERE, "all", "ref"], capture_output=True, text=True)
+def build(quiet: bool = True, reference_root: str | None = None) -> None:
+    """Compile liboracle.so, and _ref when the reference's sources are found:
+    under `reference_root` (the root of a pydensecrf checkout), else under the
+    DCRF_REFERENCE_ROOT environment variable; without either, _ref is skipped."""
+    cmd = ["make", "-C", HERE, "all", "ref"]
+    root = reference_root or os.environ.get("DCRF_REFERENCE_ROOT")
+    if root:
+        cmd.append("DCRF_REFERENCE_ROOT=" + os.path.abspath(root))
+    out = subprocess.run(cmd, capture_output=True, text=True)
     if out.returncode != 0:
         raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
     if not quiet:

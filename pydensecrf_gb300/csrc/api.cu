@@ -183,6 +183,9 @@ struct dcrf_crf {
     int variant = DCRF_VARIANT_SSE;
     int device = 0;
     cudaStream_t own = nullptr, stream = nullptr;
+    // orders work a caller queues on another stream (the allocation-free
+    // filter) against the handle's stream in both directions; created once
+    cudaEvent_t xorder = nullptr;
     DevStatus *status = nullptr;
     float *U = nullptr;  // [M][nslots] unary, slot-major
     bool has_unary = false;
@@ -438,6 +441,8 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
     if (cudaStreamCreateWithFlags(&h->own, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->capture, cudaStreamNonBlocking) != cudaSuccess)
         return fail(set_err(DCRF_ERR_CUDA, "cudaStreamCreate failed"));
+    if (cudaEventCreateWithFlags(&h->xorder, cudaEventDisableTiming) != cudaSuccess)
+        return fail(set_err(DCRF_ERR_CUDA, "cudaEventCreate failed"));
     prepare_kernels();
     h->stream = h->own;
     // handle memory comes from the stream-ordered pool on the handle's own
@@ -1509,6 +1514,7 @@ int dcrf_destroy(dcrf_crf *h) {
                     (void *)h->stage, (void *)h->map, (void *)h->kl_part, (void *)h->d_seg, (void *)h->d_imgW})
         dev_free_async(p, h->stream);
     if (h->gexec) cudaGraphExecDestroy(h->gexec);
+    if (h->xorder) cudaEventDestroy(h->xorder);
     if (h->capture) cudaStreamDestroy(h->capture);
     if (h->own) cudaStreamDestroy(h->own);
     delete h;
@@ -2352,6 +2358,12 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     float *in_s = scr, *pv = in_s + n_in, *V0 = pv + n_pv, *V1 = V0 + n_v;
     float *Vb[2] = {V0, V1};
     cudaStream_t s = (cudaStream_t)stream;
+    // The term's tables may still be in flight on the handle's stream (a build
+    // returns before its last kernels finish): `s` starts after them.  On the
+    // way out the handle's stream waits for this call's kernels, so that a later
+    // rebuild, clear or destroy does not free tables they still read.
+    CU(cudaEventRecord(h->xorder, h->stream));
+    CU(cudaStreamWaitEvent(s, h->xorder, 0));
     // the array keeps the previous call's contents: the zero sentinel rows are restored
     CU(cudaMemsetAsync(V0, 0, sizeof(float) * MPv, s));
     CU(cudaMemsetAsync(V1, 0, sizeof(float) * MPv, s));
@@ -2391,5 +2403,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     CU(launch_pointpass(f, MPv, s));
     CU(launch_from_slots(in_s, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots,
                          h->pt_slot, 0, out, s));
+    CU(cudaEventRecord(h->xorder, s));
+    CU(cudaStreamWaitEvent(h->stream, h->xorder, 0));
     return ok();
 }

@@ -46,7 +46,10 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 import oracle as O  # noqa: E402
 
-REF_ROOT = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF_ROOT = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("DCRF_REFERENCE_ROOT", "")
+if __name__ == "__main__" and not os.path.isdir(REF_ROOT):
+    sys.exit("usage: make_golden.py REFERENCE_ROOT [FIXTURE ...] (or set DCRF_REFERENCE_ROOT): "
+             "the root of a pydensecrf checkout")
 
 
 # ---------------------------------------------------------------------------
@@ -350,7 +353,7 @@ def gen_examples():
 
 
 if __name__ == "__main__":
-    O.build()
+    O.build(reference_root=REF_ROOT)
     if not (O.ref_available(O.VARIANT_SSE) and O.ref_available(O.VARIANT_SCALAR)):
         sys.exit("the reference could not be built from " + REF_ROOT)
     gens = {"lattice": gen_lattice, "inference": gen_inference, "gradient": gen_gradient, "energy": gen_energy,

@@ -1,0 +1,178 @@
+"""Parity at the benchmark workloads' own sizes: the CUDA path against the
+oracle (the C restatement of the reference's mean-field, same seeded inputs),
+never against another GPU handle.
+
+* 640x480, 21 labels, 10 iterations, Gaussian + bilateral Potts (the headline
+  workload), both lattice variants: Q within 1e-4 max-abs of the oracle and of
+  its FP64 twin (densecrf.cpp:115-131), argmax agreement >= 99.9 %.
+* Uneven 2D batch with a 21x21 Matrix compatibility: four images (one of
+  1024x1000) in ONE batched handle, each image's marginals against its own
+  oracle solve.
+* One 96^3 volume (N = 884 736): FULL kernel on (x/5, y/5, z/5, I/0.1) with a
+  4x4 Matrix compatibility plus a DIAG Gaussian on (x/3, y/3, z/3), T = 8.
+* Gradients (DenseCRF::gradient, densecrf.cpp:238-297): at 64x64, M = 4 and
+  at 512x512, M = 21 (T = 5, cross-entropy against a piecewise-constant label
+  map), dL/dU and dL/d(compatibility) against central differences of the
+  oracle's FP64 mean-field; bar 1e-3 of the gradient's largest magnitude.
+"""
+import numpy as np
+import pytest
+
+from pydensecrf_gb300 import synthetic as S
+
+pytestmark = pytest.mark.gpu
+QTOL = 1e-4
+AGREE = 0.999
+GTOL = 1e-3
+
+
+def _stats(Q, Qo):
+    return float(np.abs(Q - Qo).max()), float((Q.argmax(1) == Qo.argmax(1)).mean())
+
+
+@pytest.mark.parametrize("variant", [0, 1], ids=["sse", "scalar"])
+def test_plain_vga_vs_oracle(engine, oracle_mod, variant):
+    O = oracle_mod
+    cfg = S.plain_vga(0)
+    W, H, M, T = cfg["W"], cfg["H"], cfg["M"], cfg["T"]
+    d = engine.DenseCRF2D(W, H, M)
+    d.set_variant(variant)
+    d.setUnaryEnergy(cfg["U"])
+    d.addPairwiseGaussian(sxy=3, compat=3)
+    d.addPairwiseBilateral(sxy=80, srgb=13, rgbim=cfg["img"], compat=10)
+    Q = np.array(d.inference(T)).T  # (N, M)
+    o = O.OracleCRF(W * H, M, variant)
+    o.set_unary(np.ascontiguousarray(cfg["U"].T))
+    o.add_pairwise(O.features_gaussian_2d(W, H, 3, 3), 3.0)
+    o.add_pairwise(O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13), 10.0)
+    err, agree = _stats(Q, o.inference(T))
+    err64, agree64 = _stats(Q, o.inference_f64(T))
+    print(f"640x480x21 T=10 variant {variant}: |Q - oracle| {err:.2e} (argmax {agree:.5f}), "
+          f"|Q - FP64| {err64:.2e} (argmax {agree64:.5f})")
+    assert err <= QTOL and agree >= AGREE
+    assert err64 <= QTOL and agree64 >= AGREE
+
+
+def _uneven_subset(seed, sizes, M):
+    """Per-image inputs of the uneven batch (logits ~N(0,2), 12-rectangle
+    image), for the given sizes, and its shared 21x21 Matrix compatibility."""
+    rng = np.random.default_rng(seed)
+    Us, imgs = [], []
+    for W, H in sizes:
+        logits = rng.normal(0, 2, size=(M, H * W)).astype(np.float32)
+        Us.append(np.ascontiguousarray(S.neg_log_softmax(logits, axis=0), np.float32))
+        imgs.append(S.rect_image(rng, W, H))
+    return Us, imgs, S.random_sym_matrix(rng, M, 2.0, True)
+
+
+def test_uneven_batch_matrix_vs_oracle(engine, oracle_mod):
+    from pydensecrf_gb300.batch import DenseCRF2DBatch
+
+    O = oracle_mod
+    M, T = 21, 10
+    sizes = [(1024, 1000), (300, 257), (517, 733), (256, 1024)]
+    Us, imgs, compat = _uneven_subset(3, sizes, M)
+    b = DenseCRF2DBatch([w for w, _ in sizes], [h for _, h in sizes], M)
+    b.setUnaryEnergy(Us)
+    b.addPairwiseGaussian(3, compat)
+    b.addPairwiseBilateral(80, 13, imgs, compat)
+    Qs = b.inference(T)
+    for (W, H), U, img, Q in zip(sizes, Us, imgs, Qs):
+        o = O.OracleCRF(W * H, M)
+        o.set_unary(np.ascontiguousarray(U.T))
+        o.add_pairwise(O.features_gaussian_2d(W, H, 3, 3), compat)
+        o.add_pairwise(O.features_bilateral_2d(img, 80, 80, 13, 13, 13), compat)
+        err, agree = _stats(np.asarray(Q).T, o.inference(T))
+        print(f"batch image {W}x{H}: |Q - oracle| {err:.2e}, argmax {agree:.5f}")
+        assert err <= QTOL and agree >= AGREE, (W, H, err, agree)
+
+
+def test_volume_96_full_kernel_vs_oracle(engine, oracle_mod):
+    O = oracle_mod
+    cfg = S.volume_96(0, B=1)
+    Sz, M, T = cfg["S"], cfg["M"], cfg["T"]
+    N = Sz ** 3
+    zz, yy, xx = np.mgrid[0:Sz, 0:Sz, 0:Sz].astype(np.float32)
+    pos = np.ascontiguousarray(np.stack([xx / np.float32(3), yy / np.float32(3), zz / np.float32(3)]).reshape(3, -1))
+    f4, U, cm = cfg["feat"][0], cfg["U"][0], cfg["compat"]
+    d = engine.DenseCRF(N, M)
+    d.setUnaryEnergy(U)
+    d.addPairwiseEnergy(f4, cm, engine.FULL_KERNEL)
+    d.addPairwiseEnergy(pos, 1.0, engine.DIAG_KERNEL)
+    Q = np.array(d.inference(T)).T
+    o = O.OracleCRF(N, M)
+    o.set_unary(np.ascontiguousarray(U.T))
+    o.add_pairwise(np.ascontiguousarray(f4.T), cm, 2)
+    o.add_pairwise(np.ascontiguousarray(pos.T), 1.0, 1)
+    err, agree = _stats(Q, o.inference(T))
+    print(f"96^3 volume, FULL + DIAG, Matrix: |Q - oracle| {err:.2e}, argmax {agree:.5f}")
+    assert err <= QTOL and agree >= AGREE
+
+
+def _train_case(W, H, M):
+    cfg = S.train_512(0, B=1, W=W, H=H, M=M)
+    return cfg["U"][0], cfg["img"][0], cfg["gt"][0], cfg["compat"]
+
+
+def _ce_gradient_vs_fd(engine, O, W, H, M, T, n_unary, pairs):
+    """GPU dL/dU and dL/dcompat of L = -sum log Q_T[gt] against central
+    differences of the FP64 oracle, at n_unary sampled unary entries, the
+    Gaussian's Potts weight and the given symmetric Matrix entries (i, j)."""
+    U, img, gt, mat = _train_case(W, H, M)
+    N = W * H
+    fg = O.features_gaussian_2d(W, H, 3, 3)
+    fb = O.features_bilateral_2d(img, 80, 80, 13, 13, 13)
+    d = engine.DenseCRF(N, M)
+    d.setUnaryEnergy(U)
+    d.addPairwiseEnergy(np.ascontiguousarray(fg.T), 3.0)
+    d.addPairwiseEnergy(np.ascontiguousarray(fb.T), mat)
+    Q = d.inferenceCheckpointed(T)  # (M, N)
+    dQ = np.zeros((M, N), np.float32)
+    dQ[gt, np.arange(N)] = -1.0 / Q[gt, np.arange(N)]
+    dU, dcs, _ = d.backward(dQ, want_compat=True)
+    Gm = np.asarray(dcs[1]).reshape(M, M)
+
+    def loss(Uv=U, w=3.0, m=mat):
+        o = O.OracleCRF(N, M)
+        o.set_unary(np.ascontiguousarray(Uv.T))
+        o.add_pairwise(fg, w)
+        o.add_pairwise(fb, m)
+        q = o.inference_f64(T)
+        return float(-np.log(q[np.arange(N), gt]).sum())
+
+    rng = np.random.default_rng(11)
+    h = 2.0 ** -10
+    fd, got = [], []
+    for _ in range(n_unary):
+        n, m = int(rng.integers(0, N)), int(rng.integers(0, M))
+        up, dn = U.copy(), U.copy()
+        up[m, n] += np.float32(h)
+        dn[m, n] -= np.float32(h)
+        fd.append((loss(Uv=up) - loss(Uv=dn)) / (2 * h))
+        got.append(dU[m, n])
+    fd, got = np.array(fd), np.array(got)
+    errU = np.abs(got - fd).max() / max(np.abs(dU).max(), 1e-12)
+    hw = 2.0 ** -8
+    want_c = [(loss(w=3.0 + hw) - loss(w=3.0 - hw)) / (2 * hw)]
+    have_c = [dcs[0][0]]
+    for i, j in pairs:
+        e = np.zeros((M, M), np.float32)
+        e[i, j] = e[j, i] = hw
+        want_c.append((loss(m=mat + e) - loss(m=mat - e)) / (2 * hw))
+        have_c.append(Gm[i, j] + (Gm[j, i] if i != j else 0.0))
+    want_c, have_c = np.array(want_c), np.array(have_c)
+    errC = np.abs(have_c - want_c).max() / max(np.abs(want_c).max(), 1e-12)
+    print(f"{W}x{H} M={M} T={T}: dU vs FP64 FD {errU:.2e} ({n_unary} entries), "
+          f"dcompat vs FP64 FD {errC:.2e} ({len(want_c)} entries)")
+    assert errU < GTOL, (errU, got, fd)
+    assert errC < GTOL, (errC, have_c, want_c)
+
+
+def test_gradient_64x64_m4_vs_fp64_finite_differences(engine, oracle_mod):
+    M = 4
+    pairs = [(i, j) for i in range(M) for j in range(i, M)]
+    _ce_gradient_vs_fd(engine, oracle_mod, 64, 64, M, 5, 24, pairs)
+
+
+def test_gradient_512_m21_vs_fp64_finite_differences(engine, oracle_mod):
+    _ce_gradient_vs_fd(engine, oracle_mod, 512, 512, 21, 5, 3, [(0, 5), (7, 7)])
