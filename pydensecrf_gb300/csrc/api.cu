@@ -117,6 +117,7 @@ struct Term {
     std::vector<float> compat_h;
     std::vector<float> params;  // kernel parameters (DIAG d, FULL d*d row-major)
     bool params_set = false;    // the lattice uses params (else the features as given)
+    bool norm_pending = false;  // built, normalisation not yet computed (see flush_norms)
 };
 
 // Knobs of the launch sequence that the autotuner picks per configuration.
@@ -503,6 +504,11 @@ int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where, i
     return DCRF_OK;
 }
 
+// Value-size-1 rows live MP floats into the term's lattice buffers: their
+// zero row 0 is element MP (cleared at the build), and the stride-MP sentinel
+// row 0 stays untouched.
+float *v1_buffer(const dcrf_crf *h, float *V) { return h->MP > 1 ? V + h->MP : V; }
+
 // Descriptor of a term for the forward filter (or its transpose).
 TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     TermDev t{};
@@ -520,7 +526,7 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.off = T.lat.off;
     t.bary = T.lat.bary;
     t.wslice = T.lat.wslice;
-    t.V = T.V[(T.d + 1) & 1];
+    t.V = value1 ? v1_buffer(h, T.V[(T.d + 1) & 1]) : T.V[(T.d + 1) & 1];
     t.tile_pbeg = T.lat.tile_pbeg;
     t.part_mend = T.lat.part_mend;
     t.mem_pt = T.lat.mem_pt;
@@ -690,6 +696,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
                  float *const *S_out = nullptr, float *const *B_out = nullptr) {
     int MP = value1 ? 1 : h->MP;
     bool seq = value1 || h->M <= 2;
+    auto Vb = [&](const Term &T, int j) { return value1 ? v1_buffer(h, T.V[j]) : T.V[j]; };
     // Blur launches per term: passes 2i and 2i+1 share launch i (the last pass
     // alone when d+1 is odd).  Buffers are planned backwards from the final
     // output, alternating the term's two lattice buffers launch by launch, so
@@ -709,10 +716,10 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
         Term &T = h->terms[which[k]];
         Chain2 &c = plan[k];
         c.n = (T.d + 2) / 2;
-        c.fin = B_out ? B_out[k] : partial_order ? nullptr : T.V[(T.d + 1) & 1];
-        c.x[c.n - 1] = c.fin == T.V[0] ? T.V[1] : T.V[0];
-        for (int i = c.n - 2; i >= 0; i--) c.x[i] = c.x[i + 1] == T.V[0] ? T.V[1] : T.V[0];
-        float *red_out = S_out ? S_out[k] : h->tune.coop ? T.V[0] : c.x[0];
+        c.fin = B_out ? B_out[k] : partial_order ? nullptr : Vb(T, (T.d + 1) & 1);
+        c.x[c.n - 1] = c.fin == Vb(T, 0) ? Vb(T, 1) : Vb(T, 0);
+        for (int i = c.n - 2; i >= 0; i--) c.x[i] = c.x[i + 1] == Vb(T, 0) ? Vb(T, 1) : Vb(T, 0);
+        float *red_out = S_out ? S_out[k] : h->tune.coop ? Vb(T, 0) : c.x[0];
         ra.t[k] = {T.lat.red_beg, T.pout, red_out, T.lat.L, T.lat.P};
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
@@ -731,10 +738,10 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
         for (size_t k = 0; k < which.size(); k++) {
             Term &T = h->terms[which[k]];
             BlurChainArgs::C &c = ca.c[k];
-            c.S = S_out ? S_out[k] : T.V[0];
-            c.buf[0] = T.V[1];
-            c.buf[1] = T.V[0];
-            c.Out = B_out ? B_out[k] : partial_order ? nullptr : T.V[(T.d + 1) & 1];
+            c.S = S_out ? S_out[k] : Vb(T, 0);
+            c.buf[0] = Vb(T, 1);
+            c.buf[1] = Vb(T, 0);
+            c.Out = B_out ? B_out[k] : partial_order ? nullptr : Vb(T, (T.d + 1) & 1);
             c.nbr = T.lat.nbr;
             c.L = T.lat.L;
             c.d = T.d;
@@ -783,8 +790,9 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
 // buffers at stride 1, which overwrites entries that the stride-MP passes read
 // as the zero sentinel row (row 0).  Restore it afterwards.
 int zero_sentinels(dcrf_crf *h, Term &T) {
-    CU(cudaMemsetAsync(T.V[0], 0, sizeof(float) * h->MP, h->stream));
-    CU(cudaMemsetAsync(T.V[1], 0, sizeof(float) * h->MP, h->stream));
+    const size_t n = h->MP > 1 ? (size_t)h->MP + 1 : 1;  // row 0 and the value-size-1 row 0 (v1_buffer)
+    CU(cudaMemsetAsync(T.V[0], 0, sizeof(float) * n, h->stream));
+    CU(cudaMemsetAsync(T.V[1], 0, sizeof(float) * n, h->stream));
     return DCRF_OK;
 }
 
@@ -807,13 +815,9 @@ int sync_check(dcrf_crf *h) {
 }
 
 void free_term_lattice(dcrf_crf *h, Term &T) {
-    dev_free_async(T.norm, h->stream);
-    dev_free_async(T.V[0], h->stream);
-    dev_free_async(T.V[1], h->stream);
-    dev_free_async(T.pv, h->stream);
-    dev_free_async(T.pout, h->stream);
-    dev_free_async(T.mem_wn, h->stream);
+    // norm, V, pv, pout and mem_wn are carved from the lattice's memory
     dev_free_async(T.df, h->stream);
+    T.norm_pending = false;
     T.norm = T.V[0] = T.V[1] = T.pv = T.pout = T.mem_wn = T.df = nullptr;
     for (float *&b : T.bv) {
         dev_free_async(b, h->stream);
@@ -886,6 +890,7 @@ int build_term(dcrf_crf *h, int k) {
     }
     Segments seg;
     seg.start = h->seg;
+    seg.dev_start = h->d_seg;
     TileMapDev tm;
     tm.ntiles = h->ntiles;
     tm.slot_pt = h->slot_pt;
@@ -893,7 +898,8 @@ int build_term(dcrf_crf *h, int k) {
     float load = h->tune.hash_load;
     for (int attempt = 0;; attempt++) {
         ProfScope ps(h, DCRF_KCLASS_LATTICE);
-        rc = lattice_build(feat, T.d, h->N, seg, tm, T.variant, load, h->tune.task, h->stream, h->status, &T.lat);
+        rc = lattice_build(feat, T.d, h->N, seg, tm, T.variant, load, h->tune.task, h->MP, h->nslots, h->stream,
+                           h->status, &T.lat);
         if (rc == DCRF_ERR_HASH_FULL && attempt < 3) {
             load *= 4.f;
             continue;
@@ -902,35 +908,53 @@ int build_term(dcrf_crf *h, int k) {
     }
     dev_free_async(scaled, h->stream);
     if (rc) return set_err(rc, lattice_last_message());
-    size_t vrows = (size_t)T.lat.L + 1;
-    if ((rc = dev_alloc_async(&T.V[0], vrows * h->MP, h->stream))) return rc;
-    if ((rc = dev_alloc_async(&T.V[1], vrows * h->MP, h->stream))) return rc;
-    if ((rc = dev_alloc_async(&T.pv, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return rc;
-    if ((rc = dev_alloc_async(&T.pout, ((size_t)T.lat.P + 1) * h->MP, h->stream))) return rc;
-    if ((rc = dev_alloc_async(&T.norm, (size_t)h->nslots, h->stream))) return rc;
-    CU(cudaMemsetAsync(T.norm, 0, sizeof(float) * (size_t)h->nslots, h->stream));
-    // the zero sentinel rows (row 0) are never written afterwards
-    CU(cudaMemsetAsync(T.V[0], 0, vrows * h->MP * sizeof(float), h->stream));
-    CU(cudaMemsetAsync(T.V[1], 0, vrows * h->MP * sizeof(float), h->stream));
-    // normalisation: K * 1 through the value-size-1 path (pairwise.cpp:44)
-    std::vector<int> one{k};
-    PPArgs a = pp_args(h, PP_ONES | PP_SPLAT, one, false, true);
-    a.ts.t[0].pre_norm = 0;
-    a.ts.t[0].post_norm = 0;
-    CU(pp(h, a, 1));
-    if ((rc = filter_phase(h, one, false, true, false))) return rc;
-    a = pp_args(h, PP_NORM, one, false, true);
-    CU(pp(h, a, 1));
-    if ((rc = zero_sentinels(h, T))) return rc;
-    const size_t nm = (size_t)h->ntiles * SPLAT_TILE * (T.d + 1);
-    if ((rc = dev_alloc_async(&T.mem_wn, nm, h->stream))) return rc;
-    CU(launch_scale_members(T.lat.mem_pt, T.lat.mem_w, T.norm, h->ntiles, T.d + 1, T.mem_wn, h->stream));
-    // No synchronisation: the normalisation runs on while the caller goes on
-    // (the next term's build, or the inference) in stream order; a device
-    // status it leaves is reported by the next synchronising call.
+    T.V[0] = T.lat.V0;
+    T.V[1] = T.lat.V1;
+    T.pv = T.lat.pv;
+    T.pout = T.lat.pout;
+    T.norm = T.lat.norm;
+    T.mem_wn = T.lat.mem_wn;
+    // the normalisation (K * 1, pairwise.cpp:44) is computed for all new terms
+    // together before their first use (flush_norms); no synchronisation here
+    T.norm_pending = true;
     CU(cudaGetLastError());
     h->version++;
     return DCRF_OK;
+}
+
+// Normalisation of every term built since the last use (DenseKernel::initLattice,
+// pairwise.cpp:40-62): one value-size-1 filter of ones through all of them in
+// the same launches, then each term's norm and its member weights with the
+// norm folded in (the forward pre-normalisation of the splat).  Called at the
+// start of every call that uses the terms.  A device status it leaves is
+// reported by the next synchronising call.
+int flush_norms(dcrf_crf *h) {
+    std::vector<int> which;
+    for (size_t k = 0; k < h->terms.size(); k++)
+        if (h->terms[k].norm_pending) which.push_back((int)k);
+    if (which.empty()) return DCRF_OK;
+    for (int k : which) h->terms[k].norm_pending = false;
+    PPArgs a = pp_args(h, PP_ONES | PP_SPLAT, which, false, true);
+    for (size_t q = 0; q < which.size(); q++) a.ts.t[q].pre_norm = a.ts.t[q].post_norm = 0;
+    CU(pp(h, a, 1));
+    int rc;
+    if ((rc = filter_phase(h, which, false, true, false))) return rc;
+    a = pp_args(h, PP_NORM, which, false, true);
+    for (size_t q = 0; q < which.size(); q++) {
+        Term &T = h->terms[which[q]];
+        a.ts.t[q].V = v1_buffer(h, T.V[(T.d + 1) & 1]);
+        const bool fold = T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_BEFORE;
+        a.wn_out[q] = fold ? T.mem_wn : nullptr;
+    }
+    CU(pp(h, a, 1));
+    return DCRF_OK;
+}
+
+// check_handle, then the normalisation of terms built since the last use.
+int check_ready(dcrf_crf *h) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    return flush_norms(h);
 }
 
 int add_term(dcrf_crf *h, const float *feat_dev_owned, int d, int compat_kind, const float *compat, int ktype,
@@ -1058,6 +1082,8 @@ int rebuild_terms(dcrf_crf *h) {
 
 // Device time of n mean-field iterations (min of reps), launched directly.
 int time_iterations(dcrf_crf *h, int n, int reps, float *ms_out) {
+    int frc = flush_norms(h);
+    if (frc) return frc;
     cudaEvent_t a = take_event(h), b = take_event(h);
     float best = 1e30f;
     int rc = DCRF_OK;
@@ -1170,6 +1196,7 @@ int maybe_autotune(dcrf_crf *h) {
 
 int run_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
     int trc = maybe_autotune(h);
+    if (!trc) trc = flush_norms(h);  // (re)built by the tuner: normalised before any capture
     if (trc) return trc;
     if (h->profiling || !h->use_graphs || h->inference_runs++ == 0) return issue_inference(h, T, final_mode, ckpt);
     cudaStream_t user = h->stream;
@@ -1522,7 +1549,7 @@ int dcrf_destroy(dcrf_crf *h) {
 }
 
 int dcrf_check_bounded_wait(dcrf_crf *h, int spins) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (spins < 1 || spins > (1 << 20)) return set_err(DCRF_ERR_INVALID_ARG, "spins must be in [1, 1048576]");
     unsigned *flag = nullptr;
@@ -1643,7 +1670,7 @@ int dcrf_add_pairwise_bilateral(dcrf_crf *h, float sx, float sy, float sr, float
 }
 
 int dcrf_inference(dcrf_crf *h, int n_iterations, float *Q, int layout, int where) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
     if ((rc = run_inference(h, n_iterations, PP_WRITE_Q))) return rc;
@@ -1653,7 +1680,7 @@ int dcrf_inference(dcrf_crf *h, int n_iterations, float *Q, int layout, int wher
 }
 
 int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
     if (!h->has_unary) {  // densecrf.cpp:179-184: zeros without a unary
@@ -1667,7 +1694,7 @@ int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where) {
 }
 
 int dcrf_step_inference(dcrf_crf *h, float *Q, int layout, int where) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null marginals");
     if ((rc = load_mn(h, Q, layout, where, h->Q))) return rc;
@@ -1683,7 +1710,7 @@ int dcrf_step_inference(dcrf_crf *h, float *Q, int layout, int where) {
 }
 
 int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, double *kl_out) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!Q || !kl_out) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     if ((rc = load_mn(h, Q, layout, where, h->Q))) return rc;
@@ -1703,7 +1730,7 @@ int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, doubl
 }
 
 int dcrf_map(dcrf_crf *h, int n_iterations, int16_t *labels, int where) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!labels) return set_err(DCRF_ERR_INVALID_ARG, "null output");
     if ((rc = run_inference(h, n_iterations, PP_MAP))) return rc;
@@ -1729,7 +1756,7 @@ static int store_energy(dcrf_crf *h, const float *src, float *energy, int where)
 }
 
 int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *energy, int where_out) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!labels || !energy) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     int16_t *lab = nullptr;
@@ -1746,7 +1773,7 @@ int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *ener
 }
 
 int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term, float *energy, int where_out) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!labels || !energy) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     if (term < -1 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
@@ -1786,7 +1813,7 @@ int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term
 }
 
 int dcrf_synchronize(dcrf_crf *h) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if ((rc = sync_check(h))) return rc;
     return ok();
@@ -1809,7 +1836,7 @@ int dcrf_lattice_info(dcrf_crf *h, int term, int *d, int *L) {
 }
 
 int dcrf_lattice_dump(dcrf_crf *h, int term, int *offset, int *rank, float *bary, int *neighbors, int16_t *keys) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
     Term &T = h->terms[term];
@@ -1851,7 +1878,7 @@ int dcrf_lattice_dump(dcrf_crf *h, int term, int *offset, int *rank, float *bary
 }
 
 int dcrf_term_norm(dcrf_crf *h, int term, float *norm) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size() || !norm) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     Term &T = h->terms[term];
@@ -1867,13 +1894,16 @@ int dcrf_term_norm(dcrf_crf *h, int term, float *norm) {
 }
 
 int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     bool v1 = value_size == 1;
     int MP = v1 ? 1 : h->MP;
     if ((rc = load_mn(h, in, DCRF_LAYOUT_LM, DCRF_HOST, h->tmp, value_size))) return rc;
+    // the value-size-1 zero row (element MP) is row 1 of the full-width passes
+    // that may have run since the build
+    if (v1 && (rc = zero_sentinels(h, h->terms[term]))) return rc;
     std::vector<int> one{term};
     PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
     a.ts.t[0].pre_norm = 0;
@@ -1914,7 +1944,7 @@ int dcrf_set_autotune(dcrf_crf *h, int on) {
 }
 
 int dcrf_autotune(dcrf_crf *h) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (h->terms.empty()) return set_err(DCRF_ERR_STATE, "autotune needs at least one pairwise term");
     if ((rc = autotune_now(h))) return rc;
@@ -1934,7 +1964,7 @@ int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float 
 }
 
 int dcrf_set_tuning(dcrf_crf *h, int split, int smem_kb, int task_len, float hash_load, int coop_blur) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (split < 0 || split > 2 || smem_kb < 0 || smem_kb > 224 || task_len < 1 || task_len > 63 ||
         !(hash_load >= 1.f) || coop_blur < 0 || coop_blur > 1)
@@ -1960,7 +1990,7 @@ int dcrf_set_profiling(dcrf_crf *h, int on) {
 }
 
 int dcrf_profile(dcrf_crf *h, int kernel_class, double *total_ms, long long *launches) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (kernel_class < 0 || kernel_class >= DCRF_NUM_KCLASSES) return set_err(DCRF_ERR_INVALID_ARG, "bad class");
     CU(cudaStreamSynchronize(h->stream));
@@ -1988,7 +2018,7 @@ int dcrf_term_stats(dcrf_crf *h, int term, int *L, int *P, int *ntiles) {
 }
 
 int dcrf_term_buffer(dcrf_crf *h, int term, int which, float *out, size_t count) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size() || !out || which < 0 || which > 2)
         return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
@@ -2014,7 +2044,7 @@ int dcrf_set_compat(dcrf_crf *h, int term, int compat_kind, const float *compat)
 }
 
 int dcrf_set_kernel_params(dcrf_crf *h, int term, const float *params) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size() || !params) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     Term &T = h->terms[term];
@@ -2034,7 +2064,7 @@ int dcrf_param_counts(dcrf_crf *h, int term, int *n_compat, int *n_kernel) {
 }
 
 int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int layout, int where) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!Q || n_iterations < 0) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     const size_t qsz = (size_t)h->MP * h->nslots, need = qsz * ((size_t)n_iterations + 1);
@@ -2096,7 +2126,7 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
 }
 
 int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU, double *dcompat, double *dkernel) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (!dQ) return set_err(DCRF_ERR_INVALID_ARG, "null gradient");
     if (h->ckpt_T < 0 || h->ckpt_version != h->version)
@@ -2338,7 +2368,7 @@ size_t pad64(size_t n) { return (n + 63) & ~(size_t)63; }
 
 extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *in, int value_size, int reverse,
                                            float *out, void *stream) {
-    int rc = check_handle(h);
+    int rc = check_ready(h);
     if (rc) return rc;
     if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");

@@ -81,12 +81,14 @@ struct EmbedArgs {
     uint8_t *rank;
     uint64_t *keys;  // [(N+n_ph)*(d+1)][KW]
     DevStatus *st;
+    ClearList clr;   // set before the build's later kernels run: hash table, scan states, counts
 };
 
 template <int D>
 __global__ void __launch_bounds__(128) embed_kernel(EmbedArgs a) {
     constexpr int KW = KeyW<D>::KW;
     const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    clear_words(a.clr, (size_t)p, (size_t)gridDim.x * blockDim.x);
     if (p >= a.N + a.n_ph) return;
     int img;
     float f[D];
@@ -103,7 +105,7 @@ __global__ void __launch_bounds__(128) embed_kernel(EmbedArgs a) {
 #pragma unroll
         for (int j = 0; j < D; j++) f[j] = a.feat[(size_t)j * a.N + p];
     } else {
-        img = a.ph_img[p - a.N];
+        img = a.ph_img ? a.ph_img[p - a.N] : 0;
 #pragma unroll
         for (int j = 0; j < D; j++) f[j] = 0.f;
     }
@@ -296,7 +298,8 @@ __global__ void first_flag_kernel(const uint32_t *__restrict__ table, const uint
 template <int D>
 __global__ void offsets_kernel(const uint64_t *__restrict__ keys, const uint32_t *__restrict__ table,
                                const uint32_t *__restrict__ slot, const uint32_t *__restrict__ vid, size_t E,
-                               int N, int *__restrict__ off, uint16_t *__restrict__ vkeys) {
+                               int N, int *__restrict__ off, uint16_t *__restrict__ vkeys,
+                               uint32_t *__restrict__ vcount) {
     constexpr int KW = KeyW<D>::KW;
     size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= E) return;
@@ -311,6 +314,7 @@ __global__ void offsets_kernel(const uint64_t *__restrict__ keys, const uint32_t
         off[(size_t)r * N + i] = (int)v;
     }
     if (rep == (uint32_t)k) {
+        vcount[v] = 0;  // partials per vertex, counted by the tile placement
 #pragma unroll
         for (int q = 0; q <= D; q++) vkeys[(size_t)v * (D + 1) + q] = (uint16_t)(keys[k * KW + (q >> 2)] >> (16 * (q & 3)));
     }
@@ -542,7 +546,9 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
                                                                int *__restrict__ part_v, int *__restrict__ part_mend,
                                                                uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
                                                                uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w,
-                                                               uint32_t *__restrict__ task) {
+                                                               uint32_t *__restrict__ task, uint32_t *__restrict__ vcount,
+                                                               int L, int P, int T, const __grid_constant__ ClearList clr,
+                                                               DevStatus *st) {
     constexpr int C = TG<D>::C, NW = TG_THREADS / 32;
     constexpr int SEG = C / NW;  // corners per warp segment (a multiple of 32)
     extern __shared__ int tp_smem[];
@@ -565,17 +571,44 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
     int mtot, ttot;
     int mrun = block_exscan256(mloc, swarp, &mtot);
     int trun = block_exscan256(tloc, swarp, &ttot);
+    // block 0: the padding after the partial and task tables, and the ranges
+    // the reduce-list kernels need cleared (scan state, sentinel rows)
+    if (t == 0) {
+        if (tid < 8) {
+            part_mend[P + tid] = 0;
+            task[T + tid] = 0;
+        }
+        clear_words(clr, (size_t)tid, TG_THREADS);
+    }
     for (int p = p0; p < p1; p++) {
         const int c = pcnt[base + p];
+        const int v = pvx[base + p];
         moff[p] = mrun;
         toff[p] = trun;
-        part_v[pb + p] = pvx[base + p];
+        part_v[pb + p] = v;
+        // partials per vertex (the reduce lists' sizes); an id outside [0, L)
+        // is reported, never used as an index
+        if (v >= 0 && v < L)
+            atomicAdd(vcount + v, 1u);
+        else
+            dcrf_set_error(st, DCRF_ERR_CUDA, (int)(pb + p));
         part_mend[pb + p] = mrun + c;  // tile-relative end of the partial's members
         for (int q = 0; q < c; q += task_len)
             task[tb + trun++] = ((uint32_t)p << 19) | ((uint32_t)(mrun + q) << 6) | (uint32_t)min(task_len, c - q);
         mrun += c;
     }
     for (int e = tid; e < NW * C; e += TG_THREADS) wc[e] = 0;
+    // members past the tile's last one, and the corners of empty slots: index 0, weight 0
+    for (int e = mtot + tid; e < C; e += TG_THREADS) {
+        mem_pt[base + e] = 0;
+        mem_w[base + e] = 0.f;
+    }
+    if (slot_pt[(size_t)t * SPLAT_TILE + tid] < 0)
+        for (int r = 0; r <= D; r++) {
+            const size_t tl = ((size_t)t * (D + 1) + r) * SPLAT_TILE + tid;
+            tl_loc[tl] = 0;
+            tl_w[tl] = 0.f;
+        }
     __syncthreads();
     // stable member ranks: warps own consecutive corner segments; each warp
     // counts its segment's corners per partial in order, then ranks them
@@ -618,18 +651,43 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
 }
 
 
-// Partials per vertex; a vertex id outside [0, L) is reported, never used as an index.
-__global__ void count_kernel(const int *__restrict__ part_v, int P, int L, uint32_t *__restrict__ cnt, DevStatus *st) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
+// Reduce lists without a sort.  place: partial p takes a position in its
+// vertex's range [red_beg[v], red_beg[v+1]) by counting that vertex's
+// remaining count down (positions in arbitrary order); rank: the partial at
+// position j moves to the position given by its rank among the range's
+// partials -- the number of smaller partial indices, i.e. tile order, since the
+// partials are numbered tile by tile -- so every vertex's list comes out in
+// tile order, deterministically.  Work per partial is the length of its
+// vertex's list (short: a vertex touches few tiles of a 16x16-pixel grid).
+__global__ void red_place_kernel(const int *__restrict__ part_v, int P, int L, const int *__restrict__ red_beg,
+                                 uint32_t *__restrict__ vcount, int *__restrict__ lst, DevStatus *st) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
     if (p >= P) return;
     const int v = part_v[p];
-    if (v >= 0 && v < L)
-        atomicAdd(&cnt[v], 1u);
-    else
+    if (v < 0 || v >= L) return;  // reported by the tile placement
+    const uint32_t left = atomicSub(vcount + v, 1u);
+    const int pos = red_beg[v] + (int)left - 1;
+    if (left == 0 || pos >= red_beg[v + 1]) {
         dcrf_set_error(st, DCRF_ERR_CUDA, p);
+        return;
+    }
+    lst[pos] = p;
 }
 
-__global__ void set_int_kernel(int *p, int v) { *p = v; }
+__global__ void red_rank_kernel(const int *__restrict__ part_v, int P, int L, const int *__restrict__ red_beg,
+                                const int *__restrict__ lst, int *__restrict__ red_list, int *__restrict__ ppos) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= P) return;
+    const int p = lst[j];
+    if (p < 0 || p >= P) return;
+    const int v = part_v[p];
+    if (v < 0 || v >= L) return;
+    const int s0 = red_beg[v], s1 = red_beg[v + 1];
+    int rank = 0;
+    for (int q = s0; q < s1; q++) rank += __ldg(lst + q) < p ? 1 : 0;
+    red_list[s0 + rank] = p;
+    ppos[p] = s0 + rank;
+}
 
 // inv[list[i]] = i for a permutation list of [0, n)
 __global__ void invert_kernel(const int *__restrict__ list, int n, int *__restrict__ inv) {
@@ -686,19 +744,6 @@ struct Arena {
     }
 };
 
-// Zeroes n1 elements at p1 and n2 at p2 (and the alignment gap between them)
-// with one memset when the second directly follows the first.
-template <class A, class B>
-void zero_pair(A *p1, size_t n1, B *p2, size_t n2, cudaStream_t s) {
-    const size_t b1 = Arena::sz<A>(n1);
-    if (reinterpret_cast<char *>(p1) + b1 == reinterpret_cast<char *>(p2)) {
-        cudaMemsetAsync(p1, 0, b1 + n2 * sizeof(B), s);
-    } else {
-        cudaMemsetAsync(p1, 0, n1 * sizeof(A), s);
-        cudaMemsetAsync(p2, 0, n2 * sizeof(B), s);
-    }
-}
-
 // The tile kernels' exact dynamic shared memory, set once per device (the 48 KB
 // default leaves no room for their static shared memory at d = 7, where the
 // placement kernel's dynamic part is exactly 48 KB).
@@ -722,9 +767,12 @@ int fail(int code, const std::string &m) {
     return code;
 }
 
+// Device counts of a build, read back at its single synchronisation.
+enum : int { BI_L = 0, BI_P = 1, BI_T = 2, BI_MAXNP = 3, BI_MAXNT = 4, BI_WORDS = 8 };
+
 template <int D>
 int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
-            int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out) {
+            int task_len, int MP, int nslots, cudaStream_t s, DevStatus *status, LatticeDev *out) {
     constexpr int KW = KeyW<D>::KW;
     LatticeDev L{};
     L.d = D;
@@ -740,27 +788,42 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
             for (int q = nb; q % 4 != 0; q++) ph_img.push_back(b);
         }
     const int n_ph = (int)ph_img.size();
+    // one image: its padding points are image 0 and need no table
+    const bool ph_table = n_ph > 0 && nseg > 1;
     const size_t E = (size_t)(N + n_ph) * (D + 1);
     const size_t Ereal = (size_t)N * (D + 1);
     if (E >= 0xFFFFFFF0ull) return fail(DCRF_ERR_INVALID_ARG, "lattice too large (more than 2^32 simplex corners)");
 
     size_t cap = 1024;
     while ((double)cap < (double)load * (double)E && cap < (1ull << 31)) cap <<= 1;
-    const size_t scan_words = scan_temp_words(E);
+    const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
+    const size_t vid_state = lb_state_words(E), tile_state = lb_state_words((size_t)tm.ntiles);
+    // The vertex count L is needed on the host only to size the neighbour and
+    // key tables.  When their upper bound (L <= E) is small, they are reserved
+    // at that size and the build runs on to its single synchronisation (L comes
+    // back with the tile counts); otherwise the host waits for L first.
+    const bool learn_L_first = (size_t)10 * E * (D + 1) > ((size_t)256 << 20);
     // temporaries and the lattice's own tables come from one block per build
     // stage (sizes known at the start of each stage)
     Arena tmp{s}, per{s};
-    tmp.reserve(Arena::sz<uint64_t>(E * KW) + 2 * Arena::sz<uint32_t>(E) + Arena::sz<uint32_t>(4) +
-                Arena::sz<int>(nseg + 1) + Arena::sz<int>(n_ph + 1) + Arena::sz<uint32_t>(cap) +
-                Arena::sz<uint32_t>(scan_words));
+    tmp.reserve(Arena::sz<uint64_t>(E * KW) + 2 * Arena::sz<uint32_t>(E) + Arena::sz<uint32_t>(E + 1) +
+                Arena::sz<uint32_t>(BI_WORDS) + Arena::sz<int>(n_ph + 1) + Arena::sz<uint32_t>(cap) +
+                Arena::sz<unsigned long long>(vid_state) + Arena::sz<unsigned long long>(tile_state) +
+                Arena::sz<uint16_t>(ntl) + 2 * Arena::sz<int>(ntl) + 2 * Arena::sz<uint32_t>(tm.ntiles + 1));
     uint64_t *keys = tmp.get<uint64_t>(E * KW);
     uint32_t *slot = tmp.get<uint32_t>(E);
     uint32_t *vid = tmp.get<uint32_t>(E);
-    uint32_t *d_L = tmp.get<uint32_t>(4);
-    int *d_seg = tmp.get<int>(nseg + 1);
+    uint32_t *vcount = tmp.get<uint32_t>(E + 1);  // partials per vertex (indexed by vertex id < L <= E)
+    uint32_t *info = tmp.get<uint32_t>(BI_WORDS);
     int *d_ph = tmp.get<int>(n_ph + 1);
     uint32_t *table = tmp.get<uint32_t>(cap);
-    uint32_t *stemp = tmp.get<uint32_t>(scan_words);
+    unsigned long long *st_vid = tmp.get<unsigned long long>(vid_state);
+    unsigned long long *st_tile = tmp.get<unsigned long long>(tile_state);
+    uint16_t *cl = tmp.get<uint16_t>(ntl);
+    int *pvx = tmp.get<int>(ntl);
+    int *pcnt = tmp.get<int>(ntl);
+    uint32_t *tile_np = tmp.get<uint32_t>(tm.ntiles + 1);
+    uint32_t *tile_nt = tmp.get<uint32_t>(tm.ntiles + 1);
     if (tmp.failed) {
         tmp.release();
         return fail(DCRF_ERR_OOM, "device allocation failed in lattice build");
@@ -781,11 +844,12 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         if (st.code != 0) return bail(st.code, "lattice build failed");
         return 0;
     };
-    cudaMemcpyAsync(d_seg, seg.start.data(), sizeof(int) * (nseg + 1), cudaMemcpyHostToDevice, s);
-    if (n_ph) cudaMemcpyAsync(d_ph, ph_img.data(), sizeof(int) * n_ph, cudaMemcpyHostToDevice, s);
-    cudaMemsetAsync(table, 0xFF, cap * sizeof(uint32_t), s);
+    if (ph_table) cudaMemcpyAsync(d_ph, ph_img.data(), sizeof(int) * n_ph, cudaMemcpyHostToDevice, s);
 
-    per.reserve(Arena::sz<int>(Ereal) + 2 * Arena::sz<float>(Ereal) + Arena::sz<uint8_t>(Ereal));
+    const size_t Lcap0 = learn_L_first ? 0 : E;  // rows reserved for the neighbour and key tables before L is known
+    per.reserve(Arena::sz<int>(Ereal) + 2 * Arena::sz<float>(Ereal) + Arena::sz<uint8_t>(Ereal) +
+                Arena::sz<int2>(Lcap0 * (D + 1)) + Arena::sz<uint16_t>(Lcap0 * (D + 1)) +
+                2 * Arena::sz<int>(tm.ntiles + 1) + 2 * (Arena::sz<uint16_t>(ntl) + Arena::sz<float>(ntl)));
     L.off = per.get<int>(Ereal);
     L.bary = per.get<float>(Ereal);
     L.wslice = per.get<float>(Ereal);
@@ -796,8 +860,8 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     ea.feat = feat;
     ea.N = N;
     ea.n_ph = n_ph;
-    ea.ph_img = d_ph;
-    ea.seg_start = d_seg;
+    ea.ph_img = ph_table ? d_ph : nullptr;
+    ea.seg_start = seg.dev_start;
     ea.nseg = nseg;
     {
         // float(sqrt(2/3)*(d+1)), scale = float(1/sqrt((i+2)(i+1)) * inv_std_dev)
@@ -814,139 +878,181 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     ea.rank = L.rank;
     ea.keys = keys;
     ea.st = status;
-    int npts = N + n_ph;
-    if (npts > 0) DCRF_LAUNCH(embed_kernel<D><<<ceil_div_u(npts, 128), 128, 0, s>>>(ea));
+    // cleared by the embed launch, before the kernels that use them
+    ea.clr.add(table, cap, EMPTY);
+    ea.clr.add(info, BI_WORDS, 0u);
+    ea.clr.add(st_vid, 2 * vid_state, 0u);
+    ea.clr.add(st_tile, 2 * tile_state, 0u);
+    const int npts = N + n_ph;
+    DCRF_LAUNCH(embed_kernel<D><<<std::max(1u, ceil_div_u(npts, 128)), 128, 0, s>>>(ea));
     if (E > 0) DCRF_LAUNCH(insert_kernel<KW><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, E, table, (uint32_t)(cap - 1), slot, status));
-    if (E > 0) DCRF_LAUNCH(first_flag_kernel<<<ceil_div_u(E, 256), 256, 0, s>>>(table, slot, E, vid));
-    if (scan_exclusive_u32(vid, vid, E, d_L, stemp, s) != cudaSuccess) return bail(DCRF_ERR_CUDA, "scan failed");
-    // The vertex count L is needed on the host only to size the neighbour and
-    // key tables.  When their upper bound (L <= E) is small, they are reserved
-    // at that size and the build runs on to its single synchronisation (L comes
-    // back with the tile counts); otherwise the host waits for L here.
-    uint32_t hL = 0;
+    {  // vertex ids: first occurrences, numbered in corner order (one launch)
+        LBScanArgs sa;
+        sa.n = E;
+        sa.out[0] = vid;
+        sa.total[0][0] = info + BI_L;
+        sa.table = table;
+        sa.slot = slot;
+        sa.state = st_vid;
+        sa.st = status;
+        if (lb_scan(sa, s) != cudaSuccess) return bail(DCRF_ERR_CUDA, "scan failed");
+    }
+    uint32_t hinfo[BI_WORDS] = {};
     DevStatus hst{};
     cudaError_t ce = cudaSuccess;
-    const bool learn_L_first = (size_t)10 * E * (D + 1) > ((size_t)256 << 20);
     if (learn_L_first) {
-        cudaMemcpyAsync(&hL, d_L, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(hinfo, info, sizeof(hinfo), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
         ce = cudaStreamSynchronize(s);
         if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice build: ") + cudaGetErrorString(ce));
         if (int rc = status_error(hst)) return rc;
-        L.L = (int)hL;
+        L.L = (int)hinfo[BI_L];
+        per.reserve(Arena::sz<int2>((size_t)L.L * (D + 1)) + Arena::sz<uint16_t>((size_t)L.L * (D + 1)));
     }
-    const size_t Lcap = learn_L_first ? (size_t)L.L : E;  // rows reserved for the neighbour and key tables
-
-    const size_t ntl = (size_t)tm.ntiles * (D + 1) * SPLAT_TILE;
-    per.reserve(Arena::sz<int2>(Lcap * (D + 1)) + Arena::sz<uint16_t>(Lcap * (D + 1)) +
-                2 * Arena::sz<int>(tm.ntiles + 1) + 2 * (Arena::sz<uint16_t>(ntl) + Arena::sz<float>(ntl)));
-    tmp.reserve(Arena::sz<uint16_t>(ntl) + 2 * Arena::sz<int>(ntl) + 2 * Arena::sz<uint32_t>(tm.ntiles + 1) +
-                Arena::sz<uint32_t>(4));
+    const size_t Lcap = learn_L_first ? (size_t)L.L : E;
     L.nbr = per.get<int2>(Lcap * (D + 1));
     L.vkeys = per.get<uint16_t>(Lcap * (D + 1));
     if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (neighbours)");
     if (E > 0)
-        DCRF_LAUNCH(offsets_kernel<D><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, table, slot, vid, E, N, L.off, L.vkeys));
+        DCRF_LAUNCH(offsets_kernel<D><<<ceil_div_u(E, 256), 256, 0, s>>>(keys, table, slot, vid, E, N, L.off, L.vkeys,
+                                                                         vcount));
     if (Lcap > 0) {
         const unsigned nb = (unsigned)std::min<size_t>(ceil_div_u(Lcap * (D + 1), 256), 4096);
-        DCRF_LAUNCH(neighbors_kernel<D><<<nb, 256, 0, s>>>(keys, table, (uint32_t)(cap - 1), vid, L.vkeys, d_L, L.nbr));
+        DCRF_LAUNCH(neighbors_kernel<D><<<nb, 256, 0, s>>>(keys, table, (uint32_t)(cap - 1), vid, L.vkeys,
+                                                            info + BI_L, L.nbr));
     }
     // ---- splat tiles: partials, member lists, slice tables, tasks ----------------
     L.ntiles = tm.ntiles;
     L.tile_pbeg = per.get<int>(L.ntiles + 1);
     L.tile_tbeg = per.get<int>(L.ntiles + 1);
-    // member and slice tables side by side: zeroed as two memsets
     L.mem_pt = per.get<uint16_t>(ntl);
     L.mem_w = per.get<float>(ntl);
     L.tl_loc = per.get<uint16_t>(ntl);
     L.tl_w = per.get<float>(ntl);
-    uint16_t *cl = tmp.get<uint16_t>(ntl);
-    int *pvx = tmp.get<int>(ntl);
-    int *pcnt = tmp.get<int>(ntl);
-    uint32_t *tile_np = tmp.get<uint32_t>(L.ntiles + 1);
-    uint32_t *tile_nt = tmp.get<uint32_t>(L.ntiles + 1);
-    uint32_t *maxes = tmp.get<uint32_t>(4);
-    if (per.failed || tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
-    // empty slots and padding: local index 0, weight 0
-    zero_pair(L.mem_pt, ntl, L.mem_w, ntl, s);
-    zero_pair(L.tl_loc, ntl, L.tl_w, ntl, s);
-    cudaMemsetAsync(maxes, 0, 4 * sizeof(uint32_t), s);
+    if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (tiles)");
     const size_t smem_g = (2 * (size_t)TG<D>::HT + TG<D>::C) * sizeof(int);
     const size_t smem_p = 2 * (size_t)TG<D>::C * sizeof(int) + (TG_THREADS / 32) * (size_t)TG<D>::C * sizeof(uint16_t);
     if (tile_kernels_optin<D>(smem_g, smem_p) != cudaSuccess)
         return bail(DCRF_ERR_CUDA, "tile kernels: shared-memory opt-in failed");
-    uint32_t hcnt[4] = {0, 0, 0, 0};  // P, T, max partials, max tasks of a tile
     if (L.ntiles > 0) {
         DCRF_LAUNCH(tile_group_kernel<D><<<L.ntiles, TG_THREADS, smem_g, s>>>(L.off, N, tm.slot_pt, task_len, cl, pvx,
-                                                                             pcnt, tile_np, tile_nt, maxes, status));
+                                                                             pcnt, tile_np, tile_nt, info + BI_MAXNP,
+                                                                             status));
         // a launch that did not start must not leave its outputs to the next kernels
         if ((ce = cudaGetLastError()) != cudaSuccess)
             return bail(DCRF_ERR_CUDA, std::string("tile grouping launch: ") + cudaGetErrorString(ce));
-        if (scan_exclusive_u32_pair(tile_np, (uint32_t *)L.tile_pbeg, (uint32_t *)L.tile_pbeg + L.ntiles, tile_nt,
-                                    (uint32_t *)L.tile_tbeg, (uint32_t *)L.tile_tbeg + L.ntiles, L.ntiles, stemp,
-                                    s) != cudaSuccess)
-            return bail(DCRF_ERR_CUDA, "scan failed");
-        cudaMemcpyAsync(hcnt, L.tile_pbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(hcnt + 1, L.tile_tbeg + L.ntiles, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(hcnt + 2, maxes, 2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
-    } else {
-        cudaMemsetAsync(L.tile_pbeg, 0, sizeof(int), s);
-        cudaMemsetAsync(L.tile_tbeg, 0, sizeof(int), s);
     }
-    if (!learn_L_first) cudaMemcpyAsync(&hL, d_L, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+    {  // partial and task ranges of the tiles (one launch, both arrays)
+        LBScanArgs sa;
+        sa.narr = 2;
+        sa.n = (size_t)L.ntiles;
+        sa.in[0] = tile_np;
+        sa.in[1] = tile_nt;
+        sa.out[0] = (uint32_t *)L.tile_pbeg;
+        sa.out[1] = (uint32_t *)L.tile_tbeg;
+        sa.total[0][0] = (uint32_t *)L.tile_pbeg + L.ntiles;
+        sa.total[0][1] = info + BI_P;
+        sa.total[1][0] = (uint32_t *)L.tile_tbeg + L.ntiles;
+        sa.total[1][1] = info + BI_T;
+        sa.state = st_tile;
+        sa.st = status;
+        if (lb_scan(sa, s) != cudaSuccess) return bail(DCRF_ERR_CUDA, "scan failed");
+    }
+    cudaMemcpyAsync(hinfo, info, sizeof(hinfo), cudaMemcpyDeviceToHost, s);
     cudaMemcpyAsync(&hst, status, sizeof(DevStatus), cudaMemcpyDeviceToHost, s);
     ce = cudaStreamSynchronize(s);
     if (ce != cudaSuccess) return bail(DCRF_ERR_CUDA, std::string("lattice tiles: ") + cudaGetErrorString(ce));
     if (int rc = status_error(hst)) return rc;
-    if (!learn_L_first) L.L = (int)hL;
-    L.P = (int)hcnt[0];
-    L.max_np = (int)hcnt[2];
-    L.max_nt = (int)hcnt[3];
-    per.reserve(3 * Arena::sz<int>((size_t)L.P + 1) + Arena::sz<int>((size_t)L.P + 8) + Arena::sz<int>((size_t)L.L + 1) +
-                Arena::sz<uint32_t>((size_t)hcnt[1] + 8));
-    const size_t radix_words = radix_temp_words((size_t)L.P) + scan_temp_words((size_t)L.L + 1);
-    tmp.reserve(Arena::sz<uint32_t>((size_t)L.L + 1) + 4 * Arena::sz<uint32_t>((size_t)L.P + 1) +
-                Arena::sz<uint32_t>(radix_words));
-    L.part_v = per.get<int>((size_t)L.P + 1);
-    L.red_beg = per.get<int>((size_t)L.L + 1);
-    L.red_list = per.get<int>((size_t)L.P + 1);
-    L.ppos = per.get<int>((size_t)L.P + 1);
+    L.L = (int)hinfo[BI_L];
+    L.P = (int)hinfo[BI_P];
+    const int T = (int)hinfo[BI_T];
+    L.max_np = (int)hinfo[BI_MAXNP];
+    L.max_nt = (int)hinfo[BI_MAXNT];
+    // ---- partial tables, reduce lists and the value buffers --------------------
+    const size_t Pn = (size_t)L.P + 1, Ln = (size_t)L.L + 1;
+    const size_t red_state = lb_state_words(Ln - 1);
+    // a vertex shared by very many tiles on average makes the rank counting
+    // quadratic in its list length: such lattices take the radix sort
+    const bool radix = (size_t)L.P > 64 * std::max<size_t>(1, (size_t)L.L);
+    const size_t radix_words = radix ? radix_temp_words((size_t)L.P) : 0;
+    per.reserve(3 * Arena::sz<int>(Pn) + Arena::sz<int>((size_t)L.P + 8) + Arena::sz<int>(Ln) +
+                Arena::sz<uint32_t>((size_t)T + 8) + 2 * Arena::sz<float>(Ln * MP) + 2 * Arena::sz<float>(Pn * MP) +
+                Arena::sz<float>((size_t)nslots) + Arena::sz<float>(ntl));
+    L.part_v = per.get<int>(Pn);
+    L.red_beg = per.get<int>(Ln);
+    L.red_list = per.get<int>(Pn);
+    L.ppos = per.get<int>(Pn);
     L.part_mend = per.get<int>((size_t)L.P + 8);
-    L.task = per.get<uint32_t>((size_t)hcnt[1] + 8);
+    L.task = per.get<uint32_t>((size_t)T + 8);
+    L.V0 = per.get<float>(Ln * MP);
+    L.V1 = per.get<float>(Ln * MP);
+    L.pv = per.get<float>(Pn * MP);
+    L.pout = per.get<float>(Pn * MP);
+    L.norm = per.get<float>((size_t)nslots);
+    L.mem_wn = per.get<float>(ntl);
     if (per.failed) return bail(DCRF_ERR_OOM, "device allocation failed (partials)");
-    zero_pair(L.part_mend, (size_t)L.P + 8, L.task, (size_t)hcnt[1] + 8, s);
+    Arena red{s};
+    red.reserve(Arena::sz<unsigned long long>(red_state) + Arena::sz<int>(Pn) +
+                (radix ? 4 * Arena::sz<uint32_t>(Pn) + Arena::sz<uint32_t>(radix_words) : 0));
+    unsigned long long *st_red = red.get<unsigned long long>(red_state);
+    int *lst = red.get<int>(Pn);
+    if (red.failed) {
+        red.release();
+        return bail(DCRF_ERR_OOM, "device allocation failed (reduce lists)");
+    }
     if (L.ntiles > 0) {
+        // also cleared there: the reduce-list scan's state, and the sentinel rows
+        // (row 0 and element MP) of both value buffers
+        ClearList clr;
+        clr.add(st_red, 2 * red_state, 0u);
+        clr.add(L.V0, (size_t)MP + 1, 0u);
+        clr.add(L.V1, (size_t)MP + 1, 0u);
         DCRF_LAUNCH(tile_place_kernel<D><<<L.ntiles, TG_THREADS, smem_p, s>>>(
             cl, pvx, pcnt, L.bary, N, tm.slot_pt, (const uint32_t *)L.tile_pbeg, (const uint32_t *)L.tile_tbeg,
-            task_len, L.part_v, L.part_mend, L.mem_pt, L.mem_w, L.tl_loc, L.tl_w, L.task));
-        if ((ce = cudaGetLastError()) != cudaSuccess)
+            task_len, L.part_v, L.part_mend, L.mem_pt, L.mem_w, L.tl_loc, L.tl_w, L.task, vcount, L.L, L.P, T, clr,
+            status));
+        if ((ce = cudaGetLastError()) != cudaSuccess) {
+            red.release();
             return bail(DCRF_ERR_CUDA, std::string("tile placement launch: ") + cudaGetErrorString(ce));
+        }
     }
-    // ---- reduce lists: partials grouped by vertex, in tile order ------------
-    {
-        uint32_t *cnt = tmp.get<uint32_t>((size_t)L.L + 1);
-        uint32_t *k0 = tmp.get<uint32_t>((size_t)L.P + 1), *v0 = tmp.get<uint32_t>((size_t)L.P + 1);
-        uint32_t *k1 = tmp.get<uint32_t>((size_t)L.P + 1), *v1 = tmp.get<uint32_t>((size_t)L.P + 1);
-        uint32_t *rtemp = tmp.get<uint32_t>(radix_words);
-        if (tmp.failed) return bail(DCRF_ERR_OOM, "device allocation failed (reduce lists)");
-        cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * ((size_t)L.L + 1), s);
-        if (L.P > 0) DCRF_LAUNCH(count_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, L.L, cnt, status));
-        if (scan_exclusive_u32(cnt, (uint32_t *)L.red_beg, (size_t)L.L, (uint32_t *)(L.red_beg + L.L), rtemp, s) !=
-            cudaSuccess)
+    {  // red_beg = exclusive scan of the partials per vertex; red_beg[L] = P
+        LBScanArgs sa;
+        sa.n = (size_t)L.L;
+        sa.in[0] = vcount;
+        sa.out[0] = (uint32_t *)L.red_beg;
+        sa.total[0][0] = (uint32_t *)L.red_beg + L.L;
+        sa.state = st_red;
+        sa.st = status;
+        if (L.ntiles > 0 && lb_scan(sa, s) != cudaSuccess) {
+            red.release();
             return bail(DCRF_ERR_CUDA, "scan failed");
-        if (L.L == 0) DCRF_LAUNCH(set_int_kernel<<<1, 1, 0, s>>>(L.red_beg, 0));
-        if (L.P > 0) {
+        }
+    }
+    if (L.P > 0) {
+        if (!radix) {
+            DCRF_LAUNCH(red_place_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, L.L, L.red_beg, vcount,
+                                                                              lst, status));
+            DCRF_LAUNCH(red_rank_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.part_v, L.P, L.L, L.red_beg, lst,
+                                                                             L.red_list, L.ppos));
+        } else {
+            uint32_t *k0 = red.get<uint32_t>(Pn), *v0 = red.get<uint32_t>(Pn);
+            uint32_t *k1 = red.get<uint32_t>(Pn), *v1 = red.get<uint32_t>(Pn);
+            uint32_t *rtemp = red.get<uint32_t>(radix_words);
             int bits = 1;
             while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)L.L) bits++;
-            if (radix_argsort_u32((const uint32_t *)L.part_v, (size_t)L.P, bits, (uint32_t *)L.red_list, k0, v0, k1,
-                                  v1, rtemp, s) != cudaSuccess)
+            if (red.failed || radix_argsort_u32((const uint32_t *)L.part_v, (size_t)L.P, bits, (uint32_t *)L.red_list,
+                                                k0, v0, k1, v1, rtemp, s) != cudaSuccess) {
+                red.release();
                 return bail(DCRF_ERR_CUDA, "radix sort failed");
+            }
             DCRF_LAUNCH(invert_kernel<<<ceil_div_u(L.P, 256), 256, 0, s>>>(L.red_list, L.P, L.ppos));
         }
     }
     // no synchronisation here: the temporaries go back to the pool in stream
-    // order, and the caller checks the device status block (count_kernel's
-    // consistency check included) at its next synchronisation
+    // order, and the caller checks the device status block (the placement's
+    // consistency checks included) at its next synchronisation
+    red.release();
     tmp.release();
     ce = cudaGetLastError();
     if (ce != cudaSuccess) {
@@ -967,13 +1073,14 @@ void lattice_free(LatticeDev *L, cudaStream_t s) {
 }
 
 int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
-                  int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out) {
+                  int task_len, int MP, int nslots, cudaStream_t s, DevStatus *status, LatticeDev *out) {
     if (task_len < 1 || task_len > 63) return fail(DCRF_ERR_INVALID_ARG, "splat task length must be in [1, 63]");
-    if (N < 0 || (seg.start.size() < 2)) return fail(DCRF_ERR_INVALID_ARG, "bad point segmentation");
+    if (N < 0 || seg.start.size() < 2 || !seg.dev_start) return fail(DCRF_ERR_INVALID_ARG, "bad point segmentation");
+    if (MP < 1 || nslots < 0) return fail(DCRF_ERR_INVALID_ARG, "bad value-buffer sizes");
     switch (d) {
 #define DCRF_CASE(D) \
     case D:          \
-        return build_d<D>(feat, N, seg, tm, variant, load, task_len, s, status, out);
+        return build_d<D>(feat, N, seg, tm, variant, load, task_len, MP, nslots, s, status, out);
         DCRF_CASE(1) DCRF_CASE(2) DCRF_CASE(3) DCRF_CASE(4) DCRF_CASE(5) DCRF_CASE(6) DCRF_CASE(7) DCRF_CASE(8)
         DCRF_CASE(9) DCRF_CASE(10) DCRF_CASE(11) DCRF_CASE(12) DCRF_CASE(13) DCRF_CASE(14) DCRF_CASE(15)
         DCRF_CASE(16)

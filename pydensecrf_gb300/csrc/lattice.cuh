@@ -41,13 +41,19 @@ struct LatticeDev {
     // tile-ordered slice tables: corner r of slot li of tile t at (t*(d+1)+r)*SPLAT_TILE+li
     uint16_t *tl_loc = nullptr;  // index of the corner's vertex among the tile's partials
     float *tl_w = nullptr;       // the corner's barycentric weight
+    // value buffers of the mean-field passes, carved from the lattice's memory
+    // (sizes from the build's MP and slot count): V0, V1 [L+1][MP] (row 0 and
+    // element MP zeroed: the sentinel rows of the stride-MP and value-size-1
+    // passes), pv and pout [P+1][MP], norm [nslots], mem_wn [ntiles][SPLAT_TILE*(d+1)]
+    float *V0 = nullptr, *V1 = nullptr, *pv = nullptr, *pout = nullptr, *norm = nullptr, *mem_wn = nullptr;
     size_t bytes = 0;
     std::vector<void *> blocks;  // the pool blocks the tables above are carved from
 };
 
 // Image segmentation of the point set (a single image: nseg = 1).
 struct Segments {
-    std::vector<int> start;  // nseg+1 prefix offsets of the images' points
+    std::vector<int> start;       // nseg+1 prefix offsets of the images' points
+    const int *dev_start = nullptr;  // the same on the device
 };
 
 // Assignment of points to splat tiles: tile t owns slots [t*SPLAT_TILE,
@@ -59,16 +65,18 @@ struct TileMapDev {
     const int *tile_vbase = nullptr;  // device [ntiles+1]
 };
 
-// Builds the lattice of `feat` ([d][N], device) on `s`.  `variant` selects the
-// x86 (SSE) or scalar arithmetic of the reference; SSE also inserts the
+// Builds the lattice of `feat` ([d][N], device) on `s`, with its value
+// buffers for MP-float rows and `nslots` slots.  `variant` selects the x86
+// (SSE) or scalar arithmetic of the reference; SSE also inserts the
 // zero-feature padding points of each image (N_img % 4 != 0).  `load` is the
 // hash-table capacity factor (capacity = pow2 >= load * corners); `task_len`
 // the most members of one splat task (1..63).  Returns a DCRF status; on
-// DCRF_ERR_HASH_FULL the caller may retry with a larger load.  Work may still
-// be in flight on return: the caller synchronises and checks `status` (a
-// non-zero code means the lattice is unusable).
+// DCRF_ERR_HASH_FULL the caller may retry with a larger load.  The host waits
+// once, for the vertex and partial counts (a failed insert or an overflowing key
+// is reported then); the kernels after it may still be in flight on return,
+// and a status they leave is reported at the caller's next synchronisation.
 int lattice_build(const float *feat, int d, int N, const Segments &seg, const TileMapDev &tm, int variant, float load,
-                  int task_len, cudaStream_t s, DevStatus *status, LatticeDev *out);
+                  int task_len, int MP, int nslots, cudaStream_t s, DevStatus *status, LatticeDev *out);
 
 void lattice_free(LatticeDev *lat, cudaStream_t s);
 

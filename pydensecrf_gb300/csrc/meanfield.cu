@@ -683,29 +683,42 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
     }
     const size_t s = (size_t)blockIdx.x * SPLAT_TILE + threadIdx.x;
     const int i = a.slot_pt[s];
-    if (i < 0) return;
     const int N = a.N, M = a.M;
     if (a.mode & PP_NORM) {
-        // value size 1, seqCompute slice: out += (w * v) * alpha (permutohedral.cpp:513-521)
+        // value size 1, seqCompute slice: out += (w * v) * alpha (permutohedral.cpp:513-521);
+        // then, per term that folds its norm into the splat, the tile's member
+        // weights times their point's norm (from this tile's norms in shared memory)
+        __shared__ float sNorm[SPLAT_TILE];
         for (int k = 0; k < a.ts.n; k++) {
             const TermDev &T = a.ts.t[k];
-            float n = 0.f;
-            for (int r = 0; r <= T.d; r++) {
-                int o = T.off[(size_t)r * N + i] + 1;
-                float w = T.bary[(size_t)r * N + i];
-                n = fadd(n, fmul(fmul(w, __ldg(T.V + o)), T.alpha));
+            float out = 0.f;
+            if (i >= 0) {
+                float n = 0.f;
+                for (int r = 0; r <= T.d; r++) {
+                    int o = T.off[(size_t)r * N + i] + 1;
+                    float w = T.bary[(size_t)r * N + i];
+                    n = fadd(n, fmul(fmul(w, __ldg(T.V + o)), T.alpha));
+                }
+                if (a.ntype[k] == DCRF_NORMALIZE_SYMMETRIC)  // pairwise.cpp:54-57
+                    out = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn((double)n, 1e-20))));
+                else if (a.ntype[k] == DCRF_NO_NORMALIZATION)
+                    out = n;  // raw K*1; the host derives the mean (pairwise.cpp:46-53)
+                else  // pairwise.cpp:58-61
+                    out = __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
             }
-            float out;
-            if (a.ntype[k] == DCRF_NORMALIZE_SYMMETRIC)  // pairwise.cpp:54-57
-                out = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn((double)n, 1e-20))));
-            else if (a.ntype[k] == DCRF_NO_NORMALIZATION)
-                out = n;  // raw K*1; the host derives the mean (pairwise.cpp:46-53)
-            else  // pairwise.cpp:58-61
-                out = __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
             a.norm_out[k][s] = out;
+            if (a.wn_out[k]) {  // the block's threads are its tile's slots
+                sNorm[threadIdx.x] = out;
+                __syncthreads();
+                const size_t base = (size_t)blockIdx.x * SPLAT_TILE * (T.d + 1);
+                for (int e = threadIdx.x; e < SPLAT_TILE * (T.d + 1); e += blockDim.x)
+                    a.wn_out[k][base + e] = fmul(T.mem_w[base + e], sNorm[T.mem_pt[base + e]]);
+                __syncthreads();
+            }
         }
         return;
     }
+    if (i < 0) return;
     // PP_FILTER: raw K v of term 0
     const TermDev &T = a.ts.t[0];
     float acc[MP];
@@ -1187,14 +1200,6 @@ __global__ void scale_features_kernel(const float *__restrict__ in, float *__res
     }
 }
 
-__global__ void scale_members_kernel(const uint16_t *__restrict__ mem_pt, const float *__restrict__ mem_w,
-                                     const float *__restrict__ norm, int d1, float *__restrict__ wn) {
-    const int t = blockIdx.x;
-    const size_t base = (size_t)t * SPLAT_TILE * d1;
-    for (int e = threadIdx.x; e < SPLAT_TILE * d1; e += blockDim.x)
-        wn[base + e] = fmul(mem_w[base + e], norm[(size_t)t * SPLAT_TILE + mem_pt[base + e]]);
-}
-
 // ---------------------------------------------------------------------------
 int pointpass_smem_budget(int MP) { return MP <= 20 ? 72 * 1024 : 108 * 1024; }
 
@@ -1384,12 +1389,6 @@ cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *
     } else {
         DCRF_LAUNCH(from_slots_lm_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, ld, N, seg, nseg, pt_slot, out));
     }
-    return cudaGetLastError();
-}
-
-cudaError_t launch_scale_members(const uint16_t *mem_pt, const float *mem_w, const float *norm, int ntiles, int d1,
-                                 float *wn, cudaStream_t s) {
-    if (ntiles > 0) DCRF_LAUNCH(scale_members_kernel<<<ntiles, 256, 0, s>>>(mem_pt, mem_w, norm, d1, wn));
     return cudaGetLastError();
 }
 

@@ -40,8 +40,10 @@ struct PPArgs {
     // Gacc += compat(F') (rows; null to skip).  Qout (raw F) may be null.
     float *Fpost;
     float *Gacc;
-    // PP_NORM outputs, per term ([nslots] each)
+    // PP_NORM outputs, per term ([nslots] each; empty slots get 0), and the
+    // splat member weights times their point's norm (null: not wanted)
     float *norm_out[DCRF_MAX_TERMS];
+    float *wn_out[DCRF_MAX_TERMS];
     int ntype[DCRF_MAX_TERMS];
     TermSet ts;
 };
@@ -118,9 +120,6 @@ cudaError_t launch_features_2d(int N, const int *seg, const int *imgW, int nseg,
                                const uint8_t *rgb, float sr, float sg, float sb, float *feat, cudaStream_t s);
 cudaError_t launch_scale_features(const float *in, float *out, const float *scale_or_matrix, int d, int N, int full,
                                   cudaStream_t s);
-// wn[e] = w[e] * norm[slot of member e] over the padded per-tile member lists
-cudaError_t launch_scale_members(const uint16_t *mem_pt, const float *mem_w, const float *norm, int ntiles, int d1,
-                                 float *wn, cudaStream_t s);
 // Opts every point-pass instantiation in to its dynamic shared-memory budget.
 void prepare_pointpass_kernels();
 // Largest dynamic shared memory the point pass may use per CTA.

@@ -7,6 +7,8 @@
 #include "dcrf_common.cuh"
 #include "primitives.cuh"
 
+#include <algorithm>
+
 namespace dcrf {
 
 constexpr int SCAN_THREADS = 256;
@@ -184,6 +186,165 @@ cudaError_t scan_exclusive_u32_pair(const uint32_t *in0, uint32_t *out0, uint32_
     cudaError_t e = scan_exclusive_u32(in0, out0, n, total0, temp, s);
     if (e != cudaSuccess) return e;
     return scan_exclusive_u32(in1, out1, n, total1, temp, s);
+}
+
+// ---------------------------------------------------------------------------
+// Single-pass exclusive scan with decoupled look-back.
+// ---------------------------------------------------------------------------
+// A tile descriptor holds its kind in the top two bits (0: nothing yet, 1: the
+// tile's own sum, 2: the inclusive prefix through the tile) and the value below.
+constexpr unsigned long long LB_AGG = 1ull << 62, LB_INC = 2ull << 62, LB_VAL = (1ull << 62) - 1;
+constexpr int LB_SPINS = 1 << 20;  // polls of one look-back window before giving up
+
+static unsigned lb_tiles(size_t n) { return (unsigned)std::max<size_t>(1, (n + LB_TILE - 1) / LB_TILE); }
+
+size_t lb_state_words(size_t n) { return 2 * (size_t)lb_tiles(n) + 1; }
+
+__device__ __forceinline__ unsigned long long lb_load(const unsigned long long *p) {
+    return *reinterpret_cast<const volatile unsigned long long *>(p);
+}
+
+__global__ void __launch_bounds__(LB_THREADS) lb_scan_kernel(const __grid_constant__ LBScanArgs a, unsigned ntiles) {
+    __shared__ unsigned s_tile;
+    __shared__ uint32_t s_warp[LB_THREADS / 32];
+    __shared__ unsigned long long s_prefix;
+    __shared__ int s_ok;
+    const int arr = blockIdx.x >= ntiles ? 1 : 0;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    unsigned *tickets = reinterpret_cast<unsigned *>(a.state + 2 * (size_t)ntiles);
+    if (tid == 0) s_tile = atomicAdd(tickets + arr, 1u);
+    __syncthreads();
+    const unsigned tile = s_tile;
+    unsigned long long *desc = a.state + (size_t)arr * ntiles;
+    const size_t n = a.n;
+    const size_t base = (size_t)tile * LB_TILE + (size_t)tid * LB_ITEMS;
+    const uint32_t *in = a.in[arr];
+    uint32_t v[LB_ITEMS];
+    const bool full = base + LB_ITEMS <= n;
+    if (in) {
+        if (full && ((reinterpret_cast<uintptr_t>(in) & 15) == 0)) {
+            const uint4 *q = reinterpret_cast<const uint4 *>(in + base);
+#pragma unroll
+            for (int c = 0; c < LB_ITEMS / 4; c++) {
+                const uint4 x = q[c];
+                v[4 * c] = x.x, v[4 * c + 1] = x.y, v[4 * c + 2] = x.z, v[4 * c + 3] = x.w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < LB_ITEMS; j++) v[j] = base + j < n ? in[base + j] : 0u;
+        }
+    } else {  // flag mode: first occurrences of the hash table's keys
+        uint32_t sl[LB_ITEMS];
+        if (full && ((reinterpret_cast<uintptr_t>(a.slot) & 15) == 0)) {
+            const uint4 *q = reinterpret_cast<const uint4 *>(a.slot + base);
+#pragma unroll
+            for (int c = 0; c < LB_ITEMS / 4; c++) {
+                const uint4 x = q[c];
+                sl[4 * c] = x.x, sl[4 * c + 1] = x.y, sl[4 * c + 2] = x.z, sl[4 * c + 3] = x.w;
+            }
+        } else {
+#pragma unroll
+            for (int j = 0; j < LB_ITEMS; j++) sl[j] = base + j < n ? a.slot[base + j] : 0u;
+        }
+#pragma unroll
+        for (int j = 0; j < LB_ITEMS; j++) v[j] = (base + j < n && a.table[sl[j]] == (uint32_t)(base + j)) ? 1u : 0u;
+    }
+    // block-wide exclusive scan of the thread sums
+    uint32_t tsum = 0;
+#pragma unroll
+    for (int j = 0; j < LB_ITEMS; j++) tsum += v[j];
+    uint32_t x = tsum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    uint32_t wpre = 0, agg = 0;
+#pragma unroll
+    for (int w = 0; w < LB_THREADS / 32; w++) {
+        const uint32_t c = s_warp[w];
+        wpre += w < warp ? c : 0u;
+        agg += c;
+    }
+    const uint32_t texcl = wpre + x - tsum;
+    // the tile's prefix: publish the own sum, then look back (warp 0)
+    if (warp == 0) {
+        unsigned long long prefix = 0;
+        int ok = 1;
+        if (tile == 0) {
+            if (lane == 0) atomicExch(desc, LB_INC | (unsigned long long)agg);
+        } else {
+            if (lane == 0) atomicExch(desc + tile, LB_AGG | (unsigned long long)agg);
+            long long pred = (long long)tile - 1;
+            int spins = 0;
+            for (;;) {
+                const long long idx = pred - lane;
+                const unsigned long long d = idx >= 0 ? lb_load(desc + idx) : LB_INC;
+                if (__all_sync(0xffffffffu, (d >> 62) != 0)) {
+                    const unsigned inc = __ballot_sync(0xffffffffu, (d >> 62) == 2);
+                    const int stop = inc ? __ffs(inc) - 1 : 31;
+                    unsigned long long val = lane <= stop ? (d & LB_VAL) : 0ull;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) val += __shfl_xor_sync(0xffffffffu, val, o);
+                    prefix += val;
+                    if (inc) break;
+                    pred -= 32;
+                    spins = 0;
+                    continue;
+                }
+                if (++spins > LB_SPINS) {
+                    ok = 0;
+                    break;
+                }
+                if (spins > 32) __nanosleep(64);
+            }
+            if (lane == 0 && ok) atomicExch(desc + tile, LB_INC | ((prefix + agg) & LB_VAL));
+        }
+        if (lane == 0) {
+            s_prefix = prefix;
+            s_ok = ok;
+        }
+    }
+    __syncthreads();
+    if (!s_ok) {
+        if (tid == 0) dcrf_set_error(a.st, DCRF_ERR_TIMEOUT, (int)tile);
+        return;
+    }
+    const unsigned long long prefix = s_prefix;
+    uint32_t run = (uint32_t)prefix + texcl;
+    uint32_t *out = a.out[arr];
+    if (full && ((reinterpret_cast<uintptr_t>(out) & 15) == 0)) {
+        uint32_t o[LB_ITEMS];
+#pragma unroll
+        for (int j = 0; j < LB_ITEMS; j++) {
+            o[j] = run;
+            run += v[j];
+        }
+        uint4 *q = reinterpret_cast<uint4 *>(out + base);
+#pragma unroll
+        for (int c = 0; c < LB_ITEMS / 4; c++) q[c] = make_uint4(o[4 * c], o[4 * c + 1], o[4 * c + 2], o[4 * c + 3]);
+    } else {
+#pragma unroll
+        for (int j = 0; j < LB_ITEMS; j++) {
+            if (base + j < n) out[base + j] = run;
+            run += v[j];
+        }
+    }
+    if (tile == ntiles - 1 && tid == 0) {
+        const uint32_t total = (uint32_t)(prefix + agg);
+        if (a.total[arr][0]) *a.total[arr][0] = total;
+        if (a.total[arr][1]) *a.total[arr][1] = total;
+    }
+}
+
+cudaError_t lb_scan(const LBScanArgs &a, cudaStream_t s) {
+    if (a.narr < 1 || a.narr > 2 || !a.state || (!a.in[0] && (!a.table || !a.slot || a.narr != 1)))
+        return cudaErrorInvalidValue;
+    const unsigned nt = lb_tiles(a.n);
+    DCRF_LAUNCH(lb_scan_kernel<<<nt * (unsigned)a.narr, LB_THREADS, 0, s>>>(a, nt));
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

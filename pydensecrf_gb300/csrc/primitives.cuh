@@ -4,7 +4,56 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include "dcrf_common.cuh"
+
 namespace dcrf {
+
+// ---- single-pass exclusive scan (decoupled look-back) ----------------------
+// One launch scans up to two u32 arrays of the same length: each CTA takes
+// tiles in ticket order (an atomic counter, so that every tile it waits on
+// belongs to a CTA that is already running), scans its tile, publishes the
+// tile's sum, and looks back over its predecessors' published sums and
+// prefixes.  The look-back wait is bounded: a CTA that gives up records
+// DCRF_ERR_TIMEOUT in `st` and leaves its outputs unwritten.
+constexpr int LB_THREADS = 256, LB_ITEMS = 16, LB_TILE = LB_THREADS * LB_ITEMS;
+
+struct LBScanArgs {
+    int narr = 1;             // arrays in this launch (1 or 2)
+    size_t n = 0;             // items per array
+    const uint32_t *in[2] = {nullptr, nullptr};
+    uint32_t *out[2] = {nullptr, nullptr};        // exclusive prefix sums (in place allowed)
+    uint32_t *total[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};  // the sum, to each non-null place
+    // flag mode (in[0] == null): item k of array 0 is 1 when table[slot[k]] == k
+    const uint32_t *table = nullptr, *slot = nullptr;
+    unsigned long long *state = nullptr;  // lb_state_words(n) words, zero before the launch
+    DevStatus *st = nullptr;
+};
+
+// 64-bit words of tile state a launch over n items per array needs (tile
+// descriptors of both arrays plus the two tickets); they must be zero when the
+// launch starts (a preceding kernel clears them, see ClearList).
+size_t lb_state_words(size_t n);
+cudaError_t lb_scan(const LBScanArgs &a, cudaStream_t s);
+
+// Ranges of 32-bit words that a kernel sets (grid-stride) before later kernels
+// of the same stream use them: hash tables, scan states, counters.
+struct ClearList {
+    int n = 0;
+    uint32_t *p[6];
+    size_t words[6];
+    uint32_t val[6];
+    void add(void *ptr, size_t nwords, uint32_t v) {
+        p[n] = static_cast<uint32_t *>(ptr);
+        words[n] = nwords;
+        val[n] = v;
+        n++;
+    }
+};
+
+__device__ __forceinline__ void clear_words(const ClearList &c, size_t tid, size_t stride) {
+    for (int j = 0; j < c.n; j++)
+        for (size_t w = tid; w < c.words[j]; w += stride) c.p[j][w] = c.val[j];
+}
 
 // Workspace (in 32-bit words) needed by scan_exclusive_u32 for n elements.
 size_t scan_temp_words(size_t n);
