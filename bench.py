@@ -694,6 +694,9 @@ def run_gpu(args):
     # lists (uint16 point + float weight), partial rows written; plus the slot map.
     pp_bytes = N * M * 4 + N * 4 + sum(N * (d + 1) * 8 + N * 4 + L * MP * 4 + N * (d + 1) * 6 + P * MP * 4
                                        for d, L, P in zip(d_terms, Ls, Ps))
+    # the lattice builds (Permutohedral::init + the kernel normalisation): algorithmic bytes
+    # per term N*d*4 (features) + N*(d+1)*8 (offsets + weights) + L*d*2 (keys) + (d+1)*L*8 (neighbours)
+    build_bytes = sum(N * d * 4 + N * (d + 1) * 8 + L * d * 2 + (d + 1) * L * 8 for d, L in zip(d_terms, Ls))
     peak, peak_kind = measured_peak()
     if args.traffic is not None:
         traffic, traffic_src = args.traffic, "--traffic argument"
@@ -705,6 +708,11 @@ def run_gpu(args):
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 3), "traffic": traffic, "traffic_source": traffic_src,
                 "algorithmic_bytes_per_launch": int(pp_bytes), "avg_launch_us": round(prof["point"]["avg_us"], 2),
                 "peak_kind": peak_kind}
+    lat_s = prof["lattice"]["ms_per_step"] / 1e3
+    lattice_roofline = {"bound": "latency (dependent launches, one host wait per term)",
+                        "algorithmic_bytes_per_step": int(build_bytes), "ms_per_step": round(1e3 * lat_s, 4),
+                        "achieved": round(build_bytes / lat_s / 1e9, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(build_bytes / lat_s / 1e9 / peak, 4)}
 
     # ---- end to end through the public Python API, pinned host buffers
     U_h = torch.from_numpy(cfg["U"]).pin_memory().numpy()
@@ -784,6 +792,7 @@ def run_gpu(args):
             "lattice": {"L": Ls, "partials": Ps},
             "tuning": tuning,
             "roofline": roofline,
+            "lattice_roofline": lattice_roofline,
             "cpu_baseline": cpu,
             "accuracy": accuracy,
             "learning": learning,

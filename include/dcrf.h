@@ -86,7 +86,13 @@ int dcrf_abi_version(void);
 int dcrf_last_error(char *buf, size_t len);
 
 /* DenseCRF(N, M): densecrf.pyx:51-63 -> densecrf.cpp:39-40.
- * Binds the handle to the current CUDA device and creates its own stream. */
+ * Binds the handle to the current CUDA device and creates its own stream.
+ * M may be 1 .. DCRF_MAX_LABELS (4096).  With more than 32 labels the labels
+ * are processed in chunks of 32: inference, start/step, klDivergence, map and
+ * the unary energy work as for any M; the adjoint (dcrf_inference_checkpointed,
+ * dcrf_backward), dcrf_pairwise_energy and the full-width raw filters
+ * (dcrf_lattice_filter / _noalloc with value_size M) return
+ * DCRF_ERR_INVALID_ARG. */
 int dcrf_create(int N, int M, dcrf_crf **out);
 
 /* DenseCRF2D(W, H, M): densecrf.pyx:107-118 -> densecrf.cpp:47-48. */
@@ -252,7 +258,7 @@ int dcrf_launch_count(unsigned long long *count);
 #define DCRF_KCLASS_POINT 0   /* slice + compatibility + softmax + tile splat */
 #define DCRF_KCLASS_REDUCE 1  /* per-vertex sum of the splat partials */
 #define DCRF_KCLASS_BLUR 2    /* one blur axis */
-#define DCRF_KCLASS_LATTICE 3 /* lattice build (all of its launches) */
+#define DCRF_KCLASS_LATTICE 3 /* lattice build and its normalisation (all of their launches) */
 #define DCRF_KCLASS_OTHER 4   /* layout conversions, feature generation */
 #define DCRF_NUM_KCLASSES 5
 

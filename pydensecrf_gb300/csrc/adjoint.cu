@@ -295,12 +295,12 @@ __global__ void onehot_kernel(const int16_t *__restrict__ labels, int M, int ld,
 // energy[pt] (+)= scale * x[slot of pt][label of pt] for 0 <= label < M, else
 // (+)= 0 (densecrf.cpp:146-150, 169-174)
 __global__ void label_energy_kernel(const float *__restrict__ x, const int16_t *__restrict__ labels, int M, int ld,
-                                    int N, const int *__restrict__ pt_slot, float scale, int accumulate,
+                                    int ns, int N, const int *__restrict__ pt_slot, float scale, int accumulate,
                                     float *__restrict__ energy) {
     const int pt = blockIdx.x * blockDim.x + threadIdx.x;
     if (pt >= N) return;
     const int l = labels[pt];
-    const float v = (x && l >= 0 && l < M) ? scale * x[(size_t)pt_slot[pt] * ld + l] : 0.f;
+    const float v = (x && l >= 0 && l < M) ? scale * x[chunk_offset((size_t)ns, ld, (size_t)pt_slot[pt], l)] : 0.f;
     energy[pt] = accumulate ? energy[pt] + v : v;
 }
 
@@ -525,9 +525,9 @@ cudaError_t launch_onehot(const int16_t *labels, int M, int ns, const int *slot_
     return cudaGetLastError();
 }
 
-cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int N, const int *pt_slot, float scale,
-                                int accumulate, float *energy, cudaStream_t s) {
-    DCRF_LAUNCH(label_energy_kernel<<<blocks(N), 256, 0, s>>>(x, labels, M, pad_labels(M), N, pt_slot, scale,
+cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int ns, int N, const int *pt_slot,
+                                float scale, int accumulate, float *energy, cudaStream_t s) {
+    DCRF_LAUNCH(label_energy_kernel<<<blocks(N), 256, 0, s>>>(x, labels, M, pad_labels(M), ns, N, pt_slot, scale,
                                                                accumulate, energy));
     return cudaGetLastError();
 }

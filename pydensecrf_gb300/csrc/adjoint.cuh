@@ -39,8 +39,8 @@ cudaError_t launch_norm_terms(const float *b, const float *y, const float *F, co
                               float *x1, cudaStream_t s);
 // one-hot slot rows of a point-order labelling; per-point energy from slot rows
 cudaError_t launch_onehot(const int16_t *labels, int M, int ns, const int *slot_pt, float *out, cudaStream_t s);
-cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int N, const int *pt_slot, float scale,
-                                int accumulate, float *energy, cudaStream_t s);
+cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int ns, int N, const int *pt_slot,
+                                float scale, int accumulate, float *energy, cudaStream_t s);
 int label_products_blocks(int ns);
 // mode 0: out[m] (+)= sum a[m].*b[m]; mode 1: out[m*M+k] (+)= sum a[m].*b[k]; part: [blocks][K] doubles
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,

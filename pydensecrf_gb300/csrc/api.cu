@@ -218,6 +218,8 @@ struct dcrf_crf {
     size_t cky_cap = 0;
     std::vector<long long> cky_off;  // per term, -1: not kept
     std::vector<size_t> ckv_off, ckv_layout;
+    float *wideF = nullptr;  // more than 32 labels: the Matrix terms' sliced messages (WideArgs::F)
+    size_t wideF_cap = 0;
     float *bw[14] = {};     // adjoint work buffers, [nslots][MP] each
     float *bw1[2] = {};     // adjoint work buffers, [nslots] each
     unsigned *bar = nullptr;  // grid-barrier state of the single-launch blur
@@ -236,6 +238,7 @@ struct dcrf_crf {
     cudaGraphExec_t gexec = nullptr;
     // profiling: events bracketing launches, by kernel class
     bool profiling = false;
+    int prof_class = -1;  // >= 0: every launch is counted in this kernel class (the normalisation: lattice)
     struct Mark {
         int cls;
         cudaEvent_t a, b;
@@ -262,7 +265,7 @@ struct ProfScope {
     dcrf_crf *h;
     int cls;
     cudaEvent_t a = nullptr;
-    ProfScope(dcrf_crf *h_, int c) : h(h_), cls(c) {
+    ProfScope(dcrf_crf *h_, int c) : h(h_), cls(h_->prof_class >= 0 ? h_->prof_class : c) {
         if (h->profiling) {
             a = take_event(h);
             cudaEventRecord(a, h->stream);
@@ -414,9 +417,9 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
     if (total > 0x7FFFFFF0LL) return set_err(DCRF_ERR_INVALID_ARG, "too many points (more than 2^31)");
     const int N = (int)total;
     if (M <= 0) return set_err(DCRF_ERR_INVALID_ARG, "N and M must be positive");
-    if (M > DCRF_MAX_MP)
-        return set_err(DCRF_ERR_INVALID_ARG, "at most " + std::to_string(DCRF_MAX_MP) + " labels are supported, got " +
-                                                 std::to_string(M));
+    if (M > DCRF_MAX_LABELS)
+        return set_err(DCRF_ERR_INVALID_ARG, "at most " + std::to_string(DCRF_MAX_LABELS) +
+                                                 " labels are supported, got " + std::to_string(M));
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
         cudaGetLastError();
@@ -472,10 +475,11 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
 }
 
 // Copies an M x N quantity from the caller (label- or point-major, host or
-// device) into device slot rows dst [nslots][ld] (ld = MP, or 1 for M = 1).
+// device) into device slot rows dst [nslots][ld] (ld = MP, or 1 for M = 1),
+// label chunk by label chunk when M > 32 (chunk_offset layout).
 int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst, int M = -1) {
     if (M < 0) M = h->M;
-    const int ld = M == h->M ? h->MP : M;
+    const bool full = M == h->M;
     if (layout != DCRF_LAYOUT_LM && layout != DCRF_LAYOUT_PM) return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
     const float *dsrc = src;
     if (where != DCRF_DEVICE) {
@@ -483,31 +487,42 @@ int load_mn(dcrf_crf *h, const float *src, int layout, int where, float *dst, in
         dsrc = h->stage;
     }
     ProfScope ps(h, DCRF_KCLASS_OTHER);
-    CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, M, ld, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt,
-                       h->nslots, dst, h->stream));
+    const int nc = full ? label_chunks(h->MP) : 1;
+    for (int c = 0; c < nc; c++) {
+        const int w = full ? chunk_width(h->MP, c) : M, m0 = DCRF_LCHUNK * c;
+        CU(launch_to_slots(dsrc, layout == DCRF_LAYOUT_PM, std::min(w, M - m0), M, m0, w, h->N, h->d_seg,
+                           (int)h->seg.size() - 1, h->slot_pt, h->nslots, dst + chunk_base(h->nslots, c), h->stream));
+    }
     return DCRF_OK;
 }
 
 // Copies the slot rows src [nslots][ld] out to the caller's layout.
 int store_mn(dcrf_crf *h, const float *src, float *dst, int layout, int where, int M = -1) {
     if (M < 0) M = h->M;
-    const int ld = M == h->M ? h->MP : M;
+    const bool full = M == h->M;
     if (layout != DCRF_LAYOUT_LM && layout != DCRF_LAYOUT_PM) return set_err(DCRF_ERR_INVALID_ARG, "unknown layout");
     float *ddst = where == DCRF_DEVICE ? dst : h->stage;
     {
         ProfScope ps(h, DCRF_KCLASS_OTHER);
-        CU(launch_from_slots(src, M, ld, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, h->pt_slot,
-                             layout == DCRF_LAYOUT_PM, ddst, h->stream));
+        const int nc = full ? label_chunks(h->MP) : 1;
+        for (int c = 0; c < nc; c++) {
+            const int w = full ? chunk_width(h->MP, c) : M, m0 = DCRF_LCHUNK * c;
+            CU(launch_from_slots(src + chunk_base(h->nslots, c), std::min(w, M - m0), M, m0, w, h->N, h->d_seg,
+                                 (int)h->seg.size() - 1, h->slot_pt, h->nslots, h->pt_slot, layout == DCRF_LAYOUT_PM,
+                                 ddst, h->stream));
+        }
     }
     if (where != DCRF_DEVICE)
         CU(cudaMemcpyAsync(dst, h->stage, sizeof(float) * (size_t)h->N * M, cudaMemcpyDeviceToHost, h->stream));
     return DCRF_OK;
 }
 
-// Value-size-1 rows live MP floats into the term's lattice buffers: their
-// zero row 0 is element MP (cleared at the build), and the stride-MP sentinel
-// row 0 stays untouched.
-float *v1_buffer(const dcrf_crf *h, float *V) { return h->MP > 1 ? V + h->MP : V; }
+// Value-size-1 rows live in the last L+1 floats of the term's lattice
+// buffers (lattice_v1_offset): clear of every label chunk's zero row 0, their
+// own zero row 0 cleared at the build.
+float *v1_buffer(const dcrf_crf *h, const Term &T, float *V) {
+    return V + lattice_v1_offset((size_t)T.lat.L, h->MP);
+}
 
 // Descriptor of a term for the forward filter (or its transpose).
 TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
@@ -526,7 +541,7 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.off = T.lat.off;
     t.bary = T.lat.bary;
     t.wslice = T.lat.wslice;
-    t.V = value1 ? v1_buffer(h, T.V[(T.d + 1) & 1]) : T.V[(T.d + 1) & 1];
+    t.V = value1 ? v1_buffer(h, T, T.V[(T.d + 1) & 1]) : T.V[(T.d + 1) & 1];
     t.tile_pbeg = T.lat.tile_pbeg;
     t.part_mend = T.lat.part_mend;
     t.mem_pt = T.lat.mem_pt;
@@ -649,36 +664,48 @@ cudaError_t pp(dcrf_crf *h, const PPArgs &a, int MP) {
 // rows of 8k floats without a Matrix compatibility (measured: two threads win
 // for Potts/Diagonal, one for Matrix, whose products then need the partner's
 // labels).
-int pick_split(const dcrf_crf *h, bool value1) {
-    if (value1 || h->MP % 8 != 0) return 1;
+int pick_split(const dcrf_crf *h, bool value1, int MP) {
+    if (value1 || MP % 8 != 0) return 1;
     if (h->tune.split == 1 || h->tune.split == 2) return h->tune.split;
     for (const Term &T : h->terms)
         if (T.ckind == DCRF_COMPAT_MATRIX) return 1;
     return 2;
 }
 
-PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transpose, bool value1) {
+// Point-pass arguments for the listed terms; `chunk` >= 0 selects one label
+// chunk of a handle with more than 32 labels (its rows, its lattice rows).
+PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transpose, bool value1, int chunk = -1) {
+    const int c = chunk < 0 || value1 ? 0 : chunk;
+    const int MPc = value1 ? 1 : chunk_width(h->MP, c);
+    const size_t so = chunk_base(h->nslots, c);
     PPArgs a{};
     a.N = h->N;
-    a.M = value1 ? 1 : h->M;
+    a.M = value1 ? 1 : std::min(MPc, h->M - DCRF_LCHUNK * c);
     a.mode = mode;
     a.ntiles = h->ntiles;
     a.nslots = h->nslots;
     a.slot_pt = h->slot_pt;
-    a.U = h->has_unary ? h->U : nullptr;
-    a.Qin = h->Q;
-    a.Qout = h->Q;
+    a.U = h->has_unary ? h->U + so : nullptr;
+    a.Qin = h->Q + so;
+    a.Qout = h->Q + so;
     a.map_out = h->map;
     a.kl_part = h->kl_part;
     a.status = h->status;
     a.ts.n = (int)which.size();
     for (size_t k = 0; k < which.size(); k++) {
-        a.ts.t[k] = term_dev(h, h->terms[which[k]], transpose, value1);
-        a.ntype[k] = h->terms[which[k]].ntype;
-        a.norm_out[k] = h->terms[which[k]].norm;
+        const Term &T = h->terms[which[k]];
+        TermDev &t = a.ts.t[k];
+        t = term_dev(h, T, transpose, value1);
+        if (c > 0) {
+            t.pv += chunk_base((size_t)T.lat.P + 1, c);
+            t.pout += chunk_base((size_t)T.lat.P + 1, c);
+            t.V += chunk_base((size_t)T.lat.L + 1, c);
+        }
+        a.ntype[k] = T.ntype;
+        a.norm_out[k] = T.norm;
     }
-    a.split = pick_split(h, value1);
-    plan_smem(h, a, which, (mode & PP_MSG) != 0, value1 ? 1 : h->MP);
+    a.split = pick_split(h, value1, MPc);
+    plan_smem(h, a, which, (mode & PP_MSG) != 0, MPc);
     return a;
 }
 
@@ -693,10 +720,15 @@ std::vector<int> all_terms(dcrf_crf *h) {
 // input of the mean-field point pass) instead of vertex order (V, input of the
 // point-order slice).
 int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, bool value1, bool partial_order,
-                 float *const *S_out = nullptr, float *const *B_out = nullptr) {
-    int MP = value1 ? 1 : h->MP;
+                 float *const *S_out = nullptr, float *const *B_out = nullptr, int chunk = 0) {
+    const int ch = value1 ? 0 : chunk;
+    int MP = value1 ? 1 : chunk_width(h->MP, ch);
     bool seq = value1 || h->M <= 2;
-    auto Vb = [&](const Term &T, int j) { return value1 ? v1_buffer(h, T.V[j]) : T.V[j]; };
+    // lattice rows of label chunk ch (the whole rows when MP <= 32)
+    auto Vb = [&](const Term &T, int j) {
+        return value1 ? v1_buffer(h, T, T.V[j]) : T.V[j] + chunk_base((size_t)T.lat.L + 1, ch);
+    };
+    auto Pb = [&](const Term &T, float *p) { return p + (value1 ? 0 : chunk_base((size_t)T.lat.P + 1, ch)); };
     // Blur launches per term: passes 2i and 2i+1 share launch i (the last pass
     // alone when d+1 is odd).  Buffers are planned backwards from the final
     // output, alternating the term's two lattice buffers launch by launch, so
@@ -720,7 +752,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
         c.x[c.n - 1] = c.fin == Vb(T, 0) ? Vb(T, 1) : Vb(T, 0);
         for (int i = c.n - 2; i >= 0; i--) c.x[i] = c.x[i + 1] == Vb(T, 0) ? Vb(T, 1) : Vb(T, 0);
         float *red_out = S_out ? S_out[k] : h->tune.coop ? Vb(T, 0) : c.x[0];
-        ra.t[k] = {T.lat.red_beg, T.pout, red_out, T.lat.L, T.lat.P};
+        ra.t[k] = {T.lat.red_beg, Pb(T, T.pout), red_out, T.lat.L, T.lat.P};
         maxd = std::max(maxd, T.d);
         if (T.variant == DCRF_VARIANT_SCALAR) seq = true;
     }
@@ -748,7 +780,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
             c.reverse = transpose ? 1 : 0;
             c.red_beg = T.lat.red_beg;
             c.red_list = T.lat.red_list;
-            c.pv = partial_order ? T.pv : nullptr;
+            c.pv = partial_order ? Pb(T, T.pv) : nullptr;
         }
         ProfScope ps(h, DCRF_KCLASS_BLUR);
         CU(launch_blur_chains(ca, MP, seq, h->stream));
@@ -774,7 +806,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
             bt.axis2 = p + 1 > T.d ? -1 : transpose ? T.d - (p + 1) : p + 1;
             bt.red_beg = T.lat.red_beg;
             bt.red_list = T.lat.red_list;
-            bt.pv = (last && partial_order) ? T.pv : nullptr;
+            bt.pv = (last && partial_order) ? Pb(T, T.pv) : nullptr;
             ba.begin[ba.n + 1] = ba.begin[ba.n] + (long long)T.lat.L * NV;
             ba.n++;
         }
@@ -790,9 +822,7 @@ int filter_phase(dcrf_crf *h, const std::vector<int> &which, bool transpose, boo
 // buffers at stride 1, which overwrites entries that the stride-MP passes read
 // as the zero sentinel row (row 0).  Restore it afterwards.
 int zero_sentinels(dcrf_crf *h, Term &T) {
-    const size_t n = h->MP > 1 ? (size_t)h->MP + 1 : 1;  // row 0 and the value-size-1 row 0 (v1_buffer)
-    CU(cudaMemsetAsync(T.V[0], 0, sizeof(float) * n, h->stream));
-    CU(cudaMemsetAsync(T.V[1], 0, sizeof(float) * n, h->stream));
+    CU(launch_lattice_zero_rows(T.V[0], T.V[1], (size_t)T.lat.L, h->MP, h->stream));
     return DCRF_OK;
 }
 
@@ -934,6 +964,12 @@ int flush_norms(dcrf_crf *h) {
         if (h->terms[k].norm_pending) which.push_back((int)k);
     if (which.empty()) return DCRF_OK;
     for (int k : which) h->terms[k].norm_pending = false;
+    // profiled as part of the lattice build (DenseKernel::initLattice)
+    struct ForceClass {
+        dcrf_crf *h;
+        ~ForceClass() { h->prof_class = -1; }
+    } force{h};
+    h->prof_class = DCRF_KCLASS_LATTICE;
     PPArgs a = pp_args(h, PP_ONES | PP_SPLAT, which, false, true);
     for (size_t q = 0; q < which.size(); q++) a.ts.t[q].pre_norm = a.ts.t[q].post_norm = 0;
     CU(pp(h, a, 1));
@@ -942,7 +978,7 @@ int flush_norms(dcrf_crf *h) {
     a = pp_args(h, PP_NORM, which, false, true);
     for (size_t q = 0; q < which.size(); q++) {
         Term &T = h->terms[which[q]];
-        a.ts.t[q].V = v1_buffer(h, T.V[(T.d + 1) & 1]);
+        a.ts.t[q].V = v1_buffer(h, T, T.V[(T.d + 1) & 1]);
         const bool fold = T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_BEFORE;
         a.wn_out[q] = fold ? T.mem_wn : nullptr;
     }
@@ -1003,9 +1039,93 @@ int validate_kn(int ktype, int ntype) {
     return DCRF_OK;
 }
 
+// ---- more than 32 labels --------------------------------------------------------
+// The labels are processed in chunks of 32 (chunk_offset layout): the splat,
+// reduce and blur are linear per label and run chunk by chunk through the same
+// kernels as narrower handles; the messages, compatibilities and the softmax,
+// which mix labels, run in wide_kernel.
+bool is_wide(const dcrf_crf *h) { return h->MP > DCRF_MAX_MP; }
+
+int wide_unsupported(const char *what) {
+    return set_err(DCRF_ERR_INVALID_ARG, std::string(what) + " supports at most " + std::to_string(DCRF_MAX_MP) +
+                                             " labels");
+}
+
+WideArgs wide_args(dcrf_crf *h, int mode, const std::vector<int> &w) {
+    WideArgs a{};
+    a.N = h->N;
+    a.M = h->M;
+    a.MP = h->MP;
+    a.mode = mode;
+    a.ntiles = h->ntiles;
+    a.nslots = h->nslots;
+    a.slot_pt = h->slot_pt;
+    a.U = h->has_unary ? h->U : nullptr;
+    a.Qin = h->Q;
+    a.Qout = h->Q;
+    a.F = h->wideF;
+    a.map_out = h->map;
+    a.kl_part = h->kl_part;
+    a.ts.n = (int)w.size();
+    for (size_t k = 0; k < w.size(); k++) {
+        const Term &T = h->terms[w[k]];
+        a.ts.t[k] = term_dev(h, T, false, false);
+        a.pv_chunk[k] = (long long)chunk_base((size_t)T.lat.P + 1, 1);
+    }
+    return a;
+}
+
+// The Matrix terms' message rows of wide_kernel (allocated outside any graph capture).
+int ensure_wide_bufs(dcrf_crf *h) {
+    if (!is_wide(h)) return DCRF_OK;
+    size_t nmat = 0;
+    for (const Term &T : h->terms) nmat += T.ckind == DCRF_COMPAT_MATRIX ? 1 : 0;
+    const size_t need = nmat * (size_t)h->nslots * h->MP;
+    if (need > h->wideF_cap) {
+        dev_free_async(h->wideF, h->stream);
+        h->wideF = nullptr;
+        h->wideF_cap = 0;
+        int rc = dev_alloc_async(&h->wideF, need, h->stream);
+        if (rc) return rc;
+        h->wideF_cap = need;
+    }
+    return DCRF_OK;
+}
+
+int wide(dcrf_crf *h, int mode, const std::vector<int> &w) {
+    ProfScope ps(h, DCRF_KCLASS_POINT);
+    CU(launch_wide(wide_args(h, mode, w), h->stream));
+    return DCRF_OK;
+}
+
+// splat h->Q into every term's lattice and filter it, label chunk by chunk
+int wide_splat_filter(dcrf_crf *h, const std::vector<int> &w) {
+    const int nc = label_chunks(h->MP);
+    for (int c = 0; c < nc; c++) CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false, c), chunk_width(h->MP, c)));
+    for (int c = 0; c < nc; c++) {
+        int rc = filter_phase(h, w, false, false, true, nullptr, nullptr, c);
+        if (rc) return rc;
+    }
+    return DCRF_OK;
+}
+
+int issue_inference_wide(dcrf_crf *h, int T, int final_mode) {
+    std::vector<int> w = all_terms(h);
+    const int fin = (final_mode & PP_MAP) ? WP_MAP : WP_WRITE_Q;
+    if (T <= 0 || w.empty()) return wide(h, fin, w);
+    int rc;
+    if ((rc = wide(h, WP_WRITE_Q, w))) return rc;  // Q_0 = softmax(-U)
+    for (int it = 1; it <= T; it++) {
+        if ((rc = wide_splat_filter(h, w))) return rc;
+        if ((rc = wide(h, WP_MSG | (it < T ? WP_WRITE_Q : fin), w))) return rc;
+    }
+    return DCRF_OK;
+}
+
 // Launch sequence of T mean-field iterations starting from softmax(-U); the
 // final pass writes per final_mode (Q into h->Q, or the MAP labels).
 int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
+    if (is_wide(h)) return issue_inference_wide(h, T, final_mode);
     std::vector<int> w = all_terms(h);
     const size_t qsz = (size_t)h->MP * h->nslots;
     int rc;
@@ -1083,6 +1203,7 @@ int rebuild_terms(dcrf_crf *h) {
 // Device time of n mean-field iterations (min of reps), launched directly.
 int time_iterations(dcrf_crf *h, int n, int reps, float *ms_out) {
     int frc = flush_norms(h);
+    if (!frc) frc = ensure_wide_bufs(h);
     if (frc) return frc;
     cudaEvent_t a = take_event(h), b = take_event(h);
     float best = 1e30f;
@@ -1197,6 +1318,7 @@ int maybe_autotune(dcrf_crf *h) {
 int run_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
     int trc = maybe_autotune(h);
     if (!trc) trc = flush_norms(h);  // (re)built by the tuner: normalised before any capture
+    if (!trc) trc = ensure_wide_bufs(h);
     if (trc) return trc;
     if (h->profiling || !h->use_graphs || h->inference_runs++ == 0) return issue_inference(h, T, final_mode, ckpt);
     cudaStream_t user = h->stream;
@@ -1537,6 +1659,7 @@ int dcrf_destroy(dcrf_crf *h) {
     for (float *&b : h->bw1) dev_free_async(b, h->stream);
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
+    dev_free_async(h->wideF, h->stream);
     for (void *p : {(void *)h->status, (void *)h->bar, (void *)h->U, (void *)h->Q, (void *)h->tmp,
                     (void *)h->stage, (void *)h->map, (void *)h->kl_part, (void *)h->d_seg, (void *)h->d_imgW})
         dev_free_async(p, h->stream);
@@ -1685,6 +1808,8 @@ int dcrf_start_inference(dcrf_crf *h, float *Q, int layout, int where) {
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null output");
     if (!h->has_unary) {  // densecrf.cpp:179-184: zeros without a unary
         CU(cudaMemsetAsync(h->Q, 0, sizeof(float) * (size_t)h->nslots * h->MP, h->stream));
+    } else if (is_wide(h)) {
+        if ((rc = wide(h, WP_WRITE_Q, {}))) return rc;
     } else {
         CU(pp(h, pp_args(h, PP_WRITE_Q, {}, false, false), h->MP));
     }
@@ -1699,11 +1824,17 @@ int dcrf_step_inference(dcrf_crf *h, float *Q, int layout, int where) {
     if (!Q) return set_err(DCRF_ERR_INVALID_ARG, "null marginals");
     if ((rc = load_mn(h, Q, layout, where, h->Q))) return rc;
     std::vector<int> w = all_terms(h);
-    if (!w.empty()) {
-        CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
-        if ((rc = filter_phase(h, w, false, false, true))) return rc;
+    if (is_wide(h)) {
+        if ((rc = ensure_wide_bufs(h))) return rc;
+        if (!w.empty() && (rc = wide_splat_filter(h, w))) return rc;
+        if ((rc = wide(h, (w.empty() ? 0 : WP_MSG) | WP_WRITE_Q, w))) return rc;
+    } else {
+        if (!w.empty()) {
+            CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
+            if ((rc = filter_phase(h, w, false, false, true))) return rc;
+        }
+        CU(pp(h, pp_args(h, PP_MSG | PP_WRITE_Q, w, false, false), h->MP));
     }
-    CU(pp(h, pp_args(h, PP_MSG | PP_WRITE_Q, w, false, false), h->MP));
     if ((rc = store_mn(h, h->Q, Q, layout, where))) return rc;
     if ((rc = sync_check(h))) return rc;
     return ok();
@@ -1715,11 +1846,17 @@ int dcrf_kl_divergence(dcrf_crf *h, const float *Q, int layout, int where, doubl
     if (!Q || !kl_out) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     if ((rc = load_mn(h, Q, layout, where, h->Q))) return rc;
     std::vector<int> w = all_terms(h);
-    if (!w.empty()) {
-        CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
-        if ((rc = filter_phase(h, w, false, false, true))) return rc;
+    if (is_wide(h)) {
+        if ((rc = ensure_wide_bufs(h))) return rc;
+        if (!w.empty() && (rc = wide_splat_filter(h, w))) return rc;
+        if ((rc = wide(h, WP_LOAD_Q | WP_KL | (w.empty() ? 0 : WP_MSG), w))) return rc;
+    } else {
+        if (!w.empty()) {
+            CU(pp(h, pp_args(h, PP_LOAD_Q | PP_SPLAT, w, false, false), h->MP));
+            if ((rc = filter_phase(h, w, false, false, true))) return rc;
+        }
+        CU(pp(h, pp_args(h, PP_LOAD_Q | PP_MSG | PP_KL, w, false, false), h->MP));
     }
-    CU(pp(h, pp_args(h, PP_LOAD_Q | PP_MSG | PP_KL, w, false, false), h->MP));
     std::vector<double> part(h->ntiles);
     CU(cudaMemcpyAsync(part.data(), h->kl_part, sizeof(double) * h->ntiles, cudaMemcpyDeviceToHost, h->stream));
     if ((rc = sync_check(h))) return rc;
@@ -1763,7 +1900,8 @@ int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *ener
     float *e = nullptr;
     if ((rc = load_labels(h, labels, where, &lab))) return rc;
     if ((rc = dev_alloc_async(&e, (size_t)h->N, h->stream))) return rc;
-    CU(launch_label_energy(h->has_unary ? h->U : nullptr, lab, h->M, h->N, h->pt_slot, 1.f, 0, e, h->stream));
+    CU(launch_label_energy(h->has_unary ? h->U : nullptr, lab, h->M, h->nslots, h->N, h->pt_slot, 1.f, 0, e,
+                           h->stream));
     rc = store_energy(h, e, energy, where_out);
     dev_free_async(lab, h->stream);
     dev_free_async(e, h->stream);
@@ -1775,6 +1913,7 @@ int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *ener
 int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term, float *energy, int where_out) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (is_wide(h)) return wide_unsupported("dcrf_pairwise_energy");
     if (!labels || !energy) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     if (term < -1 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
     const int M = h->M, ns = h->nslots;
@@ -1803,7 +1942,7 @@ int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term
         if ((rc = slice_from(h, k, Tk.bv[1], nullptr, false, fwd_post(Tk), nullptr, g))) return rc;
     }
     // r = -0.5 * message at the point's own label (densecrf.cpp:169-174)
-    CU(launch_label_energy(g, lab, M, h->N, h->pt_slot, -0.5f, 0, e, h->stream));
+    CU(launch_label_energy(g, lab, M, ns, h->N, h->pt_slot, -0.5f, 0, e, h->stream));
     rc = store_energy(h, e, energy, where_out);
     dev_free_async(lab, h->stream);
     dev_free_async(e, h->stream);
@@ -1896,6 +2035,7 @@ int dcrf_term_norm(dcrf_crf *h, int term, float *norm) {
 int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (is_wide(h) && value_size != 1) return wide_unsupported("dcrf_lattice_filter with value_size M");
     if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     bool v1 = value_size == 1;
@@ -1956,7 +2096,7 @@ int dcrf_get_tuning(dcrf_crf *h, int *split, int *smem_kb, int *task_len, float 
     int rc = check_handle(h);
     if (rc) return rc;
     if (coop_blur) *coop_blur = h->tune.coop;
-    if (split) *split = pick_split(h, false);
+    if (split) *split = pick_split(h, false, chunk_width(h->MP, 0));
     if (smem_kb) *smem_kb = h->tune.smem_kb > 0 ? h->tune.smem_kb : pointpass_smem_budget(h->MP) / 1024;
     if (task_len) *task_len = h->tune.task;
     if (hash_load) *hash_load = h->tune.hash_load;
@@ -2066,6 +2206,7 @@ int dcrf_param_counts(dcrf_crf *h, int term, int *n_compat, int *n_kernel) {
 int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int layout, int where) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (is_wide(h)) return wide_unsupported("the adjoint (dcrf_inference_checkpointed / dcrf_backward)");
     if (!Q || n_iterations < 0) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     const size_t qsz = (size_t)h->MP * h->nslots, need = qsz * ((size_t)n_iterations + 1);
     if (need > h->ckpt_cap) {
@@ -2128,6 +2269,7 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
 int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU, double *dcompat, double *dkernel) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (is_wide(h)) return wide_unsupported("the adjoint (dcrf_inference_checkpointed / dcrf_backward)");
     if (!dQ) return set_err(DCRF_ERR_INVALID_ARG, "null gradient");
     if (h->ckpt_T < 0 || h->ckpt_version != h->version)
         return set_err(DCRF_ERR_STATE, "dcrf_backward needs a dcrf_inference_checkpointed of the current model");
@@ -2370,6 +2512,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
                                            float *out, void *stream) {
     int rc = check_ready(h);
     if (rc) return rc;
+    if (is_wide(h) && value_size != 1) return wide_unsupported("dcrf_lattice_filter_noalloc with value_size M");
     if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     const bool v1 = value_size == 1;
@@ -2397,7 +2540,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     // the array keeps the previous call's contents: the zero sentinel rows are restored
     CU(cudaMemsetAsync(V0, 0, sizeof(float) * MPv, s));
     CU(cudaMemsetAsync(V1, 0, sizeof(float) * MPv, s));
-    CU(launch_to_slots(in, 0, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, in_s,
+    CU(launch_to_slots(in, 0, value_size, value_size, 0, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, in_s,
                        s));
     std::vector<int> one{term};
     PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
@@ -2431,7 +2574,7 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     f.ts.t[0].V = Vb[(T.d + 1) & 1];
     f.Qout = in_s;
     CU(launch_pointpass(f, MPv, s));
-    CU(launch_from_slots(in_s, value_size, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots,
+    CU(launch_from_slots(in_s, value_size, value_size, 0, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots,
                          h->pt_slot, 0, out, s));
     CU(cudaEventRecord(h->xorder, s));
     CU(cudaStreamWaitEvent(h->stream, h->xorder, 0));

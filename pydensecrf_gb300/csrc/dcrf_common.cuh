@@ -20,7 +20,26 @@
 
 #define DCRF_MAX_TERMS 16
 #define DCRF_MAX_D 16
-#define DCRF_MAX_MP 32  // thread-per-point kernels keep MP labels in registers
+#define DCRF_MAX_MP 32  // labels one thread-per-point kernel keeps in registers (one label chunk)
+#define DCRF_MAX_LABELS 4096  // labels of a handle (label ids are int16 in the MAP output)
+
+// Label chunks.  Quantities with more than DCRF_MAX_MP labels are stored
+// chunk-major: labels [32c, 32c + w_c) of every row form chunk c, a block of
+// rows of w_c floats (w_c = 32 except the last), after the blocks of chunks
+// < c.  With MP <= 32 there is one chunk and this is the plain row layout.
+#define DCRF_LCHUNK 32
+static inline int label_chunks(int MP) { return MP <= DCRF_LCHUNK ? 1 : (MP + DCRF_LCHUNK - 1) / DCRF_LCHUNK; }
+static inline int chunk_width(int MP, int c) {
+    return MP <= DCRF_LCHUNK ? MP : (MP - DCRF_LCHUNK * c < DCRF_LCHUNK ? MP - DCRF_LCHUNK * c : DCRF_LCHUNK);
+}
+// first float of chunk c in a buffer of `rows` rows
+static inline size_t chunk_base(size_t rows, int c) { return (size_t)DCRF_LCHUNK * c * rows; }
+// offset of (row r, label l) in such a buffer
+__host__ __device__ __forceinline__ size_t chunk_offset(size_t rows, int MP, size_t r, int l) {
+    if (MP <= DCRF_LCHUNK) return r * MP + l;
+    const int c = l / DCRF_LCHUNK, w = MP - DCRF_LCHUNK * c < DCRF_LCHUNK ? MP - DCRF_LCHUNK * c : DCRF_LCHUNK;
+    return (size_t)DCRF_LCHUNK * c * rows + r * w + (l - DCRF_LCHUNK * c);
+}
 
 namespace dcrf {
 // Counts every kernel launch of the library (dcrf_launch_count).

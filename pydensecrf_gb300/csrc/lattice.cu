@@ -391,6 +391,25 @@ __global__ void neighbors_kernel(const uint64_t *__restrict__ keys, const uint32
 // counts their members; tile_place, after the tiles' partial and task counts
 // are scanned, lays out the member lists (stable, warp-sequential ranking),
 // the tile-local slice tables and the splat tasks.
+// Sentinel rows of a lattice's two value buffers (lattice_v1_offset, chunk_offset).
+__device__ __forceinline__ void zero_value_rows(float *V0, float *V1, size_t L, int MP, int tid, int nthreads) {
+    const int nc = MP <= DCRF_LCHUNK ? 1 : (MP + DCRF_LCHUNK - 1) / DCRF_LCHUNK;
+    for (int e = tid; e < nc * DCRF_LCHUNK; e += nthreads) {
+        const int c = e / DCRF_LCHUNK, m = e - c * DCRF_LCHUNK;
+        const int w = MP <= DCRF_LCHUNK ? MP : min(DCRF_LCHUNK, MP - DCRF_LCHUNK * c);
+        if (m < w) {
+            const size_t o = (size_t)DCRF_LCHUNK * c * (L + 1) + m;
+            V0[o] = 0.f;
+            V1[o] = 0.f;
+        }
+    }
+    if (tid == 0 && MP > 1) {
+        const size_t o = (L + 1) * (size_t)(MP - 1);
+        V0[o] = 0.f;
+        V1[o] = 0.f;
+    }
+}
+
 constexpr int TG_THREADS = 256;
 
 template <int D>
@@ -548,7 +567,7 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
                                                                uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w,
                                                                uint32_t *__restrict__ task, uint32_t *__restrict__ vcount,
                                                                int L, int P, int T, const __grid_constant__ ClearList clr,
-                                                               DevStatus *st) {
+                                                               float *V0, float *V1, int MP, DevStatus *st) {
     constexpr int C = TG<D>::C, NW = TG_THREADS / 32;
     constexpr int SEG = C / NW;  // corners per warp segment (a multiple of 32)
     extern __shared__ int tp_smem[];
@@ -579,6 +598,7 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
             task[T + tid] = 0;
         }
         clear_words(clr, (size_t)tid, TG_THREADS);
+        zero_value_rows(V0, V1, (size_t)L, MP, tid, TG_THREADS);
     }
     for (int p = p0; p < p1; p++) {
         const int c = pcnt[base + p];
@@ -687,6 +707,15 @@ __global__ void red_rank_kernel(const int *__restrict__ part_v, int P, int L, co
     for (int q = s0; q < s1; q++) rank += __ldg(lst + q) < p ? 1 : 0;
     red_list[s0 + rank] = p;
     ppos[p] = s0 + rank;
+}
+
+__global__ void zero_value_rows_kernel(float *V0, float *V1, size_t L, int MP) {
+    zero_value_rows(V0, V1, L, MP, threadIdx.x, blockDim.x);
+}
+
+cudaError_t launch_lattice_zero_rows(float *V0, float *V1, size_t L, int MP, cudaStream_t s) {
+    DCRF_LAUNCH(zero_value_rows_kernel<<<1, 256, 0, s>>>(V0, V1, L, MP));
+    return cudaGetLastError();
 }
 
 // inv[list[i]] = i for a permutation list of [0, n)
@@ -1002,15 +1031,13 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     }
     if (L.ntiles > 0) {
         // also cleared there: the reduce-list scan's state, and the sentinel rows
-        // (row 0 and element MP) of both value buffers
+        // of both value buffers
         ClearList clr;
         clr.add(st_red, 2 * red_state, 0u);
-        clr.add(L.V0, (size_t)MP + 1, 0u);
-        clr.add(L.V1, (size_t)MP + 1, 0u);
         DCRF_LAUNCH(tile_place_kernel<D><<<L.ntiles, TG_THREADS, smem_p, s>>>(
             cl, pvx, pcnt, L.bary, N, tm.slot_pt, (const uint32_t *)L.tile_pbeg, (const uint32_t *)L.tile_tbeg,
             task_len, L.part_v, L.part_mend, L.mem_pt, L.mem_w, L.tl_loc, L.tl_w, L.task, vcount, L.L, L.P, T, clr,
-            status));
+            L.V0, L.V1, MP, status));
         if ((ce = cudaGetLastError()) != cudaSuccess) {
             red.release();
             return bail(DCRF_ERR_CUDA, std::string("tile placement launch: ") + cudaGetErrorString(ce));

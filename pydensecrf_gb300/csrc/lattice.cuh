@@ -42,9 +42,9 @@ struct LatticeDev {
     uint16_t *tl_loc = nullptr;  // index of the corner's vertex among the tile's partials
     float *tl_w = nullptr;       // the corner's barycentric weight
     // value buffers of the mean-field passes, carved from the lattice's memory
-    // (sizes from the build's MP and slot count): V0, V1 [L+1][MP] (row 0 and
-    // element MP zeroed: the sentinel rows of the stride-MP and value-size-1
-    // passes), pv and pout [P+1][MP], norm [nslots], mem_wn [ntiles][SPLAT_TILE*(d+1)]
+    // (sizes from the build's MP and slot count): V0, V1 [L+1][MP] in label
+    // chunks (sentinel rows zeroed, see launch_lattice_zero_rows), pv and pout
+    // [P+1][MP], norm [nslots], mem_wn [ntiles][SPLAT_TILE*(d+1)]
     float *V0 = nullptr, *V1 = nullptr, *pv = nullptr, *pout = nullptr, *norm = nullptr, *mem_wn = nullptr;
     size_t bytes = 0;
     std::vector<void *> blocks;  // the pool blocks the tables above are carved from
@@ -79,6 +79,15 @@ int lattice_build(const float *feat, int d, int N, const Segments &seg, const Ti
                   int task_len, int MP, int nslots, cudaStream_t s, DevStatus *status, LatticeDev *out);
 
 void lattice_free(LatticeDev *lat, cudaStream_t s);
+
+// The value-size-1 passes of a lattice with MP-label rows (MP > 1) use the
+// last L+1 floats of its value buffers, whose row 0 is their zero sentinel:
+// that region holds no label chunk's row 0.
+inline size_t lattice_v1_offset(size_t L, int MP) { return MP > 1 ? (L + 1) * (size_t)(MP - 1) : 0; }
+
+// Zeroes the sentinel rows of both value buffers: row 0 of every label chunk
+// and the value-size-1 row 0 (one launch).
+cudaError_t launch_lattice_zero_rows(float *V0, float *V1, size_t L, int MP, cudaStream_t s);
 
 // Host-side error text of the last failing build.
 const char *lattice_last_message();

@@ -668,6 +668,227 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
     }
 }
 
+// ---------------------------------------------------------------------------
+// More than 32 labels: the update chunk by chunk (a thread per point)
+// ---------------------------------------------------------------------------
+constexpr int WC = DCRF_LCHUNK;
+
+// acc = slice of term T's blurred partial rows (chunk c, w labels) at the
+// point of slot li of tile t (permutohedral.cpp:574-584 / 513-521)
+__device__ __forceinline__ void wide_slice(const TermDev &T, long long pv_chunk, int t, int li, int c, int w,
+                                           float (&acc)[WC]) {
+#pragma unroll
+    for (int e = 0; e < WC; e++) acc[e] = 0.f;
+    const int pb = T.tile_pbeg[t];
+    const size_t tb = (size_t)t * SPLAT_TILE * (T.d + 1);
+    const float *pv = T.pv + pv_chunk * c;
+    for (int r = 0; r <= T.d; r++) {
+        const int loc = T.tl_loc[tb + (size_t)r * SPLAT_TILE + li];
+        const float bw = T.tl_w[tb + (size_t)r * SPLAT_TILE + li];
+        const float *row = pv + (size_t)(pb + loc) * w;
+        const float wa = fmul(bw, T.alpha);
+#pragma unroll
+        for (int q = 0; q < WC / 4; q++) {
+            if (4 * q >= w) break;
+            const float4 v4 = __ldg(reinterpret_cast<const float4 *>(row) + q);
+            const float v[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int e = 4 * q + u;
+                if (T.seq)  // (w * v) * alpha (permutohedral.cpp:520)
+                    acc[e] = fmaf(fmul(bw, v[u]), T.alpha, acc[e]);
+                else  // (w * alpha) * v (permutohedral.cpp:579-581)
+                    acc[e] = fmaf(wa, v[u], acc[e]);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void wide_load(const float *row, int w, float (&x)[WC]) {
+#pragma unroll
+    for (int q = 0; q < WC / 4; q++) {
+        if (4 * q >= w) break;
+        const float4 v4 = *reinterpret_cast<const float4 *>(row + 4 * q);
+        x[4 * q] = v4.x, x[4 * q + 1] = v4.y, x[4 * q + 2] = v4.z, x[4 * q + 3] = v4.w;
+    }
+}
+
+__device__ __forceinline__ void wide_store(float *row, int w, const float (&x)[WC]) {
+#pragma unroll
+    for (int q = 0; q < WC / 4; q++) {
+        if (4 * q >= w) break;
+        *reinterpret_cast<float4 *>(row + 4 * q) = make_float4(x[4 * q], x[4 * q + 1], x[4 * q + 2], x[4 * q + 3]);
+    }
+}
+
+// One CTA per tile, one thread per point.  The operations and their order
+// are those of the point pass: per chunk, x = -U (or the given marginals),
+// then per term in order x -= compatibility(post-normalised slice) -- a
+// Matrix sums over all labels in label order from the term's sliced rows,
+// stored first -- then the softmax over all chunks (maximum, exponentials
+// summed in label order, one reciprocal) (densecrf.cpp:98-129).
+__global__ void __launch_bounds__(SPLAT_TILE) wide_kernel(const __grid_constant__ WideArgs a) {
+    __shared__ double sKL[SPLAT_TILE / 32];
+    const int t = blockIdx.x, li = threadIdx.x, lane = li & 31, warp = li >> 5;
+    const size_t s = (size_t)t * SPLAT_TILE + li;
+    const int i = a.slot_pt[s];
+    const int M = a.M, MP = a.MP, ns = a.nslots, mode = a.mode;
+    const int nc = (MP + WC - 1) / WC;
+    const bool kl_mode = (mode & WP_KL) != 0;
+    double kl = 0.0;
+    if (i >= 0) {
+        if (mode & WP_MSG) {  // Matrix terms: every chunk of their post-normalised slice first
+            int j = 0;
+            for (int k = 0; k < a.ts.n; k++) {
+                const TermDev &T = a.ts.t[k];
+                if (T.ckind != DCRF_COMPAT_MATRIX) continue;
+                float *Fj = a.F + (size_t)j * ns * MP;
+                for (int c = 0; c < nc; c++) {
+                    const int w = min(WC, MP - WC * c);
+                    float acc[WC];
+                    wide_slice(T, a.pv_chunk[k], t, li, c, w, acc);
+                    if (T.post_norm) {
+                        const float nn = T.norm[s];
+#pragma unroll
+                        for (int e = 0; e < WC; e++) acc[e] = fmul(acc[e], nn);
+                    }
+                    wide_store(Fj + (size_t)WC * c * ns + s * w, w, acc);
+                }
+                j++;
+            }
+        }
+        float mx = -INFINITY;
+        for (int c = 0; c < nc; c++) {
+            const int w = min(WC, MP - WC * c), m0 = WC * c;
+            const size_t ro = (size_t)WC * c * ns + s * w;
+            float x[WC];
+#pragma unroll
+            for (int e = 0; e < WC; e++) x[e] = 0.f;
+            if (mode & WP_LOAD_Q) {
+                wide_load(a.Qin + ro, w, x);
+            } else if (a.U) {
+                wide_load(a.U + ro, w, x);
+#pragma unroll
+                for (int e = 0; e < WC; e++) x[e] = -x[e];
+            }
+            if (mode & WP_MSG) {
+                int j = 0;
+                for (int k = 0; k < a.ts.n; k++) {
+                    const TermDev &T = a.ts.t[k];
+                    float cc[WC];
+                    if (T.ckind == DCRF_COMPAT_MATRIX) {
+                        const float *Fj = a.F + (size_t)j * ns * MP;
+#pragma unroll
+                        for (int e = 0; e < WC; e++) cc[e] = 0.f;
+                        for (int kk = 0; kk < M; kk++) {
+                            const float f = Fj[chunk_offset((size_t)ns, MP, s, kk)];
+#pragma unroll
+                            for (int e = 0; e < WC; e++)
+                                if (e < w && m0 + e < M) cc[e] = fmaf(__ldg(T.compat + (size_t)(m0 + e) * M + kk), f, cc[e]);
+                        }
+                        j++;
+                    } else {
+                        float acc[WC];
+                        wide_slice(T, a.pv_chunk[k], t, li, c, w, acc);
+                        if (T.post_norm) {
+                            const float nn = T.norm[s];
+#pragma unroll
+                            for (int e = 0; e < WC; e++) acc[e] = fmul(acc[e], nn);
+                        }
+                        if (T.ckind == DCRF_COMPAT_POTTS) {
+                            const float nw = -T.potts_w;
+#pragma unroll
+                            for (int e = 0; e < WC; e++) cc[e] = fmul(nw, acc[e]);
+                        } else {
+#pragma unroll
+                            for (int e = 0; e < WC; e++) cc[e] = (e < w && m0 + e < M) ? fmul(__ldg(T.compat + m0 + e), acc[e]) : 0.f;
+                        }
+                    }
+#pragma unroll
+                    for (int e = 0; e < WC; e++) {
+                        if (e >= w || m0 + e >= M) continue;
+                        if (kl_mode)
+                            kl += (double)fmul(x[e], cc[e]);
+                        else
+                            x[e] = fsub(x[e], cc[e]);
+                    }
+                }
+            }
+            if (kl_mode) {  // entropy and unary parts (densecrf.cpp:216-226)
+                float u[WC];
+#pragma unroll
+                for (int e = 0; e < WC; e++) u[e] = 0.f;
+                if (a.U) wide_load(a.U + ro, w, u);
+#pragma unroll
+                for (int e = 0; e < WC; e++)
+                    if (e < w && m0 + e < M) {
+                        kl += (double)x[e] * log((double)fmaxf(x[e], 1e-20f));
+                        kl += (double)fmul(u[e], x[e]);
+                    }
+            } else {
+#pragma unroll
+                for (int e = 0; e < WC; e++) {
+                    if (m0 + e >= M) x[e] = -INFINITY;
+                    mx = fmaxf(mx, x[e]);
+                }
+                wide_store(a.Qout + ro, w, x);  // the logits, until the softmax below
+            }
+        }
+        if (!kl_mode && (mode & (WP_WRITE_Q | WP_MAP))) {
+            float sum = 0.f;
+            for (int c = 0; c < nc; c++) {
+                const int w = min(WC, MP - WC * c);
+                float *row = a.Qout + (size_t)WC * c * ns + s * w;
+                float x[WC];
+                wide_load(row, w, x);
+#pragma unroll
+                for (int e = 0; e < WC; e++) {
+                    if (e >= w) break;
+                    x[e] = __expf(fsub(x[e], mx));
+                    sum = fadd(sum, x[e]);
+                }
+                wide_store(row, w, x);
+            }
+            const float rs = __frcp_rn(sum);
+            int best = 0;
+            float bv = -1.f;
+            for (int c = 0; c < nc; c++) {
+                const int w = min(WC, MP - WC * c), m0 = WC * c;
+                float *row = a.Qout + (size_t)WC * c * ns + s * w;
+                float x[WC];
+                wide_load(row, w, x);
+#pragma unroll
+                for (int e = 0; e < WC; e++) {
+                    x[e] = fmul(x[e], rs);
+                    if (e < w && m0 + e < M && x[e] > bv) {  // first maximum (densecrf.cpp:132-137)
+                        bv = x[e];
+                        best = m0 + e;
+                    }
+                }
+                if (mode & WP_WRITE_Q) wide_store(row, w, x);
+            }
+            if (mode & WP_MAP) a.map_out[i] = (int16_t)best;
+        }
+    }
+    if (kl_mode) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) kl += __shfl_down_sync(0xffffffffu, kl, o);
+        if (lane == 0) sKL[warp] = kl;
+        __syncthreads();
+        if (li == 0) {
+            double ssum = 0.0;
+            for (int w = 0; w < SPLAT_TILE / 32; w++) ssum += sKL[w];
+            a.kl_part[t] = ssum;
+        }
+    }
+}
+
+cudaError_t launch_wide(const WideArgs &a, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    DCRF_LAUNCH(wide_kernel<<<a.ntiles, SPLAT_TILE, 0, s>>>(a));
+    return cudaGetLastError();
+}
+
 // Value-size-1 normalisation slice and raw lattice filter (point-order gather
 // from the vertex-order blurred values; used off the iteration loop).
 template <int MP>
@@ -1078,14 +1299,14 @@ struct SlotTile {
     int pt[SPLAT_TILE];
 };
 
-__device__ __forceinline__ void slot_tile_points(SlotTile &st, int point_major, int M, int N, const int *seg, int nseg,
-                                                 const int *slot_pt) {
+__device__ __forceinline__ void slot_tile_points(SlotTile &st, int point_major, int M, int Mu, int m0, int N,
+                                                 const int *seg, int nseg, const int *slot_pt) {
     const int li = threadIdx.x;
     const int p = slot_pt[(size_t)blockIdx.x * SPLAT_TILE + li];
     size_t o0 = 0, step = 0;
     if (p >= 0) {
-        o0 = user_offset(point_major, M, N, seg, nseg, p, 0);
-        step = M > 1 ? user_offset(point_major, M, N, seg, nseg, p, 1) - o0 : 0;
+        o0 = user_offset(point_major, Mu, N, seg, nseg, p, m0);
+        step = M > 1 ? user_offset(point_major, Mu, N, seg, nseg, p, m0 + 1) - o0 : 0;
     }
     st.pt[li] = p;
     st.o0[li] = o0;
@@ -1103,15 +1324,16 @@ __device__ __forceinline__ void slot_tile_elem(int f, int point_major, int M, in
     }
 }
 
-// out[slot][m] = in(m, slot_pt[slot]) for m < M; 0 for padding labels m < ld
-// and for empty slots
+// out[slot][m] = in(m0 + m, slot_pt[slot]) for m < M (Mu: the caller's label
+// count); 0 for padding labels m < ld and for empty slots
 __global__ void __launch_bounds__(SPLAT_TILE) to_slots_kernel(const float *__restrict__ in, int point_major, int M,
-                                                              int ld, int N, const int *__restrict__ seg, int nseg,
+                                                              int Mu, int m0, int ld, int N,
+                                                              const int *__restrict__ seg, int nseg,
                                                               const int *__restrict__ slot_pt,
                                                               float *__restrict__ out) {
     __shared__ SlotTile st;
     const int li = threadIdx.x, pitch = ld + 1;
-    slot_tile_points(st, point_major, M, N, seg, nseg, slot_pt);
+    slot_tile_points(st, point_major, M, Mu, m0, N, seg, nseg, slot_pt);
     __syncthreads();
     // eight independent loads in flight per thread
 #pragma unroll 8
@@ -1131,24 +1353,25 @@ __global__ void __launch_bounds__(SPLAT_TILE) to_slots_kernel(const float *__res
 // out(m, pt) = in[pt_slot[pt]][m], one thread per point: label-major output is
 // written a whole image row at a time (consecutive points on consecutive
 // addresses for every label)
-__global__ void from_slots_lm_kernel(const float *__restrict__ in, int M, int ld, int N, const int *__restrict__ seg,
-                                     int nseg, const int *__restrict__ pt_slot, float *__restrict__ out) {
+__global__ void from_slots_lm_kernel(const float *__restrict__ in, int M, int Mu, int m0, int ld, int N,
+                                     const int *__restrict__ seg, int nseg, const int *__restrict__ pt_slot,
+                                     float *__restrict__ out) {
     const int pt = blockIdx.x * blockDim.x + threadIdx.x;
     if (pt >= N) return;
     const float *src = in + (size_t)pt_slot[pt] * ld;
-    const size_t o0 = user_offset(0, M, N, seg, nseg, pt, 0);
-    const size_t step = M > 1 ? user_offset(0, M, N, seg, nseg, pt, 1) - o0 : 0;
+    const size_t o0 = user_offset(0, Mu, N, seg, nseg, pt, m0);
+    const size_t step = M > 1 ? user_offset(0, Mu, N, seg, nseg, pt, m0 + 1) - o0 : 0;
     for (int m = 0; m < M; m++) out[o0 + m * step] = src[m];
 }
 
 // out(m, pt) = in[slot of pt][m] through a shared-memory tile (point-major output)
-__global__ void __launch_bounds__(SPLAT_TILE) from_slots_kernel(const float *__restrict__ in, int M, int ld, int N,
-                                                                const int *__restrict__ seg, int nseg,
+__global__ void __launch_bounds__(SPLAT_TILE) from_slots_kernel(const float *__restrict__ in, int M, int Mu, int m0,
+                                                                int ld, int N, const int *__restrict__ seg, int nseg,
                                                                 const int *__restrict__ slot_pt, int point_major,
                                                                 float *__restrict__ out) {
     __shared__ SlotTile st;
     const int li = threadIdx.x, pitch = ld + 1;
-    slot_tile_points(st, point_major, M, N, seg, nseg, slot_pt);
+    slot_tile_points(st, point_major, M, Mu, m0, N, seg, nseg, slot_pt);
     const float *src = in + (size_t)blockIdx.x * SPLAT_TILE * ld;
 #pragma unroll 8
     for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE) {
@@ -1369,25 +1592,27 @@ cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStr
 #undef DCRF_BC
 }
 
-cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,
-                            const int *slot_pt, int nslots, float *out, cudaStream_t s) {
-    if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0) return cudaErrorInvalidValue;
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int Mu, int m0, int ld, int N, const int *seg,
+                            int nseg, const int *slot_pt, int nslots, float *out, cudaStream_t s) {
+    if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0 || m0 + M > Mu) return cudaErrorInvalidValue;
     if (nslots > 0)
-        DCRF_LAUNCH(to_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, point_major, M, ld, N, seg, nseg,
-                                                                               slot_pt, out));
+        DCRF_LAUNCH(to_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, point_major, M, Mu, m0, ld, N, seg,
+                                                                               nseg, slot_pt, out));
     return cudaGetLastError();
 }
 
-cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *slot_pt,
-                              int nslots, const int *pt_slot, int point_major, float *out, cudaStream_t s) {
-    if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0) return cudaErrorInvalidValue;
+cudaError_t launch_from_slots(const float *in, int M, int Mu, int m0, int ld, int N, const int *seg, int nseg,
+                              const int *slot_pt, int nslots, const int *pt_slot, int point_major, float *out,
+                              cudaStream_t s) {
+    if (ld < M || ld > DCRF_MAX_MP || nslots % SPLAT_TILE != 0 || m0 + M > Mu) return cudaErrorInvalidValue;
     if (N <= 0) return cudaGetLastError();
     if (point_major) {
         if (nslots > 0)
-            DCRF_LAUNCH(from_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, M, ld, N, seg, nseg, slot_pt,
-                                                                                     point_major, out));
+            DCRF_LAUNCH(from_slots_kernel<<<nslots / SPLAT_TILE, SPLAT_TILE, 0, s>>>(in, M, Mu, m0, ld, N, seg, nseg,
+                                                                                     slot_pt, point_major, out));
     } else {
-        DCRF_LAUNCH(from_slots_lm_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, ld, N, seg, nseg, pt_slot, out));
+        DCRF_LAUNCH(from_slots_lm_kernel<<<(N + 255) / 256, 256, 0, s>>>(in, M, Mu, m0, ld, N, seg, nseg, pt_slot,
+                                                                         out));
     }
     return cudaGetLastError();
 }

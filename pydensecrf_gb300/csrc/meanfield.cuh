@@ -48,6 +48,32 @@ struct PPArgs {
     TermSet ts;
 };
 
+// The mean-field update for more than 32 labels (label chunks of 32, see
+// chunk_offset): one CTA per tile, a thread per point walks the chunks.
+enum : int {
+    WP_MSG = 1,      // slice every term's blurred lattice (pv, chunk by chunk) into messages
+    WP_LOAD_Q = 2,   // the marginals are given (Qin); with WP_KL: klDivergence's partial sums
+    WP_WRITE_Q = 4,  // softmax, Qout = the new marginals
+    WP_MAP = 8,      // softmax, map_out = argmax (first maximum)
+    WP_KL = 16,
+};
+
+struct WideArgs {
+    int N, M, MP, mode;
+    int ntiles, nslots;
+    const int *slot_pt;
+    const float *U;     // chunked slot rows, or nullptr (zero unary)
+    const float *Qin;   // chunked slot rows (WP_LOAD_Q)
+    float *Qout;        // chunked slot rows; also the logits' scratch of the softmax
+    float *F;           // per Matrix term j (in term order), chunked slot rows of its sliced
+                        // messages at F + j * nslots * MP
+    int16_t *map_out;   // [N]
+    double *kl_part;    // [ntiles]
+    long long pv_chunk[DCRF_MAX_TERMS];  // floats between consecutive chunks of a term's pv (32 (P+1))
+    TermSet ts;         // terms; pv, tile tables, norm and compatibility of chunk 0
+};
+cudaError_t launch_wide(const WideArgs &a, cudaStream_t s);
+
 struct ReduceArgs {
     int n;  // number of terms
     struct T {
@@ -111,10 +137,12 @@ cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStr
 // per image an M x N_b block, images one after another -- [M][N] for one image)
 // and the device slot rows [nslots][ld] (ld >= M; padding labels and empty
 // slots hold 0).  seg[0..nseg] are the images' point offsets on the device.
-cudaError_t launch_to_slots(const float *in, int point_major, int M, int ld, int N, const int *seg, int nseg,
-                            const int *slot_pt, int nslots, float *out, cudaStream_t s);
-cudaError_t launch_from_slots(const float *in, int M, int ld, int N, const int *seg, int nseg, const int *slot_pt,
-                              int nslots, const int *pt_slot, int point_major, float *out, cudaStream_t s);
+// Labels m0 .. m0+M-1 of a caller buffer with Mu labels (M <= ld <= 32).
+cudaError_t launch_to_slots(const float *in, int point_major, int M, int Mu, int m0, int ld, int N, const int *seg,
+                            int nseg, const int *slot_pt, int nslots, float *out, cudaStream_t s);
+cudaError_t launch_from_slots(const float *in, int M, int Mu, int m0, int ld, int N, const int *seg, int nseg,
+                              const int *slot_pt, int nslots, const int *pt_slot, int point_major, float *out,
+                              cudaStream_t s);
 // 2D features of DenseCRF2D (densecrf.cpp:61-81) of every image into [d][N]
 cudaError_t launch_features_2d(int N, const int *seg, const int *imgW, int nseg, float sx, float sy,
                                const uint8_t *rgb, float sr, float sg, float sb, float *feat, cudaStream_t s);

@@ -242,4 +242,4 @@ def test_shape_errors(engine):
     with pytest.raises(TypeError):
         d.addPairwiseEnergy(None, compat=1.0)
     with pytest.raises(ValueError):
-        engine.DenseCRF(100, 64)  # more labels than the engine supports is an explicit error
+        engine.DenseCRF(100, 5000)  # more labels than the engine supports (4096) is an explicit error
