@@ -132,6 +132,12 @@ int dcrf_set_variant(dcrf_crf *h, int variant);
  * (ConstUnaryEnergy, unary.cpp:42-46).  U is M x N in `layout`. */
 int dcrf_set_unary(dcrf_crf *h, const float *U, int layout, int where);
 
+/* setUnaryEnergy(L, f) / LogisticUnary(L, f): densecrf.pyx:44-46,80-89 ->
+ * LogisticUnaryEnergy (unary.cpp:48-52): U = L f, computed on the device into
+ * the unary rows.  L is M x nfeat and f is nfeat x N, both C-order in `where`.
+ * Later dcrf_set_unary_parameters calls change L and recompute U. */
+int dcrf_set_unary_logistic(dcrf_crf *h, const float *L, int nfeat, const float *f, int where);
+
 /* addPairwiseEnergy(features, compat, kernel, normalization):
  * densecrf.pyx:71-75 -> densecrf.cpp:54-57 -> pairwise.cpp:116-122,170-172.
  * feat is (d, N) C-order.  Builds the lattice and the normalisation on the
@@ -205,6 +211,27 @@ int dcrf_set_compat(dcrf_crf *h, int term, int compat_kind, const float *compat)
  * lattice and the normalisation.  CONST_KERNEL has no parameters. */
 int dcrf_set_kernel_params(dcrf_crf *h, int term, const float *params);
 
+/* The reference's parameter vectors (densecrf.cpp:298-360).  Each getter
+ * writes the count to *n (may be NULL) and, when out is non-NULL, the values
+ * (DCRF_ERR_INVALID_ARG if capacity < count); each setter takes exactly that
+ * many values.
+ *   unary: a logistic unary's L in column-major order, m + M j
+ *          (LogisticUnaryEnergy::parameters, unary.cpp:53-57); none for a
+ *          constant unary (unary.cpp:32-36).
+ *   label compatibility: the terms' LabelCompatibility::parameters one after
+ *          another -- Potts w; Diagonal the M weights; Matrix the upper
+ *          triangle of the symmetric matrix row by row, M(M+1)/2 values
+ *          (labelcompatibility.cpp:50-54,69-71,88-100).
+ *   kernel: the terms' DenseKernel::parameters one after another -- DIAG the d
+ *          feature scales, FULL the d x d matrix column-major, CONST none
+ *          (pairwise.cpp:129-151); setting them rebuilds the lattices. */
+int dcrf_unary_parameters(dcrf_crf *h, float *out, int capacity, int *n);
+int dcrf_set_unary_parameters(dcrf_crf *h, const float *v, int n);
+int dcrf_label_compatibility_parameters(dcrf_crf *h, float *out, int capacity, int *n);
+int dcrf_set_label_compatibility_parameters(dcrf_crf *h, const float *v, int n);
+int dcrf_kernel_parameters(dcrf_crf *h, float *out, int capacity, int *n);
+int dcrf_set_kernel_parameters(dcrf_crf *h, const float *v, int n);
+
 /* Number of compatibility and kernel parameters of term `term` in the layout
  * of dcrf_backward: compatibility Potts 1, Diagonal M, Matrix M*M; kernel
  * CONST 0, DIAG d, FULL d*d. */
@@ -225,6 +252,13 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
  * The lattice filter's transpose is the reverse-order blur
  * (permutohedral.cpp:556). */
 int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU, double *dcompat, double *dkernel);
+
+/* The logistic unary's parameter gradient after dcrf_backward: dL/dL =
+ * (dL/dU) f^T, the sum over the iterations of LogisticUnaryEnergy::gradient(b)
+ * that DenseCRF::gradient adds (unary.cpp:64-67, densecrf.cpp:292-294), in the
+ * order of dcrf_unary_parameters; *n = M * nfeat (0 for a constant unary).
+ * Labels M <= 32. */
+int dcrf_unary_gradient(dcrf_crf *h, double *out, int capacity, int *n);
 
 /* ---- autotuning (no reference counterpart) --------------------------------
  * The engine's launch and build knobs -- threads per point of the mean-field

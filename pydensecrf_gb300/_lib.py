@@ -78,6 +78,14 @@ _SIGS = {
     "dcrf_param_counts": ([_vp, _i, _pi, _pi], _i),
     "dcrf_inference_checkpointed": ([_vp, _i, _vp, _i, _i], _i),
     "dcrf_backward": ([_vp, _vp, _i, _i, _vp, _vp, _vp], _i),
+    "dcrf_set_unary_logistic": ([_vp, _vp, _i, _vp, _i], _i),
+    "dcrf_unary_parameters": ([_vp, _vp, _i, _pi], _i),
+    "dcrf_set_unary_parameters": ([_vp, _vp, _i], _i),
+    "dcrf_label_compatibility_parameters": ([_vp, _vp, _i, _pi], _i),
+    "dcrf_set_label_compatibility_parameters": ([_vp, _vp, _i], _i),
+    "dcrf_kernel_parameters": ([_vp, _vp, _i, _pi], _i),
+    "dcrf_set_kernel_parameters": ([_vp, _vp, _i], _i),
+    "dcrf_unary_gradient": ([_vp, _vp, _i, _pi], _i),
 }
 
 _LIB = None

@@ -534,6 +534,11 @@ cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, in
 
 int label_products_blocks(int ns) { return (ns + LP_ROWS - 1) / LP_ROWS; }
 
+cudaError_t launch_sum_parts(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s) {
+    DCRF_LAUNCH(sum_parts_kernel<<<(K + 7) / 8, 256, 0, s>>>(part, nblk, K, out, accumulate));
+    return cudaGetLastError();
+}
+
 static cudaError_t sum_parts(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s) {
     DCRF_LAUNCH(sum_parts_kernel<<<(K + 7) / 8, 256, 0, s>>>(part, nblk, K, out, accumulate));
     return cudaGetLastError();

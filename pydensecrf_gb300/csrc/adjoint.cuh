@@ -46,6 +46,17 @@ int label_products_blocks(int ns);
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
                                   double *part, double *out, int accumulate, cudaStream_t s);
 cudaError_t launch_slice_grad(const SliceGradArgs &a, int MP, cudaStream_t s);
+// out[k] (+)= sum over blocks of part[k][blk] (fixed order)
+cudaError_t launch_sum_parts(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s);
+// LogisticUnaryEnergy (unary.cpp:48-68): U = L f into slot rows (chunk_offset
+// layout; L is M x F, f is F x N), and the parameter gradient b f^T summed over
+// the points (M <= 32; out has M*F doubles, column-major in L; part holds
+// logistic_grad_blocks * M * F doubles)
+cudaError_t launch_logistic_unary(const float *L, const float *f, int M, int F, int N, int ns, const int *slot_pt,
+                                  float *U, cudaStream_t s);
+int logistic_grad_blocks(int ns, int M, int F);
+cudaError_t launch_logistic_grad(const float *b, const float *f, int M, int F, int N, int ns, const int *slot_pt,
+                                 double *part, double *out, cudaStream_t s);
 int kernel_param_blocks(int N);
 cudaError_t launch_kernel_param_grad(const float *f, const float *fg, int d, int N, int full, double *part,
                                      double *out, int accumulate, cudaStream_t s);

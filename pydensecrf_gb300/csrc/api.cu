@@ -190,6 +190,11 @@ struct dcrf_crf {
     DevStatus *status = nullptr;
     float *U = nullptr;  // [M][nslots] unary, slot-major
     bool has_unary = false;
+    // logistic unary U = L f (unary.cpp:48-68): L [M][nfeat] (host copy and
+    // device), f [nfeat][N] on the device; nfeat = 0 for a constant unary
+    int nfeat = 0;
+    std::vector<float> L_h;
+    float *L_d = nullptr, *f_d = nullptr;
     float *Q = nullptr;      // [M][nslots] working marginals, slot-major
     float *tmp = nullptr;    // [M][nslots] scratch of the raw-filter path
     float *stage = nullptr;  // [N*M] user-layout staging of host copies
@@ -205,6 +210,7 @@ struct dcrf_crf {
     // model version (bumped by every change of unary, terms or parameters) and
     // the per-iteration checkpoints of the last dcrf_inference_checkpointed
     unsigned long long version = 0, ckpt_version = ~0ull;
+    unsigned long long du_version = ~0ull;  // model version whose dL/dU bw[2] holds (after dcrf_backward)
     int ckpt_T = -1;
     float *ckpt = nullptr;  // [(T+1)][nslots][MP]
     size_t ckpt_cap = 0;
@@ -1083,6 +1089,8 @@ int ensure_wide_bufs(dcrf_crf *h) {
     const size_t need = nmat * (size_t)h->nslots * h->MP;
     if (need > h->wideF_cap) {
         dev_free_async(h->wideF, h->stream);
+    dev_free_async(h->L_d, h->stream);
+    dev_free_async(h->f_d, h->stream);
         h->wideF = nullptr;
         h->wideF_cap = 0;
         int rc = dev_alloc_async(&h->wideF, need, h->stream);
@@ -1660,6 +1668,8 @@ int dcrf_destroy(dcrf_crf *h) {
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
     dev_free_async(h->wideF, h->stream);
+    dev_free_async(h->L_d, h->stream);
+    dev_free_async(h->f_d, h->stream);
     for (void *p : {(void *)h->status, (void *)h->bar, (void *)h->U, (void *)h->Q, (void *)h->tmp,
                     (void *)h->stage, (void *)h->map, (void *)h->kl_part, (void *)h->d_seg, (void *)h->d_imgW})
         dev_free_async(p, h->stream);
@@ -1710,8 +1720,214 @@ int dcrf_set_unary(dcrf_crf *h, const float *U, int layout, int where) {
     if (rc) return rc;
     if (!U) return set_err(DCRF_ERR_INVALID_ARG, "null unary");
     if ((rc = load_mn(h, U, layout, where, h->U))) return rc;
+    h->nfeat = 0;  // a constant unary from now on
     h->has_unary = true;
     h->version++;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+// ---- logistic unary and the parameter vectors ------------------------------
+static int upload_logistic_L(dcrf_crf *h) {
+    CU(cudaMemcpyAsync(h->L_d, h->L_h.data(), h->L_h.size() * sizeof(float), cudaMemcpyHostToDevice, h->stream));
+    CU(launch_logistic_unary(h->L_d, h->f_d, h->M, h->nfeat, h->N, h->nslots, h->slot_pt, h->U, h->stream));
+    return DCRF_OK;
+}
+
+int dcrf_set_unary_logistic(dcrf_crf *h, const float *L, int nfeat, const float *f, int where) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (!L || !f) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
+    if (nfeat < 1) return set_err(DCRF_ERR_INVALID_ARG, "the logistic unary needs at least one feature");
+    const size_t nL = (size_t)h->M * nfeat, nf = (size_t)nfeat * h->N;
+    h->L_h.resize(nL);
+    if (where == DCRF_DEVICE)
+        CU(cudaMemcpy(h->L_h.data(), L, nL * sizeof(float), cudaMemcpyDeviceToHost));
+    else
+        std::memcpy(h->L_h.data(), L, nL * sizeof(float));
+    dev_free_async(h->L_d, h->stream);
+    dev_free_async(h->f_d, h->stream);
+    h->L_d = h->f_d = nullptr;
+    h->nfeat = 0;
+    if ((rc = dev_alloc_async(&h->L_d, nL, h->stream)) || (rc = dev_alloc_async(&h->f_d, nf, h->stream))) return rc;
+    CU(cudaMemcpyAsync(h->f_d, f, nf * sizeof(float),
+                       where == DCRF_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, h->stream));
+    h->nfeat = nfeat;
+    if ((rc = upload_logistic_L(h))) return rc;
+    h->has_unary = true;
+    h->version++;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+// Copies n = count values to out when out is non-null and capacity >= n.
+static int give_vector(const std::vector<float> &v, float *out, int capacity, int *n) {
+    if (n) *n = (int)v.size();
+    if (out) {
+        if (capacity < (int)v.size())
+            return set_err(DCRF_ERR_INVALID_ARG, "output holds " + std::to_string(capacity) + " values, " +
+                                                     std::to_string(v.size()) + " needed");
+        std::copy(v.begin(), v.end(), out);
+    }
+    return ok();
+}
+
+int dcrf_unary_parameters(dcrf_crf *h, float *out, int capacity, int *n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    std::vector<float> v((size_t)h->M * h->nfeat);
+    for (int m = 0; m < h->M; m++)
+        for (int j = 0; j < h->nfeat; j++) v[(size_t)m + (size_t)h->M * j] = h->L_h[(size_t)m * h->nfeat + j];
+    return give_vector(v, out, capacity, n);
+}
+
+int dcrf_set_unary_parameters(dcrf_crf *h, const float *v, int n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (n != h->M * h->nfeat)
+        return set_err(DCRF_ERR_INVALID_ARG, "the unary has " + std::to_string(h->M * h->nfeat) + " parameters, got " +
+                                                 std::to_string(n));
+    if (n == 0) return ok();  // a constant unary has none (UnaryEnergy::setParameters, unary.cpp:35-36)
+    if (!v) return set_err(DCRF_ERR_INVALID_ARG, "null parameters");
+    for (int m = 0; m < h->M; m++)
+        for (int j = 0; j < h->nfeat; j++) h->L_h[(size_t)m * h->nfeat + j] = v[(size_t)m + (size_t)h->M * j];
+    if ((rc = upload_logistic_L(h))) return rc;
+    h->version++;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+// LabelCompatibility::parameters of term k (labelcompatibility.cpp:50-54,69-71,88-94)
+static std::vector<float> compat_parameters(const dcrf_crf *h, const Term &T) {
+    const int M = h->M;
+    if (T.ckind == DCRF_COMPAT_POTTS) return {T.potts_w};
+    if (T.ckind == DCRF_COMPAT_DIAGONAL) return T.compat_h;
+    std::vector<float> r;
+    for (int i = 0; i < M; i++)
+        for (int j = i; j < M; j++) r.push_back(T.compat_h[(size_t)i * M + j]);
+    return r;
+}
+
+// DenseKernel::parameters (pairwise.cpp:129-139): DIAG the d scales, FULL the
+// d x d matrix column-major, CONST none
+static std::vector<float> kernel_parameters(const Term &T) {
+    if (T.ktype == DCRF_DIAG_KERNEL) return T.params;
+    if (T.ktype != DCRF_FULL_KERNEL) return {};
+    std::vector<float> r((size_t)T.d * T.d);
+    for (int a = 0; a < T.d; a++)
+        for (int b = 0; b < T.d; b++) r[(size_t)a + (size_t)T.d * b] = T.params[(size_t)a * T.d + b];
+    return r;
+}
+
+int dcrf_label_compatibility_parameters(dcrf_crf *h, float *out, int capacity, int *n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    std::vector<float> v;
+    for (const Term &T : h->terms) {
+        std::vector<float> p = compat_parameters(h, T);
+        v.insert(v.end(), p.begin(), p.end());
+    }
+    return give_vector(v, out, capacity, n);
+}
+
+int dcrf_set_label_compatibility_parameters(dcrf_crf *h, const float *v, int n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    int total = 0;
+    for (const Term &T : h->terms) total += (int)compat_parameters(h, T).size();
+    if (n != total)
+        return set_err(DCRF_ERR_INVALID_ARG, "the compatibilities have " + std::to_string(total) +
+                                                 " parameters, got " + std::to_string(n));
+    if (n > 0 && !v) return set_err(DCRF_ERR_INVALID_ARG, "null parameters");
+    const int M = h->M;
+    int i = 0;
+    for (Term &T : h->terms) {
+        if (T.ckind == DCRF_COMPAT_POTTS) {
+            if ((rc = set_term_compat(h, T, DCRF_COMPAT_POTTS, v + i))) return rc;
+            i += 1;
+        } else if (T.ckind == DCRF_COMPAT_DIAGONAL) {
+            if ((rc = set_term_compat(h, T, DCRF_COMPAT_DIAGONAL, v + i))) return rc;
+            i += M;
+        } else {  // the packed upper triangle of the symmetric matrix (labelcompatibility.cpp:95-100)
+            std::vector<float> m((size_t)M * M);
+            for (int a = 0; a < M; a++)
+                for (int b = a; b < M; b++) m[(size_t)a * M + b] = m[(size_t)b * M + a] = v[i++];
+            if ((rc = set_term_compat(h, T, DCRF_COMPAT_MATRIX, m.data()))) return rc;
+        }
+    }
+    h->version++;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
+int dcrf_kernel_parameters(dcrf_crf *h, float *out, int capacity, int *n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    std::vector<float> v;
+    for (const Term &T : h->terms) {
+        std::vector<float> p = kernel_parameters(T);
+        v.insert(v.end(), p.begin(), p.end());
+    }
+    return give_vector(v, out, capacity, n);
+}
+
+int dcrf_set_kernel_parameters(dcrf_crf *h, const float *v, int n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    int total = 0;
+    for (const Term &T : h->terms) total += (int)kernel_parameters(T).size();
+    if (n != total)
+        return set_err(DCRF_ERR_INVALID_ARG, "the kernels have " + std::to_string(total) + " parameters, got " +
+                                                 std::to_string(n));
+    if (n > 0 && !v) return set_err(DCRF_ERR_INVALID_ARG, "null parameters");
+    int i = 0;
+    for (int k = 0; k < (int)h->terms.size(); k++) {
+        Term &T = h->terms[k];
+        if (T.ktype == DCRF_CONST_KERNEL) continue;
+        std::vector<float> p;
+        if (T.ktype == DCRF_DIAG_KERNEL) {
+            p.assign(v + i, v + i + T.d);
+            i += T.d;
+        } else {  // column-major d x d (pairwise.cpp:146-150) -> row-major P
+            p.resize((size_t)T.d * T.d);
+            for (int a = 0; a < T.d; a++)
+                for (int b = 0; b < T.d; b++) p[(size_t)a * T.d + b] = v[i + a + T.d * b];
+            i += T.d * T.d;
+        }
+        if ((rc = dcrf_set_kernel_params(h, k, p.data()))) return rc;
+    }
+    return ok();
+}
+
+int dcrf_unary_gradient(dcrf_crf *h, double *out, int capacity, int *n) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    const int K = h->M * h->nfeat;
+    if (n) *n = K;
+    if (!out || K == 0) return ok();
+    if (capacity < K) return set_err(DCRF_ERR_INVALID_ARG, "output too small for the unary gradient");
+    if (h->du_version != h->version || !h->bw[2])
+        return set_err(DCRF_ERR_STATE, "dcrf_unary_gradient needs a dcrf_backward of the current model");
+    const size_t npart = (size_t)logistic_grad_blocks(h->nslots, h->M, h->nfeat) * K;
+    if (npart == 0) return set_err(DCRF_ERR_INVALID_ARG, "too many logistic features for the gradient kernel");
+    if (npart > h->dpart_cap) {
+        dev_free_async(h->dpart, h->stream);
+        h->dpart = nullptr;
+        h->dpart_cap = 0;
+        if ((rc = dev_alloc_async(&h->dpart, npart, h->stream))) return rc;
+        h->dpart_cap = npart;
+    }
+    if ((size_t)K + 1 > h->dacc_cap) {
+        dev_free_async(h->dacc, h->stream);
+        h->dacc = nullptr;
+        h->dacc_cap = 0;
+        if ((rc = dev_alloc_async(&h->dacc, (size_t)K + 1, h->stream))) return rc;
+        h->dacc_cap = (size_t)K + 1;
+    }
+    // LogisticUnaryEnergy::gradient (unary.cpp:64-67) of the summed adjoint: (sum_t b_t) f^T = dL/dU f^T
+    CU(launch_logistic_grad(h->bw[2], h->f_d, h->M, h->nfeat, h->N, h->nslots, h->slot_pt, h->dpart, h->dacc,
+                            h->stream));
+    CU(cudaMemcpyAsync(out, h->dacc, sizeof(double) * K, cudaMemcpyDeviceToHost, h->stream));
     if ((rc = sync_check(h))) return rc;
     return ok();
 }
@@ -1925,6 +2141,7 @@ int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term
     if ((rc = load_labels(h, labels, where, &lab))) return rc;
     if ((rc = dev_alloc_async(&e, (size_t)h->N, h->stream))) return rc;
     float *q = h->bw[0], *qn = h->bw[1], *g = h->bw[2];
+    h->du_version = ~0ull;  // bw[2] no longer holds dL/dU
     CU(launch_onehot(lab, M, ns, h->slot_pt, q, h->stream));
     CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
     // g = sum over the terms of PairwisePotential::apply(one-hot) (pairwise.cpp:173-178)
@@ -2439,6 +2656,7 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
         CU(launch_softmax_adjoint(Qt, g, b, du, M, ns, h->slot_pt, h->stream));
     }
     if (dU && (rc = store_mn(h, du, dU, layout, where))) return rc;
+    h->du_version = h->version;
     if (want_kernel)
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];

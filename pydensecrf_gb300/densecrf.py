@@ -98,30 +98,12 @@ class ConstUnary(Unary):
 
 
 class LogisticUnary(Unary):
-    """Logistic unary energy U = L f (densecrf.pyx:44-46, unary.cpp:48-52)."""
+    """Logistic unary energy U = L f (densecrf.pyx:44-46, unary.cpp:48-52),
+    computed on the device by the engine."""
 
     def __init__(self, L, f):
         self.L = np.array(as_float_buffer(L, 2, "L"), dtype=np.float32, copy=True)
         self.f = np.array(as_float_buffer(f, 2, "f"), dtype=np.float32, copy=True)
-
-    def _matrix(self, M, N):
-        return logistic_unary(self.L, self.f)
-
-
-def logistic_unary(L: np.ndarray, f: np.ndarray) -> np.ndarray:
-    """U = L @ f in float32, on the GPU (cuBLAS through torch, TF32 off)."""
-    import torch
-
-    if not torch.cuda.is_available():
-        raise RuntimeError("a CUDA device is required")
-    prev = torch.backends.cuda.matmul.allow_tf32
-    torch.backends.cuda.matmul.allow_tf32 = False
-    try:
-        Ld = torch.from_numpy(np.ascontiguousarray(L)).cuda()
-        fd = torch.from_numpy(np.ascontiguousarray(f)).cuda()
-        return (Ld @ fd).cpu().numpy()
-    finally:
-        torch.backends.cuda.matmul.allow_tf32 = prev
 
 
 class DenseCRF:
@@ -195,7 +177,19 @@ class DenseCRF:
         """densecrf.pyx:77-78."""
         if not isinstance(u, Unary):
             raise TypeError("Argument 'u' has incorrect type (expected Unary)")
-        self._set_unary_matrix(u._matrix(self._nlabel, self._nvar))
+        if isinstance(u, LogisticUnary):
+            self._set_logistic(u.L, u.f)
+        else:
+            self._set_unary_matrix(u._matrix(self._nlabel, self._nvar))
+
+    def _set_logistic(self, L: np.ndarray, f: np.ndarray) -> None:
+        """LogisticUnaryEnergy(L, f) (unary.cpp:48-52): L is (M, K), f is (K, N)."""
+        L = np.ascontiguousarray(L, np.float32)
+        f = np.ascontiguousarray(f, np.float32)
+        if L.shape[0] != self._nlabel or f.shape != (L.shape[1], self._nvar):
+            raise ValueError("Bad shape for logistic unary energy (Need L ({}, K), f (K, {}); got {} and {})".format(
+                self._nlabel, self._nvar, L.shape, f.shape))
+        _lib.check(_lib.load().dcrf_set_unary_logistic(self._h, _ptr(L), L.shape[1], _ptr(f), _lib.HOST))
 
     def setUnaryEnergy(self, u, f=None) -> None:
         """densecrf.pyx:80-89; with ``f`` the unary is logistic, U = u f.  ``u``
@@ -212,8 +206,7 @@ class DenseCRF:
         if f is None:
             self._set_unary_matrix(u)
         else:
-            f = as_float_buffer(f, 2, "f")
-            self._set_unary_matrix(logistic_unary(u, f))
+            self._set_logistic(u, as_float_buffer(f, 2, "f"))
 
     def _set_unary_matrix(self, U: np.ndarray) -> None:
         U = np.ascontiguousarray(U, dtype=np.float32)
@@ -324,12 +317,69 @@ class DenseCRF:
         kind, c = _labelcomp(compat, self._nlabel)
         _lib.check(_lib.load().dcrf_set_compat(self._h, int(term), kind, _ptr(c)))
 
-    def setKernelParameters(self, term: int, params) -> None:
-        """Kernel parameters of term ``term`` (DenseKernel::setParameters):
-        DIAG d feature scales, FULL a d x d matrix (row-major).  Rebuilds the
-        lattice."""
+    def setKernelParameters(self, *args) -> None:
+        """``setKernelParameters(v)``: DenseCRF::setKernelParameters
+        (densecrf.cpp:348-360), the concatenation over the terms of DIAG
+        scales / FULL d x d matrices in column-major order, as kernelParameters()
+        returns it.  ``setKernelParameters(term, params)``: one term's
+        parameters (DenseKernel::setParameters, pairwise.cpp:140-151): DIAG d
+        feature scales, FULL a d x d matrix (row-major, features become P f).
+        Either rebuilds the lattices."""
+        if len(args) == 1:
+            v = np.ascontiguousarray(np.asarray(args[0], np.float32).reshape(-1))
+            _lib.check(_lib.load().dcrf_set_kernel_parameters(self._h, _ptr(v), int(v.size)))
+            return
+        if len(args) != 2:
+            raise TypeError("setKernelParameters(v) or setKernelParameters(term, params)")
+        term, params = args
         p = np.ascontiguousarray(np.asarray(params, np.float32).reshape(-1))
         _lib.check(_lib.load().dcrf_set_kernel_params(self._h, int(term), _ptr(p)))
+
+    def _vector(self, fn) -> np.ndarray:
+        n = ctypes.c_int()
+        _lib.check(fn(self._h, None, 0, ctypes.byref(n)))
+        out = np.empty(n.value, np.float32)
+        if n.value:
+            _lib.check(fn(self._h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
+
+    def _set_vector(self, fn, v) -> None:
+        v = np.ascontiguousarray(np.asarray(v, np.float32).reshape(-1))
+        _lib.check(fn(self._h, _ptr(v) if v.size else None, int(v.size)))
+
+    def unaryParameters(self) -> np.ndarray:
+        """DenseCRF::unaryParameters (densecrf.cpp:298-302): a logistic unary's L
+        in column-major order; empty for a constant unary."""
+        return self._vector(_lib.load().dcrf_unary_parameters)
+
+    def setUnaryParameters(self, v) -> None:
+        """DenseCRF::setUnaryParameters (densecrf.cpp:303-306)."""
+        self._set_vector(_lib.load().dcrf_set_unary_parameters, v)
+
+    def labelCompatibilityParameters(self) -> np.ndarray:
+        """DenseCRF::labelCompatibilityParameters (densecrf.cpp:307-320): per term
+        Potts w / the Diagonal weights / the Matrix's packed upper triangle."""
+        return self._vector(_lib.load().dcrf_label_compatibility_parameters)
+
+    def setLabelCompatibilityParameters(self, v) -> None:
+        """DenseCRF::setLabelCompatibilityParameters (densecrf.cpp:321-333)."""
+        self._set_vector(_lib.load().dcrf_set_label_compatibility_parameters, v)
+
+    def kernelParameters(self) -> np.ndarray:
+        """DenseCRF::kernelParameters (densecrf.cpp:334-347)."""
+        return self._vector(_lib.load().dcrf_kernel_parameters)
+
+    def unaryParameterGradient(self) -> np.ndarray:
+        """After backward(): dL/d(unaryParameters()) = (dL/dU) f^T for a logistic
+        unary (LogisticUnaryEnergy::gradient summed over the iterations,
+        unary.cpp:64-67); empty for a constant unary."""
+        n = ctypes.c_int()
+        lib = _lib.load()
+        _lib.check(lib.dcrf_unary_gradient(self._h, None, 0, ctypes.byref(n)))
+        out = np.zeros(n.value, np.float64)
+        if n.value:
+            _lib.check(lib.dcrf_unary_gradient(self._h, _ptr(out), n.value, ctypes.byref(n)))
+        return out
 
     def paramCounts(self, term: int):
         """(number of compatibility values, number of kernel parameters) of a term."""
