@@ -73,7 +73,8 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(s, verbose, list(extra_flags)), srcs))
     tmp = LIB + ".tmp"
-    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-o", tmp, *objs]
+    # -z defs: a symbol no translation unit defines fails the link, not the load
+    cmd = [nvcc(), *ARCH, "-shared", "-cudart", "static", "-Xlinker", "-z", "-Xlinker", "defs", "-o", tmp, *objs]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}{r.stderr}")

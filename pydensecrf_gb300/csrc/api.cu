@@ -557,6 +557,7 @@ TermDev term_dev(dcrf_crf *h, const Term &T, bool transpose, bool value1) {
     t.tl_loc = T.lat.tl_loc;
     t.tl_w = T.lat.tl_w;
     t.task = T.lat.task;
+    t.tsched = T.lat.tsched;
     t.tile_tbeg = T.lat.tile_tbeg;
     t.pv = T.pv;
     t.pout = T.pout;
@@ -612,6 +613,8 @@ void plan_smem(dcrf_crf *h, PPArgs &a, const std::vector<int> &which, bool msg, 
             a.ts.t[k].sm_norm = (int)off;
             off = align128(off + 1024);
             a.ts.t[k].sm_task = (int)off;
+            off = align128(off + ((size_t)T.lat.max_nt + 8) * 4);
+            a.ts.t[k].sm_sched = (int)off;
             off = align128(off + ((size_t)T.lat.max_nt + 8) * 4);
             a.ts.t[k].sm_mpt = (int)off;
             off = align128(off + d1 * SPLAT_TILE * 2);

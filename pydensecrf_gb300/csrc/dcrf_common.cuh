@@ -136,6 +136,7 @@ struct TermDev {
     const uint16_t *tl_loc;  // [ntiles][d+1][SPLAT_TILE] corner -> index among the tile's partials
     const float *tl_w;       // [ntiles][d+1][SPLAT_TILE] corner barycentric weight
     const uint32_t *task;    // splat tasks (see LatticeDev::task)
+    const uint32_t *tsched;  // per tile, task indices by descending length (LatticeDev::tsched)
     const int *tile_tbeg;    // [ntiles+1] task range of each tile
     float *pv;               // [P][MP] blurred values in partial order (slice input)
     float *pout;             // [P][MP] splat partials, grouped by vertex (row ppos[p] for partial p)
@@ -144,7 +145,7 @@ struct TermDev {
     const float *compat;     // Diagonal [M] / Matrix [M][M] (symmetrised)
     // shared-memory plan of the point pass (byte offsets; staged = 0: global reads)
     int staged, vcap;
-    int sm_loc, sm_w, sm_norm, sm_task, sm_mpt, sm_mw, sm_vp;
+    int sm_loc, sm_w, sm_norm, sm_task, sm_sched, sm_mpt, sm_mw, sm_vp;
     int sm_cmp;  // Matrix compatibility staged as [k][MP] (transposed, zero padded); -1: global reads
 };
 

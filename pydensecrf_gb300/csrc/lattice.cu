@@ -565,7 +565,8 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
                                                                int *__restrict__ part_v, int *__restrict__ part_mend,
                                                                uint16_t *__restrict__ mem_pt, float *__restrict__ mem_w,
                                                                uint16_t *__restrict__ tl_loc, float *__restrict__ tl_w,
-                                                               uint32_t *__restrict__ task, uint32_t *__restrict__ vcount,
+                                                               uint32_t *__restrict__ task, uint32_t *__restrict__ tsched,
+                                                               uint32_t *__restrict__ vcount,
                                                                int L, int P, int T, const __grid_constant__ ClearList clr,
                                                                float *V0, float *V1, int MP, DevStatus *st) {
     constexpr int C = TG<D>::C, NW = TG_THREADS / 32;
@@ -596,6 +597,7 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
         if (tid < 8) {
             part_mend[P + tid] = 0;
             task[T + tid] = 0;
+            tsched[T + tid] = 0;
         }
         clear_words(clr, (size_t)tid, TG_THREADS);
         zero_value_rows(V0, V1, (size_t)L, MP, tid, TG_THREADS);
@@ -618,6 +620,18 @@ __global__ void __launch_bounds__(TG_THREADS) tile_place_kernel(const uint16_t *
         mrun += c;
     }
     for (int e = tid; e < NW * C; e += TG_THREADS) wc[e] = 0;
+    __syncthreads();  // the tile's tasks are written
+    // the schedule: task indices by descending length, ties in task order, so
+    // that the lane groups of one warp get tasks of similar length
+    for (int j = tid; j < ttot; j += TG_THREADS) {
+        const uint32_t lj = task[tb + j] & 63u;
+        int rank = 0;
+        for (int i = 0; i < ttot; i++) {
+            const uint32_t li = task[tb + i] & 63u;
+            rank += (li > lj || (li == lj && i < j)) ? 1 : 0;
+        }
+        tsched[tb + rank] = (uint32_t)j;
+    }
     // members past the tile's last one, and the corners of empty slots: index 0, weight 0
     for (int e = mtot + tid; e < C; e += TG_THREADS) {
         mem_pt[base + e] = 0;
@@ -1005,7 +1019,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     const bool radix = (size_t)L.P > 64 * std::max<size_t>(1, (size_t)L.L);
     const size_t radix_words = radix ? radix_temp_words((size_t)L.P) : 0;
     per.reserve(3 * Arena::sz<int>(Pn) + Arena::sz<int>((size_t)L.P + 8) + Arena::sz<int>(Ln) +
-                Arena::sz<uint32_t>((size_t)T + 8) + 2 * Arena::sz<float>(Ln * MP) + 2 * Arena::sz<float>(Pn * MP) +
+                2 * Arena::sz<uint32_t>((size_t)T + 8) + 2 * Arena::sz<float>(Ln * MP) + 2 * Arena::sz<float>(Pn * MP) +
                 Arena::sz<float>((size_t)nslots) + Arena::sz<float>(ntl));
     L.part_v = per.get<int>(Pn);
     L.red_beg = per.get<int>(Ln);
@@ -1013,6 +1027,7 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
     L.ppos = per.get<int>(Pn);
     L.part_mend = per.get<int>((size_t)L.P + 8);
     L.task = per.get<uint32_t>((size_t)T + 8);
+    L.tsched = per.get<uint32_t>((size_t)T + 8);
     L.V0 = per.get<float>(Ln * MP);
     L.V1 = per.get<float>(Ln * MP);
     L.pv = per.get<float>(Pn * MP);
@@ -1036,7 +1051,8 @@ int build_d(const float *feat, int N, const Segments &seg, const TileMapDev &tm,
         clr.add(st_red, 2 * red_state, 0u);
         DCRF_LAUNCH(tile_place_kernel<D><<<L.ntiles, TG_THREADS, smem_p, s>>>(
             cl, pvx, pcnt, L.bary, N, tm.slot_pt, (const uint32_t *)L.tile_pbeg, (const uint32_t *)L.tile_tbeg,
-            task_len, L.part_v, L.part_mend, L.mem_pt, L.mem_w, L.tl_loc, L.tl_w, L.task, vcount, L.L, L.P, T, clr,
+            task_len, L.part_v, L.part_mend, L.mem_pt, L.mem_w, L.tl_loc, L.tl_w, L.task, L.tsched, vcount, L.L, L.P,
+            T, clr,
             L.V0, L.V1, MP, status));
         if ((ce = cudaGetLastError()) != cudaSuccess) {
             red.release();

@@ -33,6 +33,8 @@ struct LatticeDev {
     // task = (local partial << 19) | (first member << 6) | length
     int max_nt = 0;               // largest number of tasks of one tile
     uint32_t *task = nullptr;     // [T+8]
+    uint32_t *tsched = nullptr;   // [T+8] per tile, its task indices by descending length (the
+                                  // order the point pass deals tasks to its lane groups)
     int *tile_tbeg = nullptr;     // [ntiles+1] task range of tile t
     int *red_beg = nullptr;      // [L+1]
     int *red_list = nullptr;     // [P] partials grouped by vertex (each vertex's in tile order)

@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
             const TileBlocks b = sTB[k];
             if (!T.staged) continue;
             const uint32_t d1 = T.d + 1;
-            total += 1024u + (uint32_t)b.nwin * 4u + d1 * SPLAT_TILE * 6u;  // norm, tasks, members
+            total += 1024u + (uint32_t)b.nwin * 8u + d1 * SPLAT_TILE * 6u;  // norm, tasks, schedule, members
             if (mode & PP_MSG) {
                 total += d1 * SPLAT_TILE * 6u;                                // corner tables
                 if (b.vp_staged) total += (uint32_t)b.np * MP * 4u;           // blurred rows
@@ -397,6 +397,7 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
             const size_t tb = (size_t)t * SPLAT_TILE * d1;
             bulk_g2s(smem + T.sm_norm, T.norm + (size_t)t * SPLAT_TILE, 1024u, &mbar);
             bulk_g2s(smem + T.sm_task, T.task + b.a0, (uint32_t)b.nwin * 4u, &mbar);
+            bulk_g2s(smem + T.sm_sched, T.tsched + b.a0, (uint32_t)b.nwin * 4u, &mbar);
             bulk_g2s(smem + T.sm_mpt, T.mem_pt + tb, (uint32_t)(d1 * SPLAT_TILE * 2), &mbar);
             bulk_g2s(smem + T.sm_mw, T.mem_w + tb, (uint32_t)(d1 * SPLAT_TILE * 4), &mbar);
             if (mode & PP_MSG) {
@@ -602,7 +603,9 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
     // ---- 4. splat the tile's q into each term's partials.  Each task sums at
     // most SPLAT_TASK members of one partial in member order; a partial made of
     // several tasks adds the task sums in task order.  A group of lanes takes
-    // one task at a time, each lane its own labels.
+    // one task at a time, each lane its own labels; the tasks are dealt in the
+    // tile's schedule (descending length), so that the groups of one warp,
+    // which run in lock step, get tasks of similar length.
     if (mode & PP_SPLAT) {
         float *sQ = reinterpret_cast<float *>(smem + a.sm_q);
         float *sRes = reinterpret_cast<float *>(smem + a.sm_res);
@@ -617,10 +620,13 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
             const size_t tbm = (size_t)t * SPLAT_TILE * (T.d + 1);
             const uint32_t *tasks = T.staged ? reinterpret_cast<const uint32_t *>(smem + T.sm_task) + (b.tb - b.a0)
                                              : T.task + b.tb;
+            const uint32_t *sched = T.staged ? reinterpret_cast<const uint32_t *>(smem + T.sm_sched) + (b.tb - b.a0)
+                                             : T.tsched + b.tb;
             const uint16_t *mpt = T.staged ? reinterpret_cast<const uint16_t *>(smem + T.sm_mpt) : T.mem_pt + tbm;
             const float *mw = T.staged ? reinterpret_cast<const float *>(smem + T.sm_mw) : T.mem_w + tbm;
             if (gactive) {
-                for (int j = gid; j < b.nt; j += NG) {
+                for (int sj = gid; sj < b.nt; sj += NG) {
+                    const int j = (int)sched[sj];
                     const uint32_t tk = tasks[j];
                     const int pl = (int)(tk >> 19), e0 = (int)((tk >> 6) & 0x1FFFu), len = (int)(tk & 63u);
                     // the partial's output row, fetched before the member loop hides its latency
