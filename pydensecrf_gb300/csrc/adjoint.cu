@@ -5,7 +5,10 @@
 // All point quantities are slot-major [M][nslots] (empty slots hold zero).
 // Reductions are two-level and deterministic: per-block partial sums in
 // double, then one block adds them in block order.
+#include <algorithm>
+
 #include "adjoint.cuh"
+#include "labelprod.cuh"
 
 namespace dcrf {
 
@@ -313,20 +316,19 @@ __global__ void row_sum_kernel(const float *__restrict__ x, float *__restrict__ 
     out[s] = t;
 }
 
-// Per-block partial sums of the label products over the occupied slots, a
-// tall-skinny product of two [rows][ld] blocks staged in shared memory:
-//  mode 0 (per label):  part[blk][m]      = sum_s a[s][m] * b[s][m]
-//  mode 1 (outer):      part[blk][m*M+k]  = sum_s a[s][m] * b[s][k]
-// Each block takes LP_ROWS slots; each thread owns outputs threadIdx.x + 256 j
-// and accumulates them over the block's rows in slot order (float), the block
-// result is stored as double.  Padding slots (slot_pt < 0) are left out
-// whatever they contain.
+// Label products of slot rows a, b over the slots, per block of LP_ROWS slots
+// (staged in shared memory):
+//  mode 0 (per label):  part[blk][m]      (+)= sum_s a[s][m] * b[s][m]
+//  mode 1 (outer):      part[blk][m*M+k]  (+)= sum_s a[s][m] * b[s][k]
+// (block_label_products); the block's result is stored (or added, accumulate)
+// block-major, so that the block's writes are contiguous.  Padding slots
+// (slot_pt < 0) are left out whatever they contain.
 constexpr int LP_ROWS = 128;
 
 __global__ void __launch_bounds__(256) label_products_kernel(const float *__restrict__ a, const float *__restrict__ b,
                                                              int M, int ld, int ns, const int *__restrict__ slot_pt,
-                                                             int mode, double *__restrict__ part) {
-    extern __shared__ float sab[];  // [LP_ROWS][ld] of a, then of b
+                                                             int mode, int accumulate, double *__restrict__ part) {
+    extern __shared__ float sab[];  // [LP_ROWS][ld] of a, then of b; the groups' sums after them
     float *sa = sab, *sb = sab + LP_ROWS * ld;
     const int K = mode == 0 ? M : M * M;
     const size_t r0 = (size_t)blockIdx.x * LP_ROWS;
@@ -338,12 +340,26 @@ __global__ void __launch_bounds__(256) label_products_kernel(const float *__rest
         sb[e] = ok ? b[r0 * ld + e] : 0.f;
     }
     __syncthreads();
-    for (int kk = threadIdx.x; kk < K; kk += blockDim.x) {
-        const int m = mode == 0 ? kk : kk / M, k = mode == 0 ? kk : kk % M;
-        float t = 0.f;
-        for (int r = 0; r < LP_ROWS; r++) t = fmaf(sa[r * ld + m], sb[r * ld + k], t);
-        part[(size_t)kk * gridDim.x + blockIdx.x] = (double)t;
-    }
+    block_label_products(sa, sb, LP_ROWS, ld, M, mode, sb + LP_ROWS * ld, part + (size_t)blockIdx.x * K, accumulate);
+}
+
+// out[k] (+)= sum over blocks of part[blk][k] (block-major partials): one warp
+// per output, lanes striding over the blocks, then a fixed shuffle tree
+__global__ void sum_parts_bm_kernel(const double *__restrict__ part, int nblk, int K, double *__restrict__ out,
+                                    int accumulate) {
+    const int k = blockIdx.x * (blockDim.x / 32) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (k >= K) return;
+    double t = 0.0;
+    for (int b = lane; b < nblk; b += 32) t += part[(size_t)b * K + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (lane == 0) out[k] = accumulate ? out[k] + t : t;
+}
+
+cudaError_t launch_sum_parts_bm(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s) {
+    DCRF_LAUNCH(sum_parts_bm_kernel<<<(K + 7) / 8, 256, 0, s>>>(part, nblk, K, out, accumulate));
+    return cudaGetLastError();
 }
 
 // out[k] (+)= sum over blocks of part[k][blk] (output-major partials): one
@@ -544,14 +560,22 @@ static cudaError_t sum_parts(const double *part, int nblk, int K, double *out, i
     return cudaGetLastError();
 }
 
+cudaError_t launch_label_products_part(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
+                                       double *part, int accumulate, cudaStream_t s) {
+    const int ld = pad_labels(M);
+    const unsigned nb = (unsigned)label_products_blocks(ns);
+    const size_t smem = (2 * (size_t)LP_ROWS * ld + block_label_products_words(M, mode)) * sizeof(float);
+    if (smem > 48 * 1024) return cudaErrorInvalidValue;
+    DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, ld, ns, slot_pt, mode, accumulate, part));
+    return cudaGetLastError();
+}
+
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
                                   double *part, double *out, int accumulate, cudaStream_t s) {
     const int K = mode == 0 ? M : M * M;
-    const int ld = pad_labels(M);
-    const unsigned nb = (unsigned)label_products_blocks(ns);
-    const size_t smem = 2 * (size_t)LP_ROWS * ld * sizeof(float);  // at most 32 KB
-    DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, ld, ns, slot_pt, mode, part));
-    return sum_parts(part, (int)nb, K, out, accumulate, s);
+    cudaError_t e = launch_label_products_part(a, b, M, ns, slot_pt, mode, part, 0, s);
+    if (e != cudaSuccess) return e;
+    return launch_sum_parts_bm(part, label_products_blocks(ns), K, out, accumulate, s);
 }
 
 template <int MP>

@@ -45,9 +45,14 @@ int label_products_blocks(int ns);
 // mode 0: out[m] (+)= sum a[m].*b[m]; mode 1: out[m*M+k] (+)= sum a[m].*b[k]; part: [blocks][K] doubles
 cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
                                   double *part, double *out, int accumulate, cudaStream_t s);
+// the block partials only, stored or added (accumulate) into part ([blocks][K]);
+// launch_sum_parts_bm reduces such block-major partials
+cudaError_t launch_label_products_part(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
+                                       double *part, int accumulate, cudaStream_t s);
 cudaError_t launch_slice_grad(const SliceGradArgs &a, int MP, cudaStream_t s);
 // out[k] (+)= sum over blocks of part[k][blk] (fixed order)
 cudaError_t launch_sum_parts(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s);
+cudaError_t launch_sum_parts_bm(const double *part, int nblk, int K, double *out, int accumulate, cudaStream_t s);
 // LogisticUnaryEnergy (unary.cpp:48-68): U = L f into slot rows (chunk_offset
 // layout; L is M x F, f is F x N), and the parameter gradient b f^T summed over
 // the points (M <= 32; out has M*F doubles, column-major in L; part holds

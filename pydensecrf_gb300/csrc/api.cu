@@ -224,6 +224,9 @@ struct dcrf_crf {
     size_t cky_cap = 0;
     std::vector<long long> cky_off;  // per term, -1: not kept
     std::vector<size_t> ckv_off, ckv_layout;
+    // per term with kernel gradients, the adjoint's raw slices F ([nslots][MP])
+    // and, when the forward kept none, its sliced y = K_raw [norm] Q_t
+    std::vector<float *> adjF, adjY;
     float *wideF = nullptr;  // more than 32 labels: the Matrix terms' sliced messages (WideArgs::F)
     size_t wideF_cap = 0;
     float *bw[14] = {};     // adjoint work buffers, [nslots][MP] each
@@ -988,8 +991,9 @@ int flush_norms(dcrf_crf *h) {
     for (size_t q = 0; q < which.size(); q++) {
         Term &T = h->terms[which[q]];
         a.ts.t[q].V = v1_buffer(h, T, T.V[(T.d + 1) & 1]);
-        const bool fold = T.ntype == DCRF_NORMALIZE_SYMMETRIC || T.ntype == DCRF_NORMALIZE_BEFORE;
-        a.wn_out[q] = fold ? T.mem_wn : nullptr;
+        // the forward (SYMMETRIC, BEFORE) or the transpose (SYMMETRIC, AFTER)
+        // normalises before its splat
+        a.wn_out[q] = T.ntype != DCRF_NO_NORMALIZATION ? T.mem_wn : nullptr;
     }
     CU(pp(h, a, 1));
     return DCRF_OK;
@@ -1092,6 +1096,8 @@ int ensure_wide_bufs(dcrf_crf *h) {
     const size_t need = nmat * (size_t)h->nslots * h->MP;
     if (need > h->wideF_cap) {
         dev_free_async(h->wideF, h->stream);
+    for (auto *v : {&h->adjF, &h->adjY})
+        for (float *p : *v) dev_free_async(p, h->stream);
     dev_free_async(h->L_d, h->stream);
     dev_free_async(h->f_d, h->stream);
         h->wideF = nullptr;
@@ -1395,13 +1401,15 @@ int ensure_adjoint_bufs(dcrf_crf *h, Term &T) {
 
 // S (vertex rows) = splat of the slot rows x with the plain barycentric weights
 // (the splat of Permutohedral::compute, permutohedral.cpp:545-553).
-int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1) {
+// With prenorm, the splat of norm .* x, through the member weights that carry
+// the norm of their point (the term must be normalised).
+int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1, bool prenorm = false) {
     Term &T = h->terms[k];
     const int MP = value1 ? 1 : h->MP;
     std::vector<int> one{k};
     PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, false, value1);
     a.ts.t[0].pre_norm = 0;
-    a.ts.t[0].mem_w = T.lat.mem_w;
+    a.ts.t[0].mem_w = prenorm ? T.mem_wn : T.lat.mem_w;
     a.Qin = x;
     CU(pp(h, a, MP));
     ReduceArgs ra{};
@@ -1671,6 +1679,8 @@ int dcrf_destroy(dcrf_crf *h) {
     dev_free_async(h->dpart, h->stream);
     dev_free_async(h->dacc, h->stream);
     dev_free_async(h->wideF, h->stream);
+    for (auto *v : {&h->adjF, &h->adjY})
+        for (float *p : *v) dev_free_async(p, h->stream);
     dev_free_async(h->L_d, h->stream);
     dev_free_async(h->f_d, h->stream);
     for (void *p : {(void *)h->status, (void *)h->bar, (void *)h->U, (void *)h->Q, (void *)h->tmp,
@@ -2514,8 +2524,16 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
         nacc += (size_t)Tk.d * Tk.d;
         maxd = std::max(maxd, Tk.d);
     }
-    const size_t npart = std::max((size_t)label_products_blocks(ns) * M * M,
-                                  (size_t)kernel_param_blocks(h->N) * maxd * maxd);
+    // label products: one partial block per term, added up over the iterations
+    // and reduced once at the end
+    const size_t lpb = std::max((size_t)label_products_blocks(ns), (size_t)h->ntiles);
+    std::vector<size_t> lpoff(nt);
+    size_t nlp = 0;
+    for (int k = 0; k < nt; k++) {
+        lpoff[k] = nlp;
+        nlp += lpb * (h->terms[k].ckind == DCRF_COMPAT_MATRIX ? (size_t)M * M : (size_t)M);
+    }
+    const size_t npart = std::max(want_compat ? nlp : 0, (size_t)kernel_param_blocks(h->N) * maxd * maxd);
     if (npart > h->dpart_cap) {
         dev_free_async(h->dpart, h->stream);
         h->dpart = nullptr;
@@ -2536,7 +2554,7 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
                 CU(cudaMemsetAsync(Tk.df, 0, sizeof(float) * (size_t)h->N * Tk.d, h->stream));
             }
     // slot-row work buffers
-    float *b = h->bw[0], *g = h->bw[1], *du = h->bw[2], *xn = h->bw[3], *F = h->bw[4], *Fn = h->bw[5],
+    float *b = h->bw[0], *g = h->bw[1], *du = h->bw[2], *xn = h->bw[3], *Fn = h->bw[5],
           *y = h->bw[6], *cq = h->bw[8], *yn = h->bw[9], *fb = h->bw[10], *c1 = h->bw[11];
     float *x1 = h->bw1[0], *ones1 = h->bw1[1];
     CU(launch_fill(ones1, 1.f, 1, ns, h->slot_pt, h->stream));
@@ -2555,9 +2573,23 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
     if ((rc = load_mn(h, dQ, layout, where, g))) return rc;
     CU(launch_softmax_adjoint(h->ckpt + (size_t)T * qsz, g, b, nullptr, M, ns, h->slot_pt, h->stream));
     CU(cudaMemcpyAsync(du, b, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+    // rows of 4k labels: the per-point work of an iteration in one tile pass
+    // (launch_adjoint_tile), the next b into a second buffer
+    const bool fused = h->MP % 4 == 0;
+    float *bnext = h->bw[12];
+    if (fused) {
+        for (auto *v : {&h->adjF, &h->adjY})
+            if (v->size() < (size_t)nt) v->resize(nt, nullptr);
+        for (int k = 0; k < nt; k++) {
+            if (!want_kernel || h->terms[k].ktype == DCRF_CONST_KERNEL) continue;
+            if (!h->adjF[k] && (rc = dev_alloc_async(&h->adjF[k], qsz, h->stream))) return rc;
+            if (!h->adjY[k] && !(h->cky && h->cky_off[k] >= 0) && (rc = dev_alloc_async(&h->adjY[k], qsz, h->stream)))
+                return rc;
+        }
+    }
     for (int it = T - 1; it >= 0; it--) {
         const float *Qt = h->ckpt + (size_t)it * qsz;
-        CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
+        if (!fused) CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
         // x~ = b with the transpose's first normalisation (per term)
         auto xtilde = [&](Term &Tk) -> const float * {
             if (!tr_pre(Tk)) return b;
@@ -2573,9 +2605,8 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
             const size_t rows = (size_t)Tk.lat.L + 1;
             const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];  // forward splat of Q_t
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
-            const float *xs = xtilde(Tk);
-            if (!xs) return set_err(DCRF_ERR_CUDA, "scale launch failed");
-            if ((rc = splat_into(h, k, xs, Tk.bv[0], false))) return rc;
+            // S_b = splat of x~ = norm .* b when the transpose starts normalised (the norm in the weights)
+            if ((rc = splat_into(h, k, b, Tk.bv[0], false, tr_pre(Tk)))) return rc;
             chains.push_back(Chain{k, Tk.bv[0], {Tk.V[1], Tk.V[0]}, Tk.bv[1], true});
             if (kgrad) {
                 CU(launch_compat(St, Tk.bv[2], M, (int)rows, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
@@ -2584,38 +2615,79 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
             }
         }
         if ((rc = blur_chains(h, chains, false))) return rc;
-        // phase 2, per term: slices and gradient contractions
+        // phase 2: per term F = K_raw^T x~ and Fp = K^T b = [norm .*] F, g += C^T Fp
+        // (applyTranspose, pairwise.cpp:179-183; the compatibilities are
+        // symmetric), the compatibility gradients sum b (K Q_t)^T = sum (K^T b)
+        // Q_t^T (PairwisePotential::gradient, pairwise.cpp:190-195), then the
+        // next b from g; then the kernel gradients of the terms that have them
+        auto need_F_of = [&](const Term &Tk) {
+            return want_kernel && Tk.ktype != DCRF_CONST_KERNEL &&
+                   (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_BEFORE);
+        };
+        // y = K_raw [norm] Q_t of each term with kernel gradients (SYMMETRIC,
+        // AFTER): kept by the forward, else sliced from its blurred lattice
+        std::vector<const float *> yk(nt, nullptr);
+        for (int k = 0; k < nt; k++) {
+            Term &Tk = h->terms[k];
+            const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
+            if (!kgrad || !(Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER)) continue;
+            if (h->cky && h->cky_off[k] >= 0) {
+                yk[k] = h->cky + h->cky_off[k] + (size_t)it * qsz;
+            } else {
+                float *yb = fused ? h->adjY[k] : h->bw[6];
+                const float *Bt = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k] + ((size_t)Tk.lat.L + 1) * h->MP;
+                if ((rc = slice_from(h, k, Bt, yb, false))) return rc;
+                yk[k] = yb;
+            }
+        }
+        if (fused) {
+            AdjArgs aa{};
+            aa.N = h->N;
+            aa.M = M;
+            aa.nslots = ns;
+            aa.ntiles = h->ntiles;
+            aa.slot_pt = h->slot_pt;
+            aa.Qt = Qt;
+            aa.b_next = bnext;
+            aa.du = du;
+            aa.lp_accum = it < T - 1 ? 1 : 0;
+            aa.n = nt;
+            aa.ts.n = nt;
+            for (int k = 0; k < nt; k++) {
+                Term &Tk = h->terms[k];
+                aa.ts.t[k] = term_dev(h, Tk, true, false);
+                aa.a[k].A = Tk.bv[1];
+                aa.a[k].post = tr_post(Tk) ? 1 : 0;
+                aa.a[k].Fraw = need_F_of(Tk) ? h->adjF[k] : nullptr;
+                aa.a[k].lp = want_compat ? h->dpart + lpoff[k] : nullptr;
+                aa.a[k].lp_mode = Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0;
+            }
+            ProfScope ps(h, DCRF_KCLASS_OTHER);
+            CU(launch_adjoint_tile(aa, h->MP, h->stream));
+        }
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];
             const size_t rows = (size_t)Tk.lat.L + 1;
             const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];
             const float *Bt = St + rows * h->MP;  // the forward's blurred lattice of Q_t
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
-            // F = K_raw^T x~ and Fp = K^T b = [norm .*] F; g += C^T Fp
-            // (applyTranspose, pairwise.cpp:179-183; the compatibilities are symmetric)
-            const bool need_F =
-                kgrad && (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_BEFORE);
-            if ((rc = slice_from(h, k, Tk.bv[1], need_F ? F : nullptr, false, tr_post(Tk), want_compat ? Fn : nullptr,
-                                 g)))
-                return rc;
-            if (want_compat) {  // PairwisePotential::gradient (pairwise.cpp:190-195): sum b (K Q_t)^T = sum (K^T b) Q_t^T
-                CU(launch_label_products(Fn, Qt, M, ns, h->slot_pt, Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0, h->dpart,
-                                         h->dacc + coff[k], 1, h->stream));
+            const bool need_F = need_F_of(Tk);
+            float *F = fused && need_F ? h->adjF[k] : h->bw[4];
+            if (!fused) {
+                if ((rc = slice_from(h, k, Tk.bv[1], need_F ? F : nullptr, false, tr_post(Tk),
+                                     want_compat ? Fn : nullptr, g)))
+                    return rc;
+                if (want_compat)
+                    CU(launch_label_products_part(Fn, Qt, M, ns, h->slot_pt, Tk.ckind == DCRF_COMPAT_MATRIX ? 1 : 0,
+                                                  h->dpart + lpoff[k], it < T - 1 ? 1 : 0, h->stream));
             }
             if (!kgrad) continue;
             // kernelGradient (pairwise.cpp:202-207) through featureGradient (87-114)
             // y = K_raw [norm] Q_t: kept by the forward, else sliced from its blurred lattice
-            const bool need_y = Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER;
-            const float *yt = y;
-            if (need_y) {
-                if (h->cky && h->cky_off[k] >= 0)
-                    yt = h->cky + h->cky_off[k] + (size_t)it * qsz;
-                else if ((rc = slice_from(h, k, Bt, y, false)))
-                    return rc;
-            }
+            const float *yt = yk[k] ? yk[k] : y;
             const float *xs = xtilde(Tk);
             if (!xs) return set_err(DCRF_ERR_CUDA, "scale launch failed");
-            if (h->MP % 4 == 0) {
+            if (fused) {
                 // y~ = [norm] C Q_t and the normalisation's coefficients in one pass
                 CU(launch_norm_terms(b, yt, F, Qt, Tk.norm, M, ns, Tk.ntype, Tk.ckind, Tk.potts_w, Tk.compat, yn, x1,
                                      h->stream));
@@ -2656,8 +2728,18 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
             }
         }
         // b = -dL/dA_t (densecrf.cpp:290)
-        CU(launch_softmax_adjoint(Qt, g, b, du, M, ns, h->slot_pt, h->stream));
+        if (fused)
+            std::swap(b, bnext);
+        else
+            CU(launch_softmax_adjoint(Qt, g, b, du, M, ns, h->slot_pt, h->stream));
     }
+    if (want_compat && T > 0)
+        for (int k = 0; k < nt; k++) {
+            const int K = h->terms[k].ckind == DCRF_COMPAT_MATRIX ? M * M : M;
+            // the fused pass leaves one partial per tile, the separate products one per LP block
+            CU(launch_sum_parts_bm(h->dpart + lpoff[k], fused ? h->ntiles : (int)lpb, K, h->dacc + coff[k], 0,
+                                   h->stream));
+        }
     if (dU && (rc = store_mn(h, du, dU, layout, where))) return rc;
     h->du_version = h->version;
     if (want_kernel)

@@ -37,6 +37,7 @@
 #include <atomic>
 
 #include "meanfield.cuh"
+#include "labelprod.cuh"
 
 namespace dcrf {
 
@@ -987,6 +988,146 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
 #pragma unroll
         for (int m = 0; m < MP; m++) gv[m] = m < M ? -neg[m] : 0.f;
         store_row<MP>(a.Gacc + s * MP, gv);
+    }
+}
+
+// See AdjArgs.  Dynamic shared memory: the tile's Q_t rows and F' rows
+// (SPLAT_TILE x MP each), the products' group sums, and every Matrix term's
+// compatibility as [k][MP].
+// Floats of the products' group sums, rounded up to 16 bytes: the Matrix
+// compatibilities after them are read as float4 rows.
+__host__ __device__ inline int adj_group_words(int M) {
+    const int w0 = block_label_products_words(M, 0), w1 = block_label_products_words(M, 1);
+    return ((w0 > w1 ? w0 : w1) + 3) & ~3;
+}
+
+template <int MP>
+__global__ void __launch_bounds__(SPLAT_TILE) adjoint_tile_kernel(const __grid_constant__ AdjArgs a) {
+    extern __shared__ __align__(16) float adj_smem[];
+    float *sQ = adj_smem, *sF = sQ + SPLAT_TILE * MP, *sG = sF + SPLAT_TILE * MP;
+    float *sCT = sG + adj_group_words(a.M);
+    const int M = a.M, N = a.N;
+    {  // Matrix compatibilities, transposed into [k][MP] (zero padded); symmetric, so equal
+        int j = 0;
+        for (int k = 0; k < a.ts.n; k++) {
+            const TermDev &T = a.ts.t[k];
+            if (T.ckind != DCRF_COMPAT_MATRIX) continue;
+            for (int e = threadIdx.x; e < MP * MP; e += blockDim.x) {
+                const int kk = e / MP, m = e - kk * MP;
+                sCT[j * MP * MP + e] = (kk < M && m < M) ? T.compat[(size_t)m * M + kk] : 0.f;
+            }
+            j++;
+        }
+    }
+    const size_t s = (size_t)blockIdx.x * SPLAT_TILE + threadIdx.x;
+    const int i = a.slot_pt[s];
+    const bool ok = i >= 0;
+    float q[MP];
+    if (ok)
+        load_row<MP>(a.Qt + s * MP, q);
+    else
+#pragma unroll
+        for (int m = 0; m < MP; m++) q[m] = 0.f;
+    store_row<MP>(sQ + threadIdx.x * MP, q);
+    float x[MP];  // -g: x -= C F' per term
+#pragma unroll
+    for (int m = 0; m < MP; m++) x[m] = 0.f;
+    __syncthreads();
+    int jm = 0;
+    for (int k = 0; k < a.ts.n; k++) {
+        const TermDev &T = a.ts.t[k];
+        const AdjArgs::T &A = a.a[k];
+        float acc[MP];
+#pragma unroll
+        for (int m = 0; m < MP; m++) acc[m] = 0.f;
+        if (ok) {
+            for (int r = 0; r <= T.d; r++) {
+                const int o = T.off[(size_t)r * N + i] + 1;
+                float v[MP];
+                load_row<MP>(A.A + (size_t)o * MP, v);
+                if (T.seq) {  // (w * v) * alpha, then the sum (permutohedral.cpp:513-521)
+                    const float w = T.bary[(size_t)r * N + i];
+#pragma unroll
+                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(w, v[m]), T.alpha));
+                } else {  // (w * alpha) * v (permutohedral.cpp:579-581)
+                    const float w = T.wslice[(size_t)r * N + i];
+#pragma unroll
+                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < MP; m++)
+                if (m >= M) acc[m] = 0.f;
+            if (A.Fraw) store_row<MP>(A.Fraw + s * MP, acc);
+            if (A.post) {
+                const float nn = T.norm[s];
+#pragma unroll
+                for (int m = 0; m < MP; m++) acc[m] = fmul(acc[m], nn);
+            }
+            double unused = 0.0;
+            const bool mat = T.ckind == DCRF_COMPAT_MATRIX && MP % 4 == 0;
+            fold_compat<MP>(T, mat ? sCT + jm * MP * MP : nullptr, acc, x, M, false, unused);
+        }
+        if (T.ckind == DCRF_COMPAT_MATRIX) jm++;
+        if (A.lp) {  // sum over the tile of F' (x) Q_t (labelcompatibility.cpp:57-61,76-78,101-107)
+            store_row<MP>(sF + threadIdx.x * MP, acc);
+            __syncthreads();
+            const int K = A.lp_mode == 0 ? M : M * M;
+            block_label_products(sF, sQ, SPLAT_TILE, MP, M, A.lp_mode, sG, A.lp + (size_t)blockIdx.x * K, a.lp_accum);
+        }
+    }
+    if (!ok) return;
+    // b_next = softmax adjoint of g = -x at Q_t (densecrf.cpp:107-114, 290)
+    float dot = 0.f;
+#pragma unroll
+    for (int m = 0; m < MP; m++)
+        if (m < M) dot = fmaf(-x[m], q[m], dot);
+    float o[MP];
+#pragma unroll
+    for (int m = 0; m < MP; m++) o[m] = m < M ? fmaf(q[m], dot, x[m] * q[m]) : 0.f;
+    store_row<MP>(a.b_next + s * MP, o);
+    if (a.du) {
+        float u[MP];
+        load_row<MP>(a.du + s * MP, u);
+#pragma unroll
+        for (int m = 0; m < MP; m++) u[m] += o[m];
+        store_row<MP>(a.du + s * MP, u);
+    }
+}
+
+template <int MP>
+static cudaError_t adj_launch(const AdjArgs &a, cudaStream_t s) {
+    int nmat = 0;
+    for (int k = 0; k < a.ts.n; k++) nmat += a.ts.t[k].ckind == DCRF_COMPAT_MATRIX ? 1 : 0;
+    const size_t words = 2 * (size_t)SPLAT_TILE * MP + adj_group_words(a.M) + (size_t)nmat * MP * MP;
+    const size_t smem = words * sizeof(float);
+    static std::atomic<uint64_t> opted{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const uint64_t bit = dev < 64 ? 1ull << dev : 0;
+    if (smem > 48 * 1024 && !(opted.load() & bit)) {
+        cudaError_t e = cudaFuncSetAttribute(adjoint_tile_kernel<MP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             POINTPASS_SMEM_MAX);
+        if (e != cudaSuccess) return e;
+        opted.fetch_or(bit);
+    }
+    if (smem > (size_t)POINTPASS_SMEM_MAX) return cudaErrorInvalidValue;
+    DCRF_LAUNCH(adjoint_tile_kernel<MP><<<a.ntiles, SPLAT_TILE, smem, s>>>(a));
+    return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint_tile(const AdjArgs &a, int MP, cudaStream_t s) {
+    if (a.ntiles <= 0) return cudaSuccess;
+    switch (MP) {
+        case 4: return adj_launch<4>(a, s);
+        case 8: return adj_launch<8>(a, s);
+        case 12: return adj_launch<12>(a, s);
+        case 16: return adj_launch<16>(a, s);
+        case 20: return adj_launch<20>(a, s);
+        case 24: return adj_launch<24>(a, s);
+        case 28: return adj_launch<28>(a, s);
+        case 32: return adj_launch<32>(a, s);
+        default: return cudaErrorInvalidValue;
     }
 }
 

@@ -74,6 +74,32 @@ struct WideArgs {
 };
 cudaError_t launch_wide(const WideArgs &a, cudaStream_t s);
 
+// One iteration of the adjoint's per-point work (DenseCRF::gradient,
+// densecrf.cpp:271-290) for all terms, one CTA per tile (a thread per slot):
+// per term F = the raw slice of its reverse-blurred splat A (vertex order,
+// permutohedral.cpp:574-584), F' = [norm .*] F (the transpose's last
+// normalisation, pairwise.cpp:78-79), g += C F' (C symmetric, so C^T = C), and
+// the compatibility-gradient products sum F' (x) Q_t per tile; then
+// b_next = the softmax adjoint of g at Q_t and du += b_next.
+struct AdjArgs {
+    int N, M, nslots, ntiles;
+    const int *slot_pt;
+    const float *Qt;    // [nslots][MP] the iterate Q_t
+    float *b_next;      // [nslots][MP]
+    float *du;          // [nslots][MP], += b_next
+    int lp_accum;       // add to the products' partials (not the first iteration)
+    int n;
+    struct T {
+        const float *A;  // [L+1][MP]
+        int post;        // F' = norm .* F
+        float *Fraw;     // F stored when non-null (kernel gradients)
+        double *lp;      // [ntiles][K] products' partials, null: not wanted
+        int lp_mode;     // 0: per label (Potts, Diagonal), 1: outer (Matrix)
+    } a[DCRF_MAX_TERMS];
+    TermSet ts;          // off, bary, wslice, alpha, seq, d, compatibility, norm of every term
+};
+cudaError_t launch_adjoint_tile(const AdjArgs &a, int MP, cudaStream_t s);
+
 struct ReduceArgs {
     int n;  // number of terms
     struct T {
