@@ -716,7 +716,9 @@ PPArgs pp_args(dcrf_crf *h, int mode, const std::vector<int> &which, bool transp
         a.ntype[k] = T.ntype;
         a.norm_out[k] = T.norm;
     }
-    a.split = pick_split(h, value1, MPc);
+    // without messages there is no compatibility product: two threads per
+    // point give the splat twice the lane groups
+    a.split = (mode & PP_MSG) || value1 || MPc % 8 != 0 ? pick_split(h, value1, MPc) : 2;
     plan_smem(h, a, which, (mode & PP_MSG) != 0, MPc);
     return a;
 }
