@@ -242,6 +242,16 @@ int dcrf_param_counts(dcrf_crf *h, int term, int *n_compat, int *n_kernel);
  * densecrf.cpp:240-253). */
 int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int layout, int where);
 
+/* Memory of the checkpointed forward: with every = k > 1, only the iterates
+ * Q_0, Q_k, Q_2k, ... and Q_T are kept, and dcrf_backward recomputes each
+ * k-iteration segment from its first iterate before taking it apart (the
+ * recomputed iterates equal the forward's bit for bit).  Iterate storage goes
+ * from T+1 rows to T/k + 2 rows plus k+1 for the segment, the per-step lattice
+ * and slice storage from T steps to k; the forward's kernels run once more.
+ * every = 1 (the default) keeps every iterate, as DenseCRF::gradient does
+ * (densecrf.cpp:240-253).  Applies from the next dcrf_inference_checkpointed. */
+int dcrf_set_checkpoint_interval(dcrf_crf *h, int every);
+
 /* Adjoint of the last dcrf_inference_checkpointed (DenseCRF::gradient,
  * densecrf.cpp:255-296, for any loss): given dQ = dL/dQ_T (M x N in `layout`,
  * `where`), writes dU = dL/dU (same layout and place; NULL to skip), and, on the

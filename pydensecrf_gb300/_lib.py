@@ -86,6 +86,7 @@ _SIGS = {
     "dcrf_kernel_parameters": ([_vp, _vp, _i, _pi], _i),
     "dcrf_set_kernel_parameters": ([_vp, _vp, _i], _i),
     "dcrf_unary_gradient": ([_vp, _vp, _i, _pi], _i),
+    "dcrf_set_checkpoint_interval": ([_vp, _i], _i),
 }
 
 _LIB = None

@@ -118,6 +118,7 @@ class DenseCRFBatch:
     autotune = DenseCRF.autotune
     tuning = DenseCRF.tuning
     set_tuning = DenseCRF.set_tuning
+    setCheckpointInterval = DenseCRF.setCheckpointInterval
 
     # -- inference ------------------------------------------------------------------
     def _flat(self) -> np.ndarray:

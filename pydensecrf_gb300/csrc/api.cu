@@ -212,8 +212,14 @@ struct dcrf_crf {
     unsigned long long version = 0, ckpt_version = ~0ull;
     unsigned long long du_version = ~0ull;  // model version whose dL/dU bw[2] holds (after dcrf_backward)
     int ckpt_T = -1;
-    float *ckpt = nullptr;  // [(T+1)][nslots][MP]
+    float *ckpt = nullptr;  // [(T+1)][nslots][MP]; with an interval k > 1: Q_0, Q_k, Q_2k, ..., then Q_T
     size_t ckpt_cap = 0;
+    // checkpoint interval (dcrf_set_checkpoint_interval) and the one the last
+    // dcrf_inference_checkpointed used; with k > 1 the backward recomputes each
+    // segment's iterates into segq ([k+1][nslots][MP]) and ckv / cky (k steps)
+    int ckpt_every = 1, ckpt_every_used = 1;
+    float *segq = nullptr;
+    size_t segq_cap = 0;
     // per iteration t < T and term k: the forward's splat S and blurred lattice
     // B of Q_t, each [L_k+1][MP], at ckv + t * ckv_iter + ckv_off[k] (+ (L_k+1)*MP for B)
     float *ckv = nullptr;
@@ -1184,6 +1190,58 @@ int issue_inference(dcrf_crf *h, int T, int final_mode, float *ckpt = nullptr) {
     return DCRF_OK;
 }
 
+// n mean-field iterations from Q_start (device slot rows; null: softmax(-U)).
+// With ckq (n+1 rows) every iterate Q_0..Q_n of the range is written there and,
+// with ckv / cky, the splats and blurred lattices / sliced values of its steps
+// (the layout of dcrf_inference_checkpointed, relative to the range); without
+// ckq only the last iterate, into q_last.  The arithmetic is the forward's, so
+// a range recomputed from a stored iterate reproduces its iterates bit for bit.
+int issue_steps(dcrf_crf *h, const float *Qstart, int n, float *ckq, float *ckv, float *cky, float *q_last) {
+    std::vector<int> w = all_terms(h);
+    const size_t qsz = (size_t)h->MP * h->nslots;
+    int rc;
+    if (n <= 0 || w.empty()) {  // every iterate equals the start
+        float *dst = ckq ? ckq : q_last;
+        if (Qstart) {
+            CU(cudaMemcpyAsync(dst, Qstart, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+        } else {
+            PPArgs a = pp_args(h, PP_WRITE_Q, w, false, false);
+            a.Qout = dst;
+            CU(pp(h, a, h->MP));
+        }
+        for (int it = 1; ckq && it <= n; it++)
+            CU(cudaMemcpyAsync(ckq + it * qsz, ckq, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+        if (!ckq && n > 0 && q_last != dst)
+            CU(cudaMemcpyAsync(q_last, dst, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+        return DCRF_OK;
+    }
+    {
+        PPArgs a = pp_args(h, PP_SPLAT | (Qstart ? PP_LOAD_Q : 0) | (ckq ? PP_WRITE_Q : 0), w, false, false);
+        if (Qstart) a.Qin = Qstart;
+        if (ckq) a.Qout = ckq;
+        CU(pp(h, a, h->MP));
+    }
+    for (int it = 1; it <= n; it++) {
+        if (ckv) {
+            float *S[DCRF_MAX_TERMS], *B[DCRF_MAX_TERMS];
+            for (size_t k = 0; k < w.size(); k++) {
+                S[k] = ckv + (size_t)(it - 1) * h->ckv_iter + h->ckv_off[w[k]];
+                B[k] = S[k] + ((size_t)h->terms[w[k]].lat.L + 1) * h->MP;
+            }
+            if ((rc = filter_phase(h, w, false, false, true, S, B))) return rc;
+        } else if ((rc = filter_phase(h, w, false, false, true))) {
+            return rc;
+        }
+        PPArgs a = pp_args(h, PP_MSG | (it < n ? PP_SPLAT : 0) | (ckq || it == n ? PP_WRITE_Q : 0), w, false, false);
+        a.Qout = ckq ? ckq + it * qsz : q_last;
+        if (ckq && cky)
+            for (size_t k = 0; k < w.size(); k++)
+                if (h->cky_off[w[k]] >= 0) a.ckY[k] = cky + h->cky_off[w[k]] + (size_t)(it - 1) * qsz;
+        CU(pp(h, a, h->MP));
+    }
+    return DCRF_OK;
+}
+
 // Runs issue_inference as one CUDA graph: captured on the handle's capture
 // stream, instantiated once and afterwards updated in place (same kernels,
 // new arguments), launched on the handle's stream.  Profiling launches the
@@ -1674,6 +1732,7 @@ int dcrf_destroy(dcrf_crf *h) {
     h->event_pool.clear();
     for (Term &T : h->terms) free_term(h, T);
     dev_free_async(h->ckpt, h->stream);
+    dev_free_async(h->segq, h->stream);
     dev_free_async(h->ckv, h->stream);
     dev_free_async(h->cky, h->stream);
     for (float *&b : h->bw) dev_free_async(b, h->stream);
@@ -2435,12 +2494,33 @@ int dcrf_param_counts(dcrf_crf *h, int term, int *n_compat, int *n_kernel) {
     return ok();
 }
 
+int dcrf_set_checkpoint_interval(dcrf_crf *h, int every) {
+    int rc = check_handle(h);
+    if (rc) return rc;
+    if (every < 1) return set_err(DCRF_ERR_INVALID_ARG, "the checkpoint interval must be at least 1");
+    h->ckpt_every = every;
+    return ok();
+}
+
 int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int layout, int where) {
     int rc = check_ready(h);
     if (rc) return rc;
     if (is_wide(h)) return wide_unsupported("the adjoint (dcrf_inference_checkpointed / dcrf_backward)");
     if (!Q || n_iterations < 0) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
-    const size_t qsz = (size_t)h->MP * h->nslots, need = qsz * ((size_t)n_iterations + 1);
+    const int every = std::max(1, std::min(h->ckpt_every, std::max(1, n_iterations)));
+    const size_t qsz = (size_t)h->MP * h->nslots;
+    // stored iterates: all of them, or Q_0, Q_k, ... and Q_T; the steps kept
+    // (splats, blurred lattices, sliced values): all, or one segment's
+    const size_t nstore = every > 1 ? (size_t)n_iterations / every + 2 : (size_t)n_iterations + 1;
+    const size_t kept = every > 1 ? (size_t)every : (size_t)n_iterations;
+    const size_t need = qsz * nstore;
+    if (every > 1 && qsz * (kept + 1) > h->segq_cap) {
+        dev_free_async(h->segq, h->stream);
+        h->segq = nullptr;
+        h->segq_cap = 0;
+        if ((rc = dev_alloc_async(&h->segq, qsz * (kept + 1), h->stream))) return rc;
+        h->segq_cap = qsz * (kept + 1);
+    }
     if (need > h->ckpt_cap) {
         dev_free_async(h->ckpt, h->stream);
         h->ckpt = nullptr;
@@ -2455,7 +2535,7 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
         h->ckv_off[k] = per_it;
         per_it += 2 * ((size_t)h->terms[k].lat.L + 1) * h->MP;
     }
-    const size_t vneed = std::max<size_t>(per_it * (size_t)n_iterations, 1);
+    const size_t vneed = std::max<size_t>(per_it * kept, 1);
     bool fresh = per_it != h->ckv_iter;
     h->ckv_iter = per_it;
     if (vneed > h->ckv_cap) {
@@ -2475,7 +2555,7 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
         if (Tk.ktype != DCRF_CONST_KERNEL &&
             (Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER)) {
             h->cky_off[k] = (long long)ny;
-            ny += qsz * (size_t)n_iterations;
+            ny += qsz * kept;
         }
     }
     if (ny > h->cky_cap) {
@@ -2490,10 +2570,27 @@ int dcrf_inference_checkpointed(dcrf_crf *h, int n_iterations, float *Q, int lay
     for (const Term &Tk : h->terms) sig.push_back((size_t)Tk.lat.L);
     if (fresh || h->ckv_layout != sig) CU(cudaMemsetAsync(h->ckv, 0, sizeof(float) * vneed, h->stream));
     h->ckv_layout = sig;
-    if ((rc = run_inference(h, n_iterations, 0, h->ckpt))) return rc;
-    if ((rc = store_mn(h, h->ckpt + (size_t)n_iterations * qsz, Q, layout, where))) return rc;
+    const float *qT;
+    if (every == 1) {
+        if ((rc = run_inference(h, n_iterations, 0, h->ckpt))) return rc;
+        qT = h->ckpt + (size_t)n_iterations * qsz;
+    } else {  // segments of `every` iterations, each stored iterate the start of the next
+        if ((rc = maybe_autotune(h)) || (rc = flush_norms(h))) return rc;
+        float *last = h->ckpt + (nstore - 1) * qsz;
+        if ((rc = issue_steps(h, nullptr, 0, nullptr, nullptr, nullptr, h->ckpt))) return rc;
+        for (int j = 0, t0 = 0; t0 < n_iterations; j++, t0 += every) {
+            const int n = std::min(every, n_iterations - t0);
+            float *dst = t0 + n == n_iterations ? last : h->ckpt + (size_t)(j + 1) * qsz;
+            if ((rc = issue_steps(h, h->ckpt + (size_t)j * qsz, n, nullptr, nullptr, nullptr, dst))) return rc;
+        }
+        if (n_iterations == 0)
+            CU(cudaMemcpyAsync(last, h->ckpt, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
+        qT = last;
+    }
+    if ((rc = store_mn(h, qT, Q, layout, where))) return rc;
     if ((rc = sync_check(h))) return rc;
     h->ckpt_T = n_iterations;
+    h->ckpt_every_used = every;
     h->ckpt_version = h->version;
     return ok();
 }
@@ -2573,7 +2670,9 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
     }
     // seed: b = -dL/dA_T from dL/dQ_T (densecrf.cpp:256-258)
     if ((rc = load_mn(h, dQ, layout, where, g))) return rc;
-    CU(launch_softmax_adjoint(h->ckpt + (size_t)T * qsz, g, b, nullptr, M, ns, h->slot_pt, h->stream));
+    const int every = h->ckpt_every_used;
+    const float *qT = every > 1 ? h->ckpt + ((size_t)T / every + 1) * qsz : h->ckpt + (size_t)T * qsz;
+    CU(launch_softmax_adjoint(qT, g, b, nullptr, M, ns, h->slot_pt, h->stream));
     CU(cudaMemcpyAsync(du, b, qsz * sizeof(float), cudaMemcpyDeviceToDevice, h->stream));
     // rows of 4k labels: the per-point work of an iteration in one tile pass
     // (launch_adjoint_tile), the next b into a second buffer
@@ -2589,8 +2688,23 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
                 return rc;
         }
     }
+    // iterations in segments: all at once, or (interval k) the k-step segments
+    // from the last, each recomputed from its stored first iterate
+    int t0 = T, seg_end = T;
+    const float *segQ = h->ckpt;
     for (int it = T - 1; it >= 0; it--) {
-        const float *Qt = h->ckpt + (size_t)it * qsz;
+        if (it < t0) {
+            seg_end = it + 1;
+            t0 = every > 1 ? (it / every) * every : 0;
+            if (every > 1) {
+                if ((rc = issue_steps(h, h->ckpt + (size_t)(t0 / every) * qsz, seg_end - t0, h->segq, h->ckv, h->cky,
+                                      nullptr)))
+                    return rc;
+                segQ = h->segq;
+            }
+        }
+        const int rel = it - t0;  // the step within the segment's stored data
+        const float *Qt = segQ + (size_t)rel * qsz;
         if (!fused) CU(cudaMemsetAsync(g, 0, qsz * sizeof(float), h->stream));
         // x~ = b with the transpose's first normalisation (per term)
         auto xtilde = [&](Term &Tk) -> const float * {
@@ -2605,7 +2719,7 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];
             const size_t rows = (size_t)Tk.lat.L + 1;
-            const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];  // forward splat of Q_t
+            const float *St = h->ckv + (size_t)rel * h->ckv_iter + h->ckv_off[k];  // forward splat of Q_t
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
             // S_b = splat of x~ = norm .* b when the transpose starts normalised (the norm in the weights)
             if ((rc = splat_into(h, k, b, Tk.bv[0], false, tr_pre(Tk)))) return rc;
@@ -2634,10 +2748,10 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
             if (!kgrad || !(Tk.ntype == DCRF_NORMALIZE_SYMMETRIC || Tk.ntype == DCRF_NORMALIZE_AFTER)) continue;
             if (h->cky && h->cky_off[k] >= 0) {
-                yk[k] = h->cky + h->cky_off[k] + (size_t)it * qsz;
+                yk[k] = h->cky + h->cky_off[k] + (size_t)rel * qsz;
             } else {
                 float *yb = fused ? h->adjY[k] : h->bw[6];
-                const float *Bt = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k] + ((size_t)Tk.lat.L + 1) * h->MP;
+                const float *Bt = h->ckv + (size_t)rel * h->ckv_iter + h->ckv_off[k] + ((size_t)Tk.lat.L + 1) * h->MP;
                 if ((rc = slice_from(h, k, Bt, yb, false))) return rc;
                 yk[k] = yb;
             }
@@ -2670,7 +2784,7 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];
             const size_t rows = (size_t)Tk.lat.L + 1;
-            const float *St = h->ckv + (size_t)it * h->ckv_iter + h->ckv_off[k];
+            const float *St = h->ckv + (size_t)rel * h->ckv_iter + h->ckv_off[k];
             const float *Bt = St + rows * h->MP;  // the forward's blurred lattice of Q_t
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
             const bool need_F = need_F_of(Tk);

@@ -392,6 +392,11 @@ class DenseCRF:
         _lib.check(_lib.load().dcrf_info(self._h, None, None, ctypes.byref(n)))
         return n.value
 
+    def setCheckpointInterval(self, every: int) -> None:
+        """Keep every ``every``-th iterate in inferenceCheckpointed and recompute
+        the others segment by segment in backward() (1: keep all)."""
+        _lib.check(_lib.load().dcrf_set_checkpoint_interval(self._h, int(every)))
+
     def inferenceCheckpointed(self, niter: int) -> np.ndarray:
         """inference(niter) keeping every iterate on the device for backward();
         returns Q as an (M, N) array."""

@@ -158,3 +158,26 @@ def test_autograd_function(engine, oracle_mod):
     # the matrix gradient is symmetric (W = (m + m^T)/2)
     G = mt.grad.cpu().numpy()
     assert np.abs(G - G.T).max() <= 1e-6 * max(1e-12, np.abs(G).max())
+
+
+@pytest.mark.parametrize("every", [2, 3, 5, 8])
+def test_checkpoint_interval_recompute_matches_full_storage(engine, oracle_mod, every):
+    """Keeping only every k-th iterate and recomputing the segments in the
+    backward gives the gradients of full storage bit for bit (the recomputed
+    iterates are the forward's): unary, Matrix compatibility and DIAG kernel."""
+    O = oracle_mod
+    W, H, M, T, N, U, wt, fg, fb, rng = _fd_setup(O, 11)
+    mat = rng.uniform(0, 1, size=(M, M)).astype(np.float32)
+    dQ = np.ascontiguousarray(wt.T).astype(np.float32)
+    out = []
+    for k in (1, every):
+        crf = engine.DenseCRF(N, M)
+        crf.setCheckpointInterval(k)
+        crf.setUnaryEnergy(np.ascontiguousarray(U.T))
+        crf.addPairwiseEnergy(np.ascontiguousarray(fg.T), 3.0)
+        crf.addPairwiseEnergy(np.ascontiguousarray(fb.T), mat)
+        Q = crf.inferenceCheckpointed(T + 2)
+        dU, dcs, dks = crf.backward(dQ, want_compat=True, want_kernel=True)
+        out.append((Q, dU, np.concatenate(dcs), np.concatenate(dks)))
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a, b), (every, np.abs(a - b).max())
