@@ -624,7 +624,8 @@ def run_gpu(args):
     _lib.check(lib.dcrf_create_2d(W, H, M, ctypes.byref(h)))
     stream = torch.cuda.current_stream(dev)
     _lib.check(lib.dcrf_set_stream(h, ctypes.c_void_p(stream.cuda_stream)))
-    _lib.check(lib.dcrf_set_autotune(h, 1))  # tuned during the first warm-up step
+    if not args.fixed_knobs:
+        _lib.check(lib.dcrf_set_autotune(h, 1))  # tuned during the first warm-up step
     cg = np.array([3.0], np.float32)
     cb = np.array([10.0], np.float32)
 
@@ -674,7 +675,7 @@ def run_gpu(args):
         flush.zero_()
         step_device()
     prof = {}
-    for cls, name in ((0, "point"), (1, "reduce"), (2, "blur"), (3, "lattice"), (4, "other")):
+    for cls, name in ((0, "point"), (1, "reduce"), (2, "blur"), (3, "lattice"), (4, "other"), (5, "norm")):
         ms, n = ctypes.c_double(), ctypes.c_longlong()
         _lib.check(lib.dcrf_profile(h, cls, ctypes.byref(ms), ctypes.byref(n)))
         prof[name] = {"ms_per_step": ms.value / nprof, "launches_per_step": n.value // nprof,
@@ -710,6 +711,7 @@ def run_gpu(args):
                 "peak_kind": peak_kind}
     lat_s = prof["lattice"]["ms_per_step"] / 1e3
     lattice_roofline = {"bound": "latency (dependent launches, one host wait per term)",
+                        "scope": "the two lattice builds (Permutohedral::init); their normalisation is 'norm'",
                         "algorithmic_bytes_per_step": int(build_bytes), "ms_per_step": round(1e3 * lat_s, 4),
                         "achieved": round(build_bytes / lat_s / 1e9, 1), "peak": peak, "unit": "GB/s",
                         "frac": round(build_bytes / lat_s / 1e9 / peak, 4)}
@@ -815,6 +817,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-learning", action="store_true", help="skip the forward+backward timing")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-loop timing")
+    ap.add_argument("--fixed-knobs", action="store_true",
+                    help="no autotuning of the main solve (the default knobs; a fixed launch sequence for profilers)")
     ap.add_argument("--traffic", type=float, default=None,
                     help="DRAM bytes per point-pass launch from an ncu capture (reported as roofline.traffic)")
     args = ap.parse_args()

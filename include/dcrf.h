@@ -302,9 +302,10 @@ int dcrf_launch_count(unsigned long long *count);
 #define DCRF_KCLASS_POINT 0   /* slice + compatibility + softmax + tile splat */
 #define DCRF_KCLASS_REDUCE 1  /* per-vertex sum of the splat partials */
 #define DCRF_KCLASS_BLUR 2    /* one blur axis */
-#define DCRF_KCLASS_LATTICE 3 /* lattice build and its normalisation (all of their launches) */
+#define DCRF_KCLASS_LATTICE 3 /* lattice build (all of its launches) */
 #define DCRF_KCLASS_OTHER 4   /* layout conversions, feature generation */
-#define DCRF_NUM_KCLASSES 5
+#define DCRF_KCLASS_NORM 5    /* the kernel normalisation of new terms (DenseKernel::initLattice) */
+#define DCRF_NUM_KCLASSES 6
 
 /* on = 1: bracket every kernel launch of the handle with CUDA events on its
  * stream (adds a little overhead); 0: off.  Resets the accumulated profile. */

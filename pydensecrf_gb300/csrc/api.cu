@@ -984,12 +984,12 @@ int flush_norms(dcrf_crf *h) {
         if (h->terms[k].norm_pending) which.push_back((int)k);
     if (which.empty()) return DCRF_OK;
     for (int k : which) h->terms[k].norm_pending = false;
-    // profiled as part of the lattice build (DenseKernel::initLattice)
+    // profiled as a class of its own
     struct ForceClass {
         dcrf_crf *h;
         ~ForceClass() { h->prof_class = -1; }
     } force{h};
-    h->prof_class = DCRF_KCLASS_LATTICE;
+    h->prof_class = DCRF_KCLASS_NORM;
     PPArgs a = pp_args(h, PP_ONES | PP_SPLAT, which, false, true);
     for (size_t q = 0; q < which.size(); q++) a.ts.t[q].pre_norm = a.ts.t[q].post_norm = 0;
     CU(pp(h, a, 1));
