@@ -435,6 +435,23 @@ def learning_step_times(lib, _lib, dev, stream, reps: int = 2):
             "grads": "dU, dcompat (Potts + 21x21), dkernel (bilateral 5 scales)"}
 
 
+PHASES = ((0, "point"), (1, "reduce"), (2, "blur"), (3, "lattice"), (4, "other"), (5, "norm"))
+
+
+def phase_ms(handles, lib, _lib):
+    """Device milliseconds per kernel class recorded by the handles' profiling
+    mode, summed over the handles (profiling must be on while they ran)."""
+    out = {}
+    for cls, name in PHASES:
+        tot = 0.0
+        for h in handles:
+            ms, n = ctypes.c_double(), ctypes.c_longlong()
+            _lib.check(lib.dcrf_profile(h, cls, ctypes.byref(ms), ctypes.byref(n)))
+            tot += ms.value
+        out[name] = round(tot, 3)
+    return out
+
+
 def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
     """The batched form against a per-image loop on 64 uneven images
     (W, H ~ U[256, 1024], M=21, T=10, Gaussian sxy=3 + bilateral sxy=80
@@ -490,6 +507,11 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
         return float(np.median(ms))
 
     batch_ms = timed(lambda: solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all)))
+    # per-phase device time of one solve (profiling mode: events around every launch)
+    _lib.check(lib.dcrf_set_profiling(hb, 1))
+    solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all))
+    batch_phases = phase_ms([hb], lib, _lib)
+    _lib.check(lib.dcrf_set_profiling(hb, 0))
     c0, c1 = ctypes.c_ulonglong(), ctypes.c_ulonglong()
     lib.dcrf_launch_count(ctypes.byref(c0))
     solve(hb, ptr(U_all), ptr(img_all), ptr(Q_all))
@@ -516,6 +538,10 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
 
     loop_ms = timed(loop)
     for h in hs:
+        _lib.check(lib.dcrf_set_profiling(h, 1))
+    loop()
+    loop_phases = phase_ms(hs, lib, _lib)
+    for h in hs:
         lib.dcrf_destroy(h)
     same = bool(torch.equal(Qb, Q_all))
     units = Ntot * Mb * Tb / 1e6
@@ -525,6 +551,9 @@ def batched_vs_loop(lib, _lib, dev, stream, reps: int = 2, n_images: int = 64):
             "batched_value": round(units / (batch_ms / 1e3), 1), "loop_value": round(units / (loop_ms / 1e3), 1),
             "unit": "MPix*label*iter/s", "batched_launches": int(batch_launches),
             "batched_equals_loop": same,
+            # device time per kernel class of one solve, summed over the handles (profiling mode);
+            # the per-pixel classes (point, reduce, blur) bound what batching can remove
+            "breakdown_ms": {"batched": batch_phases, "loop": loop_phases},
             "tuning": {"split": knobs[0].value, "smem_kb": knobs[1].value, "task_len": knobs[2].value,
                        "hash_load": round(knobs[3].value, 2), "coop_blur": knobs[4].value}}
 
@@ -675,7 +704,7 @@ def run_gpu(args):
         flush.zero_()
         step_device()
     prof = {}
-    for cls, name in ((0, "point"), (1, "reduce"), (2, "blur"), (3, "lattice"), (4, "other"), (5, "norm")):
+    for cls, name in PHASES:
         ms, n = ctypes.c_double(), ctypes.c_longlong()
         _lib.check(lib.dcrf_profile(h, cls, ctypes.byref(ms), ctypes.byref(n)))
         prof[name] = {"ms_per_step": ms.value / nprof, "launches_per_step": n.value // nprof,

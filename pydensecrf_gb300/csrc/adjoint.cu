@@ -380,39 +380,53 @@ __global__ void sum_parts_kernel(const double *__restrict__ part, int nblk, int 
 // permutohedral.cpp:660-690): with V the blurred lattice of one direction and
 // z the contraction values, df[i][j-1] += sum_k z[k] * sf[j-1] * (sm_k - j * ra_j[k]),
 // ra_j = alpha/(d+1) * (V[off[r0]] - V[off[r1]]), r0 = d - rank_j, r1 = r0+1 mod (d+1),
-// sm the running sum of ra_0..ra_{j-1}.
-// Contribution of one (V, z) pair to the point's feature gradient grad[j-1].
+// sm the running sum of ra_0..ra_{j-1}.  Summed over the labels first:
+//   D_j = sum_k z[k] ra_j[k] = alpha * sum_k z[k] (V[r0][k] - V[r1][k])
+//   df[i][j-1] += sf[j-1] * (D_0 + ... + D_{j-1} - j D_j)
+// (the per-label differences are taken first, as in the per-label form), so a
+// thread keeps only the point's z row and streams the corner rows through it.
 template <int MP>
 __device__ __forceinline__ void slice_grad_pair(const SliceGradArgs &a, const float *V, const float *zrow, float alpha,
-                                                size_t s, int i, float (&grad)[DCRF_MAX_D]) {
+                                                const float *zscale, size_t s, int i, float (&grad)[DCRF_MAX_D]) {
+    constexpr int VW = MP % 4 == 0 ? 4 : 1;
     const int d = a.d, N = a.N, M = a.M;
     float z[MP];
     row_load<MP>(zrow + s * MP, z);
+    if (zscale) {
+        const float f = zscale[s];
+#pragma unroll
+        for (int m = 0; m < MP; m++) z[m] = z[m] * f;
+    }
 #pragma unroll
     for (int m = 0; m < MP; m++)
         if (m >= M) z[m] = 0.f;
-    float sm[MP];
+    // the row of corner r (row 0 is the zero sentinel)
+    auto row = [&](int r) -> const float * { return V + (size_t)(a.off[(size_t)r * N + i] + 1) * MP; };
+    float S = 0.f;  // D_0 + ... + D_{j-1}
+    // unrolled over the largest d so that grad[] stays in registers
 #pragma unroll
-    for (int m = 0; m < MP; m++) sm[m] = 0.f;
-    for (int j = 0; j <= d; j++) {
+    for (int j = 0; j <= DCRF_MAX_D; j++) {
+        if (j > d) break;
         const int r0 = d - (int)a.rank[(size_t)j * N + i];
         const int r1 = r0 + 1 > d ? 0 : r0 + 1;
-        float v0[MP], v1[MP];
-        row_load<MP>(V + (size_t)(a.off[(size_t)r0 * N + i] + 1) * MP, v0);
-        row_load<MP>(V + (size_t)(a.off[(size_t)r1 * N + i] + 1) * MP, v1);
-        float gj = 0.f;
+        const float *p0 = row(r0), *p1 = row(r1);
+        float dot = 0.f;
 #pragma unroll
-        for (int m = 0; m < MP; m++) {
-            const float ra = alpha * (v0[m] - v1[m]);
-            if (j > 0) gj = fmaf(z[m], a.sf[j - 1] * (sm[m] - (float)j * ra), gj);
-            sm[m] += ra;
+        for (int c = 0; c < MP / VW; c++) {
+            float v0[VW], v1[VW];
+            row_load<VW>(p0 + c * VW, v0);
+            row_load<VW>(p1 + c * VW, v1);
+#pragma unroll
+            for (int e = 0; e < VW; e++) dot = fmaf(z[c * VW + e], v0[e] - v1[e], dot);
         }
-        if (j > 0) grad[j - 1] += gj;
+        const float Dj = alpha * dot;
+        if (j > 0) grad[j - 1] += a.sf[j - 1] * (S - (float)j * Dj);
+        S += Dj;
     }
 }
 
 template <int MP>
-__global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
+__global__ void __launch_bounds__(256, 4) slice_grad_kernel(SliceGradArgs a) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)a.nslots) return;
     const int i = a.slot_pt[s];
@@ -420,9 +434,11 @@ __global__ void __launch_bounds__(256) slice_grad_kernel(SliceGradArgs a) {
     float grad[DCRF_MAX_D];
 #pragma unroll
     for (int j = 0; j < DCRF_MAX_D; j++) grad[j] = 0.f;
-    slice_grad_pair<MP>(a, a.V, a.z, a.alpha, s, i, grad);
-    if (a.V2) slice_grad_pair<MP>(a, a.V2, a.z2, a.alpha2, s, i, grad);
-    for (int j = 0; j < a.d; j++) a.df[(size_t)i * a.d + j] += grad[j];
+    slice_grad_pair<MP>(a, a.V, a.z, a.alpha, nullptr, s, i, grad);
+    if (a.V2) slice_grad_pair<MP>(a, a.V2, a.z2, a.alpha2, a.z2scale, s, i, grad);
+#pragma unroll
+    for (int j = 0; j < DCRF_MAX_D; j++)
+        if (j < a.d) a.df[(size_t)i * a.d + j] += grad[j];
 }
 
 // Kernel-parameter gradient from the feature gradient: DIAG g[j] = sum_n f[j][n] fg[n][j];

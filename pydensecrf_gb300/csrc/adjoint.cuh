@@ -15,6 +15,7 @@ struct SliceGradArgs {
     const float *z;       // [nslots][MP] contraction values (slot rows)
     const float *V2;      // optional second (V, z) pair, added in the same pass (null: none)
     const float *z2;
+    const float *z2scale; // optional [nslots]: the second pair's z is z2 .* z2scale
     float sf[DCRF_MAX_D];
     float alpha;          // sign / (1+2^-d) / (d+1) for the first pair
     float alpha2;         // and for the second

@@ -1480,6 +1480,28 @@ int splat_into(dcrf_crf *h, int k, const float *x, float *S, bool value1, bool p
     return DCRF_OK;
 }
 
+// The splat of the same slot rows x through several terms in one point pass
+// and one reduce: S[q] (vertex rows) of term ks[q], with its norm folded into
+// the member weights where prenorm[q] (see splat_into).
+int splat_terms_into(dcrf_crf *h, const std::vector<int> &ks, const float *x, const std::vector<float *> &S,
+                     const std::vector<bool> &prenorm) {
+    if (ks.empty()) return DCRF_OK;
+    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, ks, false, false);
+    ReduceArgs ra{};
+    ra.n = (int)ks.size();
+    for (size_t q = 0; q < ks.size(); q++) {
+        Term &T = h->terms[ks[q]];
+        a.ts.t[q].pre_norm = 0;
+        a.ts.t[q].mem_w = prenorm[q] ? T.mem_wn : T.lat.mem_w;
+        ra.t[q] = {T.lat.red_beg, T.pout, S[q], T.lat.L, T.lat.P};
+    }
+    a.Qin = x;
+    CU(pp(h, a, h->MP));
+    ProfScope ps(h, DCRF_KCLASS_REDUCE);
+    CU(launch_reduce(ra, h->MP, h->stream));
+    return DCRF_OK;
+}
+
 // Independent blur chains advanced together, one launch per axis pass: chain c
 // blurs S along axes 0..d (d..0 when reverse, permutohedral.cpp:556) through
 // the ping-pong pair b[0], b[1] into Out.  Chains of one launch must not share
@@ -1632,10 +1654,13 @@ int slice_from(dcrf_crf *h, int k, const float *V, float *out, bool value1, bool
 
 // T.df += sign * sum over labels of z . d(slice of V)/d(features): the
 // per-point part of Permutohedral::gradient (permutohedral.cpp:612-695).
+// z2scale (optional, [nslots]): the second pair's z is z2 .* z2scale per point.
 int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float sign, bool value1,
-                    const float *V2 = nullptr, const float *z2 = nullptr, float sign2 = 1.f) {
+                    const float *V2 = nullptr, const float *z2 = nullptr, float sign2 = 1.f,
+                    const float *z2scale = nullptr) {
     Term &T = h->terms[k];
     SliceGradArgs g{};
+    g.z2scale = z2scale;
     g.V2 = V2;
     g.z2 = z2;
     g.N = h->N;
@@ -2716,13 +2741,23 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
         // Then all blur chains of all terms advance together: A = K_raw^T
         // (reverse) of S_b, B = forward blur of S_b, C = reverse blur of C S_t.
         std::vector<Chain> chains;
+        {  // S_b = splat of x~ = norm .* b when the transpose starts normalised (the
+           // norm in the weights), all terms in one pass
+            std::vector<int> ks(nt);
+            std::vector<float *> Ss(nt);
+            std::vector<bool> pre(nt);
+            for (int k = 0; k < nt; k++) {
+                ks[k] = k;
+                Ss[k] = h->terms[k].bv[0];
+                pre[k] = tr_pre(h->terms[k]);
+            }
+            if ((rc = splat_terms_into(h, ks, b, Ss, pre))) return rc;
+        }
         for (int k = 0; k < nt; k++) {
             Term &Tk = h->terms[k];
             const size_t rows = (size_t)Tk.lat.L + 1;
             const float *St = h->ckv + (size_t)rel * h->ckv_iter + h->ckv_off[k];  // forward splat of Q_t
             const bool kgrad = want_kernel && Tk.ktype != DCRF_CONST_KERNEL;
-            // S_b = splat of x~ = norm .* b when the transpose starts normalised (the norm in the weights)
-            if ((rc = splat_into(h, k, b, Tk.bv[0], false, tr_pre(Tk)))) return rc;
             chains.push_back(Chain{k, Tk.bv[0], {Tk.V[1], Tk.V[0]}, Tk.bv[1], true});
             if (kgrad) {
                 CU(launch_compat(St, Tk.bv[2], M, (int)rows, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
@@ -2801,15 +2836,17 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
             // kernelGradient (pairwise.cpp:202-207) through featureGradient (87-114)
             // y = K_raw [norm] Q_t: kept by the forward, else sliced from its blurred lattice
             const float *yt = yk[k] ? yk[k] : y;
-            const float *xs = xtilde(Tk);
-            if (!xs) return set_err(DCRF_ERR_CUDA, "scale launch failed");
             if (fused) {
                 // y~ = [norm] C Q_t and the normalisation's coefficients in one pass
                 CU(launch_norm_terms(b, yt, F, Qt, Tk.norm, M, ns, Tk.ntype, Tk.ckind, Tk.potts_w, Tk.compat, yn, x1,
                                      h->stream));
                 // d/df x~^T K_raw y~: the forward-blurred S_b against y~ plus the
                 // reverse-blurred splat of y~ (= C S_t) against x~, in one pass
-                if ((rc = slice_grad_into(h, k, Tk.bv[5], yn, 1.f, false, Tk.bv[8], xs, 1.f))) return rc;
+                // (x~ = norm .* b when the transpose starts normalised: the norm is
+                // applied to b as the pass reads it)
+                if ((rc = slice_grad_into(h, k, Tk.bv[5], yn, 1.f, false, Tk.bv[8], b, 1.f,
+                                          tr_pre(Tk) ? Tk.norm : nullptr)))
+                    return rc;
                 if (Tk.ntype != DCRF_NO_NORMALIZATION) {
                     if ((rc = splat_into(h, k, x1, Tk.b1[0], true))) return rc;
                     if ((rc = blur_into(h, k, Tk.b1[0], Tk.b1[1], false, true))) return rc;
@@ -2817,6 +2854,8 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
                 }
                 continue;
             }
+            const float *xs = xtilde(Tk);
+            if (!xs) return set_err(DCRF_ERR_CUDA, "scale launch failed");
             const float *y_ = yt;
             CU(launch_compat(Qt, cq, M, ns, Tk.ckind, Tk.potts_w, Tk.compat, 0, 0, h->stream));
             const float *ys = cq;  // y~ = C Q_t with the forward's first normalisation

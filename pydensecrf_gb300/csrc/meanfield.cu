@@ -625,6 +625,8 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
                                              : T.tsched + b.tb;
             const uint16_t *mpt = T.staged ? reinterpret_cast<const uint16_t *>(smem + T.sm_mpt) : T.mem_pt + tbm;
             const float *mw = T.staged ? reinterpret_cast<const float *>(smem + T.sm_mw) : T.mem_w + tbm;
+            // every partial of this term in this tile is one task: no combine phase
+            const bool whole = b.nt == b.np;
             if (gactive) {
                 for (int sj = gid; sj < b.nt; sj += NG) {
                     const int j = (int)sched[sj];
@@ -645,12 +647,13 @@ __global__ void __launch_bounds__(PPT<MP, S>::NT, PPT<MP, S>::MINB) pointpass_ke
 #pragma unroll
                         for (int f = 0; f < VW; f++) acc[f] = fmaf(w, v[f], acc[f]);
                     }
-                    const bool first = j == 0 || (int)(tasks[j - 1] >> 19) != pl;
-                    const bool last = j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
+                    const bool first = whole || j == 0 || (int)(tasks[j - 1] >> 19) != pl;
+                    const bool last = whole || j == b.nt - 1 || (int)(tasks[j + 1] >> 19) != pl;
                     float *dst = (first && last) ? T.pout + (size_t)prow * MP : sRes + (size_t)j * MP;
                     vstore<VW>(dst + m0, acc);
                 }
             }
+            if (whole) continue;  // nothing went to sRes (the flag is uniform over the CTA)
             __syncthreads();
             if (gactive) {
                 for (int j = gid; j < b.nt; j += NG) {
@@ -1002,11 +1005,11 @@ __host__ __device__ inline int adj_group_words(int M) {
 }
 
 template <int MP>
-__global__ void __launch_bounds__(SPLAT_TILE) adjoint_tile_kernel(const __grid_constant__ AdjArgs a) {
+__global__ void __launch_bounds__(SPLAT_TILE, 3) adjoint_tile_kernel(const __grid_constant__ AdjArgs a) {
     extern __shared__ __align__(16) float adj_smem[];
     float *sQ = adj_smem, *sF = sQ + SPLAT_TILE * MP, *sG = sF + SPLAT_TILE * MP;
     float *sCT = sG + adj_group_words(a.M);
-    const int M = a.M, N = a.N;
+    const int M = a.M;
     {  // Matrix compatibilities, transposed into [k][MP] (zero padded); symmetric, so equal
         int j = 0;
         for (int k = 0; k < a.ts.n; k++) {
@@ -1022,18 +1025,21 @@ __global__ void __launch_bounds__(SPLAT_TILE) adjoint_tile_kernel(const __grid_c
     const size_t s = (size_t)blockIdx.x * SPLAT_TILE + threadIdx.x;
     const int i = a.slot_pt[s];
     const bool ok = i >= 0;
-    float q[MP];
-    if (ok)
-        load_row<MP>(a.Qt + s * MP, q);
-    else
+    {  // Q_t's row goes to shared memory (the products read it; the softmax adjoint re-reads it)
+        float q[MP];
+        if (ok)
+            load_row<MP>(a.Qt + s * MP, q);
+        else
 #pragma unroll
-        for (int m = 0; m < MP; m++) q[m] = 0.f;
-    store_row<MP>(sQ + threadIdx.x * MP, q);
+            for (int m = 0; m < MP; m++) q[m] = 0.f;
+        store_row<MP>(sQ + threadIdx.x * MP, q);
+    }
     float x[MP];  // -g: x -= C F' per term
 #pragma unroll
     for (int m = 0; m < MP; m++) x[m] = 0.f;
     __syncthreads();
     int jm = 0;
+    constexpr int VW = MP % 4 == 0 ? 4 : 1;
     for (int k = 0; k < a.ts.n; k++) {
         const TermDev &T = a.ts.t[k];
         const AdjArgs::T &A = a.a[k];
@@ -1041,18 +1047,22 @@ __global__ void __launch_bounds__(SPLAT_TILE) adjoint_tile_kernel(const __grid_c
 #pragma unroll
         for (int m = 0; m < MP; m++) acc[m] = 0.f;
         if (ok) {
+            // the point-order gather from A (vertex order), each row streamed in vectors
             for (int r = 0; r <= T.d; r++) {
-                const int o = T.off[(size_t)r * N + i] + 1;
-                float v[MP];
-                load_row<MP>(A.A + (size_t)o * MP, v);
-                if (T.seq) {  // (w * v) * alpha, then the sum (permutohedral.cpp:513-521)
-                    const float w = T.bary[(size_t)r * N + i];
+                const float *row = A.A + (size_t)(T.off[(size_t)r * a.N + i] + 1) * MP;
+                const float w = T.seq ? T.bary[(size_t)r * a.N + i] : T.wslice[(size_t)r * a.N + i];
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(fmul(w, v[m]), T.alpha));
-                } else {  // (w * alpha) * v (permutohedral.cpp:579-581)
-                    const float w = T.wslice[(size_t)r * N + i];
+                for (int c = 0; c < MP / VW; c++) {
+                    float v[VW];
+                    vload_g<VW>(row + c * VW, v);
 #pragma unroll
-                    for (int m = 0; m < MP; m++) acc[m] = fadd(acc[m], fmul(w, v[m]));
+                    for (int e = 0; e < VW; e++) {
+                        const int m = c * VW + e;
+                        if (T.seq)  // (w * v) * alpha, then the sum (permutohedral.cpp:513-521)
+                            acc[m] = fadd(acc[m], fmul(fmul(w, v[e]), T.alpha));
+                        else  // (w * alpha) * v (permutohedral.cpp:579-581)
+                            acc[m] = fadd(acc[m], fmul(w, v[e]));
+                    }
                 }
             }
 #pragma unroll
@@ -1078,6 +1088,8 @@ __global__ void __launch_bounds__(SPLAT_TILE) adjoint_tile_kernel(const __grid_c
     }
     if (!ok) return;
     // b_next = softmax adjoint of g = -x at Q_t (densecrf.cpp:107-114, 290)
+    float q[MP];
+    load_row_s<MP>(sQ + threadIdx.x * MP, q);
     float dot = 0.f;
 #pragma unroll
     for (int m = 0; m < MP; m++)
