@@ -1005,7 +1005,9 @@ __host__ __device__ inline int adj_group_words(int M) {
 }
 
 template <int MP>
-__global__ void __launch_bounds__(SPLAT_TILE, 3) adjoint_tile_kernel(const __grid_constant__ AdjArgs a) {
+// (three CTAs per SM at 16 labels or more, where each thread holds long rows;
+// measured: the same bound at 4 labels made the 96^3 volumes' backward 20 % slower)
+__global__ void __launch_bounds__(SPLAT_TILE, MP >= 16 ? 3 : 1) adjoint_tile_kernel(const __grid_constant__ AdjArgs a) {
     extern __shared__ __align__(16) float adj_smem[];
     float *sQ = adj_smem, *sF = sQ + SPLAT_TILE * MP, *sG = sF + SPLAT_TILE * MP;
     float *sCT = sG + adj_group_words(a.M);
