@@ -351,7 +351,7 @@ def run_reference(args):
 
 
 # ----------------------------------------------------------------------------
-def learning_step_times(lib, _lib, dev, stream, reps: int = 2):
+def learning_step_times(lib, _lib, dev, stream, reps: int = 2, profile_one: bool = False):
     """Forward and forward+backward of the differentiable mean-field on the
     training workload (512x512, 21 labels, 5 iterations, Gaussian Potts with
     a CONST kernel + bilateral with a 21x21 Matrix compatibility and DIAG
@@ -415,6 +415,15 @@ def learning_step_times(lib, _lib, dev, stream, reps: int = 2):
     fwd(0)
     bwd(0)
     torch.cuda.synchronize()
+    if profile_one:  # one forward + backward between cudaProfilerStart/Stop (ncu --profile-from-start off)
+        fwd(1)
+        bwd(1)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        fwd(2)
+        bwd(2)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     f_ms, b_ms = [], []
     for _ in range(reps):
         for i in range(len(Us)):
@@ -846,6 +855,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline sample")
     ap.add_argument("--no-learning", action="store_true", help="skip the forward+backward timing")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-vs-loop timing")
+    ap.add_argument("--learning-only", action="store_true",
+                    help="only the forward+backward timing, one step of it between cudaProfilerStart/Stop "
+                         "(for ncu --profile-from-start off); prints its JSON object")
     ap.add_argument("--fixed-knobs", action="store_true",
                     help="no autotuning of the main solve (the default knobs; a fixed launch sequence for profilers)")
     ap.add_argument("--traffic", type=float, default=None,
@@ -853,6 +865,16 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.learning_only:
+        import torch
+
+        from pydensecrf_gb300 import _lib
+
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(dev)
+        r = learning_step_times(_lib.load(), _lib, dev, torch.cuda.current_stream(dev), profile_one=True)
+        print(json.dumps(r))
+        return 0
     return run_gpu(args)
 
 
