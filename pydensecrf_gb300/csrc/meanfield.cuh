@@ -16,6 +16,9 @@ enum : int {
     PP_KL = 64,      // per-block KL-divergence partial sums (needs LOAD_Q|MSG)
     PP_NORM = 128,   // slice (value size 1) and write each term's normalisation
     PP_FILTER = 256, // Qout = raw lattice filter of term 0 (no normalisation, compatibility or softmax)
+    // the mean-field iteration's passes, compiled as their own instances
+    PP_HOT_STEP = PP_MSG | PP_SPLAT,    // messages, softmax, splat of the new marginals
+    PP_HOT_LAST = PP_MSG | PP_WRITE_Q,  // the last iteration: messages, softmax, marginals out
 };
 
 struct PPArgs {
@@ -155,6 +158,8 @@ struct BlurChainArgs {
 
 // Launchers; MP is the padded label count (1, 2, 4, 8, ..., 32).
 cudaError_t launch_pointpass(const PPArgs &a, int MP, cudaStream_t s);
+// the PP_NORM / PP_FILTER passes (point-order slice; launch_pointpass routes them here)
+cudaError_t launch_slice(const PPArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_reduce(const ReduceArgs &a, int MP, cudaStream_t s);
 cudaError_t launch_blur(const BlurArgs &a, int MP, bool seq, cudaStream_t s);
 cudaError_t launch_blur_chains(const BlurChainArgs &a, int MP, bool seq, cudaStream_t s);
