@@ -1104,10 +1104,6 @@ int ensure_wide_bufs(dcrf_crf *h) {
     const size_t need = nmat * (size_t)h->nslots * h->MP;
     if (need > h->wideF_cap) {
         dev_free_async(h->wideF, h->stream);
-    for (auto *v : {&h->adjF, &h->adjY})
-        for (float *p : *v) dev_free_async(p, h->stream);
-    dev_free_async(h->L_d, h->stream);
-    dev_free_async(h->f_d, h->stream);
         h->wideF = nullptr;
         h->wideF_cap = 0;
         int rc = dev_alloc_async(&h->wideF, need, h->stream);

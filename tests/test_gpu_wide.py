@@ -145,3 +145,40 @@ def test_wide_unsupported_calls_are_errors(engine):
         d.lattice_filter(0, np.ones((40, 16 * 12), np.float32), False)
     out = d.lattice_filter(0, np.ones((1, 16 * 12), np.float32), False)  # value size 1 works
     assert np.isfinite(out).all()
+
+
+def test_wide_logistic_unary_with_matrix_keeps_parameters(engine, oracle_mod):
+    """A logistic unary (unary.cpp:48-68) on a handle of 40 labels with a Matrix
+    term: the first inference sizes the Matrix terms' message rows, and the
+    unary's parameters must survive it -- setUnaryParameters afterwards and a
+    second inference give the marginals of a fresh handle built with the new
+    parameters and of the oracle solved with U = L2 f."""
+    rng = np.random.default_rng(83)
+    W, H, M, K, T = 23, 17, 40, 6, 3
+    N = W * H
+    L = rng.normal(0, 1, (M, K)).astype(np.float32)
+    L2 = rng.normal(0, 1, (M, K)).astype(np.float32)
+    f = rng.normal(0, 1, (K, N)).astype(np.float32)
+    img = rng.integers(0, 256, size=(H, W, 3)).astype(np.uint8)
+    mat = rng.uniform(0, 2, size=(M, M)).astype(np.float32)
+
+    def crf(Lm):
+        d = engine.DenseCRF2D(W, H, M)
+        d.setUnaryEnergy(Lm, f)
+        d.addPairwiseGaussian(3, mat)
+        d.addPairwiseBilateral(8, 13, img, 5.0)
+        return d
+
+    d = crf(L)
+    d.inference(T)
+    d.setUnaryParameters(L2.reshape(-1, order="F"))
+    assert np.array_equal(d.unaryParameters(), L2.reshape(-1, order="F"))
+    q = np.array(d.inference(T))
+    q_fresh = np.array(crf(L2).inference(T))
+    assert np.abs(q - q_fresh).max() == 0.0
+    U2 = (L2.astype(np.float64) @ f.astype(np.float64)).astype(np.float32)
+    o = oracle_mod.OracleCRF(N, M)
+    o.set_unary(np.ascontiguousarray(U2.T))
+    o.add_pairwise(oracle_mod.features_gaussian_2d(W, H, 3, 3), mat)
+    o.add_pairwise(oracle_mod.features_bilateral_2d(img, 8, 8, 13, 13, 13), 5.0)
+    assert np.abs(q.T - o.inference(T)).max() < QTOL
