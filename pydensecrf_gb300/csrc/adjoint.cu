@@ -295,6 +295,17 @@ __global__ void onehot_kernel(const int16_t *__restrict__ labels, int M, int ld,
     for (int m = 0; m < ld; m++) out[s * ld + m] = (m == l && l < M) ? 1.f : 0.f;
 }
 
+// The same one-hot rows in the label-chunk layout of more than 32 labels
+// (chunk_offset), all MP padded labels of every slot written.
+__global__ void onehot_chunked_kernel(const int16_t *__restrict__ labels, int M, int MP, int ns,
+                                      const int *__restrict__ slot_pt, float *__restrict__ out) {
+    const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= (size_t)ns) return;
+    const int pt = slot_pt[s];
+    const int l = pt >= 0 ? (int)labels[pt] : -1;
+    for (int m = 0; m < MP; m++) out[chunk_offset((size_t)ns, MP, s, m)] = (m == l && l < M) ? 1.f : 0.f;
+}
+
 // energy[pt] (+)= scale * x[slot of pt][label of pt] for 0 <= label < M, else
 // (+)= 0 (densecrf.cpp:146-150, 169-174)
 __global__ void label_energy_kernel(const float *__restrict__ x, const int16_t *__restrict__ labels, int M, int ld,
@@ -549,6 +560,12 @@ cudaError_t launch_norm_terms(const float *b, const float *y, const float *F, co
 #undef DCRF_NT
         default: return cudaErrorInvalidValue;  // M <= 2 takes the unfused path
     }
+    return cudaGetLastError();
+}
+
+cudaError_t launch_onehot_chunked(const int16_t *labels, int M, int MP, int ns, const int *slot_pt, float *out,
+                                  cudaStream_t s) {
+    DCRF_LAUNCH(onehot_chunked_kernel<<<blocks(ns), 256, 0, s>>>(labels, M, MP, ns, slot_pt, out));
     return cudaGetLastError();
 }
 

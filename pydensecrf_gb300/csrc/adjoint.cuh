@@ -40,6 +40,9 @@ cudaError_t launch_norm_terms(const float *b, const float *y, const float *F, co
                               float *x1, cudaStream_t s);
 // one-hot slot rows of a point-order labelling; per-point energy from slot rows
 cudaError_t launch_onehot(const int16_t *labels, int M, int ns, const int *slot_pt, float *out, cudaStream_t s);
+// the same for more than 32 labels, in the label-chunk layout (chunk_offset)
+cudaError_t launch_onehot_chunked(const int16_t *labels, int M, int MP, int ns, const int *slot_pt, float *out,
+                                  cudaStream_t s);
 cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int ns, int N, const int *pt_slot,
                                 float scale, int accumulate, float *energy, cudaStream_t s);
 int label_products_blocks(int ns);

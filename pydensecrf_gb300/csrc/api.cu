@@ -2203,6 +2203,36 @@ static int store_energy(dcrf_crf *h, const float *src, float *energy, int where)
     return DCRF_OK;
 }
 
+// pairwiseEnergy for more than 32 labels (densecrf.cpp:160-177): the one-hot
+// labelling in the label-chunk layout goes through the chunked splat and
+// filter of the selected terms like a marginal, and the wide update pass in
+// energy mode adds -1/2 * each term's message at the point's own label.
+static int pairwise_energy_wide(dcrf_crf *h, const int16_t *labels, int where, int term, float *energy,
+                                int where_out) {
+    int rc;
+    std::vector<int> w;
+    for (int k = 0; k < (int)h->terms.size(); k++)
+        if (term < 0 || k == term) w.push_back(k);
+    int16_t *lab = nullptr;
+    float *e = nullptr;
+    if ((rc = ensure_wide_bufs(h)) || (rc = load_labels(h, labels, where, &lab))) return rc;
+    if ((rc = dev_alloc_async(&e, (size_t)h->N, h->stream))) return rc;
+    CU(cudaMemsetAsync(e, 0, sizeof(float) * h->N, h->stream));  // points of no slot (none) stay 0
+    // h->Q is the handle's scratch marginals (every call that reads it loads it first)
+    CU(launch_onehot_chunked(lab, h->M, h->MP, h->nslots, h->slot_pt, h->Q, h->stream));
+    if ((rc = wide_splat_filter(h, w))) return rc;
+    WideArgs a = wide_args(h, WP_MSG | WP_LOAD_Q | WP_ENERGY, w);
+    a.labels = lab;
+    a.energy = e;
+    CU(launch_wide(a, h->stream));
+    rc = store_energy(h, e, energy, where_out);
+    dev_free_async(lab, h->stream);
+    dev_free_async(e, h->stream);
+    if (rc) return rc;
+    if ((rc = sync_check(h))) return rc;
+    return ok();
+}
+
 int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *energy, int where_out) {
     int rc = check_ready(h);
     if (rc) return rc;
@@ -2224,9 +2254,9 @@ int dcrf_unary_energy(dcrf_crf *h, const int16_t *labels, int where, float *ener
 int dcrf_pairwise_energy(dcrf_crf *h, const int16_t *labels, int where, int term, float *energy, int where_out) {
     int rc = check_ready(h);
     if (rc) return rc;
-    if (is_wide(h)) return wide_unsupported("dcrf_pairwise_energy");
     if (!labels || !energy) return set_err(DCRF_ERR_INVALID_ARG, "null argument");
     if (term < -1 || term >= (int)h->terms.size()) return set_err(DCRF_ERR_INVALID_ARG, "no such term");
+    if (is_wide(h)) return pairwise_energy_wide(h, labels, where, term, energy, where_out);
     const int M = h->M, ns = h->nslots;
     const size_t qsz = (size_t)h->MP * ns;
     for (float *&b : h->bw)

@@ -109,6 +109,10 @@ __global__ void __launch_bounds__(SPLAT_TILE) wide_kernel(const __grid_constant_
     const int M = a.M, MP = a.MP, ns = a.nslots, mode = a.mode;
     const int nc = (MP + WC - 1) / WC;
     const bool kl_mode = (mode & WP_KL) != 0;
+    const bool en_mode = (mode & WP_ENERGY) != 0;
+    // the point's label and its pairwise energy (densecrf.cpp:160-177)
+    const int lab = (en_mode && i >= 0) ? (int)a.labels[i] : -1;
+    float energy = 0.f;
     double kl = 0.0;
     if (i >= 0) {
         if (mode & WP_MSG) {  // Matrix terms: every chunk of their post-normalised slice first
@@ -185,9 +189,12 @@ __global__ void __launch_bounds__(SPLAT_TILE) wide_kernel(const __grid_constant_
                             kl += (double)fmul(x[e], cc[e]);
                         else
                             x[e] = fsub(x[e], cc[e]);
+                        // r += -0.5 * tmp(l, i) per term, in term order (densecrf.cpp:172-174)
+                        if (en_mode && m0 + e == lab && lab < M) energy = fadd(energy, fmul(-0.5f, cc[e]));
                     }
                 }
             }
+            if (en_mode) continue;  // no softmax: only the energy is wanted
             if (kl_mode) {  // entropy and unary parts (densecrf.cpp:216-226)
                 float u[WC];
 #pragma unroll
@@ -243,6 +250,7 @@ __global__ void __launch_bounds__(SPLAT_TILE) wide_kernel(const __grid_constant_
             }
             if (mode & WP_MAP) a.map_out[i] = (int16_t)best;
         }
+        if (en_mode) a.energy[i] = energy;
     }
     if (kl_mode) {
 #pragma unroll

@@ -59,6 +59,8 @@ enum : int {
     WP_WRITE_Q = 4,  // softmax, Qout = the new marginals
     WP_MAP = 8,      // softmax, map_out = argmax (first maximum)
     WP_KL = 16,
+    WP_ENERGY = 32,  // with WP_MSG | WP_LOAD_Q (a one-hot labelling): energy[i] = the pairwise
+                     // energy of the point's label, -1/2 * message, added term by term
 };
 
 struct WideArgs {
@@ -72,6 +74,8 @@ struct WideArgs {
                         // messages at F + j * nslots * MP
     int16_t *map_out;   // [N]
     double *kl_part;    // [ntiles]
+    const int16_t *labels;  // [N] (WP_ENERGY)
+    float *energy;          // [N] (WP_ENERGY)
     long long pv_chunk[DCRF_MAX_TERMS];  // floats between consecutive chunks of a term's pv (32 (P+1))
     TermSet ts;         // terms; pv, tile tables, norm and compatibility of chunk 0
 };

@@ -182,3 +182,49 @@ def test_wide_logistic_unary_with_matrix_keeps_parameters(engine, oracle_mod):
     o.add_pairwise(oracle_mod.features_gaussian_2d(W, H, 3, 3), mat)
     o.add_pairwise(oracle_mod.features_bilateral_2d(img, 8, 8, 13, 13, 13), 5.0)
     assert np.abs(q.T - o.inference(T)).max() < QTOL
+
+
+@pytest.mark.parametrize("ntype", [0, 1, 2, 3])
+def test_wide_pairwise_energy_vs_oracle(engine, oracle_mod, ntype):
+    """pairwiseEnergy (densecrf.cpp:160-177) at 40 labels, per term and summed
+    over a Matrix, a Potts and a Diagonal term, against the one-hot messages of
+    the oracle's lattice filter (1e-5 of the largest magnitude, the energy
+    tests' bar); labels outside [0, M) give 0."""
+    rng = np.random.default_rng(91 + ntype)
+    N, M = 900, 40
+    feats = [rng.normal(0, s, size=(N, dd)).astype(np.float32) for s, dd in ((1.5, 3), (2.0, 2), (1.0, 4))]
+    compats = [rng.uniform(-1, 1, size=(M, M)).astype(np.float32), 2.5, rng.uniform(-2, 0, size=M).astype(np.float32)]
+    d = engine.DenseCRF(N, M)
+    d.setUnaryEnergy(rng.random((M, N)).astype(np.float32))
+    for f, c in zip(feats, compats):
+        d.addPairwiseEnergy(np.ascontiguousarray(f.T), c, normalization=ntype)
+    lab = rng.integers(-1, M + 1, size=N).astype(np.int16)  # -1 and M: no label
+    ok = (lab >= 0) & (lab < M)
+    oh = np.zeros((N, M), np.float32)
+    oh[np.arange(N)[ok], lab[ok]] = 1.0
+    want_terms = []
+    for f, c in zip(feats, compats):
+        lat = oracle_mod.Lattice(f, "oracle", 0)
+        raw1 = lat.compute(np.ones((N, 1), np.float32), False)[:, 0].astype(np.float64)
+        if ntype == 0:
+            n_pre = n_post = np.ones(N)
+        elif ntype == 3:
+            n_pre = n_post = 1.0 / np.sqrt(raw1 + 1e-20)
+        else:
+            n = 1.0 / (raw1 + 1e-20)
+            n_pre, n_post = (n, np.ones(N)) if ntype == 1 else (np.ones(N), n)
+        kq = lat.compute(np.ascontiguousarray((oh * n_pre[:, None]).astype(np.float32)), False) * n_post[:, None]
+        if np.ndim(c) == 0:
+            msg = -float(c) * kq
+        elif np.ndim(c) == 1:
+            msg = kq * c[None, :]
+        else:
+            msg = kq @ (0.5 * (c + c.T)).T
+        want_terms.append(np.where(ok, -0.5 * msg[np.arange(N), np.clip(lab, 0, M - 1)], 0.0))
+    for k, want in enumerate(want_terms):
+        got = d.pairwiseEnergy(lab, k)
+        assert np.abs(got - want).max() <= 1e-5 * max(1.0, np.abs(want).max()), (k, np.abs(got - want).max())
+    want = sum(want_terms)
+    got = d.pairwiseEnergy(lab)
+    assert np.abs(got - want).max() <= 1e-5 * max(1.0, np.abs(want).max()), np.abs(got - want).max()
+    assert (got[~ok] == 0).all()
