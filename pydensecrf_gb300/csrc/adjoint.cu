@@ -194,11 +194,6 @@ __global__ void prod_kernel(const float *__restrict__ x1, const float *__restric
     y[o] = v * f;
 }
 
-__global__ void add_kernel(const float *__restrict__ x, float *__restrict__ y, size_t n) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) y[i] += x[i];
-}
-
 __global__ void fill_kernel(float *__restrict__ y, float v, int M, int ld, int ns, const int *__restrict__ slot_pt) {
     const size_t s = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (s >= (size_t)ns) return;
@@ -532,11 +527,6 @@ cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const
     return cudaGetLastError();
 }
 
-cudaError_t launch_add(const float *x, float *y, size_t n, cudaStream_t s) {
-    if (n) DCRF_LAUNCH(add_kernel<<<blocks(n), 256, 0, s>>>(x, y, n));
-    return cudaGetLastError();
-}
-
 cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cudaStream_t s) {
     DCRF_LAUNCH(fill_kernel<<<blocks(ns), 256, 0, s>>>(y, v, M, pad_labels(M), ns, slot_pt));
     return cudaGetLastError();
@@ -601,14 +591,6 @@ cudaError_t launch_label_products_part(const float *a, const float *b, int M, in
     if (smem > 48 * 1024) return cudaErrorInvalidValue;
     DCRF_LAUNCH(label_products_kernel<<<nb, 256, smem, s>>>(a, b, M, ld, ns, slot_pt, mode, accumulate, part));
     return cudaGetLastError();
-}
-
-cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
-                                  double *part, double *out, int accumulate, cudaStream_t s) {
-    const int K = mode == 0 ? M : M * M;
-    cudaError_t e = launch_label_products_part(a, b, M, ns, slot_pt, mode, part, 0, s);
-    if (e != cudaSuccess) return e;
-    return launch_sum_parts_bm(part, label_products_blocks(ns), K, out, accumulate, s);
 }
 
 template <int MP>

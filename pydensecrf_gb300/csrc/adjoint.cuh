@@ -30,7 +30,6 @@ cudaError_t launch_compat(const float *x, float *y, int M, int ns, int kind, flo
 cudaError_t launch_scale_norm(const float *x, float *y, const float *norm, int M, int ns, int pw, cudaStream_t s);
 cudaError_t launch_prod(const float *x1, const float *x2, const float *x3, const float *x4, float scale,
                         const float *norm, int pw, float *y, int M, int ns, cudaStream_t s);
-cudaError_t launch_add(const float *x, float *y, size_t n, cudaStream_t s);
 cudaError_t launch_fill(float *y, float v, int M, int ns, const int *slot_pt, cudaStream_t s);
 cudaError_t launch_row_sum(const float *x, float *out, int M, int ns, cudaStream_t s);
 // ys = [norm .*] C Q and x1 = sum of the normalisation coefficients c1 per point
@@ -46,11 +45,9 @@ cudaError_t launch_onehot_chunked(const int16_t *labels, int M, int MP, int ns, 
 cudaError_t launch_label_energy(const float *x, const int16_t *labels, int M, int ns, int N, const int *pt_slot,
                                 float scale, int accumulate, float *energy, cudaStream_t s);
 int label_products_blocks(int ns);
-// mode 0: out[m] (+)= sum a[m].*b[m]; mode 1: out[m*M+k] (+)= sum a[m].*b[k]; part: [blocks][K] doubles
-cudaError_t launch_label_products(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
-                                  double *part, double *out, int accumulate, cudaStream_t s);
-// the block partials only, stored or added (accumulate) into part ([blocks][K]);
-// launch_sum_parts_bm reduces such block-major partials
+// label products per block: mode 0: out[m] = sum a[m].*b[m]; mode 1: out[m*M+k] =
+// sum a[m].*b[k]; the block partials are stored or added (accumulate) into part
+// ([blocks][K] doubles), and launch_sum_parts_bm reduces such block-major partials
 cudaError_t launch_label_products_part(const float *a, const float *b, int M, int ns, const int *slot_pt, int mode,
                                        double *part, int accumulate, cudaStream_t s);
 cudaError_t launch_slice_grad(const SliceGradArgs &a, int MP, cudaStream_t s);

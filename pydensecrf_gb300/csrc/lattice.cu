@@ -23,8 +23,10 @@
 //                 ("partials"), the member lists and splat tasks of the
 //                 in-kernel splat, and per corner the index of its vertex among
 //                 the tile's partials (the tile-local slice table).
-//   7. reduce     stable radix sort of the tiles' partials by vertex: the
-//                 order in which a vertex's partial sums are added.
+//   7. reduce     the tiles' partials grouped by vertex, each vertex's in tile
+//                 order: the order in which its partial sums are added (a
+//                 counting placement and a rank within each vertex's range; a
+//                 stable radix sort when vertices have very many partials).
 // Bounded probing everywhere: a full table sets DCRF_ERR_HASH_FULL and the
 // host retries with a larger table; no kernel waits on another thread.
 #include <algorithm>
@@ -286,13 +288,6 @@ __global__ void insert_kernel(const uint64_t *__restrict__ keys, size_t E, uint3
         if (!done) dcrf_set_error(st, DCRF_ERR_HASH_FULL, 0);
     }
     slot[k] = __shfl_sync(peers, h, leader);
-}
-
-__global__ void first_flag_kernel(const uint32_t *__restrict__ table, const uint32_t *__restrict__ slot, size_t E,
-                                  uint32_t *__restrict__ flag) {
-    size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= E) return;
-    flag[k] = table[slot[k]] == (uint32_t)k ? 1u : 0u;
 }
 
 template <int D>

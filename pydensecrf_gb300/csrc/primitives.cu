@@ -176,18 +176,6 @@ cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, size_t n, uint
     return scan_rec(in, out, n, d_total, temp, s);
 }
 
-cudaError_t scan_exclusive_u32_pair(const uint32_t *in0, uint32_t *out0, uint32_t *total0, const uint32_t *in1,
-                                    uint32_t *out1, uint32_t *total1, size_t n, uint32_t *temp, cudaStream_t s) {
-    if (n > 1024 && n <= SCAN_SMALL_MAX) {
-        const SmallScan a = {{in0, in1}, {out0, out1}, {total0, total1}};
-        DCRF_LAUNCH(scan_small_kernel<<<2, SMALL_THREADS, 0, s>>>(a, n));
-        return cudaGetLastError();
-    }
-    cudaError_t e = scan_exclusive_u32(in0, out0, n, total0, temp, s);
-    if (e != cudaSuccess) return e;
-    return scan_exclusive_u32(in1, out1, n, total1, temp, s);
-}
-
 // ---------------------------------------------------------------------------
 // Single-pass exclusive scan with decoupled look-back.
 // ---------------------------------------------------------------------------

@@ -61,11 +61,6 @@ size_t scan_temp_words(size_t n);
 cudaError_t scan_exclusive_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *d_total, uint32_t *temp,
                                cudaStream_t s);
 
-// Two independent scans of arrays of the same length (one launch when they fit
-// the single-block scan); temp as for scan_exclusive_u32 of n elements.
-cudaError_t scan_exclusive_u32_pair(const uint32_t *in0, uint32_t *out0, uint32_t *total0, const uint32_t *in1,
-                                    uint32_t *out1, uint32_t *total1, size_t n, uint32_t *temp, cudaStream_t s);
-
 // Workspace (in 32-bit words) needed by radix_argsort_u32 for n elements.
 size_t radix_temp_words(size_t n);
 // Stable argsort by the low `bits` bits of keys[0..n): vals_out[j] = the index
