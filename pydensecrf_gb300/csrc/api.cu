@@ -1305,7 +1305,8 @@ int autotune_now(dcrf_crf *h) {
     TuneCfg best = h->tune;
     double best_score = 1e30;
     const float loads[3] = {1.5f, 2.0f, 3.0f};
-    const int tasks[3] = {16, 24, 32};
+    // longer tasks split fewer partials, so more tiles skip the splat's combine phase
+    const int tasks[4] = {16, 24, 32, 48};
     for (float ld : loads)
         for (int tk : tasks) {
             h->tune.hash_load = ld;
