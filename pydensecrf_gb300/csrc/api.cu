@@ -474,7 +474,6 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
     if ((rc = build_tiles(h))) return fail(rc);
     if ((rc = dev_alloc_async(&h->U, (size_t)h->nslots * h->MP, s))) return fail(rc);
     if ((rc = dev_alloc_async(&h->Q, (size_t)h->nslots * h->MP, s))) return fail(rc);
-    if ((rc = dev_alloc_async(&h->tmp, (size_t)h->nslots * h->MP, s))) return fail(rc);
     if ((rc = dev_alloc_async(&h->stage, (size_t)N * M, s))) return fail(rc);
     if ((rc = dev_alloc_async(&h->map, (size_t)N, s))) return fail(rc);
     // pooled memory may hold an earlier handle's data: status, the grid
@@ -482,8 +481,7 @@ int create(int M, const std::vector<int> &Ns, const std::vector<int> &Ws, const 
     if (cudaMemsetAsync(h->status, 0, sizeof(DevStatus), s) != cudaSuccess ||
         cudaMemsetAsync(h->bar, 0, 2 * sizeof(unsigned), s) != cudaSuccess ||
         cudaMemsetAsync(h->U, 0, rows * sizeof(float), s) != cudaSuccess ||
-        cudaMemsetAsync(h->Q, 0, rows * sizeof(float), s) != cudaSuccess ||
-        cudaMemsetAsync(h->tmp, 0, rows * sizeof(float), s) != cudaSuccess)
+        cudaMemsetAsync(h->Q, 0, rows * sizeof(float), s) != cudaSuccess)
         return fail(set_err(DCRF_ERR_CUDA, "cudaMemsetAsync failed"));
     *out = h;
     return ok();
@@ -2383,6 +2381,11 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     bool v1 = value_size == 1;
     int MP = v1 ? 1 : h->MP;
+    if (!h->tmp) {  // the raw filter's slot rows, made at its first use
+        const size_t rows = (size_t)h->nslots * h->MP;
+        if ((rc = dev_alloc_async(&h->tmp, rows, h->stream))) return rc;
+        CU(cudaMemsetAsync(h->tmp, 0, rows * sizeof(float), h->stream));
+    }
     if ((rc = load_mn(h, in, DCRF_LAYOUT_LM, DCRF_HOST, h->tmp, value_size))) return rc;
     // the value-size-1 zero row (element MP) is row 1 of the full-width passes
     // that may have run since the build
