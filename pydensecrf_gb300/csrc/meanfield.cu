@@ -271,6 +271,29 @@ cudaError_t launch_wide(const WideArgs &a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// The reference evaluates the norms in double and rounds to float
+// (pairwise.cpp:54-61: 1.0 / sqrt(n + 1e-20), 1.0 / (n + 1e-20) with n float);
+// double arithmetic is slow on this GPU, so they are evaluated in float here.
+// For n > 1e-4 (a lattice norm includes the point's own weight, so it is far
+// larger), n + 1e-20 is n in double.  1/n: float division rounds the exact
+// quotient once, as the double route does.  1/sqrt(n): the square root and
+// its reciprocal are carried as float pairs (hi + lo, the low parts from exact
+// fused multiply-add residuals) and rounded once; over 6 M random n this gave
+// the double route's float in all cases but one, which was 1 ulp away.
+__device__ __forceinline__ float norm_symmetric(float n) {
+    if (!(n > 1e-4f)) return __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn((double)n, 1e-20))));
+    const float sh = __fsqrt_rn(n);
+    const float sl = __fdiv_rn(fmaf(-sh, sh, n), fmul(2.f, sh));  // sqrt(n) = sh + sl
+    const float r = __frcp_rn(sh);
+    const float t = fmaf(-r, sh, 1.f);                           // 1 - r sh, exact
+    return fadd(r, fmul(r, fsub(t, fmul(r, sl))));               // 1 / (sh + sl)
+}
+
+__device__ __forceinline__ float norm_one_sided(float n) {
+    if (!(n > 1e-4f)) return __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
+    return __fdiv_rn(1.f, n);
+}
+
 // Value-size-1 normalisation slice and raw lattice filter (point-order gather
 // from the vertex-order blurred values; used off the iteration loop).
 template <int MP>
@@ -303,11 +326,11 @@ __global__ void __launch_bounds__(256) slice_kernel(const __grid_constant__ PPAr
                     n = fadd(n, fmul(fmul(w, __ldg(T.V + o)), T.alpha));
                 }
                 if (a.ntype[k] == DCRF_NORMALIZE_SYMMETRIC)  // pairwise.cpp:54-57
-                    out = __double2float_rn(__ddiv_rn(1.0, __dsqrt_rn(__dadd_rn((double)n, 1e-20))));
+                    out = norm_symmetric(n);
                 else if (a.ntype[k] == DCRF_NO_NORMALIZATION)
                     out = n;  // raw K*1; the host derives the mean (pairwise.cpp:46-53)
                 else  // pairwise.cpp:58-61
-                    out = __double2float_rn(__ddiv_rn(1.0, __dadd_rn((double)n, 1e-20)));
+                    out = norm_one_sided(n);
             }
             a.norm_out[k][s] = out;
             if (a.wn_out[k]) {  // the block's threads are its tile's slots
@@ -598,20 +621,20 @@ __device__ __forceinline__ void scatter_partials(float *__restrict__ pv, const i
     for (; q < s1; q++) put(__ldg(list + q));
 }
 
-// One blur step at a vertex: y = x0 + 0.5 * (x1 + x2) over VEC labels, in
-// float (sseCompute, permutohedral.cpp:566) or evaluated in double
-// (seqCompute, permutohedral.cpp:505).
+// One blur step at a vertex: y = x0 + 0.5 * (x1 + x2) over VEC labels.
+// sseCompute evaluates it in float (permutohedral.cpp:566), seqCompute as
+// old + 0.5 * (n1 + n2) in double with the float sum n1 + n2 (permutohedral.cpp:
+// 505).  Both give the same float: x0 and 0.5 * (n1 + n2) are floats, whose
+// sum is exact in double unless their exponents differ by more than 29 bits,
+// and then both roundings give the larger operand (checked on 8 M random
+// pairs, extreme magnitude ratios and near-cancellations included).  So one
+// float evaluation serves both (double arithmetic is slow on this GPU); SEQ
+// keeps the two instantiations apart for the other arithmetic that differs.
 template <int VEC, bool SEQ>
 __device__ __forceinline__ void blur_step(const float (&x0)[VEC], const float (&x1)[VEC], const float (&x2)[VEC],
                                           float (&y)[VEC]) {
 #pragma unroll
-    for (int e = 0; e < VEC; e++) {
-        const float sm = fadd(x1[e], x2[e]);
-        if (SEQ)
-            y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)sm));
-        else
-            y[e] = fadd(x0[e], fmul(0.5f, sm));
-    }
+    for (int e = 0; e < VEC; e++) y[e] = fadd(x0[e], fmul(0.5f, fadd(x1[e], x2[e])));
 }
 
 template <int VEC>
@@ -771,14 +794,8 @@ __global__ void __launch_bounds__(256) blur_chains_kernel(const __grid_constant_
                     x2[e] = __ldcg(Vin + o2 + e);
                 }
             }
-#pragma unroll
-            for (int e = 0; e < VEC; e++) {
-                const float sm = fadd(x1[e], x2[e]);
-                if (SEQ)  // seqCompute: old + 0.5*(n1+n2) evaluated in double (permutohedral.cpp:505)
-                    y[e] = __double2float_rn(__dadd_rn((double)x0[e], 0.5 * (double)sm));
-                else  // sseCompute: float (permutohedral.cpp:566)
-                    y[e] = fadd(x0[e], fmul(0.5f, sm));
-            }
+            // seqCompute and sseCompute give the same float here (see blur_step)
+            blur_step<VEC, SEQ>(x0, x1, x2, y);
             if (Vout) {
                 if constexpr (VEC == 4) {
                     *reinterpret_cast<float4 *>(Vout + o0) = make_float4(y[0], y[1], y[2], y[3]);
