@@ -863,16 +863,38 @@ __device__ __forceinline__ void slot_tile_points(SlotTile &st, int point_major, 
     st.step[li] = step;
 }
 
-// element f of the tile's caller-side walk: (slot q, label m)
-__device__ __forceinline__ void slot_tile_elem(int f, int point_major, int M, int &q, int &m) {
-    if (point_major) {
-        q = f / M;
-        m = f - q * M;
-    } else {
-        m = f / SPLAT_TILE;
-        q = f - m * SPLAT_TILE;
+// A thread's walk over the elements f = li, li + SPLAT_TILE, ... of a tile
+// laid out as rows of w values: (row, column) = (f / w, f % w), advanced
+// without a division per element.
+struct TileWalk {
+    int row, col, drow, dcol, w;
+    __device__ __forceinline__ TileWalk(int f, int w_) : w(w_) {
+        row = f / w;
+        col = f - row * w;
+        drow = SPLAT_TILE / w;
+        dcol = SPLAT_TILE - drow * w;
     }
-}
+    __device__ __forceinline__ void next() {
+        row += drow;
+        col += dcol;
+        if (col >= w) {
+            col -= w;
+            row++;
+        }
+    }
+};
+
+// the tile's caller-side walk from element f = li: (slot q, label m) --
+// labels of a point for point-major buffers, points of a label otherwise
+struct CallerWalk {
+    TileWalk t;
+    int point_major;
+    __device__ __forceinline__ CallerWalk(int point_major_, int M) : t(threadIdx.x, point_major_ ? M : SPLAT_TILE),
+                                                                     point_major(point_major_) {}
+    __device__ __forceinline__ int q() const { return point_major ? t.row : t.col; }
+    __device__ __forceinline__ int m() const { return point_major ? t.col : t.row; }
+    __device__ __forceinline__ void next() { t.next(); }
+};
 
 // out[slot][m] = in(m0 + m, slot_pt[slot]) for m < M (Mu: the caller's label
 // count); 0 for padding labels m < ld and for empty slots
@@ -886,18 +908,17 @@ __global__ void __launch_bounds__(SPLAT_TILE) to_slots_kernel(const float *__res
     slot_tile_points(st, point_major, M, Mu, m0, N, seg, nseg, slot_pt);
     __syncthreads();
     // eight independent loads in flight per thread
+    CallerWalk cw(point_major, M);
 #pragma unroll 8
-    for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE) {
-        int q, m;
-        slot_tile_elem(f, point_major, M, q, m);
+    for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE, cw.next()) {
+        const int q = cw.q(), m = cw.m();
         st.rows[q * pitch + m] = st.pt[q] >= 0 ? in[st.o0[q] + (size_t)m * st.step[q]] : 0.f;
     }
     __syncthreads();
     float *dst = out + (size_t)blockIdx.x * SPLAT_TILE * ld;
-    for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE) {
-        const int q = f / ld, m = f - q * ld;
-        dst[f] = m < M ? st.rows[q * pitch + m] : 0.f;
-    }
+    TileWalk tw(li, ld);
+    for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE, tw.next())
+        dst[f] = tw.col < M ? st.rows[tw.row * pitch + tw.col] : 0.f;
 }
 
 // out(m, pt) = in[pt_slot[pt]][m], one thread per point: label-major output is
@@ -923,15 +944,14 @@ __global__ void __launch_bounds__(SPLAT_TILE) from_slots_kernel(const float *__r
     const int li = threadIdx.x, pitch = ld + 1;
     slot_tile_points(st, point_major, M, Mu, m0, N, seg, nseg, slot_pt);
     const float *src = in + (size_t)blockIdx.x * SPLAT_TILE * ld;
+    TileWalk tw(li, ld);
 #pragma unroll 8
-    for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE) {
-        const int q = f / ld, m = f - q * ld;
-        if (m < M) st.rows[q * pitch + m] = src[f];
-    }
+    for (int f = li; f < SPLAT_TILE * ld; f += SPLAT_TILE, tw.next())
+        if (tw.col < M) st.rows[tw.row * pitch + tw.col] = src[f];
     __syncthreads();
-    for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE) {
-        int q, m;
-        slot_tile_elem(f, point_major, M, q, m);
+    CallerWalk cw(point_major, M);
+    for (int f = li; f < SPLAT_TILE * M; f += SPLAT_TILE, cw.next()) {
+        const int q = cw.q(), m = cw.m();
         if (st.pt[q] >= 0) out[st.o0[q] + (size_t)m * st.step[q]] = st.rows[q * pitch + m];
     }
 }
