@@ -391,13 +391,20 @@ __global__ void sum_parts_kernel(const double *__restrict__ part, int nblk, int 
 //   df[i][j-1] += sf[j-1] * (D_0 + ... + D_{j-1} - j D_j)
 // (the per-label differences are taken first, as in the per-label form), so a
 // thread keeps only the point's z row and streams the corner rows through it.
+// (zrow null: z = 1 for every label; M: the labels of this pair)
 template <int MP>
 __device__ __forceinline__ void slice_grad_pair(const SliceGradArgs &a, const float *V, const float *zrow, float alpha,
-                                                const float *zscale, size_t s, int i, float (&grad)[DCRF_MAX_D]) {
+                                                const float *zscale, int M, size_t s, int i,
+                                                float (&grad)[DCRF_MAX_D]) {
     constexpr int VW = MP % 4 == 0 ? 4 : 1;
-    const int d = a.d, N = a.N, M = a.M;
+    const int d = a.d, N = a.N;
     float z[MP];
-    row_load<MP>(zrow + s * MP, z);
+    if (zrow) {
+        row_load<MP>(zrow + s * MP, z);
+    } else {
+#pragma unroll
+        for (int m = 0; m < MP; m++) z[m] = 1.f;
+    }
     if (zscale) {
         const float f = zscale[s];
 #pragma unroll
@@ -440,8 +447,10 @@ __global__ void __launch_bounds__(256, 4) slice_grad_kernel(SliceGradArgs a) {
     float grad[DCRF_MAX_D];
 #pragma unroll
     for (int j = 0; j < DCRF_MAX_D; j++) grad[j] = 0.f;
-    slice_grad_pair<MP>(a, a.V, a.z, a.alpha, nullptr, s, i, grad);
-    if (a.V2) slice_grad_pair<MP>(a, a.V2, a.z2, a.alpha2, a.z2scale, s, i, grad);
+    slice_grad_pair<MP>(a, a.V, a.z, a.alpha, nullptr, a.M, s, i, grad);
+    if (a.V2) slice_grad_pair<MP>(a, a.V2, a.z2, a.alpha2, a.z2scale, a.M, s, i, grad);
+    if (a.V3) slice_grad_pair<1>(a, a.V3, nullptr, a.alpha3, nullptr, 1, s, i, grad);
+    if (a.V4) slice_grad_pair<1>(a, a.V4, a.z4, a.alpha4, nullptr, 1, s, i, grad);
 #pragma unroll
     for (int j = 0; j < DCRF_MAX_D; j++)
         if (j < a.d) a.df[(size_t)i * a.d + j] += grad[j];

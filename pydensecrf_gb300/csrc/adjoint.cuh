@@ -19,6 +19,12 @@ struct SliceGradArgs {
     float sf[DCRF_MAX_D];
     float alpha;          // sign / (1+2^-d) / (d+1) for the first pair
     float alpha2;         // and for the second
+    // optional value-size-1 pairs in the same pass (the normalisation's terms):
+    // V3 [L+1] with z = 1 everywhere, V4 [L+1] with z = z4 [nslots]
+    const float *V3;
+    const float *V4;
+    const float *z4;
+    float alpha3, alpha4;
     float *df;            // [N][d] accumulated feature gradient
 };
 

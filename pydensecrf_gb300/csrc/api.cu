@@ -1650,12 +1650,18 @@ int slice_from(dcrf_crf *h, int k, const float *V, float *out, bool value1, bool
 // T.df += sign * sum over labels of z . d(slice of V)/d(features): the
 // per-point part of Permutohedral::gradient (permutohedral.cpp:612-695).
 // z2scale (optional, [nslots]): the second pair's z is z2 .* z2scale per point.
+// V3, V4 (optional, value size 1, [L+1]): two more pairs in the same pass, V3
+// with z = 1 and V4 with z = z4, both with sign34.
 int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float sign, bool value1,
                     const float *V2 = nullptr, const float *z2 = nullptr, float sign2 = 1.f,
-                    const float *z2scale = nullptr) {
+                    const float *z2scale = nullptr, const float *V3 = nullptr, const float *V4 = nullptr,
+                    const float *z4 = nullptr, float sign34 = 1.f) {
     Term &T = h->terms[k];
     SliceGradArgs g{};
     g.z2scale = z2scale;
+    g.V3 = V3;
+    g.V4 = V4;
+    g.z4 = z4;
     g.V2 = V2;
     g.z2 = z2;
     g.N = h->N;
@@ -1672,6 +1678,7 @@ int slice_grad_into(dcrf_crf *h, int k, const float *V, const float *z, float si
         g.sf[i] = (float)(1.0 / std::sqrt((double)((i + 2) * (i + 1))) * (double)inv_std_dev);
     g.alpha = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1) * sign;
     g.alpha2 = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1) * sign2;
+    g.alpha3 = g.alpha4 = 1.0f / (1.0f + std::pow(2.0f, (float)-T.d)) / (float)(T.d + 1) * sign34;
     g.df = T.df;
     CU(launch_slice_grad(g, value1 ? 1 : h->MP, h->stream));
     return DCRF_OK;
@@ -2872,16 +2879,20 @@ int dcrf_backward(dcrf_crf *h, const float *dQ, int layout, int where, float *dU
                                      h->stream));
                 // d/df x~^T K_raw y~: the forward-blurred S_b against y~ plus the
                 // reverse-blurred splat of y~ (= C S_t) against x~, in one pass
-                // (x~ = norm .* b when the transpose starts normalised: the norm is
-                // applied to b as the pass reads it)
-                if ((rc = slice_grad_into(h, k, Tk.bv[5], yn, 1.f, false, Tk.bv[8], b, 1.f,
-                                          tr_pre(Tk) ? Tk.norm : nullptr)))
-                    return rc;
-                if (Tk.ntype != DCRF_NO_NORMALIZATION) {
+                // the normalisation's terms first: - d/df c1^T K_raw 1, the forward-
+                // blurred splat of c1 (one value per point) against ones and the
+                // reverse-blurred splat of ones against c1
+                const bool nrm = Tk.ntype != DCRF_NO_NORMALIZATION;
+                if (nrm) {
                     if ((rc = splat_into(h, k, x1, Tk.b1[0], true))) return rc;
                     if ((rc = blur_into(h, k, Tk.b1[0], Tk.b1[1], false, true))) return rc;
-                    if ((rc = slice_grad_into(h, k, Tk.b1[1], ones1, -1.f, true, Tk.b1[2], x1, -1.f))) return rc;
                 }
+                // then all four slice-gradient pairs in one pass (x~ = norm .* b when the
+                // transpose starts normalised: the norm is applied to b as the pass reads it)
+                if ((rc = slice_grad_into(h, k, Tk.bv[5], yn, 1.f, false, Tk.bv[8], b, 1.f,
+                                          tr_pre(Tk) ? Tk.norm : nullptr, nrm ? Tk.b1[1] : nullptr,
+                                          nrm ? Tk.b1[2] : nullptr, x1, -1.f)))
+                    return rc;
                 continue;
             }
             const float *xs = xtilde(Tk);

@@ -19,6 +19,7 @@ enum : int {
     // the mean-field iteration's passes, compiled as their own instances
     PP_HOT_STEP = PP_MSG | PP_SPLAT,    // messages, softmax, splat of the new marginals
     PP_HOT_LAST = PP_MSG | PP_WRITE_Q,  // the last iteration: messages, softmax, marginals out
+    PP_HOT_SPLAT = PP_LOAD_Q | PP_SPLAT,  // the adjoint's splat of given rows through every term
 };
 
 struct PPArgs {

@@ -1,6 +1,6 @@
 // pointpass.cu -- launchers of the mean-field point pass (pointpass.cuh):
 // one instance per padded label count and thread shape, plus compile-time
-// instances of the iteration's two passes.  Kept apart from meanfield.cu so
+// instances of the iteration's two passes and of the adjoint's splat pass.  Kept apart from meanfield.cu so
 // that the instances compile in parallel with the other kernels.
 #include <algorithm>
 
@@ -14,6 +14,7 @@ static cudaError_t pp_launch_s(const PPArgs &a, cudaStream_t s) {
     if constexpr (MP >= 4) {  // the mean-field iteration passes, specialised
         if (a.mode == PP_HOT_STEP) return launch_pdl(pointpass_kernel<MP, S, PP_HOT_STEP>, g, b, a.smem_bytes, s, a);
         if (a.mode == PP_HOT_LAST) return launch_pdl(pointpass_kernel<MP, S, PP_HOT_LAST>, g, b, a.smem_bytes, s, a);
+        if (a.mode == PP_HOT_SPLAT) return launch_pdl(pointpass_kernel<MP, S, PP_HOT_SPLAT>, g, b, a.smem_bytes, s, a);
     }
     return launch_pdl(pointpass_kernel<MP, S>, g, b, a.smem_bytes, s, a);
 }
@@ -51,6 +52,7 @@ static void pp_prepare_s() {
     if constexpr (MP >= 4) {
         pp_optin(pointpass_kernel<MP, S, PP_HOT_STEP>);
         pp_optin(pointpass_kernel<MP, S, PP_HOT_LAST>);
+        pp_optin(pointpass_kernel<MP, S, PP_HOT_SPLAT>);
     }
 }
 
