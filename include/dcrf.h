@@ -88,9 +88,9 @@ int dcrf_last_error(char *buf, size_t len);
 /* DenseCRF(N, M): densecrf.pyx:51-63 -> densecrf.cpp:39-40.
  * Binds the handle to the current CUDA device and creates its own stream.
  * M may be 1 .. DCRF_MAX_LABELS (4096).  With more than 32 labels the labels
- * are processed in chunks of 32: inference, start/step, klDivergence, map and
- * the unary energy work as for any M; the adjoint (dcrf_inference_checkpointed,
- * dcrf_backward), dcrf_pairwise_energy and the full-width raw filters
+ * are processed in chunks of 32: inference, start/step, klDivergence, map,
+ * both debug energies and the logistic unary work as for any M; the adjoint
+ * (dcrf_inference_checkpointed, dcrf_backward) and the full-width raw filters
  * (dcrf_lattice_filter / _noalloc with value_size M) return
  * DCRF_ERR_INVALID_ARG. */
 int dcrf_create(int N, int M, dcrf_crf **out);
