@@ -89,9 +89,8 @@ int dcrf_last_error(char *buf, size_t len);
  * Binds the handle to the current CUDA device and creates its own stream.
  * M may be 1 .. DCRF_MAX_LABELS (4096).  With more than 32 labels the labels
  * are processed in chunks of 32: inference, start/step, klDivergence, map,
- * both debug energies and the logistic unary work as for any M; the adjoint
- * (dcrf_inference_checkpointed, dcrf_backward) and the full-width raw filters
- * (dcrf_lattice_filter / _noalloc with value_size M) return
+ * both debug energies, the logistic unary and the raw filters work as for any
+ * M; the adjoint (dcrf_inference_checkpointed, dcrf_backward) returns
  * DCRF_ERR_INVALID_ARG. */
 int dcrf_create(int N, int M, dcrf_crf **out);
 
@@ -378,8 +377,9 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
  * share the one array and it keeps the last call's contents: calls that may
  * overlap on the GPU (other streams, other host threads) race and must be
  * serialised by the caller.  A problem whose scratch exceeds the maximum
- * (value_size*slots + (partials+1)*P + 2*(vertices+1)*P floats, P the padded
- * value size) is rejected with DCRF_ERR_INVALID_ARG.
+ * (slots*P + (partials+1)*P + 2*(vertices+1)*P floats, P the padded value
+ * size up to 32; more labels are filtered 32 at a time through the same
+ * scratch, P = 32) is rejected with DCRF_ERR_INVALID_ARG.
  * No counterpart in the reference (added for allocation-free callers). */
 int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out,
                                 void *stream);

@@ -2383,11 +2383,9 @@ int dcrf_term_norm(dcrf_crf *h, int term, float *norm) {
 int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, int reverse, float *out) {
     int rc = check_ready(h);
     if (rc) return rc;
-    if (is_wide(h) && value_size != 1) return wide_unsupported("dcrf_lattice_filter with value_size M");
     if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     bool v1 = value_size == 1;
-    int MP = v1 ? 1 : h->MP;
     if (!h->tmp) {  // the raw filter's slot rows, made at its first use
         const size_t rows = (size_t)h->nslots * h->MP;
         if ((rc = dev_alloc_async(&h->tmp, rows, h->stream))) return rc;
@@ -2398,15 +2396,22 @@ int dcrf_lattice_filter(dcrf_crf *h, int term, const float *in, int value_size, 
     // that may have run since the build
     if (v1 && (rc = zero_sentinels(h, h->terms[term]))) return rc;
     std::vector<int> one{term};
-    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
-    a.ts.t[0].pre_norm = 0;
-    a.ts.t[0].mem_w = h->terms[term].lat.mem_w;  // raw filter: no normalisation folded in
-    a.Qin = h->tmp;
-    CU(pp(h, a, MP));
-    if ((rc = filter_phase(h, one, reverse != 0, v1, false))) return rc;
-    a = pp_args(h, PP_FILTER, one, reverse != 0, v1);
-    a.Qout = h->tmp;
-    CU(pp(h, a, MP));
+    // splat, blur and slice are linear per label: more than 32 labels are
+    // filtered label chunk by label chunk, each through its own lattice rows
+    const int nc = v1 ? 1 : label_chunks(h->MP);
+    for (int c = 0; c < nc; c++) {
+        const int MPc = v1 ? 1 : chunk_width(h->MP, c);
+        float *rows = h->tmp + (v1 ? 0 : chunk_base(h->nslots, c));
+        PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1, c);
+        a.ts.t[0].pre_norm = 0;
+        a.ts.t[0].mem_w = h->terms[term].lat.mem_w;  // raw filter: no normalisation folded in
+        a.Qin = rows;
+        CU(pp(h, a, MPc));
+        if ((rc = filter_phase(h, one, reverse != 0, v1, false, nullptr, nullptr, c))) return rc;
+        a = pp_args(h, PP_FILTER, one, reverse != 0, v1, c);
+        a.Qout = rows;
+        CU(pp(h, a, MPc));
+    }
     if (v1 && (rc = zero_sentinels(h, h->terms[term]))) return rc;
     if ((rc = store_mn(h, h->tmp, out, DCRF_LAYOUT_LM, DCRF_HOST, value_size))) return rc;
     if ((rc = sync_check(h))) return rc;
@@ -3011,11 +3016,12 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
                                            float *out, void *stream) {
     int rc = check_ready(h);
     if (rc) return rc;
-    if (is_wide(h) && value_size != 1) return wide_unsupported("dcrf_lattice_filter_noalloc with value_size M");
     if (term < 0 || term >= (int)h->terms.size() || !in || !out) return set_err(DCRF_ERR_INVALID_ARG, "bad argument");
     if (value_size != 1 && value_size != h->M) return set_err(DCRF_ERR_INVALID_ARG, "value_size must be 1 or M");
     const bool v1 = value_size == 1;
-    const int MPv = v1 ? 1 : h->MP;
+    // the scratch holds one label chunk (at most 32 labels) at a time; more
+    // labels are filtered chunk by chunk through the same scratch
+    const int MPv = v1 ? 1 : chunk_width(h->MP, 0);
     Term &T = h->terms[term];
     const size_t n_in = pad64((size_t)MPv * h->nslots);
     const size_t n_pv = pad64(((size_t)T.lat.P + 1) * MPv);
@@ -3039,42 +3045,46 @@ extern "C" int dcrf_lattice_filter_noalloc(dcrf_crf *h, int term, const float *i
     // the array keeps the previous call's contents: the zero sentinel rows are restored
     CU(cudaMemsetAsync(V0, 0, sizeof(float) * MPv, s));
     CU(cudaMemsetAsync(V1, 0, sizeof(float) * MPv, s));
-    CU(launch_to_slots(in, 0, value_size, value_size, 0, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots, in_s,
-                       s));
     std::vector<int> one{term};
-    PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1);
-    a.ts.t[0].pre_norm = 0;
-    a.ts.t[0].mem_w = T.lat.mem_w;
-    a.ts.t[0].pv = pv;
-    a.ts.t[0].pout = pv;  // splat-only pass: the scratch takes the vertex-grouped partials
-    a.Qin = in_s;
-    CU(launch_pointpass(a, MPv, s));
-    ReduceArgs ra{};
-    ra.n = 1;
-    ra.t[0] = {T.lat.red_beg, pv, V0, T.lat.L, T.lat.P};
-    CU(launch_reduce(ra, MPv, s));
-    const int NV = MPv % 4 == 0 ? MPv / 4 : MPv % 2 == 0 ? MPv / 2 : MPv;
     const bool seq = v1 || h->M <= 2 || T.variant == DCRF_VARIANT_SCALAR;
-    for (int pass = 0; pass <= T.d; pass++) {
-        BlurArgs ba{};
-        ba.n = 1;
-        ba.begin[0] = 0;
-        ba.begin[1] = (long long)T.lat.L * NV;
-        ba.t[0].Vin = Vb[pass & 1];
-        ba.t[0].Vout = Vb[(pass + 1) & 1];
-        ba.t[0].nbr = T.lat.nbr;
-        ba.t[0].L = T.lat.L;
-        ba.t[0].axis = reverse ? T.d - pass : pass;
-        ba.t[0].axis2 = -1;
-        ba.t[0].pv = nullptr;
-        CU(launch_blur(ba, MPv, seq, s));
+    const int nseg = (int)h->seg.size() - 1, nc = v1 ? 1 : label_chunks(h->MP);
+    for (int c = 0; c < nc; c++) {
+        // labels [m0, m0 + mc) of the caller's rows, in slot rows of w floats
+        const int w = v1 ? 1 : chunk_width(h->MP, c), m0 = DCRF_LCHUNK * c, mc = std::min(w, value_size - m0);
+        CU(launch_to_slots(in, 0, mc, value_size, m0, w, h->N, h->d_seg, nseg, h->slot_pt, h->nslots, in_s, s));
+        PPArgs a = pp_args(h, PP_LOAD_Q | PP_SPLAT, one, reverse != 0, v1, c);
+        a.ts.t[0].pre_norm = 0;
+        a.ts.t[0].mem_w = T.lat.mem_w;
+        a.ts.t[0].pv = pv;
+        a.ts.t[0].pout = pv;  // splat-only pass: the scratch takes the vertex-grouped partials
+        a.Qin = in_s;
+        CU(launch_pointpass(a, w, s));
+        ReduceArgs ra{};
+        ra.n = 1;
+        ra.t[0] = {T.lat.red_beg, pv, V0, T.lat.L, T.lat.P};
+        CU(launch_reduce(ra, w, s));
+        const int NV = w % 4 == 0 ? w / 4 : w % 2 == 0 ? w / 2 : w;
+        for (int pass = 0; pass <= T.d; pass++) {
+            BlurArgs ba{};
+            ba.n = 1;
+            ba.begin[0] = 0;
+            ba.begin[1] = (long long)T.lat.L * NV;
+            ba.t[0].Vin = Vb[pass & 1];
+            ba.t[0].Vout = Vb[(pass + 1) & 1];
+            ba.t[0].nbr = T.lat.nbr;
+            ba.t[0].L = T.lat.L;
+            ba.t[0].axis = reverse ? T.d - pass : pass;
+            ba.t[0].axis2 = -1;
+            ba.t[0].pv = nullptr;
+            CU(launch_blur(ba, w, seq, s));
+        }
+        PPArgs f = pp_args(h, PP_FILTER, one, reverse != 0, v1, c);
+        f.ts.t[0].V = Vb[(T.d + 1) & 1];
+        f.Qout = in_s;
+        CU(launch_pointpass(f, w, s));
+        CU(launch_from_slots(in_s, mc, value_size, m0, w, h->N, h->d_seg, nseg, h->slot_pt, h->nslots, h->pt_slot, 0, out,
+                             s));
     }
-    PPArgs f = pp_args(h, PP_FILTER, one, reverse != 0, v1);
-    f.ts.t[0].V = Vb[(T.d + 1) & 1];
-    f.Qout = in_s;
-    CU(launch_pointpass(f, MPv, s));
-    CU(launch_from_slots(in_s, value_size, value_size, 0, MPv, h->N, h->d_seg, (int)h->seg.size() - 1, h->slot_pt, h->nslots,
-                         h->pt_slot, 0, out, s));
     CU(cudaEventRecord(h->xorder, s));
     CU(cudaStreamWaitEvent(h->stream, h->xorder, 0));
     return ok();

@@ -135,16 +135,38 @@ def test_wide_larger_image_and_batch(engine, oracle_mod):
 
 
 def test_wide_unsupported_calls_are_errors(engine):
-    """The adjoint and the full-width raw filter keep the 32-label limit, as an explicit error."""
+    """The adjoint keeps the 32-label limit, as an explicit error."""
     d = engine.DenseCRF2D(16, 12, 40)
     d.setUnaryEnergy(np.ones((40, 16 * 12), np.float32))
     d.addPairwiseGaussian(3, 3.0)
     with pytest.raises(ValueError):
         d.inferenceCheckpointed(2)
-    with pytest.raises(ValueError):
-        d.lattice_filter(0, np.ones((40, 16 * 12), np.float32), False)
-    out = d.lattice_filter(0, np.ones((1, 16 * 12), np.float32), False)  # value size 1 works
+    out = d.lattice_filter(0, np.ones((1, 16 * 12), np.float32), False)
     assert np.isfinite(out).all()
+
+
+@pytest.mark.parametrize("M", [40, 70])
+def test_wide_lattice_filter_vs_oracle(engine, oracle_mod, M):
+    """The raw filter (Permutohedral::compute, permutohedral.cpp:596-604) with
+    value size M above 32, both directions, on both terms: label chunks of 32
+    (70 labels: 32 + 32 + a ragged 6 padded to 8) against the oracle's filter of
+    the whole rows, within 1e-6 of the output's magnitude like the narrow
+    filter tests; value size 1 on the same handle afterwards."""
+    rng, N, U, img, diag, mat = _problem(61 + M, 29, 21, M)
+    d = engine.DenseCRF2D(29, 21, M)
+    d.setUnaryEnergy(np.ascontiguousarray(U.T))
+    d.addPairwiseGaussian(3, 3.0)
+    d.addPairwiseBilateral(8, 13, img, 5.0)
+    lats = [oracle_mod.Lattice(oracle_mod.features_gaussian_2d(29, 21, 3, 3), "oracle"),
+            oracle_mod.Lattice(oracle_mod.features_bilateral_2d(img, 8, 8, 13, 13, 13), "oracle")]
+    for term in (0, 1):
+        for reverse in (False, True):
+            for vs in (M, 1):
+                v = rng.random((vs, N)).astype(np.float32)
+                got = d.lattice_filter(term, v, reverse)
+                want = lats[term].compute(np.ascontiguousarray(v.T), reverse).T
+                err = np.abs(got - want).max()
+                assert err <= 1e-6 * np.abs(want).max(), (term, reverse, vs, err)
 
 
 def test_wide_logistic_unary_with_matrix_keeps_parameters(engine, oracle_mod):

@@ -59,6 +59,35 @@ def test_noalloc_filter_matches_filter(engine, oracle_mod):
                     assert err <= 1e-6 * np.abs(orc).max(), ("oracle", term, vs, reverse, call, err)
 
 
+def test_noalloc_filter_above_32_labels(engine, oracle_mod):
+    """70 labels: the scratch holds one label chunk of 32 at a time and the
+    three chunks (the last one 6 labels padded to 8) go through it in turn; the
+    result must match the regular filter and the oracle's filter of the whole
+    rows, after a call of value size 1 left other contents in the scratch."""
+    import torch
+
+    from pydensecrf_gb300 import _lib
+
+    lib = _lib.load()
+    rng = np.random.default_rng(27)
+    N, M = 3000, 70
+    f = rng.normal(0, 2, size=(N, 3)).astype(np.float32)
+    crf = engine.DenseCRF(N, M)
+    crf.addPairwiseEnergy(np.ascontiguousarray(f.T), 1.0)
+    lat = oracle_mod.Lattice(f, "oracle")
+    for reverse in (False, True):
+        _noalloc_filter(lib, _lib, crf, 0, rng.random((1, N)).astype(np.float32), reverse, torch)
+        v = rng.random((M, N)).astype(np.float32)
+        got = _noalloc_filter(lib, _lib, crf, 0, v, reverse, torch)
+        assert np.isfinite(got).all()
+        want = crf.lattice_filter(0, v, reverse)
+        err = np.abs(got - want).max()
+        assert err <= 1e-6 * np.abs(want).max(), (reverse, err)
+        orc = lat.compute(np.ascontiguousarray(v.T), reverse).T
+        err = np.abs(got - orc).max()
+        assert err <= 1e-6 * np.abs(orc).max(), ("oracle", reverse, err)
+
+
 def test_noalloc_right_after_build_on_another_stream(engine, oracle_mod):
     """The call is queued on a stream of the caller's own straight after a term
     is added (the build may still be running on the handle's stream), and the
