@@ -5,6 +5,9 @@ never against another GPU handle.
 * 640x480, 21 labels, 10 iterations, Gaussian + bilateral Potts (the headline
   workload), both lattice variants: Q within 1e-4 max-abs of the oracle and of
   its FP64 twin (densecrf.cpp:115-131), argmax agreement >= 99.9 %.
+* The raw filter of both 640x480 terms at 21 and 40 labels: against the
+  oracle's filter and an FP64 filter, the transpose identity
+  <K x, y> = <x, K^T y> and linearity.
 * Uneven 2D batch with a 21x21 Matrix compatibility: four images (one of
   1024x1000) in ONE batched handle, each image's marginals against its own
   oracle solve.
@@ -51,6 +54,80 @@ def test_plain_vga_vs_oracle(engine, oracle_mod, variant):
           f"|Q - FP64| {err64:.2e} (argmax {agree64:.5f})")
     assert err <= QTOL and agree >= AGREE
     assert err64 <= QTOL and agree64 >= AGREE
+
+
+def _filter_f64(lat, x):
+    """Permutohedral::compute (permutohedral.cpp:476-610) in float64 on the
+    oracle's lattice tables: x (N, vs) -> (N, vs)."""
+    N, d1 = lat.offset.shape
+    d, L = d1 - 1, lat.L
+    off = lat.offset + 1  # row 0 is the zero sentinel
+    bary = lat.bary.astype(np.float64)
+    xd = x.astype(np.float64)
+    vals = np.zeros((L + 2, x.shape[1]))
+    for k in range(x.shape[1]):
+        for r in range(d1):
+            vals[:, k] += np.bincount(off[:, r], weights=bary[:, r] * xd[:, k], minlength=L + 2)
+    for j in range(d1):
+        n1, n2 = lat.neighbors[j, :, 0] + 1, lat.neighbors[j, :, 1] + 1
+        nv = vals.copy()
+        nv[1:L + 1] = vals[1:L + 1] + 0.5 * (vals[n1] + vals[n2])
+        vals = nv
+    alpha = 1.0 / (1.0 + 2.0 ** -d)
+    out = np.zeros_like(xd)
+    for r in range(d1):
+        out += (bary[:, r, None] * alpha) * vals[off[:, r]]
+    return out
+
+
+@pytest.mark.parametrize("M", [21, 40])
+def test_vga_lattice_filter_properties(engine, oracle_mod, M):
+    """The raw filter (Permutohedral::compute, permutohedral.cpp:596-604) of
+    both 640x480 terms, value size M.
+
+    Against the oracle's float filter and against an FP64 filter on the
+    oracle's lattice tables, each within 3e-6 of the output's magnitude.  The
+    bilateral lattice sums about 150 members per vertex, which the GPU adds in
+    its tile order and the reference in point order, so the two float results
+    round differently: on this case the oracle's own float filter is already
+    about 8e-7 of the magnitude away from the FP64 one.
+
+    Two properties that hold at any size.  The reverse filter is the transpose,
+    so <K x, y> = <x, K^T y> (relative 1e-5).  The filter is linear:
+    K(a x + b y) = a K x + b K y (1e-5 of the magnitude)."""
+    O = oracle_mod
+    cfg = S.plain_vga(0)
+    W, H = cfg["W"], cfg["H"]
+    N = W * H
+    rng = np.random.default_rng(97 + M)
+    d = engine.DenseCRF2D(W, H, M)
+    d.addPairwiseGaussian(sxy=3, compat=3)
+    d.addPairwiseBilateral(sxy=80, srgb=13, rgbim=cfg["img"], compat=10)
+    feats = [O.features_gaussian_2d(W, H, 3, 3), O.features_bilateral_2d(cfg["img"], 80, 80, 13, 13, 13)]
+    x = rng.random((M, N)).astype(np.float32)
+    y = rng.random((M, N)).astype(np.float32)
+    for term in (0, 1):
+        lat = O.Lattice(feats[term], "oracle")
+        Kx = d.lattice_filter(term, x, False)
+        want = lat.compute(np.ascontiguousarray(x.T), False).T
+        scale = np.abs(want).max()
+        err = np.abs(Kx - want).max() / scale
+        k64 = _filter_f64(lat, np.ascontiguousarray(x.T)).T
+        e_gpu = np.abs(Kx - k64).max() / scale
+        e_orc = np.abs(want - k64).max() / scale
+        print(f"640x480 term {term} M={M}: |K - oracle| {err:.2e}, |K - FP64| {e_gpu:.2e}, "
+              f"|oracle - FP64| {e_orc:.2e} (of the magnitude)")
+        assert err <= 3e-6, (term, err)
+        assert e_gpu <= 3e-6, (term, e_gpu, e_orc)
+        KTy = d.lattice_filter(term, y, True)
+        lhs = float(np.dot(Kx.ravel().astype(np.float64), y.ravel().astype(np.float64)))
+        rhs = float(np.dot(x.ravel().astype(np.float64), KTy.ravel().astype(np.float64)))
+        assert abs(lhs - rhs) <= 1e-5 * abs(lhs), (term, lhs, rhs)
+        Ky = d.lattice_filter(term, y, False)
+        Kxy = d.lattice_filter(term, np.float32(2.5) * x - np.float32(0.75) * y, False)
+        lin = 2.5 * Kx.astype(np.float64) - 0.75 * Ky.astype(np.float64)
+        err = np.abs(Kxy - lin).max()
+        assert err <= 1e-5 * np.abs(lin).max(), (term, err)
 
 
 def _uneven_subset(seed, sizes, M):
