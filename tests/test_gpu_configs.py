@@ -21,6 +21,7 @@ never against another GPU handle.
 import numpy as np
 import pytest
 
+from filter_f64 import filter_f64
 from pydensecrf_gb300 import synthetic as S
 
 pytestmark = pytest.mark.gpu
@@ -56,30 +57,6 @@ def test_plain_vga_vs_oracle(engine, oracle_mod, variant):
     assert err64 <= QTOL and agree64 >= AGREE
 
 
-def _filter_f64(lat, x):
-    """Permutohedral::compute (permutohedral.cpp:476-610) in float64 on the
-    oracle's lattice tables: x (N, vs) -> (N, vs)."""
-    N, d1 = lat.offset.shape
-    d, L = d1 - 1, lat.L
-    off = lat.offset + 1  # row 0 is the zero sentinel
-    bary = lat.bary.astype(np.float64)
-    xd = x.astype(np.float64)
-    vals = np.zeros((L + 2, x.shape[1]))
-    for k in range(x.shape[1]):
-        for r in range(d1):
-            vals[:, k] += np.bincount(off[:, r], weights=bary[:, r] * xd[:, k], minlength=L + 2)
-    for j in range(d1):
-        n1, n2 = lat.neighbors[j, :, 0] + 1, lat.neighbors[j, :, 1] + 1
-        nv = vals.copy()
-        nv[1:L + 1] = vals[1:L + 1] + 0.5 * (vals[n1] + vals[n2])
-        vals = nv
-    alpha = 1.0 / (1.0 + 2.0 ** -d)
-    out = np.zeros_like(xd)
-    for r in range(d1):
-        out += (bary[:, r, None] * alpha) * vals[off[:, r]]
-    return out
-
-
 @pytest.mark.parametrize("M", [21, 40])
 def test_vga_lattice_filter_properties(engine, oracle_mod, M):
     """The raw filter (Permutohedral::compute, permutohedral.cpp:596-604) of
@@ -112,7 +89,7 @@ def test_vga_lattice_filter_properties(engine, oracle_mod, M):
         want = lat.compute(np.ascontiguousarray(x.T), False).T
         scale = np.abs(want).max()
         err = np.abs(Kx - want).max() / scale
-        k64 = _filter_f64(lat, np.ascontiguousarray(x.T)).T
+        k64 = filter_f64(lat, np.ascontiguousarray(x.T)).T
         e_gpu = np.abs(Kx - k64).max() / scale
         e_orc = np.abs(want - k64).max() / scale
         print(f"640x480 term {term} M={M}: |K - oracle| {err:.2e}, |K - FP64| {e_gpu:.2e}, "

@@ -100,7 +100,30 @@ def test_oracle_fp64_close(oracle_mod):
     assert np.abs(c.inference(5) - c.inference_f64(5)).max() < 1e-5
 
 
-requires_ref = pytest.mark.skipif("not __import__('oracle').ref_available()",
+def test_fp64_filter_and_transpose_identity(oracle_mod):
+    """The FP64 filter that the full-size GPU filter test measures against:
+    within 2e-6 of the oracle's float filter (both sseCompute and seqCompute
+    value sizes) on a small bilateral case.  The oracle's reverse filter is the
+    transpose of its forward one: <K x, y> = <x, K^T y>."""
+    from filter_f64 import filter_f64
+
+    O = oracle_mod
+    rng = np.random.default_rng(41)
+    W, H = 96, 64
+    img = rng.integers(0, 256, size=(H, W, 3)).astype(np.uint8)
+    lat = O.Lattice(O.features_bilateral_2d(img, 20, 20, 13, 13, 13), "oracle")
+    for vs in (1, 2, 21):
+        x = rng.random((W * H, vs)).astype(np.float32)
+        y = rng.random((W * H, vs)).astype(np.float32)
+        Kx = lat.compute(x, False)
+        k64 = filter_f64(lat, x)
+        assert np.abs(Kx - k64).max() <= 2e-6 * np.abs(k64).max(), vs
+        lhs = float((Kx.astype(np.float64) * y).sum())
+        rhs = float((x.astype(np.float64) * lat.compute(y, True)).sum())
+        assert abs(lhs - rhs) <= 1e-6 * abs(lhs), vs
+
+
+requires_ref =pytest.mark.skipif("not __import__('oracle').ref_available()",
                                   reason="the reference was not compiled on this machine")
 
 
